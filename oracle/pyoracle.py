@@ -1,0 +1,333 @@
+"""ctypes binding of the CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
+checker and by bench.py for the timed CPU baseline.  The product package
+(mpstools_gb300) never imports this module.
+
+Block matrices cross this boundary as plain dicts:
+  single-site / environment:  {(q0, q1, p0): 2-D float64 array}
+  two-site theta:             {(q0, q1, p0, p1): 2-D float64 array}
+  lambda:                     {q: 1-D float64 array}
+MPO matrices as lists of (wl, wr, out, in, value) plus (Dl, Dr).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def openblas_path() -> str:
+    """Locate the LP64 OpenBLAS bundled with scipy (exports scipy_dgemm_ & co)."""
+    import scipy
+
+    base = os.path.dirname(os.path.dirname(scipy.__file__))
+    cands = sorted(glob.glob(os.path.join(base, "scipy.libs", "libscipy_openblas-*.so")))
+    cands = [c for c in cands if "openblas64" not in c]
+    if not cands:
+        raise RuntimeError("scipy's bundled OpenBLAS (libscipy_openblas-*.so) not found")
+    return cands[0]
+
+
+def build(force: bool = False) -> str:
+    """Compile oracle.cpp into oracle/liboracle.so (g++, OpenMP)."""
+    out = os.path.join(_HERE, "liboracle.so")
+    src = os.path.join(_HERE, "oracle.cpp")
+    if force or not os.path.exists(out) or os.path.getmtime(out) < os.path.getmtime(src):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", out,
+                               src, "-ldl"])
+    return out
+
+
+def lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = build()
+    L = C.CDLL(path)
+    vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
+    P = C.POINTER
+    L.orc_init.argtypes = [C.c_char_p]
+    L.orc_bm_new.restype = vp
+    L.orc_bm_new.argtypes = [i32, i32, vp, vp, vp, vp, vp]
+    L.orc_bm_nblocks.argtypes = [vp]
+    L.orc_bm_nphys.argtypes = [vp]
+    L.orc_bm_size.argtypes = [vp]
+    L.orc_bm_size.restype = C.c_long
+    L.orc_bm_export.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.orc_bm_free.argtypes = [vp]
+    L.orc_mpo_new.restype = vp
+    L.orc_mpo_new.argtypes = [i32, vp, vp, vp, vp, vp, i32, i32]
+    L.orc_mpo_nterms.argtypes = [vp]
+    L.orc_mpo_export.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.orc_mpo_free.argtypes = [vp]
+    L.orc_mpo_heisenberg.argtypes = [i32, vp, vp, vp, vp]
+    L.orc_mpo_spinless.argtypes = [i32, vp, vp, vp, vp]
+    L.orc_theta.restype = vp
+    L.orc_theta.argtypes = [vp, vp]
+    L.orc_contract_twosite.restype = vp
+    L.orc_contract_twosite.argtypes = [vp, vp, vp, vp, vp, vp, i32, vp, i32, i32]
+    L.orc_add_contraction_layer.restype = vp
+    L.orc_add_contraction_layer.argtypes = [vp, vp, vp, vp, i32, i32, i32]
+    L.orc_split.argtypes = [vp, vp, i32, vp, i32, i32, i32, f64, i32, i32, P(vp), P(vp), P(vp),
+                            P(f64), P(i32)]
+    L.orc_lanczos.argtypes = [vp, vp, vp, vp, vp, vp, i32, vp, i32, i32, f64, i32, i32, P(f64),
+                              P(i32), P(vp)]
+    L.orc_dmrg_new.restype = vp
+    L.orc_dmrg_new.argtypes = [i32, vp, vp, vp, i32]
+    L.orc_dmrg_set_threads.argtypes = [vp, i32, i32]
+    L.orc_dmrg_simulate.restype = f64
+    L.orc_dmrg_simulate.argtypes = [vp, i32, f64, i32, i32, f64, f64, i32]
+    L.orc_dmrg_prepare.argtypes = [vp]
+    L.orc_dmrg_do_step.restype = f64
+    L.orc_dmrg_do_step.argtypes = [vp, i32, i32, i32, i32, f64, f64, i32]
+    L.orc_dmrg_nsteps.argtypes = [vp]
+    L.orc_dmrg_steps.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.orc_dmrg_times.argtypes = [vp, vp]
+    L.orc_dmrg_site.restype = vp
+    L.orc_dmrg_site.argtypes = [vp, i32]
+    L.orc_dmrg_lambda.restype = vp
+    L.orc_dmrg_lambda.argtypes = [vp, i32]
+    L.orc_dmrg_env.restype = vp
+    L.orc_dmrg_env.argtypes = [vp, i32, i32]
+    L.orc_dmrg_measure.restype = f64
+    L.orc_dmrg_measure.argtypes = [vp, i32]
+    L.orc_dmrg_free.argtypes = [vp]
+    rc = L.orc_init(openblas_path().encode())
+    if rc != 0:
+        raise RuntimeError(f"oracle: orc_init failed ({rc})")
+    _LIB = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
+
+
+# ------------------------------------------------------------------ conversion
+def bm_to_handle(bm: dict, nphys: int):
+    L = lib()
+    keys = sorted(bm.keys())
+    n = len(keys)
+    q = np.zeros(2 * max(n, 1), np.uint64)
+    p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+    rows = np.zeros(max(n, 1), np.int32)
+    cols = np.zeros(max(n, 1), np.int32)
+    chunks = []
+    for i, k in enumerate(keys):
+        a = np.asarray(bm[k], dtype=np.float64)
+        if nphys == 0:
+            q[2 * i] = q[2 * i + 1] = k
+            a = a.reshape(-1, 1)
+        else:
+            q[2 * i], q[2 * i + 1] = k[0], k[1]
+            for j in range(nphys):
+                p[nphys * i + j] = k[2 + j]
+        rows[i], cols[i] = a.shape
+        chunks.append(np.asfortranarray(a).ravel(order="F"))
+    data = np.concatenate(chunks) if chunks else np.zeros(1)
+    return L.orc_bm_new(nphys, n, _ptr(q), _ptr(p), _ptr(rows), _ptr(cols), _ptr(data))
+
+
+def handle_to_bm(h, free: bool = True) -> dict:
+    L = lib()
+    n = L.orc_bm_nblocks(h)
+    nphys = L.orc_bm_nphys(h)
+    size = L.orc_bm_size(h)
+    q = np.zeros(2 * max(n, 1), np.uint64)
+    p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+    rows = np.zeros(max(n, 1), np.int32)
+    cols = np.zeros(max(n, 1), np.int32)
+    data = np.zeros(max(size, 1))
+    L.orc_bm_export(h, _ptr(q), _ptr(p), _ptr(rows), _ptr(cols), _ptr(data))
+    out = {}
+    off = 0
+    for i in range(n):
+        r, c = int(rows[i]), int(cols[i])
+        a = data[off:off + r * c].reshape((r, c), order="F").copy()
+        off += r * c
+        if nphys == 0:
+            out[int(q[2 * i])] = a[:, 0].copy()
+        elif nphys == 1:
+            out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[i]))] = a
+        else:
+            out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[2 * i]), int(p[2 * i + 1]))] = a
+    if free:
+        L.orc_bm_free(h)
+    return out
+
+
+def mpo_to_handle(terms, Dl, Dr):
+    L = lib()
+    n = len(terms)
+    arr = lambda j, dt: np.array([t[j] for t in terms] or [0], dtype=dt)
+    wl, wr, out, inn = (arr(j, np.uint32) for j in range(4))
+    val = arr(4, np.float64)
+    return L.orc_mpo_new(n, _ptr(wl), _ptr(wr), _ptr(out), _ptr(inn), _ptr(val), Dl, Dr)
+
+
+def handle_to_mpo(h, free=True):
+    L = lib()
+    n = L.orc_mpo_nterms(h)
+    wl, wr, out, inn = (np.zeros(max(n, 1), np.uint32) for _ in range(4))
+    val = np.zeros(max(n, 1))
+    d = np.zeros(2, np.int32)
+    L.orc_mpo_export(h, _ptr(wl), _ptr(wr), _ptr(out), _ptr(inn), _ptr(val), _ptr(d))
+    terms = [(int(wl[i]), int(wr[i]), int(out[i]), int(inn[i]), float(val[i])) for i in range(n)]
+    if free:
+        L.orc_mpo_free(h)
+    return terms, int(d[0]), int(d[1])
+
+
+# ------------------------------------------------------------------ API mirroring the reference
+def heisenberg_mpo(Jz, Jxy, B):
+    L = lib()
+    N = len(B)
+    Jz = np.ascontiguousarray(np.r_[Jz, 0.0], np.float64)
+    Jxy = np.ascontiguousarray(np.r_[Jxy, 0.0], np.float64)
+    B = np.ascontiguousarray(B, np.float64)
+    hs = (C.c_void_p * N)()
+    L.orc_mpo_heisenberg(N, _ptr(Jz), _ptr(Jxy), _ptr(B), hs)
+    return [handle_to_mpo(hs[i]) for i in range(N)]
+
+
+def spinless_fermions_mpo(V, t, mu):
+    L = lib()
+    N = len(mu)
+    V = np.ascontiguousarray(np.r_[V, 0.0], np.float64)
+    t = np.ascontiguousarray(np.r_[t, 0.0], np.float64)
+    mu = np.ascontiguousarray(mu, np.float64)
+    hs = (C.c_void_p * N)()
+    L.orc_mpo_spinless(N, _ptr(V), _ptr(t), _ptr(mu), hs)
+    return [handle_to_mpo(hs[i]) for i in range(N)]
+
+
+def theta(A1, A2):
+    L = lib()
+    h1, h2 = bm_to_handle(A1, 1), bm_to_handle(A2, 1)
+    out = handle_to_bm(L.orc_theta(h1, h2))
+    L.orc_bm_free(h1)
+    L.orc_bm_free(h2)
+    return out
+
+
+def contract_twosite(Lenv, Renv, th, W1, W2, ik0, ik1, nthreads=8):
+    L = lib()
+    hL, hR, hT = bm_to_handle(Lenv, 1), bm_to_handle(Renv, 1), bm_to_handle(th, 2)
+    w1, w2 = mpo_to_handle(*W1), mpo_to_handle(*W2)
+    a, b = np.asarray(ik0, np.uint64), np.asarray(ik1, np.uint64)
+    out = handle_to_bm(L.orc_contract_twosite(hL, hR, hT, w1, w2, _ptr(a), len(a), _ptr(b), len(b), nthreads))
+    for h in (hL, hR, hT):
+        L.orc_bm_free(h)
+    L.orc_mpo_free(w1)
+    L.orc_mpo_free(w2)
+    return out
+
+
+def add_contraction_layer(BL, A, W, ik, direction, nthreads=8):
+    L = lib()
+    hB, hA = bm_to_handle(BL, 1), bm_to_handle(A, 1)
+    w = mpo_to_handle(*W)
+    a = np.asarray(ik, np.uint64)
+    out = handle_to_bm(L.orc_add_contraction_layer(hB, hA, w, _ptr(a), len(a), int(direction), nthreads))
+    L.orc_bm_free(hB)
+    L.orc_bm_free(hA)
+    L.orc_mpo_free(w)
+    return out
+
+
+def split(th, ik0, ik1, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, nthreads=8):
+    L = lib()
+    hT = bm_to_handle(th, 2)
+    a, b = np.asarray(ik0, np.uint64), np.asarray(ik1, np.uint64)
+    U, V, lam = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    tw, chi = C.c_double(), C.c_int()
+    L.orc_split(hT, _ptr(a), len(a), _ptr(b), len(b), int(chimax), int(doTrunc), float(tr_weight),
+                int(normalize), nthreads, C.byref(U), C.byref(V), C.byref(lam), C.byref(tw), C.byref(chi))
+    L.orc_bm_free(hT)
+    return handle_to_bm(U.value), handle_to_bm(V.value), handle_to_bm(lam.value), tw.value, chi.value
+
+
+def lanczos(Lenv, Renv, th, W1, W2, ik0, ik1, itmax=500, delta=1e-12, testenergy=True, nthreads=8):
+    L = lib()
+    hL, hR, hT = bm_to_handle(Lenv, 1), bm_to_handle(Renv, 1), bm_to_handle(th, 2)
+    w1, w2 = mpo_to_handle(*W1), mpo_to_handle(*W2)
+    a, b = np.asarray(ik0, np.uint64), np.asarray(ik1, np.uint64)
+    E0, it, st = C.c_double(), C.c_int(), C.c_void_p()
+    L.orc_lanczos(hL, hR, hT, w1, w2, _ptr(a), len(a), _ptr(b), len(b), itmax, delta, int(testenergy),
+                  nthreads, C.byref(E0), C.byref(it), C.byref(st))
+    for h in (hL, hR, hT):
+        L.orc_bm_free(h)
+    L.orc_mpo_free(w1)
+    L.orc_mpo_free(w2)
+    return E0.value, it.value, handle_to_bm(st.value)
+
+
+class DMRG:
+    """Oracle DMRGengine: sites = list of single-site dicts, mpo = list of (terms, Dl, Dr)."""
+
+    def __init__(self, sites, mpo, itokeys, maxthreads=None, matvec_threads=8):
+        L = lib()
+        N = len(sites)
+        self.N = N
+        hs = (C.c_void_p * N)(*[bm_to_handle(s, 1) for s in sites])
+        ws = (C.c_void_p * N)(*[mpo_to_handle(*w) for w in mpo])
+        d = len(itokeys[0])
+        ik = np.ascontiguousarray(np.asarray(itokeys, np.uint64).ravel())
+        self.h = L.orc_dmrg_new(N, hs, ws, _ptr(ik), d)
+        for i in range(N):
+            L.orc_bm_free(hs[i])
+            L.orc_mpo_free(ws[i])
+        if maxthreads is None:
+            maxthreads = os.cpu_count() or 1
+        L.orc_dmrg_set_threads(self.h, int(maxthreads), int(matvec_threads))
+
+    def simulate(self, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12, delta=1e-13,
+                 testenergy=True):
+        return lib().orc_dmrg_simulate(self.h, maxsteps, EnConv, chimax, int(doTrunc), tr_weight, delta,
+                                       int(testenergy))
+
+    def prepare(self):
+        lib().orc_dmrg_prepare(self.h)
+
+    def do_step(self, site, direction, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
+        return lib().orc_dmrg_do_step(self.h, site, direction, chimax, int(doTrunc), tr_weight, delta,
+                                      int(testenergy))
+
+    def steps(self):
+        L = lib()
+        n = L.orc_dmrg_nsteps(self.h)
+        a = [np.zeros(max(n, 1), np.int32) for _ in range(4)]
+        E, tw = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        L.orc_dmrg_steps(self.h, *[_ptr(x) for x in a], _ptr(E), _ptr(tw))
+        return [dict(site=int(a[0][i]), dir=int(a[1][i]), iters=int(a[2][i]), chi=int(a[3][i]),
+                     E=float(E[i]), tw=float(tw[i])) for i in range(n)]
+
+    def times(self):
+        t = np.zeros(4)
+        lib().orc_dmrg_times(self.h, _ptr(t))
+        return dict(total=t[0], matvec=t[1], env=t[2], split=t[3])
+
+    def site(self, s):
+        return handle_to_bm(lib().orc_dmrg_site(self.h, s))
+
+    def lam(self, bond):
+        return handle_to_bm(lib().orc_dmrg_lambda(self.h, bond))
+
+    def env(self, which, s):
+        return handle_to_bm(lib().orc_dmrg_env(self.h, 1 if which == "R" else 0, s))
+
+    def measure(self, nthreads=1):
+        return lib().orc_dmrg_measure(self.h, nthreads)
+
+    def __del__(self):
+        try:
+            lib().orc_dmrg_free(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,133 @@
+"""Exact diagonalisation and dense effective-Hamiltonian helpers (numpy/scipy).
+
+Independent pins for the oracle: they build the Hamiltonian from its physics
+definition (not from the MPO code) and contract environments densely.
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+
+def _basis(N, Nup):
+    states = []
+    for occ in itertools.combinations(range(N), Nup):
+        s = 0
+        for i in occ:
+            s |= 1 << i
+        states.append(s)
+    states.sort()
+    return states, {s: i for i, s in enumerate(states)}
+
+
+def xxz_ground_energy(Jz, Jxy, B, Nup):
+    """H = sum_i Jxy_i/2 (S+S- + h.c.) + Jz_i Sz Sz - sum_i B_i Sz_i, fixed up-count Nup."""
+    N = len(B)
+    states, idx = _basis(N, Nup)
+    rows, cols, vals = [], [], []
+    for k, s in enumerate(states):
+        diag = 0.0
+        for i in range(N):
+            szi = 0.5 if (s >> i) & 1 else -0.5
+            diag -= B[i] * szi
+        for i in range(N - 1):
+            a, b = (s >> i) & 1, (s >> (i + 1)) & 1
+            diag += Jz[i] * (0.5 if a else -0.5) * (0.5 if b else -0.5)
+            if a != b:
+                t = s ^ (1 << i) ^ (1 << (i + 1))
+                rows.append(idx[t]); cols.append(k); vals.append(Jxy[i] / 2.0)
+        rows.append(k); cols.append(k); vals.append(diag)
+    H = sp.csr_matrix((vals, (rows, cols)), shape=(len(states), len(states)))
+    if H.shape[0] <= 64:
+        return float(np.linalg.eigvalsh(H.toarray())[0])
+    return float(spla.eigsh(H, k=1, which="SA", tol=1e-14)[0][0])
+
+
+def tv_ground_energy(V, t, mu, Nf):
+    """Spinless fermions H = sum_i -t_i (c+_i c_i+1 + h.c.) + V_i n_i n_i+1 - mu_i n_i (open chain)."""
+    N = len(mu)
+    states, idx = _basis(N, Nf)
+    rows, cols, vals = [], [], []
+    for k, s in enumerate(states):
+        diag = 0.0
+        for i in range(N):
+            diag -= mu[i] * ((s >> i) & 1)
+        for i in range(N - 1):
+            a, b = (s >> i) & 1, (s >> (i + 1)) & 1
+            diag += V[i] * a * b
+            if a != b:  # nearest-neighbour hop: no fermion sign for adjacent sites
+                u = s ^ (1 << i) ^ (1 << (i + 1))
+                rows.append(idx[u]); cols.append(k); vals.append(-t[i])
+        rows.append(k); cols.append(k); vals.append(diag)
+    H = sp.csr_matrix((vals, (rows, cols)), shape=(len(states), len(states)))
+    if H.shape[0] <= 64:
+        return float(np.linalg.eigvalsh(H.toarray())[0])
+    return float(spla.eigsh(H, k=1, which="SA", tol=1e-14)[0][0])
+
+
+# --------------------------------------------------------------------------- dense H_eff
+def _bond_layout(charges_dims):
+    """charges_dims: {q: dim} -> {q: (offset, dim)}, total."""
+    off, lay = 0, {}
+    for q in sorted(charges_dims):
+        lay[q] = (off, charges_dims[q])
+        off += charges_dims[q]
+    return lay, off
+
+
+def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
+    """Apply L.W1.W2.R to theta by dense contraction (reference operator convention).
+
+    out(a',b';s1',s2') = sum L[a',a;wl] W1[wl,wm](out=s1,in=s1') W2[wm,wr](out=s2,in=s2')
+                         theta(a,b;s1,s2) R[b',b;wr]
+    Result blocks are keyed like theta and restricted to blocks with nonzero support.
+    """
+    # dense L[wl][a'(global), a(global)], R[wr][b', b]
+    lq, rq = {}, {}
+    for (q0, q1, w), m in Lenv.items():
+        lq.setdefault(q0, m.shape[0]); lq.setdefault(q1, m.shape[1])
+    for (q0, q1, w), m in Renv.items():
+        rq.setdefault(q0, m.shape[0]); rq.setdefault(q1, m.shape[1])
+    for (a, b, s1, s2), m in theta.items():
+        lq.setdefault(a, m.shape[0]); rq.setdefault(b, m.shape[1])
+    llay, nl = _bond_layout(lq)
+    rlay, nr = _bond_layout(rq)
+    d0, d1 = len(ik0), len(ik1)
+    DW = max(max(t[0] for t in W1[0]), max(t[1] for t in W1[0]), max(t[0] for t in W2[0]),
+             max(t[1] for t in W2[0]), max(k[2] for k in Lenv), max(k[2] for k in Renv)) + 1
+    Ld = np.zeros((DW, nl, nl))
+    Rd = np.zeros((DW, nr, nr))
+    for (q0, q1, w), m in Lenv.items():
+        o0, o1 = llay[q0][0], llay[q1][0]
+        Ld[w, o0:o0 + m.shape[0], o1:o1 + m.shape[1]] = m
+    for (q0, q1, w), m in Renv.items():
+        o0, o1 = rlay[q0][0], rlay[q1][0]
+        Rd[w, o0:o0 + m.shape[0], o1:o1 + m.shape[1]] = m
+    # W as dense [wl, wr, out, in]
+    W1d = np.zeros((DW, DW, d0, d0))
+    W2d = np.zeros((DW, DW, d1, d1))
+    for (wl, wr, o, i, v) in W1[0]:
+        W1d[wl, wr, o, i] += v
+    for (wl, wr, o, i, v) in W2[0]:
+        W2d[wl, wr, o, i] += v
+    T = np.zeros((nl, d0, d1, nr))
+    for (a, b, s1, s2), m in theta.items():
+        oa, ob = llay[a][0], rlay[b][0]
+        T[oa:oa + m.shape[0], s1, s2, ob:ob + m.shape[1]] = m
+    # out[a', s1', s2', b'] = L[wl,a',a] W1[wl,wm,s1,s1'] W2[wm,wr,s2,s2'] T[a,s1,s2,b] R[wr,b',b]
+    out = np.einsum("lxa,lmpP,mrqQ,apqb,ryb->xPQy", Ld, W1d, W2d, T, Rd, optimize=True)
+    res = {}
+    for a in lq:
+        for b in rq:
+            for s1 in range(d0):
+                for s2 in range(d1):
+                    if a + ik0[s1] + ik1[s2] != b:
+                        continue
+                    oa, na = llay[a]
+                    ob, nb = rlay[b]
+                    blk = out[oa:oa + na, s1, s2, ob:ob + nb]
+                    res[(a, b, s1, s2)] = blk.copy()
+    return res
