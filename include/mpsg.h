@@ -1,0 +1,161 @@
+/*
+ * mpsg.h -- C ABI of libmpsg, the GB300 (sm_103a) DMRG hot path of MPSTools.
+ *
+ * Plain C types only: pointers, sizes, enums and opaque handles.  Block-sparse
+ * tensors are U(1) BlockMatrix objects: a sorted list of dense column-major
+ * blocks, each keyed by two packed charge words (AbKeyType::_qn) and 0..2
+ * physical / MPO-auxiliary indices (TensorKeyType<2,Ns,AbKeyType>), with the
+ * payload in one device arena per tensor.
+ *
+ * Every entry point returns an mpsg_status; on failure mpsg_last_error()
+ * holds a one-line message.  Nothing aborts the process.
+ */
+#ifndef MPSG_H_
+#define MPSG_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MPSG_OK = 0,
+  MPSG_ERR_ARG = 1,           /* invalid argument or inconsistent block structure */
+  MPSG_ERR_CUDA = 2,          /* CUDA runtime error */
+  MPSG_ERR_SOLVER = 3,        /* cuSOLVER / dense eigen- or SVD-solver failure */
+  MPSG_ERR_NOMEM = 4,         /* device allocation failed */
+  MPSG_ERR_TIMEOUT = 5,       /* a bounded device-side wait ran out */
+  MPSG_ERR_NOT_CONVERGED = 6  /* reported by solvers that do not treat this as success */
+} mpsg_status;
+
+/* Arithmetic of the matvec / environment contractions.  The Lanczos recurrence,
+ * reorthogonalisation, SVD, truncation bookkeeping and energy measurement are
+ * always FP64. */
+typedef enum {
+  MPSG_PREC_FP64 = 0,    /* FP64 FMA on CUDA cores (drop-in path) */
+  MPSG_PREC_TF32 = 1,    /* tcgen05 kind::tf32, FP32 accumulate */
+  MPSG_PREC_TF32X3 = 2,  /* tcgen05 kind::tf32 with hi/lo split (3 products), FP32 accumulate */
+  MPSG_PREC_BF16 = 3,    /* tcgen05 kind::f16 (bf16), FP32 accumulate */
+  MPSG_PREC_BF16X3 = 4,  /* tcgen05 kind::f16 (bf16) hi/lo split (3 products), FP32 accumulate */
+  MPSG_PREC_AUTO = 5     /* Lanczos only: cheapest precision first, hi/lo split when the
+                            Ritz residual stalls, FP64 for the final Rayleigh quotient */
+} mpsg_prec;
+
+typedef struct mpsg_ctx_s* mpsg_ctx;
+typedef struct mpsg_tensor_s* mpsg_tensor;
+typedef struct mpsg_dmrg_s* mpsg_dmrg;
+
+/* One MPO matrix MPOMat<1,T> (src/MPOTypes.hpp:839-889): term i is the element
+ * (out[i], in[i]) = value[i] of the sparse operator W[wl[i], wr[i]]. */
+typedef struct {
+  int32_t nterms;
+  const uint32_t* wl;
+  const uint32_t* wr;
+  const uint32_t* out;
+  const uint32_t* in;
+  const double* value;
+  int32_t Dl, Dr;
+} mpsg_mpo;
+
+/* i_to_key<AbKeyType> (src/tensormap.hpp:280-298): local state -> charge word. */
+typedef struct {
+  int32_t d;
+  const uint64_t* charge;
+} mpsg_itokey;
+
+/* ------------------------------------------------------------------ context */
+mpsg_status mpsg_ctx_create(int32_t device, mpsg_ctx* out);
+void mpsg_ctx_destroy(mpsg_ctx ctx);
+const char* mpsg_last_error(void);
+/* stream: a cudaStream_t (NULL = the library's own non-blocking stream). */
+mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
+mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
+/* Number of kernels this library launched on ctx since creation. */
+int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
+
+/* ------------------------------------------------------------------ tensors
+ * nphys: 0 = lambda (DiagBlockMatrix: keys (q,q), blocks are n x 1 vectors),
+ *        1 = single-site MPS tensor or environment (q0,q1; p0),
+ *        2 = two-site theta (q0,q1; p0,p1).
+ * q holds 2*nblocks charge words, p holds nphys*nblocks indices.  host_data
+ * holds the blocks in the given order, column-major, concatenated (NULL: zeros).
+ * Blocks are stored sorted by key; duplicate keys are an error. */
+mpsg_status mpsg_tensor_create(mpsg_ctx ctx, int32_t nphys, int32_t nblocks, const uint64_t* q,
+                               const uint32_t* p, const int32_t* rows, const int32_t* cols,
+                               const double* host_data, mpsg_tensor* out);
+mpsg_status mpsg_tensor_shape(mpsg_tensor t, int32_t* nphys, int32_t* nblocks, int64_t* nelem);
+/* Copies structure (sorted key order) and, if host_data != NULL, the payload. */
+mpsg_status mpsg_tensor_export(mpsg_tensor t, uint64_t* q, uint32_t* p, int32_t* rows, int32_t* cols,
+                               double* host_data);
+/* Zero-copy view: device base pointer and the element offset of every block. */
+mpsg_status mpsg_tensor_device_view(mpsg_tensor t, double** dptr, int64_t* offsets);
+void mpsg_tensor_destroy(mpsg_tensor t);
+
+/* ------------------------------------------------------------------ hot-path drop-ins */
+
+/* contractTwosite(Aout, BL, BR, A, mpol, mpor, itokey)  -- src/MPSfunctions.hpp:949-981.
+ * out receives a new tensor holding exactly the blocks the reference creates. */
+mpsg_status mpsg_contract_twosite(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta,
+                                  const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
+                                  const mpsg_itokey* ikr, mpsg_prec prec, mpsg_tensor* out);
+
+/* addContractionLayer(BL, A, mpo, itokey, direction)  -- src/MPSfunctions.hpp:442-493. */
+mpsg_status mpsg_add_contraction_layer(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor A, const mpsg_mpo* W,
+                                       const mpsg_itokey* ik, int32_t direction, mpsg_prec prec,
+                                       mpsg_tensor* out);
+
+/* BlockMatrix<2>(A1, A2): theta formation  -- src/BlockTensor.hpp:285-301. */
+mpsg_status mpsg_theta(mpsg_ctx ctx, mpsg_tensor A1, mpsg_tensor A2, mpsg_tensor* out);
+
+/* split(A, mps, lambda, itokey, 0, chimax, doTrunc, tr_weight, normalize)
+ * -- src/MPSfunctions.hpp:1142-1278 (two-site, direction 0): U (left, A-form),
+ * lambda (normalised when normalize != 0), Vt (right, B-form). */
+mpsg_status mpsg_split2(mpsg_ctx ctx, mpsg_tensor theta, const mpsg_itokey* ikl, const mpsg_itokey* ikr,
+                        uint32_t chimax, int32_t doTrunc, double tr_weight, int32_t normalize,
+                        mpsg_tensor* U, mpsg_tensor* Vt, mpsg_tensor* lambda, double* tw, uint32_t* chi);
+
+/* TSLanzcosEngine(L,R,mpsl,mpsr,mpol,mpor,itokeyl,itokeyr).simulate(itmax,delta,testenergy)
+ * followed by getState(0)  -- src/lanzcos.hpp:100-114,165-278,81-92.
+ * reorth != 0 adds full FP64 reorthogonalisation (the reference has none). */
+mpsg_status mpsg_lanczos2(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor mpsl, mpsg_tensor mpsr,
+                          const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
+                          const mpsg_itokey* ikr, int32_t itmax, double delta, int32_t testenergy,
+                          mpsg_prec prec, int32_t reorth, mpsg_tensor* state, double* E0,
+                          int32_t* iterations);
+
+/* ------------------------------------------------------------------ DMRG engine
+ * DMRGengine<AbKeyType,Real>(mps, mpo)  -- src/container.hpp:236-438.  The engine
+ * copies the site tensors; MPO and itokey arrays are copied too. */
+mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* mpos,
+                             const mpsg_itokey* itokeys, mpsg_dmrg* out);
+/* prec: matvec/environment arithmetic; reorth: full reorthogonalisation in Lanczos;
+ * lanmax: Lanczos iteration cap (reference: 500). */
+mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax);
+/* DMRGengine::simulate(maxsteps, EnConv, chimax, doTrunc, tr_weight, delta, testenergy):
+ * orthonormalize("rl"), computeR, sweeps, final doStep(0,-1).  E = last Lanczos energy. */
+mpsg_status mpsg_dmrg_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, uint32_t chimax,
+                               int32_t doTrunc, double tr_weight, double delta, int32_t testenergy,
+                               double* E);
+/* The pieces of simulate, for callers that schedule sweeps themselves. */
+mpsg_status mpsg_dmrg_prepare(mpsg_dmrg e);
+mpsg_status mpsg_dmrg_do_step(mpsg_dmrg e, int32_t site, int32_t dir, uint32_t chimax, int32_t doTrunc,
+                              double tr_weight, double delta, int32_t testenergy, double* E);
+/* Step records appended by every doStep. */
+int32_t mpsg_dmrg_nsteps(mpsg_dmrg e);
+mpsg_status mpsg_dmrg_steps(mpsg_dmrg e, int32_t* site, int32_t* dir, int32_t* iters, int32_t* chi,
+                            double* E, double* tw);
+/* Accumulated counters: [0] matvecs, [1] matvec FLOPs (algorithmic), [2] matvec seconds
+ * (device events), [3] env-update seconds, [4] split seconds, [5] lanczos seconds (total),
+ * [6] theta FLOPs in env updates, [7] wall seconds of simulate. */
+mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* stats8);
+mpsg_status mpsg_dmrg_site(mpsg_dmrg e, int32_t site, mpsg_tensor* out);
+mpsg_status mpsg_dmrg_lambda(mpsg_dmrg e, int32_t bond, mpsg_tensor* out);
+/* MPO::measure(mps) in FP64 on the GPU  -- src/MPOTypes.hpp:990-1020. */
+mpsg_status mpsg_dmrg_measure_energy(mpsg_dmrg e, double* E);
+void mpsg_dmrg_destroy(mpsg_dmrg e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPSG_H_ */

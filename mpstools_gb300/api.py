@@ -1,0 +1,187 @@
+"""Reference-shaped Python API over libmpsg.
+
+Names and argument meaning follow MPSTools:
+  contractTwosite      src/MPSfunctions.hpp:949-981
+  addContractionLayer  src/MPSfunctions.hpp:442-493
+  split                src/MPSfunctions.hpp:1142-1278
+  TSLanzcosEngine      src/lanzcos.hpp:96-278
+  DMRGengine           src/container.hpp:236-438
+Block matrices are dicts keyed like TensorKeyType ((q0, q1, p0) or (q0, q1, p0, p1));
+lambdas are dicts {q: 1-D array}; MPO matrices are (terms, Dl, Dr) with
+terms (wl, wr, out, in, value).  All arithmetic runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import lib
+from .lib import Context, ItoKeyArg, MPOArg, Tensor, check
+
+_CTX = None
+
+
+def default_context() -> Context:
+    global _CTX
+    if _CTX is None:
+        _CTX = Context(0)
+    return _CTX
+
+
+def _prec(p):
+    return lib.PREC[p] if isinstance(p, str) else int(p)
+
+
+def contractTwosite(BL, BR, A, mpol, mpor, itokey, prec="fp64", ctx=None):
+    ctx = ctx or default_context()
+    tL, tR, tA = Tensor.from_dict(ctx, BL, 1), Tensor.from_dict(ctx, BR, 1), Tensor.from_dict(ctx, A, 2)
+    w1, w2 = MPOArg(mpol), MPOArg(mpor)
+    k0, k1 = ItoKeyArg(itokey[0]), ItoKeyArg(itokey[1])
+    h = C.c_void_p()
+    check(ctx.L.mpsg_contract_twosite(ctx.h, tL.h, tR.h, tA.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(),
+                                      _prec(prec), C.byref(h)))
+    return Tensor(ctx, h).to_dict()
+
+
+def addContractionLayer(BL, A, mpo, itokey, direction, prec="fp64", ctx=None):
+    ctx = ctx or default_context()
+    tB, tA = Tensor.from_dict(ctx, BL, 1), Tensor.from_dict(ctx, A, 1)
+    w = MPOArg(mpo)
+    k = ItoKeyArg(itokey)
+    h = C.c_void_p()
+    check(ctx.L.mpsg_add_contraction_layer(ctx.h, tB.h, tA.h, w.ref(), k.ref(), int(direction), _prec(prec),
+                                           C.byref(h)))
+    return Tensor(ctx, h).to_dict()
+
+
+def theta(A1, A2, ctx=None):
+    ctx = ctx or default_context()
+    t1, t2 = Tensor.from_dict(ctx, A1, 1), Tensor.from_dict(ctx, A2, 1)
+    h = C.c_void_p()
+    check(ctx.L.mpsg_theta(ctx.h, t1.h, t2.h, C.byref(h)))
+    return Tensor(ctx, h).to_dict()
+
+
+def split(A, itokey, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, ctx=None):
+    """Returns (U, Vt, lambda, truncated_weight, chi) -- direction 0 of the reference."""
+    ctx = ctx or default_context()
+    tA = Tensor.from_dict(ctx, A, 2)
+    k0, k1 = ItoKeyArg(itokey[0]), ItoKeyArg(itokey[1])
+    U, V, lam = C.c_void_p(), C.c_void_p(), C.c_void_p()
+    tw, chi = C.c_double(), C.c_uint32()
+    check(ctx.L.mpsg_split2(ctx.h, tA.h, k0.ref(), k1.ref(), int(chimax), int(doTrunc), float(tr_weight),
+                            int(normalize), C.byref(U), C.byref(V), C.byref(lam), C.byref(tw), C.byref(chi)))
+    return (Tensor(ctx, U).to_dict(), Tensor(ctx, V).to_dict(), Tensor(ctx, lam).to_dict(), tw.value, chi.value)
+
+
+class TSLanzcosEngine:
+    """Two-site Lanczos: simulate(itmax, delta, testenergy) then getState(0)."""
+
+    def __init__(self, L, R, mpsl, mpsr, mpol, mpor, itokeyl, itokeyr, prec="fp64", reorth=False, ctx=None):
+        self.ctx = ctx or default_context()
+        self.args = (L, R, mpsl, mpsr, mpol, mpor, itokeyl, itokeyr)
+        self.prec, self.reorth = prec, reorth
+        self._E0 = None
+        self._state = None
+        self.iterations = 0
+
+    def simulate(self, itmax=500, delta=1e-12, testenergy=True):
+        L, R, mpsl, mpsr, mpol, mpor, ikl, ikr = self.args
+        ctx = self.ctx
+        tL, tR = Tensor.from_dict(ctx, L, 1), Tensor.from_dict(ctx, R, 1)
+        tl, tr = Tensor.from_dict(ctx, mpsl, 1), Tensor.from_dict(ctx, mpsr, 1)
+        w1, w2 = MPOArg(mpol), MPOArg(mpor)
+        k0, k1 = ItoKeyArg(ikl), ItoKeyArg(ikr)
+        st, E0, it = C.c_void_p(), C.c_double(), C.c_int32()
+        check(ctx.L.mpsg_lanczos2(ctx.h, tL.h, tR.h, tl.h, tr.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), int(itmax),
+                                  float(delta), int(testenergy), _prec(self.prec), int(self.reorth), C.byref(st),
+                                  C.byref(E0), C.byref(it)))
+        self._state = Tensor(ctx, st)
+        self._E0 = E0.value
+        self.iterations = it.value
+        return it.value
+
+    def E(self, i=0):
+        assert i == 0, "only the ground state is kept"
+        return self._E0
+
+    def getState(self, j=0):
+        assert j == 0, "only the ground state is kept"
+        return self._state.to_dict()
+
+
+class DMRGengine:
+    """DMRGengine<AbKeyType,Real>(mps, mpo): site tensors and MPO stay on the GPU."""
+
+    def __init__(self, sites, mpo, itokeys, prec="fp64", reorth=False, lanmax=500, ctx=None):
+        self.ctx = ctx or default_context()
+        ctx = self.ctx
+        self.N = len(sites)
+        self._tensors = [Tensor.from_dict(ctx, s, 1) for s in sites]
+        self._mpos = [MPOArg(w) for w in mpo]
+        self._iks = [ItoKeyArg(k) for k in itokeys]
+        harr = (C.c_void_p * self.N)(*[t.h.value for t in self._tensors])
+        marr = (lib._MPOStruct * self.N)(*[m.s for m in self._mpos])
+        karr = (lib._ItoKeyStruct * self.N)(*[k.s for k in self._iks])
+        h = C.c_void_p()
+        check(ctx.L.mpsg_dmrg_create(ctx.h, self.N, harr, marr, karr, C.byref(h)))
+        self.h = h
+        check(ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
+
+    def simulate(self, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12, delta=1e-13,
+                 testenergy=True):
+        E = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_simulate(self.h, int(maxsteps), float(EnConv), int(chimax), int(doTrunc),
+                                            float(tr_weight), float(delta), int(testenergy), C.byref(E)))
+        return E.value
+
+    def prepare(self):
+        check(self.ctx.L.mpsg_dmrg_prepare(self.h))
+
+    def do_step(self, site, direction, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
+        E = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_do_step(self.h, int(site), int(direction), int(chimax), int(doTrunc),
+                                           float(tr_weight), float(delta), int(testenergy), C.byref(E)))
+        return E.value
+
+    def steps(self):
+        n = self.ctx.L.mpsg_dmrg_nsteps(self.h)
+        a = [np.zeros(max(n, 1), np.int32) for _ in range(4)]
+        E, tw = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        check(self.ctx.L.mpsg_dmrg_steps(self.h, *[lib.ptr(x) for x in a], lib.ptr(E), lib.ptr(tw)))
+        return [dict(site=int(a[0][i]), dir=int(a[1][i]), iters=int(a[2][i]), chi=int(a[3][i]), E=float(E[i]),
+                     tw=float(tw[i])) for i in range(n)]
+
+    def stats(self):
+        s = np.zeros(8)
+        check(self.ctx.L.mpsg_dmrg_stats(self.h, lib.ptr(s)))
+        keys = ["matvecs", "matvec_flops", "matvec_seconds", "env_seconds", "split_seconds", "lanczos_seconds",
+                "env_flops", "wall_seconds"]
+        return dict(zip(keys, s.tolist()))
+
+    def site(self, s):
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_dmrg_site(self.h, int(s), C.byref(h)))
+        return Tensor(self.ctx, h).to_dict()
+
+    def lam(self, bond):
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_dmrg_lambda(self.h, int(bond), C.byref(h)))
+        return Tensor(self.ctx, h).to_dict()
+
+    def measure_energy(self):
+        E = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_measure_energy(self.h, C.byref(E)))
+        return E.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.mpsg_dmrg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

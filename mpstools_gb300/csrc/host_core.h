@@ -1,0 +1,92 @@
+// Host-side core types of libmpsg (context, MPO terms, GEMM / lincomb plans).
+#pragma once
+#include <cusolverDn.h>
+
+#include "../../include/mpsg.h"
+#include "mpsg_internal.h"
+
+namespace mpsg {
+
+extern thread_local std::string g_last_error;
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own = nullptr;
+  cusolverDnHandle_t solver = nullptr;
+  gesvdjInfo_t svdp = nullptr;
+  double* part = nullptr;     // reduction partials (kRedBlocks) + 64 scalars
+  double* hscal = nullptr;    // pinned host scalars
+  explicit Ctx(int dev);
+  ~Ctx();
+  void* dmalloc(size_t bytes);
+  void dfree(void* p);
+  cusolverDnHandle_t svd_handle();
+  void sync();
+};
+
+// ---------------------------------------------------------------- tensors
+TensorP make_tensor(Ctx* ctx, int nphys, const Layout& lay, bool zero);
+Layout layout_of(const Tensor& t);
+TensorP tensor_from_host(Ctx* ctx, int nphys, int n, const uint64_t* q, const uint32_t* p, const int32_t* rows,
+                         const int32_t* cols, const double* data);
+void tensor_to_host(const Tensor& t, std::vector<double>& packed);  // blocks in key order, concatenated
+TensorP tensor_copy(const Tensor& t);
+
+// ---------------------------------------------------------------- MPO (MPOMat<1,T>)
+struct OpEl {  // element (out, in) of a SparseOperator<1,T>
+  uint32_t out, in;
+  double v;
+};
+struct MPOEntry {  // W[wl, wr], elements in (in, out) order
+  uint32_t wl, wr;
+  std::vector<OpEl> ops;
+};
+struct MPO {
+  std::vector<MPOEntry> e;  // (wl, wr) ascending
+  int Dl = 0, Dr = 0;
+};
+typedef std::vector<Q> ItoKey;
+MPO mpo_from_c(const mpsg_mpo* w);
+ItoKey itokey_from_c(const mpsg_itokey* ik);
+
+// ---------------------------------------------------------------- grouped GEMM plan
+// Operands are (base slot, element offset) pairs so a plan can be re-bound to new buffers.
+struct GSegH {
+  int baseA, baseB;
+  int64_t offA, offB;
+  int lda, ldb, K, tA, tB;
+  double alpha;
+};
+struct GProbH {
+  int baseC;
+  int64_t offC;
+  int ldc, M, N, seg0, seg1, beta;
+};
+struct GemmPlan {
+  Ctx* ctx = nullptr;
+  std::vector<GProbH> hprob;
+  std::vector<GSegH> hseg;
+  GProb* dprob = nullptr;
+  GSeg* dseg = nullptr;
+  GTile* dtile = nullptr;
+  int ntiles = 0;
+  double flops = 0;
+  void add_problem(int baseC, int64_t offC, int ldc, int M, int N, bool accumulate, const std::vector<GSegH>& segs);
+  void upload(Ctx* ctx);
+  void run(const double* const* bases);
+  GemmPlan() {}
+  GemmPlan(const GemmPlan&) = delete;
+  ~GemmPlan();
+};
+
+struct LincombPlan {
+  std::vector<LCOut> hout;
+  std::vector<LCTerm> hterm;
+  int64_t maxn = 0;
+  void add(double* dst, int64_t n, const std::vector<std::pair<const double*, double>>& terms);
+  void run(Ctx* ctx);
+};
+void run_copyops(Ctx* ctx, const std::vector<CopyOp>& ops);
+
+}  // namespace mpsg

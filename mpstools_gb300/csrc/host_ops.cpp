@@ -1,0 +1,892 @@
+// Host orchestration of the DMRG hot path: matvec / environment / theta plans, split with
+// global truncation, right canonicalisation and the GPU Lanczos driver.
+#include "host_ops.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <set>
+#include <tuple>
+
+namespace mpsg {
+
+static inline Q qat(const ItoKey& ik, uint32_t s) {
+  MPSG_CHECK(s < ik.size(), "physical index outside itokey");
+  return ik[s];
+}
+
+// ============================================================================ matvec
+// Visits every term of the reference's doContraction loop (src/MPSfunctions.hpp:726-804):
+// (L block i, W1 entry e1, W2 entry e2, op elements o1, o2, theta block, R block).
+template <class F>
+static void visit_matvec_terms(const Tensor& L, const Tensor& R, const Layout& th, const MPO& W1, const MPO& W2,
+                               const ItoKey& ik0, const ItoKey& ik1, F&& f) {
+  std::map<uint32_t, std::vector<int>> w2_by_wl;
+  for (int e2 = 0; e2 < (int)W2.e.size(); ++e2) w2_by_wl[W2.e[e2].wl].push_back(e2);
+  for (int i = 0; i < (int)L.b.size(); ++i) {
+    const Block& lb = L.b[i];
+    const Q a1 = lb.k.q0, a = lb.k.q1;
+    for (int e1 = 0; e1 < (int)W1.e.size(); ++e1) {
+      if (W1.e[e1].wl != lb.k.p0) continue;
+      const uint32_t wm = W1.e[e1].wr;
+      auto it2 = w2_by_wl.find(wm);
+      if (it2 == w2_by_wl.end()) continue;
+      for (int e2 : it2->second) {
+        const uint32_t wr = W2.e[e2].wr;
+        for (int o1 = 0; o1 < (int)W1.e[e1].ops.size(); ++o1) {
+          const OpEl& op1 = W1.e[e1].ops[o1];
+          for (int o2 = 0; o2 < (int)W2.e[e2].ops.size(); ++o2) {
+            const OpEl& op2 = W2.e[e2].ops[o2];
+            const Q b = a + qat(ik0, op1.out) + qat(ik1, op2.out);
+            auto ti = th.idx.find(K2(a, b, op1.out, op2.out));
+            if (ti == th.idx.end()) continue;
+            const Q b1 = a1 + qat(ik0, op1.in) + qat(ik1, op2.in);
+            const int rj = R.find(K1(b1, b, wr));
+            if (rj < 0) continue;
+            f(i, e1, o1, e2, o2, ti->second, rj, a1, a, b, b1, wm, op1, op2);
+          }
+        }
+      }
+    }
+  }
+}
+
+Layout theta_closure(const Tensor& L, const Tensor& R, const Layout& th0, const MPO& W1, const MPO& W2,
+                     const ItoKey& ik0, const ItoKey& ik1) {
+  Layout cur = th0;
+  cur.finalize();
+  for (int iter = 0; iter < 64; ++iter) {
+    std::map<BKey, std::pair<int, int>> add;
+    visit_matvec_terms(L, R, cur, W1, W2, ik0, ik1,
+                       [&](int i, int, int, int, int, int, int rj, Q a1, Q, Q, Q b1, uint32_t, const OpEl& op1,
+                           const OpEl& op2) {
+                         BKey k = K2(a1, b1, op1.in, op2.in);
+                         if (!cur.idx.count(k)) add[k] = {L.b[i].r, R.b[rj].r};
+                       });
+    if (add.empty()) return cur;
+    for (auto& x : add) cur.add(x.first, x.second.first, x.second.second);
+    cur.finalize();
+  }
+  throw Err(1, "theta block closure did not terminate");
+}
+
+MatvecPlan::~MatvecPlan() {
+  if (ctx) {
+    ctx->dfree(dLt);
+    ctx->dfree(dRt);
+    ctx->dfree(dX);
+  }
+}
+
+void MatvecPlan::run(const double* theta_in, double* theta_out) {
+  const double* bases[8] = {dLt, theta_in, dX, dRt, theta_out, nullptr, nullptr, nullptr};
+  stageA.run(bases);
+  stageC.run(bases);
+}
+
+std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th, const MPO& W1,
+                                         const MPO& W2, const ItoKey& ik0, const ItoKey& ik1,
+                                         const Layout* out_layout) {
+  std::unique_ptr<MatvecPlan> P(new MatvecPlan());
+  P->ctx = ctx;
+  std::map<K5, std::map<std::tuple<int, int, int>, double>> ltc, rtc;
+  std::map<K5, std::map<uint32_t, std::pair<K5, int>>> xterms;
+  std::map<BKey, std::set<std::pair<K5, K5>>> oterms;
+  std::map<BKey, std::pair<int, int>> odims;
+  std::set<std::tuple<int, int, int, int, int, int>> ypairs;  // survey F_B: distinct (L blk, theta blk, W pair)
+  std::set<std::tuple<Q, Q, uint32_t, uint32_t, uint32_t>> yset;
+  visit_matvec_terms(L, R, th, W1, W2, ik0, ik1,
+                     [&](int i, int e1, int o1, int e2, int o2, int ti, int rj, Q a1, Q a, Q b, Q b1, uint32_t wm,
+                         const OpEl& op1, const OpEl& op2) {
+                       K5 lk{a1, a, wm, op1.in, op1.out};
+                       ltc[lk][std::make_tuple(i, e1, o1)] = op1.v;
+                       K5 rk{b1, b, wm, op2.in, op2.out};
+                       rtc[rk][std::make_tuple(rj, e2, o2)] = op2.v;
+                       K5 xk{a1, b, wm, op1.in, op2.out};
+                       xterms[xk][op1.out] = std::make_pair(lk, ti);
+                       BKey ok = K2(a1, b1, op1.in, op2.in);
+                       oterms[ok].insert(std::make_pair(xk, rk));
+                       odims[ok] = {L.b[i].r, R.b[rj].r};
+                       const double ra1 = L.b[i].r, ca = L.b[i].c, cb = th.b[ti].c, rb1 = R.b[rj].r;
+                       P->flops_ref += 2.0 * ra1 * ca * cb + 2.0 * ra1 * cb * rb1;
+                       P->flops_survey += 2.0 * ra1 * cb;  // F_B term (W element pair on one X block)
+                       yset.insert(std::make_tuple(a1, b, W2.e[e2].wr, op1.in, op2.in));
+                     });
+  // survey F_A: every (L block, theta block with left charge a) pair; F_C: every Y block with its R block
+  {
+    std::map<Q, std::vector<int>> thby;
+    for (int t = 0; t < (int)th.b.size(); ++t) thby[th.b[t].k.q0].push_back(t);
+    for (auto& lb : L.b) {
+      auto it = thby.find(lb.k.q1);
+      if (it == thby.end()) continue;
+      for (int t : it->second) P->flops_survey += 2.0 * lb.r * lb.c * th.b[t].c;
+    }
+    for (auto& y : yset) {
+      Q a1, b;
+      uint32_t wr, s1p, s2p;
+      std::tie(a1, b, wr, s1p, s2p) = y;
+      const Q b1 = a1 + qat(ik0, s1p) + qat(ik1, s2p);
+      const int rj = R.find(K1(b1, b, wr));
+      int ra1 = 0;
+      for (auto& lb : L.b)
+        if (lb.k.q0 == a1) { ra1 = lb.r; break; }
+      if (rj >= 0) P->flops_survey += 2.0 * ra1 * R.b[rj].c * R.b[rj].r;
+    }
+  }
+  // arenas
+  for (auto& x : ltc) {
+    const Block& lb = L.b[std::get<0>(x.second.begin()->first)];
+    P->lt.add(x.first, lb.r, lb.c);
+  }
+  for (auto& x : rtc) {
+    const Block& rb = R.b[std::get<0>(x.second.begin()->first)];
+    P->rt.add(x.first, rb.r, rb.c);
+  }
+  for (auto& x : xterms) {
+    const auto& first = x.second.begin()->second;
+    const int ra1 = P->lt.at(first.first).r;
+    const int cb = th.b[first.second].c;
+    P->xa.add(x.first, ra1, cb);
+  }
+  if (out_layout) {
+    P->out = *out_layout;
+    for (auto& o : oterms) MPSG_CHECK(P->out.idx.count(o.first), "matvec output block missing from output layout");
+  } else {
+    for (auto& o : odims) P->out.add(o.first, o.second.first, o.second.second);
+    P->out.finalize();
+  }
+  P->dLt = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->lt.nelem, 2));
+  P->dRt = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->rt.nelem, 2));
+  P->dX = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->xa.nelem, 2));
+  // combined environments
+  for (auto& x : ltc) {
+    std::vector<std::pair<const double*, double>> terms;
+    for (auto& c : x.second) terms.push_back({L.ptr(std::get<0>(c.first)), c.second});
+    const auto& B = P->lt.at(x.first);
+    P->build_lt.add(P->dLt + B.off, (int64_t)B.r * B.c, terms);
+  }
+  for (auto& x : rtc) {
+    std::vector<std::pair<const double*, double>> terms;
+    for (auto& c : x.second) terms.push_back({R.ptr(std::get<0>(c.first)), c.second});
+    const auto& B = P->rt.at(x.first);
+    P->build_rt.add(P->dRt + B.off, (int64_t)B.r * B.c, terms);
+  }
+  P->build_lt.run(ctx);
+  P->build_rt.run(ctx);
+  // stage A: X = sum_s1 L~ theta
+  for (auto& x : xterms) {
+    const auto& XB = P->xa.at(x.first);
+    std::vector<GSegH> segs;
+    for (auto& s : x.second) {
+      const auto& LB = P->lt.at(s.second.first);
+      const Block& TB = th.b[s.second.second];
+      MPSG_CHECK(LB.c == TB.r && LB.r == XB.r && TB.c == XB.c, "inconsistent block sizes in matvec (stage A)");
+      segs.push_back(GSegH{0, 1, LB.off, TB.off, LB.r, TB.r, LB.c, 0, 0, 1.0});
+    }
+    P->stageA.add_problem(2, XB.off, XB.r, XB.r, XB.c, false, segs);
+  }
+  // stage C: out = sum X R~^T
+  for (auto& o : oterms) {
+    const Block& OB = P->out.b[P->out.idx.at(o.first)];
+    std::vector<GSegH> segs;
+    for (auto& pr : o.second) {
+      const auto& XB = P->xa.at(pr.first);
+      const auto& RB = P->rt.at(pr.second);
+      MPSG_CHECK(XB.c == RB.c && XB.r == OB.r && RB.r == OB.c, "inconsistent block sizes in matvec (stage C)");
+      segs.push_back(GSegH{2, 3, XB.off, RB.off, XB.r, RB.r, XB.c, 0, 1, 1.0});
+    }
+    P->stageC.add_problem(4, OB.off, OB.r, OB.r, OB.c, false, segs);
+  }
+  P->stageA.upload(ctx);
+  P->stageC.upload(ctx);
+  P->flops = P->stageA.flops + P->stageC.flops;
+  int64_t nl = 0, nr = 0, nt = 0;
+  for (auto& b : L.b) nl += (int64_t)b.r * b.c;
+  for (auto& b : R.b) nr += (int64_t)b.r * b.c;
+  for (auto& b : th.b) nt += (int64_t)b.r * b.c;
+  P->bytes_alg = 8 * (nl + nr + 2 * nt);
+  return P;
+}
+
+// ============================================================================ environment update
+EnvPlan::~EnvPlan() {
+  if (ctx) {
+    ctx->dfree(dCt);
+    ctx->dfree(dT);
+  }
+}
+void EnvPlan::run(const double* A, double* out_d) {
+  const double* bases[8] = {dCt, A, dT, out_d, nullptr, nullptr, nullptr, nullptr};
+  st1.run(bases);
+  st2.run(bases);
+}
+
+std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
+                                   int direction) {
+  std::unique_ptr<EnvPlan> P(new EnvPlan());
+  P->ctx = ctx;
+  const bool left = direction > 0;
+  std::map<std::pair<uint32_t, Q>, std::vector<int>> envby;  // (w, lower charge) -> env blocks
+  for (int i = 0; i < (int)BL.b.size(); ++i) envby[{BL.b[i].k.p0, BL.b[i].k.q1}].push_back(i);
+  std::map<K5, std::map<std::tuple<int, int, int>, double>> ctc;
+  std::map<K5, std::map<uint32_t, std::pair<K5, int>>> tterms;          // T key -> so -> (Ct key, A block)
+  std::map<BKey, std::map<std::pair<uint32_t, Q>, std::pair<int, K5>>> oterms;  // out -> (si, charge) -> (A blk, T key)
+  for (int j = 0; j < (int)A.b.size(); ++j) {
+    const Block& ad = A.b[j];
+    const Q a = ad.k.q0, b = ad.k.q1;
+    const uint32_t so = ad.k.p0;
+    for (int e = 0; e < (int)W.e.size(); ++e) {
+      const MPOEntry& en = W.e[e];
+      for (int o = 0; o < (int)en.ops.size(); ++o) {
+        const OpEl& op = en.ops[o];
+        if (op.out != so) continue;
+        const uint32_t si = op.in;
+        if (left) {
+          // add_out_sub_2, direction > 0: key_b = (p - q(out), p; out) with p = b
+          MPSG_CHECK(b == a + qat(ik, so), "MPS block violates charge conservation");
+          auto it = envby.find({en.wl, a});
+          if (it == envby.end()) continue;
+          for (int i : it->second) {
+            const Q a1 = BL.b[i].k.q0;
+            const Q b1 = a1 + qat(ik, si);
+            const int au = A.find(K1(a1, b1, si));
+            if (au < 0) continue;
+            K5 ck{a1, a, en.wr, si, so};
+            ctc[ck][std::make_tuple(i, e, o)] = op.v;
+            K5 tk{a1, b, en.wr, si, 0};
+            tterms[tk][so] = std::make_pair(ck, j);
+            oterms[K1(b1, b, en.wr)][{si, a1}] = std::make_pair(au, tk);
+          }
+        } else {
+          // direction <= 0: key_b = (p, p + q(out); out) with p = a
+          auto it = envby.find({en.wr, b});
+          if (it == envby.end()) continue;
+          for (int i : it->second) {
+            const Q b1 = BL.b[i].k.q0;
+            const Q a1 = b1 - qat(ik, si);
+            const int au = A.find(K1(a1, b1, si));
+            if (au < 0) continue;
+            K5 ck{b1, b, en.wl, si, so};
+            ctc[ck][std::make_tuple(i, e, o)] = op.v;
+            K5 tk{a, b1, en.wl, si, 0};
+            tterms[tk][so] = std::make_pair(ck, j);
+            oterms[K1(a1, a, en.wl)][{si, b1}] = std::make_pair(au, tk);
+          }
+        }
+      }
+    }
+  }
+  for (auto& x : ctc) {
+    const Block& eb = BL.b[std::get<0>(x.second.begin()->first)];
+    P->ct.add(x.first, eb.r, eb.c);
+  }
+  for (auto& x : tterms) {
+    const auto& f = x.second.begin()->second;
+    const Block& ab = A.b[f.second];
+    const auto& CB = P->ct.at(f.first);
+    if (left) P->tt.add(x.first, CB.r, ab.c);   // (chi_a' x chi_b)
+    else P->tt.add(x.first, ab.r, CB.r);        // (chi_a x chi_b')
+  }
+  for (auto& o : oterms) {
+    const auto& f = o.second.begin()->second;
+    const Block& au = A.b[f.first];
+    const auto& TB = P->tt.at(f.second);
+    if (left) P->out.add(o.first, au.c, TB.c);  // (chi_b' x chi_b)
+    else P->out.add(o.first, au.r, TB.r);       // (chi_a' x chi_a)
+  }
+  P->out.finalize();
+  P->dCt = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->ct.nelem, 2));
+  P->dT = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->tt.nelem, 2));
+  for (auto& x : ctc) {
+    std::vector<std::pair<const double*, double>> terms;
+    for (auto& c : x.second) terms.push_back({BL.ptr(std::get<0>(c.first)), c.second});
+    const auto& B = P->ct.at(x.first);
+    P->build_ct.add(P->dCt + B.off, (int64_t)B.r * B.c, terms);
+  }
+  P->build_ct.run(ctx);
+  // bases: 0 = Ct, 1 = A, 2 = T, 3 = out
+  for (auto& x : tterms) {
+    const auto& TB = P->tt.at(x.first);
+    std::vector<GSegH> segs;
+    for (auto& s : x.second) {
+      const auto& CB = P->ct.at(s.second.first);
+      const Block& ab = A.b[s.second.second];
+      if (left) {  // T(a',b) += Ct(a',a) A(a,b)
+        MPSG_CHECK(CB.c == ab.r && CB.r == TB.r && ab.c == TB.c, "inconsistent block sizes (env, stage 1)");
+        segs.push_back(GSegH{0, 1, CB.off, ab.off, CB.r, ab.r, CB.c, 0, 0, 1.0});
+      } else {     // T(a,b') += A(a,b) Ct(b',b)^T
+        MPSG_CHECK(ab.c == CB.c && ab.r == TB.r && CB.r == TB.c, "inconsistent block sizes (env, stage 1)");
+        segs.push_back(GSegH{1, 0, ab.off, CB.off, ab.r, CB.r, ab.c, 0, 1, 1.0});
+      }
+    }
+    P->st1.add_problem(2, TB.off, TB.r, TB.r, TB.c, false, segs);
+  }
+  for (auto& o : oterms) {
+    const Block& OB = P->out.b[P->out.idx.at(o.first)];
+    std::vector<GSegH> segs;
+    for (auto& s : o.second) {
+      const Block& au = A.b[s.second.first];
+      const auto& TB = P->tt.at(s.second.second);
+      if (left) {  // out(b',b) += A(a',b')^T T(a',b)
+        MPSG_CHECK(au.r == TB.r && au.c == OB.r && TB.c == OB.c, "inconsistent block sizes (env, stage 2)");
+        segs.push_back(GSegH{1, 2, au.off, TB.off, au.r, TB.r, au.r, 1, 0, 1.0});
+      } else {     // out(a',a) += A(a',b') T(a,b')^T
+        MPSG_CHECK(au.c == TB.c && au.r == OB.r && TB.r == OB.c, "inconsistent block sizes (env, stage 2)");
+        segs.push_back(GSegH{1, 2, au.off, TB.off, au.r, TB.r, au.c, 0, 1, 1.0});
+      }
+    }
+    P->st2.add_problem(3, OB.off, OB.r, OB.r, OB.c, false, segs);
+  }
+  P->st1.upload(ctx);
+  P->st2.upload(ctx);
+  P->flops = P->st1.flops + P->st2.flops;
+  return P;
+}
+
+TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
+                   double* flops_out) {
+  auto P = build_env(ctx, BL, A, W, ik, direction);
+  TensorP out = make_tensor(ctx, 1, P->out, true);
+  P->run(A.d, out->d);
+  if (flops_out) *flops_out += P->flops;
+  return out;
+}
+
+// ============================================================================ theta formation
+TensorP theta_form(Ctx* ctx, const Tensor& A1, const Tensor& A2, const Layout* layout) {
+  std::map<Q, std::vector<int>> by_left;
+  for (int j = 0; j < (int)A2.b.size(); ++j) by_left[A2.b[j].k.q0].push_back(j);
+  std::vector<std::tuple<BKey, int, int>> prods;
+  Layout lay;
+  for (int i = 0; i < (int)A1.b.size(); ++i) {
+    auto it = by_left.find(A1.b[i].k.q1);
+    if (it == by_left.end()) continue;
+    for (int j : it->second) {
+      BKey k = K2(A1.b[i].k.q0, A2.b[j].k.q1, A1.b[i].k.p0, A2.b[j].k.p0);
+      prods.emplace_back(k, i, j);
+      if (!layout) lay.add(k, A1.b[i].r, A2.b[j].c);
+    }
+  }
+  if (layout) lay = *layout;
+  else lay.finalize();
+  TensorP th = make_tensor(ctx, 2, lay, true);
+  GemmPlan g;
+  for (auto& p : prods) {
+    const int o = th->find(std::get<0>(p));
+    MPSG_CHECK(o >= 0, "theta block missing from layout");
+    const Block& a = A1.b[std::get<1>(p)];
+    const Block& b = A2.b[std::get<2>(p)];
+    MPSG_CHECK(a.c == b.r, "bond dimension mismatch between A1 and A2");
+    g.add_problem(2, th->b[o].off, a.r, a.r, b.c, false, {GSegH{0, 1, a.off, b.off, a.r, b.r, a.c, 0, 0, 1.0}});
+  }
+  g.upload(ctx);
+  const double* bases[8] = {A1.d, A2.d, th->d, nullptr, nullptr, nullptr, nullptr, nullptr};
+  g.run(bases);
+  ctx->sync();
+  return th;
+}
+
+// ============================================================================ batched SVD (cuSOLVER gesvdj)
+// Sector matrices (m x n) are stored as ms x ns with ms >= ns (transposed when m < n).  After the
+// SVD, Q (m x k) carries the left vectors and P (n x k) the right vectors (columns of P = rows of Vt);
+// FixPhase is applied so that the first abs-max entry of every Vt row is positive.
+struct SvdBatch {
+  struct Sec {
+    int m, n, ms, ns, k;
+    bool trans;
+    int64_t offM, offU, offV, offS;
+  };
+  std::vector<Sec> s;
+  Ctx* ctx = nullptr;
+  double *dM = nullptr, *dU = nullptr, *dV = nullptr, *dS = nullptr;
+  int* dinfo = nullptr;
+  int64_t nS = 0;
+  explicit SvdBatch(Ctx* c) : ctx(c) {}
+  ~SvdBatch() {
+    ctx->dfree(dM);
+    ctx->dfree(dU);
+    ctx->dfree(dV);
+    ctx->dfree(dS);
+    ctx->dfree(dinfo);
+  }
+  void plan(const std::vector<std::pair<int, int>>& mn) {
+    int64_t oM = 0, oU = 0, oV = 0, oS = 0;
+    auto al = [](int64_t x) { return (x + kAlign - 1) / kAlign * kAlign; };
+    for (auto& d : mn) {
+      Sec x;
+      x.m = d.first;
+      x.n = d.second;
+      x.trans = x.m < x.n;
+      x.ms = std::max(x.m, x.n);
+      x.ns = std::min(x.m, x.n);
+      x.k = x.ns;
+      x.offM = oM; oM += al((int64_t)x.ms * x.ns);
+      x.offU = oU; oU += al((int64_t)x.ms * x.k);
+      x.offV = oV; oV += al((int64_t)x.ns * x.k);
+      x.offS = oS; oS += x.k;
+      s.push_back(x);
+    }
+    nS = oS;
+    dM = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oM, 2));
+    dU = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oU, 2));
+    dV = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oV, 2));
+    dS = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oS, 2));
+    dinfo = (int*)ctx->dmalloc(sizeof(int) * std::max<size_t>(s.size(), 1));
+    MPSG_CUDA(cudaMemsetAsync(dM, 0, sizeof(double) * std::max<int64_t>(oM, 2), ctx->stream));
+  }
+  // destination of logical element (r, c) of sector i's m x n matrix
+  CopyOp gather_op(int i, const double* src, int rows, int cols, int r0, int c0) const {
+    const Sec& x = s[i];
+    CopyOp o;
+    o.src = src;
+    o.rs = nullptr;
+    o.cs = nullptr;
+    o.scale = 1.0;
+    o.lds = rows;
+    o.ldd = x.ms;
+    if (!x.trans) {
+      o.dst = dM + x.offM + r0 + (int64_t)c0 * x.ms;
+      o.rows = rows;
+      o.cols = cols;
+      o.trans = 0;
+    } else {
+      o.dst = dM + x.offM + c0 + (int64_t)r0 * x.ms;
+      o.rows = cols;
+      o.cols = rows;
+      o.trans = 1;
+    }
+    return o;
+  }
+  double* Qp(int i, int* ld) const {
+    const Sec& x = s[i];
+    if (!x.trans) { *ld = x.ms; return dU + x.offU; }
+    *ld = x.ns; return dV + x.offV;
+  }
+  double* Pp(int i, int* ld) const {
+    const Sec& x = s[i];
+    if (!x.trans) { *ld = x.ns; return dV + x.offV; }
+    *ld = x.ms; return dU + x.offU;
+  }
+  void run() {
+    cusolverDnHandle_t h = ctx->svd_handle();
+    int lwork = 0;
+    for (auto& x : s) {
+      if (x.k == 0) continue;
+      int lw = 0;
+      cusolverStatus_t st = cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, x.ms, x.ns, dM + x.offM, x.ms,
+                                                         dS + x.offS, dU + x.offU, x.ms, dV + x.offV, x.ns, &lw,
+                                                         ctx->svdp);
+      if (st != CUSOLVER_STATUS_SUCCESS) throw Err(3, "gesvdj_bufferSize failed");
+      lwork = std::max(lwork, lw);
+    }
+    double* work = (double*)ctx->dmalloc(sizeof(double) * std::max(lwork, 2));
+    for (size_t i = 0; i < s.size(); ++i) {
+      const Sec& x = s[i];
+      if (x.k == 0) continue;
+      cusolverStatus_t st = cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, x.ms, x.ns, dM + x.offM, x.ms,
+                                              dS + x.offS, dU + x.offU, x.ms, dV + x.offV, x.ns, work, lwork,
+                                              dinfo + i, ctx->svdp);
+      if (st != CUSOLVER_STATUS_SUCCESS) throw Err(3, "gesvdj failed");
+    }
+    ctx->dfree(work);
+    std::vector<PhaseOp> ph;
+    int maxk = 0;
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (s[i].k == 0) continue;
+      PhaseOp p;
+      int lq, lp;
+      p.Qm = Qp((int)i, &lq);
+      p.Pm = Pp((int)i, &lp);
+      p.m = s[i].m;
+      p.n = s[i].n;
+      p.k = s[i].k;
+      p.ldq = lq;
+      p.ldp = lp;
+      ph.push_back(p);
+      maxk = std::max(maxk, s[i].k);
+    }
+    if (!ph.empty()) {
+      PhaseOp* d = (PhaseOp*)ctx->dmalloc(sizeof(PhaseOp) * ph.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, ph.data(), sizeof(PhaseOp) * ph.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_fixphase(d, (int)ph.size(), maxk, ctx->stream);
+      ctx->dfree(d);
+    }
+  }
+  void check_info() {
+    std::vector<int> info(s.size());
+    if (s.empty()) return;
+    MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * s.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    for (size_t i = 0; i < s.size(); ++i)
+      if (s[i].k > 0 && info[i] != 0)
+        throw Err(3, "gesvdj did not converge (info=" + std::to_string(info[i]) + ")");
+  }
+};
+
+// ============================================================================ split
+SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
+                   double tr_weight, bool normalize, int absorb) {
+  struct SecInfo {
+    std::map<uint32_t, std::pair<int, int>> rx, ry;  // index -> (start, size)
+    std::vector<int> blocks;
+  };
+  std::map<Q, SecInfo> secs;
+  for (int i = 0; i < (int)th.b.size(); ++i) {
+    const Block& b = th.b[i];
+    const Q qc = b.k.q0 + qat(ik0, b.k.p0);
+    SecInfo& s = secs[qc];
+    s.blocks.push_back(i);
+    s.rx[b.k.p0] = {0, b.r};
+    s.ry[b.k.p1] = {0, b.c};
+  }
+  std::vector<Q> qcs;
+  std::vector<std::pair<int, int>> mn;
+  for (auto& x : secs) {
+    int st = 0;
+    for (auto& r : x.second.rx) { r.second.first = st; st += r.second.second; }
+    int m = st;
+    st = 0;
+    for (auto& r : x.second.ry) { r.second.first = st; st += r.second.second; }
+    qcs.push_back(x.first);
+    mn.push_back({m, st});
+  }
+  if (!chimax && doTrunc) chimax = 100;
+  if (!chimax && !doTrunc) chimax = 200;
+  SvdBatch sv(ctx);
+  sv.plan(mn);
+  std::vector<CopyOp> gops;
+  for (size_t si = 0; si < qcs.size(); ++si) {
+    SecInfo& s = secs[qcs[si]];
+    for (int bi : s.blocks) {
+      const Block& b = th.b[bi];
+      gops.push_back(sv.gather_op((int)si, th.d + b.off, b.r, b.c, s.rx.at(b.k.p0).first, s.ry.at(b.k.p1).first));
+    }
+  }
+  run_copyops(ctx, gops);
+  sv.run();
+  // global truncation
+  std::vector<int32_t> sec_of(sv.nS);
+  for (size_t si = 0; si < qcs.size(); ++si)
+    for (int j = 0; j < sv.s[si].k; ++j) sec_of[sv.s[si].offS + j] = (int32_t)si;
+  const int nS = (int)sv.nS;
+  int32_t* dsec = (int32_t*)ctx->dmalloc(sizeof(int32_t) * std::max(nS, 1) * 3 + sizeof(int32_t) * (qcs.size() + 1));
+  int32_t* drank = dsec + std::max(nS, 1);
+  int32_t* dcnt = drank + 2 * std::max(nS, 1);
+  double* dout3 = ctx->part + kRedBlocks;
+  if (nS) MPSG_CUDA(cudaMemcpyAsync(dsec, sec_of.data(), sizeof(int32_t) * nS, cudaMemcpyHostToDevice, ctx->stream));
+  launch_truncate(sv.dS, nS, dsec, (int)qcs.size(), chimax, doTrunc ? 1 : 0, tr_weight, drank, dcnt, dout3, ctx->stream);
+  std::vector<int32_t> counts(qcs.size() + 1);
+  MPSG_CUDA(cudaMemcpyAsync(counts.data(), dcnt, sizeof(int32_t) * qcs.size(), cudaMemcpyDeviceToHost, ctx->stream));
+  MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dout3, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+  sv.check_info();  // syncs
+  const double tw = ctx->hscal[0];
+  const int chi = (int)ctx->hscal[1];
+  const double inv_norm = normalize ? ctx->hscal[2] : 1.0;
+  ctx->dfree(dsec);
+  // result layouts (dropDangling: sectors without kept values vanish, blocks cut to the kept count)
+  Layout lu, lv, ll;
+  for (size_t si = 0; si < qcs.size(); ++si) {
+    const int c = counts[si];
+    if (c <= 0) continue;
+    const Q qc = qcs[si];
+    SecInfo& s = secs[qc];
+    for (auto& r : s.rx) lu.add(K1(qc - qat(ik0, r.first), qc, r.first), r.second.second, c);
+    for (auto& r : s.ry) lv.add(K1(qc, qc + qat(ik1, r.first), r.first), c, r.second.second);
+    ll.add(K1(qc, qc, 0), c, 1);
+  }
+  lu.finalize();
+  lv.finalize();
+  ll.finalize();
+  SplitResult R;
+  R.U = make_tensor(ctx, 1, lu, false);
+  R.Vt = make_tensor(ctx, 1, lv, false);
+  R.lam = make_tensor(ctx, 0, ll, true);
+  R.tw = tw;
+  R.chi = chi;
+  std::vector<CopyOp> ops;
+  for (size_t si = 0; si < qcs.size(); ++si) {
+    const int c = counts[si];
+    if (c <= 0) continue;
+    const Q qc = qcs[si];
+    SecInfo& s = secs[qc];
+    int ldq, ldp;
+    double* Qm = sv.Qp((int)si, &ldq);
+    double* Pm = sv.Pp((int)si, &ldp);
+    const double* Sv = sv.dS + sv.s[si].offS;
+    for (auto& r : s.rx) {
+      const int ob = R.U->find(K1(qc - qat(ik0, r.first), qc, r.first));
+      CopyOp o;
+      o.src = Qm + r.second.first;
+      o.dst = R.U->d + R.U->b[ob].off;
+      o.rs = nullptr;
+      o.cs = absorb < 0 ? Sv : nullptr;
+      o.rows = r.second.second;
+      o.cols = c;
+      o.lds = ldq;
+      o.ldd = r.second.second;
+      o.trans = 0;
+      o.scale = absorb < 0 ? inv_norm : 1.0;
+      ops.push_back(o);
+    }
+    for (auto& r : s.ry) {
+      const int ob = R.Vt->find(K1(qc, qc + qat(ik1, r.first), r.first));
+      CopyOp o;
+      o.src = Pm + r.second.first;
+      o.dst = R.Vt->d + R.Vt->b[ob].off;
+      o.rs = absorb > 0 ? Sv : nullptr;
+      o.cs = nullptr;
+      o.rows = c;
+      o.cols = r.second.second;
+      o.lds = ldp;
+      o.ldd = c;
+      o.trans = 1;
+      o.scale = absorb > 0 ? inv_norm : 1.0;
+      ops.push_back(o);
+    }
+    const int ol = R.lam->find(K1(qc, qc, 0));
+    CopyOp o;
+    o.src = Sv;
+    o.dst = R.lam->d + R.lam->b[ol].off;
+    o.rs = nullptr;
+    o.cs = nullptr;
+    o.rows = c;
+    o.cols = 1;
+    o.lds = c;
+    o.ldd = c;
+    o.trans = 0;
+    o.scale = inv_norm;
+    ops.push_back(o);
+  }
+  run_copyops(ctx, ops);
+  return R;
+}
+
+// ============================================================================ right canonicalisation
+void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, double delta) {
+  std::map<Q, std::vector<int>> groups;  // left charge -> blocks (key order)
+  for (int i = 0; i < (int)BL2->b.size(); ++i) groups[BL2->b[i].k.q0].push_back(i);
+  std::vector<Q> keys;
+  std::vector<std::pair<int, int>> mn;
+  std::vector<std::vector<int>> coloff;
+  for (auto& g : groups) {
+    int rows = BL2->b[g.second[0]].r, cols = 0;
+    std::vector<int> co;
+    for (int i : g.second) {
+      MPSG_CHECK(BL2->b[i].r == rows, "row mismatch inside a charge group");
+      co.push_back(cols);
+      cols += BL2->b[i].c;
+    }
+    keys.push_back(g.first);
+    mn.push_back({rows, cols});
+    coloff.push_back(co);
+  }
+  SvdBatch sv(ctx);
+  sv.plan(mn);
+  std::vector<CopyOp> gops;
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    const auto& bl = groups[keys[gi]];
+    for (size_t t = 0; t < bl.size(); ++t) {
+      const Block& b = BL2->b[bl[t]];
+      gops.push_back(sv.gather_op((int)gi, BL2->d + b.off, b.r, b.c, 0, coloff[gi][t]));
+    }
+  }
+  run_copyops(ctx, gops);
+  sv.run();
+  sv.check_info();
+  std::vector<double> S(std::max<int64_t>(sv.nS, 1));
+  if (sv.nS) MPSG_CUDA(cudaMemcpyAsync(S.data(), sv.dS, sizeof(double) * sv.nS, cudaMemcpyDeviceToHost, ctx->stream));
+  ctx->sync();
+  std::vector<int> keep(keys.size());
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    int l = 0;
+    while (l < sv.s[gi].k && std::fabs(S[sv.s[gi].offS + l]) > delta) ++l;  // cut(D, delta)
+    keep[gi] = l;
+  }
+  // new BL2 (Vd rows), lambdas
+  Layout l2, ll;
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    if (!keep[gi]) continue;
+    for (int i : groups[keys[gi]]) l2.add(BL2->b[i].k, keep[gi], BL2->b[i].c);
+    ll.add(K1(keys[gi], keys[gi], 0), keep[gi], 1);
+  }
+  l2.finalize();
+  ll.finalize();
+  TensorP nb2 = make_tensor(ctx, 1, l2, false);
+  TensorP lam = make_tensor(ctx, 0, ll, false);
+  std::vector<CopyOp> ops;
+  // U*D per group, into a scratch for the BL1 products
+  KeyedArena<Q> qd;
+  for (size_t gi = 0; gi < keys.size(); ++gi)
+    if (keep[gi]) qd.add(keys[gi], sv.s[gi].m, keep[gi]);
+  double* dQD = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(qd.nelem, 2));
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    const int l = keep[gi];
+    if (!l) continue;
+    int ldq, ldp;
+    double* Qm = sv.Qp((int)gi, &ldq);
+    double* Pm = sv.Pp((int)gi, &ldp);
+    const double* Sv = sv.dS + sv.s[gi].offS;
+    const auto& bl = groups[keys[gi]];
+    for (size_t t = 0; t < bl.size(); ++t) {
+      const Block& ob = nb2->b[nb2->find(BL2->b[bl[t]].k)];
+      ops.push_back(CopyOp{Pm + coloff[gi][t], nb2->d + ob.off, nullptr, nullptr, l, ob.c, ldp, l, 1, 1.0});
+    }
+    const Block& lb = lam->b[lam->find(K1(keys[gi], keys[gi], 0))];
+    ops.push_back(CopyOp{Sv, lam->d + lb.off, nullptr, nullptr, l, 1, l, l, 0, 1.0});
+    const auto& Bq = qd.at(keys[gi]);
+    ops.push_back(CopyOp{Qm, dQD + Bq.off, nullptr, Sv, sv.s[gi].m, l, ldq, sv.s[gi].m, 0, 1.0});
+  }
+  run_copyops(ctx, ops);
+  if (BL1 && *BL1) {
+    Tensor& b1 = **BL1;
+    Layout l1;
+    std::vector<std::pair<int, int>> src;  // (old block, group) ; group -1 = copy unchanged
+    std::map<Q, int> gidx;
+    for (size_t gi = 0; gi < keys.size(); ++gi) gidx[keys[gi]] = (int)gi;
+    for (int i = 0; i < (int)b1.b.size(); ++i) {
+      auto it = gidx.find(b1.b[i].k.q1);
+      if (it == gidx.end()) {
+        l1.add(b1.b[i].k, b1.b[i].r, b1.b[i].c);
+        src.push_back({i, -1});
+      } else if (keep[it->second]) {
+        l1.add(b1.b[i].k, b1.b[i].r, keep[it->second]);
+        src.push_back({i, it->second});
+      }
+    }
+    l1.finalize();
+    TensorP nb1 = make_tensor(ctx, 1, l1, true);
+    GemmPlan g;
+    std::vector<CopyOp> cps;
+    for (auto& p : src) {
+      const Block& ob = b1.b[p.first];
+      const Block& nb = nb1->b[nb1->find(ob.k)];
+      if (p.second < 0) {
+        cps.push_back(CopyOp{b1.d + ob.off, nb1->d + nb.off, nullptr, nullptr, ob.r, ob.c, ob.r, ob.r, 0, 1.0});
+      } else {
+        const auto& Bq = qd.at(keys[p.second]);
+        MPSG_CHECK(ob.c == Bq.r, "bond dimension mismatch in prepareMatrix");
+        g.add_problem(2, nb.off, nb.r, nb.r, nb.c, false, {GSegH{0, 1, ob.off, Bq.off, ob.r, Bq.r, ob.c, 0, 0, 1.0}});
+      }
+    }
+    g.upload(ctx);
+    const double* bases[8] = {b1.d, dQD, nb1->d, nullptr, nullptr, nullptr, nullptr, nullptr};
+    g.run(bases);
+    run_copyops(ctx, cps);
+    ctx->sync();
+    *BL1 = nb1;
+  }
+  ctx->dfree(dQD);
+  BL2 = nb2;
+  if (lam_out) *lam_out = lam;
+}
+
+// ============================================================================ Lanczos
+LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
+                      bool testenergy, bool reorth, LanczosStats* st) {
+  auto t_start = std::chrono::steady_clock::now();
+  const int64_t n = th_init.nelem;
+  MPSG_CHECK(psi.nelem == n, "Lanczos state layout mismatch");
+  MPSG_CHECK(itmax >= 1 && itmax <= 1000, "itmax must be in [1, 1000]");
+  cudaStream_t s = ctx->stream;
+  // device scalars: alpha[itmax+1], beta[itmax+1], norm2[itmax+2], E[itmax/5+2], z[itmax+1], coef[itmax+1]
+  const int na = itmax + 2;
+  double* dsc = (double*)ctx->dmalloc(sizeof(double) * (size_t)na * 6);
+  double *d_alpha = dsc, *d_beta = dsc + na, *d_norm2 = dsc + 2 * na, *d_E = dsc + 3 * na, *d_z = dsc + 4 * na,
+         *d_coef = dsc + 5 * na;
+  MPSG_CUDA(cudaMemsetAsync(dsc, 0, sizeof(double) * (size_t)na * 6, s));
+  double* d_proj = reorth ? (double*)ctx->dmalloc(sizeof(double) * 64 * (size_t)na) : nullptr;
+  std::vector<double*> V;
+  double** dV = (double**)ctx->dmalloc(sizeof(double*) * (size_t)na);
+  auto slot = [&](int j) -> double* {
+    while ((int)V.size() <= j) {
+      double* p = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(n, 2));
+      V.push_back(p);
+      MPSG_CUDA(cudaMemcpyAsync(dV + (V.size() - 1), &V.back(), sizeof(double*), cudaMemcpyHostToDevice, s));
+      ctx->sync();
+    }
+    return V[j];
+  };
+  double* w = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(n, 2));
+  MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * std::max<int64_t>(n, 2), s));
+  MPSG_CUDA(cudaMemcpyAsync(slot(0), th_init.d, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  launch_dot(V[0], V[0], n, ctx->part, d_norm2, s);
+  cudaEvent_t e0, e1;
+  MPSG_CUDA(cudaEventCreate(&e0));
+  MPSG_CUDA(cudaEventCreate(&e1));
+  std::vector<double> ha(na), hb(na), hn(na), hE(na);
+  int it = 0, n_es = 0;
+  double eold = 1e100;
+  bool done = false;
+  float mv_ms_total = 0;
+  while (!done) {
+    // batch up to the next energy checkpoint (it % 5 == 0, it != 0) or itmax-1
+    int ck = it;
+    while (!((ck % 5 == 0 && ck != 0) || ck >= itmax - 1)) ++ck;
+    MPSG_CUDA(cudaEventRecord(e0, s));
+    for (int j = it; j <= ck; ++j) {
+      slot(j + 1);
+      launch_scale_by_norm(V[j], n, d_norm2 + j, delta, d_beta + j, s);
+      mv.run(V[j], w);
+      launch_dot(w, V[j], n, ctx->part, d_alpha + j, s);
+      if (testenergy && j % 5 == 0 && j != 0) launch_tri_lowest(d_alpha, d_beta, j + 1, d_E + j / 5, nullptr, s);
+      launch_axpy3(V[j + 1], w, V[j], j > 0 ? V[j - 1] : nullptr, d_alpha + j, d_beta + j, n, ctx->part,
+                   d_norm2 + j + 1, s);
+      if (reorth) {
+        for (int pass = 0; pass < 2; ++pass) {
+          launch_project((const double* const*)dV, j + 1, V[j + 1], n, d_proj, d_coef, s);
+          launch_combine(V[j + 1], (const double* const*)dV, j + 1, d_coef, n, 1, s);
+        }
+        launch_dot(V[j + 1], V[j + 1], n, ctx->part, d_norm2 + j + 1, s);
+      }
+    }
+    MPSG_CUDA(cudaEventRecord(e1, s));
+    MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dsc, sizeof(double) * (size_t)na * 4, cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    mv_ms_total += ms;
+    std::memcpy(ha.data(), ctx->hscal, sizeof(double) * na);
+    std::memcpy(hb.data(), ctx->hscal + na, sizeof(double) * na);
+    std::memcpy(hn.data(), ctx->hscal + 2 * na, sizeof(double) * na);
+    std::memcpy(hE.data(), ctx->hscal + 3 * na, sizeof(double) * na);
+    if (st) {
+      st->matvecs += ck - it + 1;
+      st->matvec_flops += mv.flops * (ck - it + 1);
+    }
+    for (int j = it; j <= ck; ++j) {
+      const double k = std::sqrt(hn[j]);
+      if (std::fabs(k) < delta) { n_es = j; done = true; break; }
+      n_es = j + 1;
+      if (testenergy && j % 5 == 0 && j != 0) {
+        if (std::fabs(hE[j / 5] - eold) < delta) { done = true; break; }
+        eold = hE[j / 5];
+      }
+      if (j + 1 >= itmax) { done = true; break; }
+    }
+    it = ck + 1;
+  }
+  if (st) st->matvec_seconds += mv_ms_total * 1e-3;
+  LanczosResult res;
+  res.n = n_es;
+  res.iterations = n_es;
+  if (n_es > 0) {
+    launch_tri_lowest(d_alpha, d_beta, n_es, d_E + na - 1, d_z, s);
+    launch_combine(psi.d, (const double* const*)dV, n_es, d_z, n, 0, s);
+    MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, d_E + na - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    ctx->sync();
+    res.E0 = ctx->hscal[0];
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (double* p : V) ctx->dfree(p);
+  ctx->dfree(w);
+  ctx->dfree(dV);
+  ctx->dfree(dsc);
+  if (d_proj) ctx->dfree(d_proj);
+  ctx->sync();
+  if (st) st->seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  return res;
+}
+
+}  // namespace mpsg

@@ -1,0 +1,119 @@
+// Contraction plans and algorithms of the DMRG hot path (host orchestration of the kernels).
+#pragma once
+#include <memory>
+
+#include "host_core.h"
+
+namespace mpsg {
+
+// Arena of blocks addressed by an arbitrary ordered key (internal intermediates).
+template <class K>
+struct KeyedArena {
+  struct B {
+    int32_t r, c;
+    int64_t off;
+  };
+  std::map<K, B> m;
+  int64_t nelem = 0;
+  void add(const K& k, int r, int c) {
+    if (m.count(k)) return;
+    B b{r, c, nelem};
+    m[k] = b;
+    nelem += ((int64_t)r * c + kAlign - 1) / kAlign * kAlign;
+  }
+  const B& at(const K& k) const { return m.at(k); }
+};
+
+// 5-index key of a combined environment block (L~ / R~) or intermediate
+struct K5 {
+  Q x, y;
+  uint32_t w, s, t;
+  bool operator<(const K5& o) const {
+    if (x != o.x) return x < o.x;
+    if (y != o.y) return y < o.y;
+    if (w != o.w) return w < o.w;
+    if (s != o.s) return s < o.s;
+    return t < o.t;
+  }
+};
+
+// Matvec  theta' = L W1 W2 R theta  (contractTwosite), factored as
+//   L~(a',a;wm,s1',s1) = sum_wl W1[wl,wm](s1->s1') L(a',a;wl)
+//   R~(b',b;wm,s2',s2) = sum_wr W2[wm,wr](s2->s2') R(b',b;wr)
+//   X(a',b;wm,s1',s2)  = sum_s1 L~(a',a;wm,s1',s1) theta(a,b;s1,s2)          (stage A)
+//   theta'(a',b';s1',s2') = sum_{wm,s2,b} X(a',b;wm,s1',s2) R~(b',b;wm,s2',s2)^T   (stage C)
+struct MatvecPlan {
+  Ctx* ctx = nullptr;
+  KeyedArena<K5> lt, rt, xa;
+  double* dLt = nullptr;
+  double* dRt = nullptr;
+  double* dX = nullptr;
+  Layout out;                // output layout (reference structure unless given)
+  GemmPlan stageA, stageC;
+  LincombPlan build_lt, build_rt;
+  double flops = 0;          // algorithmic FLOPs of one matvec (stage A + stage C)
+  double flops_ref = 0;      // FLOPs of the reference's per-term schedule (2 GEMMs per term)
+  double flops_survey = 0;   // F_A + F_B + F_C of the factored (L.theta first) schedule
+  int64_t bytes_alg = 0;     // 8*(|L|+|R|+2|theta|)
+  void run(const double* theta_in, double* theta_out);
+  ~MatvecPlan();
+};
+std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th_in,
+                                         const MPO& W1, const MPO& W2, const ItoKey& ik0, const ItoKey& ik1,
+                                         const Layout* out_layout);
+// Block keys reachable from `th` by repeated application of the matvec (reference semantics).
+Layout theta_closure(const Tensor& L, const Tensor& R, const Layout& th, const MPO& W1, const MPO& W2,
+                     const ItoKey& ik0, const ItoKey& ik1);
+
+// Environment update (addContractionLayer) factored as two grouped GEMM stages.
+struct EnvPlan {
+  Ctx* ctx = nullptr;
+  KeyedArena<K5> ct;      // combined environment (L~ or R~)
+  KeyedArena<K5> tt;      // intermediate T
+  double* dCt = nullptr;
+  double* dT = nullptr;
+  Layout out;
+  GemmPlan st1, st2;
+  LincombPlan build_ct;
+  double flops = 0;
+  void run(const double* A, double* out_d);
+  ~EnvPlan();
+};
+std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
+                                   int direction);
+TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
+                   double* flops_out);
+
+// theta(a,b;s1,s2) = A1(a,c;s1) A2(c,b;s2)
+TensorP theta_form(Ctx* ctx, const Tensor& A1, const Tensor& A2, const Layout* layout);
+
+// split (two-site, direction 0) with global truncation
+struct SplitResult {
+  TensorP U, Vt, lam;
+  double tw = 0;
+  int chi = 0;
+};
+// absorb: 0 none, +1 lambda into Vt (rows), -1 lambda into U (columns)
+SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
+                   double tr_weight, bool normalize, int absorb);
+
+// prepareMatrix(BL1, lambda, BL2, "r", multiply=true, truncate=true, delta): right-orthonormalise BL2,
+// multiply U*D into BL1 (BL1 may be null at the left edge).
+void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, double delta);
+
+struct LanczosStats {
+  int64_t matvecs = 0;
+  double matvec_flops = 0;
+  double matvec_seconds = 0;
+  double seconds = 0;
+};
+struct LanczosResult {
+  double E0 = 0;
+  int iterations = 0;
+  int n = 0;
+};
+// TSLanzcosEngine::simulate + getState(0): psi receives the ground state (layout of th_init)
+LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
+                      bool testenergy, bool reorth, LanczosStats* st);
+
+}  // namespace mpsg

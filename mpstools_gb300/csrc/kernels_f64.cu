@@ -1,0 +1,511 @@
+// FP64 kernels of libmpsg (sm_103a): grouped block GEMM, block linear combinations,
+// gather/scatter copies, FixPhase, Lanczos vector operations, the tridiagonal
+// lowest-eigenpair solver and the global singular-value truncation.
+#include <cuda_runtime.h>
+#include <atomic>
+#include <cfloat>
+#include <climits>
+#include "mpsg_internal.h"
+
+namespace mpsg {
+
+static std::atomic<int64_t> g_launches{0};
+int64_t kernel_launch_count() { return g_launches.load(); }
+#define LAUNCHED() g_launches.fetch_add(1)
+
+// ============================================================================ grouped DGEMM
+// One CTA computes a 64x64 tile of one problem; the tile accumulates every segment
+// (product term) of the problem.  FP64 FMA on CUDA cores.
+constexpr int GM = 64, GN = 64, GK = 16;
+
+__global__ void __launch_bounds__(256) k_gemm_f64(const GProb* __restrict__ prob, const GSeg* __restrict__ seg,
+                                                  const GTile* __restrict__ tile, const Bases bases) {
+  __shared__ double As[GK][GM + 1];
+  __shared__ double Bs[GK][GN + 1];
+  const GTile t = tile[blockIdx.x];
+  const GProb P = prob[t.prob];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+
+  for (int s = P.seg0; s < P.seg1; ++s) {
+    const GSeg S = seg[s];
+    const double* __restrict__ Ap = bases.p[S.baseA] + S.offA;
+    const double* __restrict__ Bp = bases.p[S.baseB] + S.offB;
+    for (int k0 = 0; k0 < S.K; k0 += GK) {
+#pragma unroll
+      for (int r = 0; r < (GM * GK) / 256; ++r) {
+        const int e = tid + r * 256;
+        int m, k;
+        if (!S.tA) { m = e % GM; k = e / GM; } else { k = e % GK; m = e / GK; }
+        const int gm = t.m0 + m, gk = k0 + k;
+        double v = 0.0;
+        if (gm < P.M && gk < S.K)
+          v = S.tA ? Ap[gk + (int64_t)gm * S.lda] : Ap[gm + (int64_t)gk * S.lda];
+        As[k][m] = v * S.alpha;
+      }
+#pragma unroll
+      for (int r = 0; r < (GN * GK) / 256; ++r) {
+        const int e = tid + r * 256;
+        int n, k;
+        if (!S.tB) { k = e % GK; n = e / GK; } else { n = e % GN; k = e / GN; }
+        const int gn = t.n0 + n, gk = k0 + k;
+        double v = 0.0;
+        if (gn < P.N && gk < S.K)
+          v = S.tB ? Bp[gn + (int64_t)gk * S.ldb] : Bp[gk + (int64_t)gn * S.ldb];
+        Bs[k][n] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < GK; ++k) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[k][tx + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[k][ty + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int gn = t.n0 + ty + 16 * j;
+    if (gn >= P.N) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int gm = t.m0 + tx + 16 * i;
+      if (gm >= P.M) continue;
+      double* c = const_cast<double*>(bases.p[P.baseC]) + P.offC + gm + (int64_t)gn * P.ldc;
+      *c = P.beta ? (*c + acc[i][j]) : acc[i][j];
+    }
+  }
+}
+
+void launch_gemm_f64(const GProb* prob, const GSeg* seg, const GTile* tile, int ntiles, const Bases& bases,
+                     cudaStream_t s) {
+  if (ntiles <= 0) return;
+  k_gemm_f64<<<ntiles, 256, 0, s>>>(prob, seg, tile, bases);
+  LAUNCHED();
+}
+
+// ============================================================================ block linear combination
+__global__ void k_lincomb(const LCOut* __restrict__ outs, const LCTerm* __restrict__ terms) {
+  const LCOut o = outs[blockIdx.x];
+  for (int64_t i = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; i < o.n; i += (int64_t)gridDim.y * blockDim.x) {
+    double s = 0.0;
+    for (int t = o.t0; t < o.t1; ++t) s = fma(terms[t].coef, terms[t].src[i], s);
+    o.dst[i] = s;
+  }
+}
+void launch_lincomb(const LCOut* outs, const LCTerm* terms, int nout, int64_t maxn, cudaStream_t s) {
+  if (nout <= 0) return;
+  int chunks = (int)std::min<int64_t>((maxn + 255) / 256, 64);
+  if (chunks < 1) chunks = 1;
+  k_lincomb<<<dim3(nout, chunks), 256, 0, s>>>(outs, terms);
+  LAUNCHED();
+}
+
+// ============================================================================ strided block copies
+__global__ void k_copy(const CopyOp* __restrict__ ops) {
+  const CopyOp o = ops[blockIdx.x];
+  const int64_t tot = (int64_t)o.rows * o.cols;
+  for (int64_t e = (int64_t)blockIdx.y * blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.y * blockDim.x) {
+    const int i = (int)(e % o.rows), j = (int)(e / o.rows);
+    double v = o.trans ? o.src[j + (int64_t)i * o.lds] : o.src[i + (int64_t)j * o.lds];
+    v *= o.scale;
+    if (o.rs) v *= o.rs[i];
+    if (o.cs) v *= o.cs[j];
+    o.dst[i + (int64_t)j * o.ldd] = v;
+  }
+}
+void launch_copyops(const CopyOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_copy<<<dim3(nops, 16), 256, 0, s>>>(ops);
+  LAUNCHED();
+}
+
+// ============================================================================ FixPhase
+// For singular index i the sign of the first abs-max entry of P(:,i) (a row of Vt) is made
+// positive; the same sign multiplies Q(:,i) (blas/helperfunctions.hpp:36-51).
+__global__ void k_fixphase(const PhaseOp* __restrict__ ops) {
+  const PhaseOp o = ops[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = blockIdx.y * 8 + warp; i < o.k; i += gridDim.y * 8) {
+    double* p = o.Pm + (int64_t)i * o.ldp;
+    double best = 0.0;
+    int bi = INT_MAX;
+    for (int j = lane; j < o.n; j += 32) {
+      const double a = fabs(p[j]);
+      if (a > best) { best = a; bi = j; }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const double ob = __shfl_down_sync(0xffffffffu, best, off);
+      const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    bi = __shfl_sync(0xffffffffu, bi, 0);
+    best = __shfl_sync(0xffffffffu, best, 0);
+    if (best == 0.0) bi = 0;
+    const double sgn = (o.n > 0 && p[bi] > 0) ? 1.0 : -1.0;
+    __syncwarp();
+    if (sgn < 0) {
+      for (int j = lane; j < o.n; j += 32) p[j] = -p[j];
+      double* q = o.Qm + (int64_t)i * o.ldq;
+      for (int j = lane; j < o.m; j += 32) q[j] = -q[j];
+    }
+  }
+}
+void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s) {
+  if (nops <= 0 || maxk <= 0) return;
+  int gy = (maxk + 7) / 8;
+  if (gy > 64) gy = 64;
+  k_fixphase<<<dim3(nops, gy), 256, 0, s>>>(ops);
+  LAUNCHED();
+}
+
+// ============================================================================ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ double block_sum(double v) {  // blockDim.x == 256
+  __shared__ double sh[8];
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < 8 ? sh[threadIdx.x] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+__global__ void k_dot_part(const double* __restrict__ x, const double* __restrict__ y, int64_t n, double* part) {
+  double s = 0.0;
+  const int64_t n2 = n >> 1;
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  const double2* y2 = reinterpret_cast<const double2*>(y);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = x2[i], b = y2[i];
+    s = fma(a.x, b.x, s);
+    s = fma(a.y, b.y, s);
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) s = fma(x[n - 1], y[n - 1], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_sum_parts(const double* part, int np, double* out) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) *out = s;
+}
+void launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t s) {
+  k_dot_part<<<kRedBlocks, 256, 0, s>>>(x, y, n, part);
+  k_sum_parts<<<1, 256, 0, s>>>(part, kRedBlocks, out);
+  g_launches.fetch_add(2);
+}
+
+__global__ void k_scale_by_norm(double* x, int64_t n, const double* norm2, double delta, double* beta_out) {
+  const double k = sqrt(*norm2);
+  const double sc = (k < delta) ? 0.0 : 1.0 / k;
+  if (beta_out && blockIdx.x == 0 && threadIdx.x == 0) *beta_out = k;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= sc;
+}
+void launch_scale_by_norm(double* x, int64_t n, const double* norm2, double delta, double* beta_out,
+                          cudaStream_t s) {
+  k_scale_by_norm<<<kRedBlocks, 256, 0, s>>>(x, n, norm2, delta, beta_out);
+  LAUNCHED();
+}
+
+// out = (v*(-alpha) + w) + vprev*(-beta), and the squared norm of out
+__global__ void k_axpy3(double* __restrict__ out, const double* __restrict__ w, const double* __restrict__ v,
+                        const double* __restrict__ vp, const double* alpha, const double* beta, int64_t n,
+                        double* part) {
+  const double a = -(*alpha);
+  const double b = vp ? -(*beta) : 0.0;
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double o = v[i] * a + w[i];
+    if (vp) o = o + vp[i] * b;
+    out[i] = o;
+    s = fma(o, o, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+void launch_axpy3(double* out, const double* w, const double* v, const double* vprev, const double* alpha,
+                  const double* beta, int64_t n, double* part, double* norm2_out, cudaStream_t s) {
+  k_axpy3<<<kRedBlocks, 256, 0, s>>>(out, w, v, vprev, alpha, beta, n, part);
+  k_sum_parts<<<1, 256, 0, s>>>(part, kRedBlocks, norm2_out);
+  g_launches.fetch_add(2);
+}
+
+// y = (or -=) sum_j c[j] * V_j, V given as a device array of vector pointers
+__global__ void k_combine(double* y, const double* const* __restrict__ V, int nv, const double* __restrict__ c,
+                          int64_t n, int subtract) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < nv; ++j) s = fma(V[j][i], c[j], s);
+    y[i] = subtract ? (y[i] - s) : s;
+  }
+}
+void launch_combine(double* y, const double* const* V, int nv, const double* c, int64_t n, int subtract,
+                    cudaStream_t s) {
+  k_combine<<<kRedBlocks, 256, 0, s>>>(y, V, nv, c, n, subtract);
+  LAUNCHED();
+}
+
+constexpr int kProjChunks = 64;
+__global__ void k_project_part(const double* const* __restrict__ V, const double* __restrict__ x, int64_t n,
+                               double* part) {
+  const int j = blockIdx.y;
+  const double* v = V[j];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s = fma(v[i], x[i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[(int64_t)j * kProjChunks + blockIdx.x] = s;
+}
+__global__ void k_project_sum(const double* part, double* c) {
+  const int j = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < kProjChunks; i += blockDim.x) s += part[(int64_t)j * kProjChunks + i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) c[j] = s;
+}
+void launch_project(const double* const* V, int nv, const double* x, int64_t n, double* part_nv, double* c,
+                    cudaStream_t s) {
+  if (nv <= 0) return;
+  k_project_part<<<dim3(kProjChunks, nv), 256, 0, s>>>(V, x, n, part_nv);
+  k_project_sum<<<nv, 256, 0, s>>>(part_nv, c);
+  g_launches.fetch_add(2);
+}
+
+__global__ void k_fill(double* x, int64_t n, double v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] = v;
+}
+void launch_fill(double* x, int64_t n, double v, cudaStream_t s) {
+  if (n <= 0) return;
+  k_fill<<<kRedBlocks, 256, 0, s>>>(x, n, v);
+  LAUNCHED();
+}
+
+// ============================================================================ tridiagonal eigensolver
+// Lowest eigenvalue of T (diag a[0..n), offdiag b[1..n)) by Sturm-count multisection in one warp,
+// eigenvector by inverse iteration with a pivoted tridiagonal LU (one thread).
+__device__ int sturm_below(const double* a, const double* b, int n, double x, double pivmin) {
+  int c = 0;
+  double d = a[0] - x;
+  if (fabs(d) < pivmin) d = -pivmin;
+  if (d < 0) ++c;
+  for (int i = 1; i < n; ++i) {
+    d = a[i] - x - b[i] * b[i] / d;
+    if (fabs(d) < pivmin) d = -pivmin;
+    if (d < 0) ++c;
+  }
+  return c;
+}
+
+__global__ void k_tri_lowest(const double* __restrict__ a, const double* __restrict__ b, int n, double* E0,
+                             double* z) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x;
+  // Gershgorin interval
+  double lo = DBL_MAX, hi = -DBL_MAX, bmax = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const double r = (i > 0 ? fabs(b[i]) : 0.0) + (i + 1 < n ? fabs(b[i + 1]) : 0.0);
+    lo = fmin(lo, a[i] - r);
+    hi = fmax(hi, a[i] + r);
+    if (i > 0) bmax = fmax(bmax, b[i] * b[i]);
+  }
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+    bmax = fmax(bmax, __shfl_xor_sync(0xffffffffu, bmax, off));
+  }
+  const double pivmin = fmax(DBL_MIN, DBL_MIN * bmax);
+  const double tnorm = fmax(fabs(lo), fabs(hi));
+  lo -= 2.0 * DBL_EPSILON * tnorm + pivmin;
+  hi += 2.0 * DBL_EPSILON * tnorm + pivmin;
+  for (int round = 0; round < 80; ++round) {
+    if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin) break;
+    const double x = lo + (hi - lo) * (double)(lane + 1) / 33.0;
+    const int c = sturm_below(a, b, n, x, pivmin);
+    const unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
+    const double xprev = __shfl_up_sync(0xffffffffu, x, 1);
+    if (ball == 0) {
+      lo = __shfl_sync(0xffffffffu, x, 31);
+    } else {
+      const int l = __ffs(ball) - 1;
+      const double nhi = __shfl_sync(0xffffffffu, x, l);
+      const double nlo = (l == 0) ? lo : __shfl_sync(0xffffffffu, xprev, l);
+      lo = nlo;
+      hi = nhi;
+    }
+  }
+  const double lam = 0.5 * (lo + hi);
+  if (lane == 0) *E0 = lam;
+  if (!z || lane != 0) return;
+  // inverse iteration: (T - lam) x = rhs, LU with partial pivoting (dgttrf/dgtts2 scheme)
+  double* dl = sm;
+  double* d = sm + n;
+  double* du = sm + 2 * n;
+  double* du2 = sm + 3 * n;
+  double* x = sm + 4 * n;
+  int* piv = reinterpret_cast<int*>(sm + 5 * n);
+  const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+  for (int i = 0; i < n; ++i) {
+    d[i] = a[i] - lam;
+    dl[i] = (i + 1 < n) ? b[i + 1] : 0.0;
+    du[i] = (i + 1 < n) ? b[i + 1] : 0.0;
+    du2[i] = 0.0;
+    piv[i] = i;
+    x[i] = 1.0;
+  }
+  for (int i = 0; i < n - 1; ++i) {
+    if (fabs(d[i]) >= fabs(dl[i])) {
+      if (d[i] == 0.0) d[i] = tiny;
+      const double f = dl[i] / d[i];
+      dl[i] = f;
+      d[i + 1] -= f * du[i];
+      du2[i] = 0.0;
+    } else {
+      const double f = d[i] / dl[i];
+      d[i] = dl[i];
+      dl[i] = f;
+      const double tmp = du[i];
+      du[i] = d[i + 1];
+      d[i + 1] = tmp - f * d[i + 1];
+      if (i < n - 2) {
+        du2[i] = du[i + 1];
+        du[i + 1] = -f * du[i + 1];
+      }
+      piv[i] = i + 1;
+    }
+  }
+  if (d[n - 1] == 0.0) d[n - 1] = tiny;
+  for (int it = 0; it < 3; ++it) {
+    // forward: apply L^{-1} P
+    for (int i = 0; i < n - 1; ++i) {
+      if (piv[i] == i) {
+        x[i + 1] -= dl[i] * x[i];
+      } else {
+        const double t = x[i];
+        x[i] = x[i + 1];
+        x[i + 1] = t - dl[i] * x[i];
+      }
+    }
+    // backward: U x = y
+    x[n - 1] /= d[n - 1];
+    if (n > 1) x[n - 2] = (x[n - 2] - du[n - 2] * x[n - 1]) / d[n - 2];
+    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / d[i];
+    double nrm = 0.0, amax = 0.0;
+    int imax = 0;
+    for (int i = 0; i < n; ++i) {
+      nrm += x[i] * x[i];
+      if (fabs(x[i]) > amax) { amax = fabs(x[i]); imax = i; }
+    }
+    const double s = (x[imax] < 0 ? -1.0 : 1.0) / sqrt(nrm);
+    for (int i = 0; i < n; ++i) x[i] *= s;
+  }
+  for (int i = 0; i < n; ++i) z[i] = x[i];
+}
+void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s) {
+  if (n <= 0) return;
+  const size_t sh = (size_t)n * (5 * sizeof(double) + sizeof(int)) + 16;
+  k_tri_lowest<<<1, 32, sh, s>>>(alpha, beta, n, E0, z);
+  LAUNCHED();
+}
+
+// ============================================================================ truncation
+// rank[i] = position of value i when all values are ordered by (value desc, later insertion first),
+// the iteration order of the reference's reversed std::multimap (src/BlockTensor.hpp:236-258).
+__global__ void k_trunc_rank(const double* __restrict__ S, int n, int32_t* rank) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = S[i];
+  int r = 0;
+  for (int j = 0; j < n; ++j) {
+    const double w = S[j];
+    r += (w > v) || (w == v && j > i);
+  }
+  rank[i] = r;
+}
+// out3[0] = truncated weight, out3[1] = kept count, out3[2] = 1/norm of kept values (normalisation)
+__global__ void k_trunc_select(const double* __restrict__ S, int n, const int32_t* __restrict__ sec_of, int nsec,
+                               int chimax, int doTrunc, double tr_weight, const int32_t* __restrict__ rank,
+                               int32_t* order, int32_t* counts, double* out3) {
+  for (int i = threadIdx.x; i < nsec; i += blockDim.x) counts[i] = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) order[rank[i]] = i;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double tw;
+  int cnt = 0;
+  if (!doTrunc) {
+    tw = 1.0;
+    for (int r = 0; r < n && cnt != chimax; ++r) {
+      const double v = S[order[r]];
+      if (!(fabs(v) > 1e-15)) break;
+      tw -= v * v;
+      counts[sec_of[order[r]]]++;
+      ++cnt;
+    }
+  } else {
+    double nrm2 = 0.0;
+    for (int i = 0; i < n; ++i) nrm2 += S[i] * S[i];
+    const double norm = sqrt(nrm2);
+    tw = norm;
+    for (int r = 0; r < n && fabs(tw) > norm * tr_weight && cnt < chimax; ++r) {
+      const double v = S[order[r]];
+      tw -= (v * v) / norm;
+      counts[sec_of[order[r]]]++;
+      ++cnt;
+    }
+    if (tw < 0 && fabs(tw) < 1e-14) tw = 0.0;
+  }
+  // norm of the kept values, per sector in key order (values of a sector are stored descending)
+  double k2 = 0.0;
+  int i = 0;
+  while (i < n) {
+    const int sec = sec_of[i];
+    int j = i;
+    double part = 0.0;
+    int taken = 0;
+    while (j < n && sec_of[j] == sec) {
+      if (taken < counts[sec]) { part += S[j] * S[j]; ++taken; }
+      ++j;
+    }
+    k2 += part;
+    i = j;
+  }
+  out3[0] = tw;
+  out3[1] = (double)cnt;
+  out3[2] = k2 > 0 ? 1.0 / sqrt(k2) : 0.0;
+}
+void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, int chimax, int doTrunc,
+                     double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s) {
+  if (n > 0) {
+    k_trunc_rank<<<(n + 255) / 256, 256, 0, s>>>(S, n, rank_scratch);
+    LAUNCHED();
+  }
+  k_trunc_select<<<1, 256, 0, s>>>(S, n, sec_of, nsec, chimax, doTrunc, tr_weight, rank_scratch,
+                                   rank_scratch + n, counts, out3);
+  LAUNCHED();
+}
+
+}  // namespace mpsg

@@ -1,0 +1,161 @@
+// Internal declarations of libmpsg: block-sparse tensors, device launch descriptors.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace mpsg {
+
+typedef uint64_t Q;  // packed U(1) charge word (AbKeyType::_qn); + and - wrap like the reference
+
+struct Err : std::runtime_error {
+  int code;
+  Err(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define MPSG_CUDA(x)                                                                          \
+  do {                                                                                        \
+    cudaError_t e_ = (x);                                                                     \
+    if (e_ != cudaSuccess)                                                                    \
+      throw ::mpsg::Err(2, std::string(#x) + ": " + cudaGetErrorString(e_) + " @" +           \
+                               std::to_string(__LINE__));                                     \
+  } while (0)
+#define MPSG_CHECK(c, msg)                    \
+  do {                                        \
+    if (!(c)) throw ::mpsg::Err(1, (msg));    \
+  } while (0)
+
+// TensorKeyType<2,Ns,AbKeyType> order: charges [0],[1] then indices (0),(1)
+struct BKey {
+  Q q0 = 0, q1 = 0;
+  uint32_t p0 = 0, p1 = 0;
+  bool operator<(const BKey& o) const {
+    if (q0 != o.q0) return q0 < o.q0;
+    if (q1 != o.q1) return q1 < o.q1;
+    if (p0 != o.p0) return p0 < o.p0;
+    return p1 < o.p1;
+  }
+  bool operator==(const BKey& o) const { return q0 == o.q0 && q1 == o.q1 && p0 == o.p0 && p1 == o.p1; }
+};
+inline BKey K1(Q a, Q b, uint32_t p) { BKey k; k.q0 = a; k.q1 = b; k.p0 = p; return k; }
+inline BKey K2(Q a, Q b, uint32_t p, uint32_t pp) { BKey k; k.q0 = a; k.q1 = b; k.p0 = p; k.p1 = pp; return k; }
+
+struct Block {
+  BKey k;
+  int32_t r = 0, c = 0;
+  int64_t off = 0;  // element offset into the arena (multiple of kAlign)
+};
+constexpr int64_t kAlign = 16;  // 128-byte aligned blocks
+
+struct Ctx;
+
+// Block-sparse tensor with a device arena.  Padding between blocks is kept zero.
+struct Tensor {
+  Ctx* ctx = nullptr;
+  int nphys = 1;
+  std::vector<Block> b;         // sorted by key
+  std::map<BKey, int> idx;      // key -> position in b
+  int64_t nelem = 0;            // arena length (elements)
+  double* d = nullptr;          // device arena
+  Tensor() {}
+  Tensor(const Tensor&) = delete;
+  Tensor& operator=(const Tensor&) = delete;
+  ~Tensor();
+  int find(const BKey& k) const {
+    auto it = idx.find(k);
+    return it == idx.end() ? -1 : it->second;
+  }
+  const double* ptr(int i) const { return d + b[i].off; }
+  double* ptr(int i) { return d + b[i].off; }
+};
+typedef std::shared_ptr<Tensor> TensorP;
+
+// Structure-only description used by planners before allocation.
+struct Layout {
+  std::vector<Block> b;
+  std::map<BKey, int> idx;
+  int64_t nelem = 0;
+  void add(const BKey& k, int r, int c) {
+    Block x;
+    x.k = k; x.r = r; x.c = c;
+    b.push_back(x);
+  }
+  void finalize();  // sort, assign offsets, build index; duplicate keys are an error
+};
+
+// ----------------------------------------------------------------------------- device descriptors
+// Operands are addressed as (base slot, element offset); the base pointers are passed to the
+// kernel by value, so one uploaded descriptor set serves every call with new buffers.
+struct Bases {
+  const double* p[8];
+};
+struct GSeg {  // one product term alpha*op(A)*op(B) accumulated into a problem
+  int64_t offA, offB;
+  int32_t lda, ldb, K;
+  int8_t baseA, baseB, tA, tB;
+  double alpha;
+};
+struct GProb {  // C (M x N, col-major, ldc) = [C +] sum_segments alpha*op(A)*op(B)
+  int64_t offC;
+  int32_t ldc, M, N, seg0, seg1;
+  int8_t baseC, beta;
+};
+struct GTile {
+  int32_t prob, m0, n0;
+};
+struct LCOut {  // dst[0..n) = sum_t coef_t * src_t[0..n)
+  double* dst;
+  int64_t n;
+  int32_t t0, t1;
+};
+struct LCTerm {
+  const double* src;
+  double coef;
+};
+struct CopyOp {  // dst(i,j) = scale * rs[i] * cs[j] * (trans ? src(j,i) : src(i,j)); dst is rows x cols
+  const double* src;
+  double* dst;
+  const double* rs;
+  const double* cs;
+  int32_t rows, cols, lds, ldd, trans;
+  double scale;
+};
+struct PhaseOp {  // FixPhase on one sector: Q (m x k, ldq) and P (n x k, ldp); sign from P columns
+  double* Qm;
+  double* Pm;
+  int32_t m, n, k, ldq, ldp;
+};
+
+// ----------------------------------------------------------------------------- launchers (kernels.cu)
+void launch_gemm_f64(const GProb* prob, const GSeg* seg, const GTile* tile, int ntiles, const Bases& bases,
+                     cudaStream_t s);
+void launch_lincomb(const LCOut* outs, const LCTerm* terms, int nout, int64_t maxn, cudaStream_t s);
+void launch_copyops(const CopyOp* ops, int nops, cudaStream_t s);
+void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s);
+// Lanczos vector kernels; `part` is a scratch array of kRedBlocks doubles
+constexpr int kRedBlocks = 608;
+void launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t s);
+void launch_scale_by_norm(double* x, int64_t n, const double* norm2, double delta, double* beta_out,
+                          cudaStream_t s);
+void launch_axpy3(double* out, const double* w, const double* v, const double* vprev, const double* alpha,
+                  const double* beta, int64_t n, double* part, double* norm2_out, cudaStream_t s);
+// y[i] = sum_j V[j][i] * c[j]  (j < nv), optionally y -= instead of =; V is a device array of pointers
+void launch_combine(double* y, const double* const* V, int nv, const double* c, int64_t n, int subtract,
+                    cudaStream_t s);
+// c[j] = <V_j, x> for j < nv (block partials reduced deterministically); part_nv holds 64*nv doubles
+void launch_project(const double* const* V, int nv, const double* x, int64_t n, double* part_nv, double* c,
+                    cudaStream_t s);
+// lowest eigenpair of the symmetric tridiagonal (alpha[0..n), offdiag beta[1..n)); z may be null
+void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s);
+// global truncation over concatenated singular values (see kernels.cu)
+void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, int chimax, int doTrunc,
+                     double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s);
+void launch_fill(double* x, int64_t n, double v, cudaStream_t s);
+int64_t kernel_launch_count();
+
+}  // namespace mpsg

@@ -1,0 +1,211 @@
+"""ctypes binding of libmpsg.so (include/mpsg.h).
+
+There is no fallback: if the in-tree library is missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libmpsg.so")
+
+PREC = {"fp64": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "auto": 5}
+
+_L = None
+
+
+class MPSGError(RuntimeError):
+    pass
+
+
+def load(build_if_missing: bool = False):
+    global _L
+    if _L is not None:
+        return _L
+    if not os.path.exists(LIBPATH):
+        if not build_if_missing:
+            raise MPSGError(f"libmpsg.so not built ({LIBPATH}); run __graft_entry__.build()")
+        from .build import build
+        build()
+    L = C.CDLL(LIBPATH)
+    vp, i32, i64, f64, u32 = C.c_void_p, C.c_int32, C.c_int64, C.c_double, C.c_uint32
+    P = C.POINTER
+    L.mpsg_last_error.restype = C.c_char_p
+    L.mpsg_ctx_create.argtypes = [i32, P(vp)]
+    L.mpsg_ctx_destroy.argtypes = [vp]
+    L.mpsg_ctx_destroy.restype = None
+    L.mpsg_ctx_set_stream.argtypes = [vp, vp]
+    L.mpsg_ctx_sync.argtypes = [vp]
+    L.mpsg_ctx_kernel_launches.argtypes = [vp]
+    L.mpsg_ctx_kernel_launches.restype = i64
+    L.mpsg_tensor_create.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, P(vp)]
+    L.mpsg_tensor_shape.argtypes = [vp, P(i32), P(i32), P(i64)]
+    L.mpsg_tensor_export.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.mpsg_tensor_device_view.argtypes = [vp, P(vp), vp]
+    L.mpsg_tensor_destroy.argtypes = [vp]
+    L.mpsg_tensor_destroy.restype = None
+    L.mpsg_contract_twosite.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i32, P(vp)]
+    L.mpsg_add_contraction_layer.argtypes = [vp, vp, vp, vp, vp, i32, i32, P(vp)]
+    L.mpsg_theta.argtypes = [vp, vp, vp, P(vp)]
+    L.mpsg_split2.argtypes = [vp, vp, vp, vp, u32, i32, f64, i32, P(vp), P(vp), P(vp), P(f64), P(u32)]
+    L.mpsg_lanczos2.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, i32, P(vp), P(f64), P(i32)]
+    L.mpsg_dmrg_create.argtypes = [vp, i32, vp, vp, vp, P(vp)]
+    L.mpsg_dmrg_set_options.argtypes = [vp, i32, i32, i32]
+    L.mpsg_dmrg_simulate.argtypes = [vp, u32, f64, u32, i32, f64, f64, i32, P(f64)]
+    L.mpsg_dmrg_prepare.argtypes = [vp]
+    L.mpsg_dmrg_do_step.argtypes = [vp, i32, i32, u32, i32, f64, f64, i32, P(f64)]
+    L.mpsg_dmrg_nsteps.argtypes = [vp]
+    L.mpsg_dmrg_steps.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.mpsg_dmrg_stats.argtypes = [vp, vp]
+    L.mpsg_dmrg_site.argtypes = [vp, i32, P(vp)]
+    L.mpsg_dmrg_lambda.argtypes = [vp, i32, P(vp)]
+    L.mpsg_dmrg_measure_energy.argtypes = [vp, P(f64)]
+    L.mpsg_dmrg_destroy.argtypes = [vp]
+    L.mpsg_dmrg_destroy.restype = None
+    _L = L
+    return L
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().mpsg_last_error().decode(errors="replace")
+        raise MPSGError(f"libmpsg error {rc}: {msg}")
+
+
+def ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
+
+
+class Context:
+    """mpsg_ctx: one GPU, one stream, the device memory pool and the solver handles."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        check(self.L.mpsg_ctx_create(device, C.byref(h)))
+        self.h = h
+
+    def sync(self):
+        check(self.L.mpsg_ctx_sync(self.h))
+
+    def kernel_launches(self) -> int:
+        return int(self.L.mpsg_ctx_kernel_launches(self.h))
+
+    def set_stream(self, stream_ptr: int | None):
+        check(self.L.mpsg_ctx_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def close(self):
+        if self.h:
+            self.L.mpsg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Tensor:
+    """mpsg_tensor handle (device-resident block-sparse tensor)."""
+
+    def __init__(self, ctx: Context, h):
+        self.ctx = ctx
+        self.h = h
+
+    @staticmethod
+    def from_dict(ctx: Context, bm: dict, nphys: int) -> "Tensor":
+        keys = sorted(bm.keys())
+        n = len(keys)
+        q = np.zeros(2 * max(n, 1), np.uint64)
+        p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+        rows = np.zeros(max(n, 1), np.int32)
+        cols = np.zeros(max(n, 1), np.int32)
+        chunks = []
+        for i, k in enumerate(keys):
+            a = np.asarray(bm[k], dtype=np.float64)
+            if nphys == 0:
+                q[2 * i] = q[2 * i + 1] = k
+                a = a.reshape(-1, 1)
+            else:
+                q[2 * i], q[2 * i + 1] = k[0], k[1]
+                for j in range(nphys):
+                    p[nphys * i + j] = k[2 + j]
+            rows[i], cols[i] = a.shape
+            chunks.append(a.ravel(order="F"))
+        data = np.ascontiguousarray(np.concatenate(chunks)) if chunks else np.zeros(1)
+        h = C.c_void_p()
+        check(ctx.L.mpsg_tensor_create(ctx.h, nphys, n, ptr(q), ptr(p), ptr(rows), ptr(cols), ptr(data),
+                                       C.byref(h)))
+        return Tensor(ctx, h)
+
+    def shape(self):
+        nphys, nb, ne = C.c_int32(), C.c_int32(), C.c_int64()
+        check(self.ctx.L.mpsg_tensor_shape(self.h, C.byref(nphys), C.byref(nb), C.byref(ne)))
+        return nphys.value, nb.value, ne.value
+
+    def to_dict(self) -> dict:
+        nphys, n, ne = self.shape()
+        q = np.zeros(2 * max(n, 1), np.uint64)
+        p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+        rows = np.zeros(max(n, 1), np.int32)
+        cols = np.zeros(max(n, 1), np.int32)
+        data = np.zeros(max(ne, 1))
+        check(self.ctx.L.mpsg_tensor_export(self.h, ptr(q), ptr(p), ptr(rows), ptr(cols), ptr(data)))
+        out, off = {}, 0
+        for i in range(n):
+            r, c = int(rows[i]), int(cols[i])
+            a = data[off:off + r * c].reshape((r, c), order="F").copy()
+            off += r * c
+            if nphys == 0:
+                out[int(q[2 * i])] = a[:, 0].copy()
+            elif nphys == 1:
+                out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[i]))] = a
+            else:
+                out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[2 * i]), int(p[2 * i + 1]))] = a
+        return out
+
+    def close(self):
+        if self.h:
+            self.ctx.L.mpsg_tensor_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class _MPOStruct(C.Structure):
+    _fields_ = [("nterms", C.c_int32), ("wl", C.c_void_p), ("wr", C.c_void_p), ("out", C.c_void_p),
+                ("in_", C.c_void_p), ("value", C.c_void_p), ("Dl", C.c_int32), ("Dr", C.c_int32)]
+
+
+class _ItoKeyStruct(C.Structure):
+    _fields_ = [("d", C.c_int32), ("charge", C.c_void_p)]
+
+
+class MPOArg:
+    """Keeps the numpy arrays behind an mpsg_mpo alive."""
+
+    def __init__(self, mpo):
+        terms, Dl, Dr = mpo
+        self.arrs = [np.ascontiguousarray([t[j] for t in terms] or [0], dtype=np.uint32) for j in range(4)]
+        self.val = np.ascontiguousarray([t[4] for t in terms] or [0.0], dtype=np.float64)
+        self.s = _MPOStruct(len(terms), *[ptr(a) for a in self.arrs], ptr(self.val), Dl, Dr)
+
+    def ref(self):
+        return C.byref(self.s)
+
+
+class ItoKeyArg:
+    def __init__(self, ik):
+        self.a = np.ascontiguousarray(ik, dtype=np.uint64)
+        self.s = _ItoKeyStruct(len(self.a), ptr(self.a))
+
+    def ref(self):
+        return C.byref(self.s)

@@ -587,7 +587,7 @@ static LanczosOut lanczos(const BM& L, const BM& R, const BM& Ainit, const MPOMa
     if (it >= itmax) break;
   }
   LanczosOut o;
-  o.iterations = it;
+  o.iterations = (int)es.size();  // number of Krylov vectors (matvecs) entering the ground state
   if (!es.empty()) {
     std::vector<double> z;
     tridiag(es, ks, &z);

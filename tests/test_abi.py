@@ -1,0 +1,53 @@
+"""CPU tests of the C ABI boundary: the in-tree library loads and exports every declared symbol."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "mpsg.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(mpsg_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("mpsg_contract_twosite", "mpsg_add_contraction_layer", "mpsg_split2", "mpsg_lanczos2",
+                 "mpsg_dmrg_simulate", "mpsg_tensor_create"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from mpstools_gb300 import build as B
+    lib = B.build()
+    L = ctypes.CDLL(lib)
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_context_creation_fails_cleanly_without_gpu():
+    """No GPU here: context creation must return an error code, not abort."""
+    from conftest import gpu_available
+    if gpu_available():
+        pytest.skip("GPU present")
+    from mpstools_gb300 import lib
+    L = lib.load()
+    h = ctypes.c_void_p()
+    rc = L.mpsg_ctx_create(0, ctypes.byref(h))
+    assert rc != 0
+    assert len(L.mpsg_last_error()) > 0
+
+
+def test_itokey_and_mpo_marshalling():
+    from mpstools_gb300 import lib, models as M
+    w = M.heisenberg_mpo(np.ones(3), np.ones(3), np.zeros(4))[1]
+    arg = lib.MPOArg(w)
+    assert arg.s.nterms == len(w[0]) and arg.s.Dl == 5 and arg.s.Dr == 5
+    k = lib.ItoKeyArg([0, 1])
+    assert k.s.d == 2

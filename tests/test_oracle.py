@@ -1,0 +1,119 @@
+"""CPU tests: the oracle against exact diagonalisation, dense contractions and the golden fixtures."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import ed
+from mpstools_gb300 import models as M
+from oracle import pyoracle as O
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _dmrg(W, sites, ik, chi, sweeps, threads=4):
+    g = O.DMRG(sites, W, ik, maxthreads=threads)
+    E = g.simulate(maxsteps=sweeps, EnConv=1e-300, chimax=chi, delta=1e-12)
+    return g, E
+
+
+@pytest.mark.parametrize("N", [6, 10, 12])
+def test_heisenberg_energy_matches_ed(N):
+    Nup = N // 2
+    Jz, Jxy, B = np.ones(N - 1), np.ones(N - 1), np.zeros(N)
+    W = M.heisenberg_mpo(Jz, Jxy, B)
+    ik = M.u1_itokeys(N)
+    g, E = _dmrg(W, M.product_state(M.filling_state(N, Nup), ik), ik, 256, 4)
+    assert abs(E - ed.xxz_ground_energy(Jz, Jxy, B, Nup)) < 1e-10
+    assert abs(g.measure() - E) < 1e-10
+
+
+def test_xxz_random_start_matches_ed():
+    N, Nup = 12, 6
+    Jz, Jxy, B = M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N)
+    W = M.heisenberg_mpo(Jz, Jxy, B)
+    ik = M.u1_itokeys(N)
+    _, E = _dmrg(W, M.random_u1_mps(N, Nup, 16, 12345), ik, 64, 4)
+    assert abs(E - ed.xxz_ground_energy(Jz, Jxy, B, Nup)) < 1e-10
+
+
+def test_tv_fermions_match_ed():
+    N, Nf = 10, 5
+    V, t, mu = 2.0 * M.uniform01(2, N - 1), np.ones(N - 1), np.zeros(N)
+    W = M.spinless_fermions_mpo(V, t, mu)
+    ik = M.u1_itokeys(N)
+    _, E = _dmrg(W, M.product_state(M.filling_state(N, Nf), ik), ik, 64, 4)
+    assert abs(E - ed.tv_ground_energy(V, t, mu, Nf)) < 1e-10
+
+
+def test_mpo_builders_agree():
+    N = 7
+    Jz, Jxy, B = M.xxz_couplings(N, 3), np.full(N - 1, 0.7), np.linspace(-0.3, 0.4, N)
+    assert M.heisenberg_mpo(Jz, Jxy, B) == O.heisenberg_mpo(Jz, Jxy, B)
+    V, t, mu = M.uniform01(4, N - 1), np.ones(N - 1), np.full(N, 0.25)
+    assert M.spinless_fermions_mpo(V, t, mu) == O.spinless_fermions_mpo(V, t, mu)
+
+
+def _env_case(seed=7, N=12, chi=12, site=4):
+    Jz = M.xxz_couplings(N, 1)
+    W = M.heisenberg_mpo(Jz, np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    g = O.DMRG(M.random_u1_mps(N, N // 2, chi, seed), W, ik, maxthreads=2)
+    g.prepare()
+    for s in range(site):
+        g.do_step(s, 1, chi)
+    return g, W, ik
+
+
+def test_oracle_matvec_matches_dense_contraction():
+    g, W, ik = _env_case()
+    site = 4
+    L, R = g.env("L", site - 1), g.env("R", site + 2)
+    th = O.theta(g.site(site), g.site(site + 1))
+    rng = np.random.default_rng(0)
+    th = {k: rng.standard_normal(v.shape) for k, v in th.items()}
+    out = O.contract_twosite(L, R, th, W[site], W[site + 1], ik[site], ik[site + 1])
+    ref = ed.dense_heff_apply(L, R, th, W[site], W[site + 1], ik[site], ik[site + 1])
+    assert set(out) <= set(ref)
+    for k, v in ref.items():
+        got = out.get(k, np.zeros_like(v))
+        assert np.abs(got - v).max() < 1e-12 * max(1.0, np.abs(v).max())
+
+
+def test_oracle_env_update_matches_dense():
+    g, W, ik = _env_case()
+    site = 4
+    Lprev = g.env("L", site - 1)
+    A = g.site(site)
+    out = O.add_contraction_layer(Lprev, A, W[site], ik[site], 1)
+    # dense: L'[b',b;w'] = sum W[w,w'](out,in) A(a',b';in)^T L(a',a;w) A(a,b;out)
+    for (b1, b, w1), blk in out.items():
+        acc = np.zeros_like(blk)
+        for (wl, wr, so, si, v) in W[site][0]:
+            if wr != w1:
+                continue
+            for (a1, a, w), Lb in Lprev.items():
+                if w != wl:
+                    continue
+                au = A.get((a1, b1, si))
+                ad = A.get((a, b, so))
+                if au is None or ad is None:
+                    continue
+                acc += v * au.T @ Lb @ ad
+        assert np.abs(acc - blk).max() < 1e-12
+
+
+def test_golden_fixtures_reproduce():
+    """The committed fixtures (tests/golden/make_golden.py) are reproduced by the oracle."""
+    with open(os.path.join(GOLDEN, "ed_energies.json")) as f:
+        cases = json.load(f)
+    for c in cases:
+        assert abs(c["E_oracle"] - c["E_ed"]) < 1e-10
+    z = np.load(os.path.join(GOLDEN, "matvec_small.npz"), allow_pickle=False)
+    from golden_io import load_case
+    case = load_case(z)
+    out = O.contract_twosite(case["L"], case["R"], case["theta"], case["W1"], case["W2"], case["ik0"], case["ik1"])
+    assert set(out) == set(case["out"])
+    for k in out:
+        assert np.abs(out[k] - case["out"][k]).max() < 1e-13
