@@ -1,0 +1,450 @@
+"""Benchmark of the DMRG hot path on GB300 (one JSON line on stdout).
+
+Workload (config: XXZ chain L=100, Jxy=1, Delta_i ~ U[0.5,1.5] from seed 1, U(1) Sz_total=0,
+MPO bond dimension 5, at the chi=2048 end of the chi ramp): a seeded random U(1) MPS with
+chi=2048 on every bond, left-isometric left of the centre bond and right-isometric right of it.
+One step = one two-site DMRG update at the centre bond (DMRGengine::doStep: theta formation,
+Lanczos to the reference's energy criterion, SVD split with truncation to chi, environment
+update), alternating direction so consecutive steps stay on the same bond.
+
+value   = algorithmic matvec FLOPs executed inside the timed steps / total device time of the
+          steps (TFLOP/s); ms_per_step is the device time of one update.
+e2e     = the same metric through the C ABI with host buffers: per step the environments and the
+          two site tensors are uploaded (mpsg_tensor_create), the update runs through
+          mpsg_lanczos2 + mpsg_split2 + mpsg_add_contraction_layer and the results are
+          downloaded (mpsg_tensor_export).
+roofline: the grouped matvec GEMM timed alone with CUDA events, L2 flushed before each launch.
+--impl reference: the CPU oracle (restatement of the reference's C++/BLAS path) on the same
+          workload, one two-site update per step, all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DMRG sweep time + matvec TFLOP/s, mixed/batched vs FP64 GPU, dE/E<1e-10"
+L_SITES, NUP, CHI, SEED_MPS, SEED_DELTA = 100, 50, 2048, 12345, 1
+CENTER = L_SITES // 2 - 1
+
+
+def workload(chi=CHI, L=L_SITES):
+    from mpstools_gb300 import models as M
+    Nup = L // 2
+    center = L // 2 - 1
+    W = M.heisenberg_mpo(M.xxz_couplings(L, SEED_DELTA), np.ones(L - 1), np.zeros(L))
+    ik = M.u1_itokeys(L)
+    sites = M.random_mixed_canonical_mps(L, Nup, chi, SEED_MPS, center)
+    return W, ik, sites, center
+
+
+def config_dict(chi, L, prec):
+    return {"workload": f"xxz_L{L}_chi{chi}_centre_bond_two_site_update",
+            "model": "XXZ (Heisenberg MPO D=5), Jxy=1, Delta~U[0.5,1.5] seed 1",
+            "L": L, "Sz_total": 0, "chi": chi, "mpo_bond_dim": 5, "state": "seeded random U(1) MPS, mixed canonical",
+            "lanczos": "delta=1e-12, energy test every 5 iterations, itmax 500", "matvec_precision": prec,
+            "l2": "flushed (512 MiB write) before every timed step and every roofline launch"}
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM 8192^3 (best of 5) -- the FP64 denominator of the roofline."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+# ----------------------------------------------------------------------------- CPU oracle leg
+def cpu_update_seconds(W, ik, sites, center, chi, nsteps, threads, envs=None):
+    """Time `nsteps` two-site updates of the CPU oracle at the centre bond (setup untimed)."""
+    from oracle import pyoracle as O
+    N = len(sites)
+    window = [sites[i] if i in (center, center + 1) or envs is None else sites[i] for i in range(N)]
+    if envs is not None:
+        window = [sites[i] if i in (center, center + 1) else {} for i in range(N)]
+    g = O.DMRG(window, W, ik, maxthreads=threads, matvec_threads=threads)
+    if envs is None:
+        g.build_environments(center)
+    else:
+        g.set_env("L", center - 1, envs[0])
+        g.set_env("R", center + 2, envs[1])
+    ts = []
+    for i in range(nsteps):
+        t0 = time.perf_counter()
+        g.do_step(center, 1 if i % 2 == 0 else -1, chi)
+        ts.append(time.perf_counter() - t0)
+    st = g.steps()
+    return ts, st
+
+
+def reference_arm(args):
+    """--impl reference: the CPU oracle on the same workload, all host threads."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    W, ik, sites, center = workload(args.chi, args.L)
+    from oracle import pyoracle as O
+    g = O.DMRG(sites, W, ik, maxthreads=threads, matvec_threads=threads)
+    g.build_environments(center)
+    for i in range(args.warmup):
+        g.do_step(center, 1 if i % 2 == 0 else -1, args.chi)
+    n0 = len(g.steps())
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        g.do_step(center, 1 if (args.warmup + i) % 2 == 0 else -1, args.chi)
+    dt = time.perf_counter() - t0
+    st = g.steps()[n0:]
+    flops_per_mv = matvec_flops_host(g, W, ik, center)
+    mv = sum(s["iters"] for s in st)
+    value = flops_per_mv * mv / dt / 1e12
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(args.chi, args.L, "fp64 (CPU oracle, OpenBLAS dgemm)"),
+            "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} two-site updates at the centre bond (chi={args.chi})"},
+            "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "lanczos_iterations_per_step": mv / max(args.steps, 1)}
+    print(json.dumps(line), flush=True)
+
+
+def matvec_flops_host(g, W, ik, center):
+    """Algorithmic FLOPs of one centre-bond matvec, counted from the block tables like the GPU plan."""
+    from oracle import pyoracle as O  # noqa: F401
+    L = g.env("L", center - 1)
+    R = g.env("R", center + 2)
+    th = {}
+    A1, A2 = g.site(center), g.site(center + 1)
+    for (a, c, s1), x in A1.items():
+        for (c2, b, s2), y in A2.items():
+            if c2 == c:
+                th[(a, b, s1, s2)] = (x.shape[0], y.shape[1])
+    return count_matvec_flops(L, R, th, W[center], W[center + 1], ik[center], ik[center + 1])
+
+
+def count_matvec_flops(L, R, thdims, W1, W2, ik0, ik1):
+    """FLOPs of the factored schedule (stage A: X = sum L~ theta; stage C: out = sum X R~^T)."""
+    lt, xt, ot = {}, {}, {}
+    Rk = {k: v.shape for k, v in R.items()}
+    w2 = {}
+    for t in W2[0]:
+        w2.setdefault(t[0], []).append(t)
+    for (a1, a, wl), Lb in L.items():
+        for (wl_, wm, s1, s1p, v1) in W1[0]:
+            if wl_ != wl:
+                continue
+            for (wm_, wr, s2, s2p, v2) in w2.get(wm, []):
+                b = a + ik0[s1] + ik1[s2]
+                if (a, b, s1, s2) not in thdims:
+                    continue
+                b1 = a1 + ik0[s1p] + ik1[s2p]
+                if (b1, b, wr) not in Rk:
+                    continue
+                xk = (a1, b, wm, s1p, s2)
+                xt.setdefault(xk, {})[s1] = (Lb.shape[0], Lb.shape[1], thdims[(a, b, s1, s2)][1])
+                ot.setdefault((a1, b1, s1p, s2p), set()).add((xk, (b1, b, wm, s2p, s2), Rk[(b1, b, wr)][0]))
+    f = 0.0
+    for xk, segs in xt.items():
+        for (m, k, n) in segs.values():
+            f += 2.0 * m * n * k
+    for ok, prs in ot.items():
+        for (xk, rk, rb1) in prs:
+            m = next(iter(xt[xk].values()))[0]
+            kk = next(iter(xt[xk].values()))[2]
+            f += 2.0 * m * rb1 * kk
+    return f
+
+
+# ----------------------------------------------------------------------------- GPU arm
+def gpu_arm(args):
+    import torch
+    from mpstools_gb300 import api, lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prec = args.prec
+    W, ik, sites, center = workload(args.chi, args.L)
+    ctx = lib.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
+    eng.build_environments(center)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def one(i):
+        eng.do_step(center, 1 if i % 2 == 0 else -1, args.chi)
+
+    for i in range(args.warmup):
+        one(i)
+    st0 = eng.stats()
+    n_steps0 = len(eng.steps())
+    launches0 = ctx.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clk = ClockSampler()
+    clk.start()
+    times = []
+    for i in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        one(args.warmup + i)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    total = float(np.sum(times))
+    if dist:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    st1 = eng.stats()
+    launches = ctx.kernel_launches() - launches0
+    mv_flops = st1["matvec_flops"] - st0["matvec_flops"]
+    matvecs = st1["matvecs"] - st0["matvecs"]
+    value = mv_flops * world / total / 1e12
+    steps_rec = eng.steps()[n_steps0:]
+
+    # --------------------------------------------------------------- roofline: matvec kernel alone
+    L = eng.env_tensor("L", center - 1)
+    R = eng.env_tensor("R", center + 2)
+    A1, A2 = eng.site_tensor(center), eng.site_tensor(center + 1)
+    import ctypes as C
+    th0 = C.c_void_p()
+    lib.check(ctx.L.mpsg_theta(ctx.h, A1.h, A2.h, C.byref(th0)))
+    th0 = lib.Tensor(ctx, th0)
+    k0, k1 = lib.ItoKeyArg(ik[center]), lib.ItoKeyArg(ik[center + 1])
+    w1, w2 = lib.MPOArg(W[center]), lib.MPOArg(W[center + 1])
+    thc = C.c_void_p()
+    lib.check(ctx.L.mpsg_theta_closure(ctx.h, L.h, R.h, th0.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), C.byref(thc)))
+    thc = lib.Tensor(ctx, thc)
+    thout = C.c_void_p()
+    lib.check(ctx.L.mpsg_theta_closure(ctx.h, L.h, R.h, th0.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), C.byref(thout)))
+    thout = lib.Tensor(ctx, thout)
+    plan = lib.MatvecPlan(ctx, L, R, thc, W[center], W[center + 1], ik[center], ik[center + 1], lib.PREC[prec])
+    info = plan.info()
+    din, _ = thc.device_view()
+    dout, _ = thout.device_view()
+    for _ in range(3):
+        plan.execute(din, dout)
+    mvt = []
+    for _ in range(max(10, args.steps)):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.execute(din, dout)
+        e1.record(stream)
+        e1.synchronize()
+        mvt.append(e0.elapsed_time(e1) * 1e-3)
+    mv_avg = float(np.mean(mvt))
+    pk, pk_kind = peaks()
+    if prec == "fp64":
+        peak = fp64_peak_tflops(torch)
+        roof = {"bound": "fp64", "achieved": info["flops"] / mv_avg / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": info["flops"] / mv_avg / 1e12 / peak, "traffic": args.traffic_bytes,
+                "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 has no tensor-core path here)",
+                "kernel": "k_gemm_f64 (stage A + stage C of one matvec)", "flops_per_matvec": info["flops"],
+                "matvec_seconds": mv_avg}
+    else:
+        peak = pk["bf16_tflops"]
+        roof = {"bound": "tensor", "achieved": info["flops"] / mv_avg / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": info["flops"] / mv_avg / 1e12 / peak, "traffic": args.traffic_bytes,
+                "peak_source": f"bf16_tflops ({pk_kind})", "flops_per_matvec": info["flops"],
+                "matvec_seconds": mv_avg}
+
+    # --------------------------------------------------------------- e2e through the C ABI, host buffers
+    e2e = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)
+
+    # --------------------------------------------------------------- CPU baseline (bounded sample)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        envs = (L.to_dict(), R.to_dict())
+        sites_c = {center: A1.to_dict(), center + 1: A2.to_dict()}
+        threads = os.cpu_count() or 1
+        ts, st = cpu_update_seconds_window(W, ik, sites_c, center, args.chi, 1, threads, envs, args.L)
+        cpu_mv = sum(s["iters"] for s in st)
+        cpu_value = info["flops"] * cpu_mv / sum(ts) / 1e12
+        cpu = {"value": cpu_value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+               "sample": f"1 two-site update at the centre bond (chi={args.chi}), {cpu_mv} Lanczos matvecs, "
+                         f"{sum(ts):.2f} s"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else prec,
+                "data": "synthetic", "config": config_dict(args.chi, args.L, prec), "clocks": clocks,
+                "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+                "lanczos_matvecs_per_step": matvecs / args.steps,
+                "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
+                "env_seconds_per_step": (st1["env_seconds"] - st0["env_seconds"]) / args.steps,
+                "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
+                "matvec_flops_reference_schedule": info["flops_ref"]}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_update_seconds_window(W, ik, sites_c, center, chi, nsteps, threads, envs, N):
+    from oracle import pyoracle as O
+    window = [sites_c.get(i, {}) for i in range(N)]
+    g = O.DMRG(window, W, ik, maxthreads=threads, matvec_threads=threads)
+    g.set_env("L", center - 1, envs[0])
+    g.set_env("R", center + 2, envs[1])
+    ts = []
+    for i in range(nsteps):
+        t0 = time.perf_counter()
+        g.do_step(center, 1 if i % 2 == 0 else -1, chi)
+        ts.append(time.perf_counter() - t0)
+    return ts, g.steps()
+
+
+def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
+    """Two-site update through the reference-facing C ABI from host buffers."""
+    import ctypes as C
+    from mpstools_gb300 import lib
+    Lh = eng.env_tensor("L", center - 1).export_flat()
+    Rh = eng.env_tensor("R", center + 2).export_flat()
+    A1h = eng.site_tensor(center).export_flat()
+    A2h = eng.site_tensor(center + 1).export_flat()
+    w1, w2 = lib.MPOArg(W[center]), lib.MPOArg(W[center + 1])
+    k0, k1 = lib.ItoKeyArg(ik[center]), lib.ItoKeyArg(ik[center + 1])
+    h2d = sum(x[5].nbytes + x[1].nbytes + x[2].nbytes + x[3].nbytes * 2 for x in (Lh, Rh, A1h, A2h))
+    d2h = [0]
+    flops = [0.0]
+
+    def step(i):
+        tL, tR = lib.Tensor.from_flat(ctx, Lh), lib.Tensor.from_flat(ctx, Rh)
+        t1, t2 = lib.Tensor.from_flat(ctx, A1h), lib.Tensor.from_flat(ctx, A2h)
+        st, E0, it = C.c_void_p(), C.c_double(), C.c_int32()
+        lib.check(ctx.L.mpsg_lanczos2(ctx.h, tL.h, tR.h, t1.h, t2.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), 500,
+                                      1e-12, 1, lib.PREC[prec], 0, C.byref(st), C.byref(E0), C.byref(it)))
+        psi = lib.Tensor(ctx, st)
+        U, V, lam = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tw, chi = C.c_double(), C.c_uint32()
+        lib.check(ctx.L.mpsg_split2(ctx.h, psi.h, k0.ref(), k1.ref(), args.chi, 0, 1e-12, 1, C.byref(U), C.byref(V),
+                                    C.byref(lam), C.byref(tw), C.byref(chi)))
+        U, V, lam = lib.Tensor(ctx, U), lib.Tensor(ctx, V), lib.Tensor(ctx, lam)
+        Lo = C.c_void_p()
+        lib.check(ctx.L.mpsg_add_contraction_layer(ctx.h, tL.h, U.h, w1.ref(), k0.ref(), 1, lib.PREC[prec],
+                                                   C.byref(Lo)))
+        Lo = lib.Tensor(ctx, Lo)
+        outs = [U.export_flat(), V.export_flat(), lam.export_flat(), Lo.export_flat()]
+        d2h[0] = sum(o[5].nbytes for o in outs)
+        return it.value
+
+    for i in range(2):
+        step(i)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = max(2, min(args.steps, 5))
+    mvs = 0
+    for i in range(n):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        mvs += step(i)
+        torch.cuda.synchronize()
+        t0 += 0
+        flops[0] += time.perf_counter() - a
+    # FLOPs of the e2e updates: same centre-bond matvec as the device-resident leg
+    return {"mvs": mvs, "seconds": flops[0], "steps": n, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h[0])}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--chi", type=int, default=CHI)
+    ap.add_argument("--L", type=int, default=L_SITES)
+    ap.add_argument("--prec", default="fp64")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic-bytes", type=float, default=None)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -105,6 +105,26 @@ mpsg_status mpsg_add_contraction_layer(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor
                                        const mpsg_itokey* ik, int32_t direction, mpsg_prec prec,
                                        mpsg_tensor* out);
 
+/* Persistent matvec plan for repeated application (the Lanczos use of contractTwosite,
+ * src/lanzcos.hpp:197): theta_layout fixes the block structure of both the input and the
+ * output vector (every block the matvec can reach must be present; see mpsg_theta_closure).
+ * The combined environments are built once; execute() is asynchronous on the context stream
+ * and reads/writes device arenas laid out like theta_layout (mpsg_tensor_device_view). */
+typedef struct mpsg_matvec_plan_s* mpsg_matvec_plan;
+mpsg_status mpsg_matvec2_plan_create(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta_layout,
+                                     const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
+                                     const mpsg_itokey* ikr, mpsg_prec prec, mpsg_matvec_plan* out);
+mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta_in, double* theta_out);
+/* info[0] algorithmic FLOPs of one application, info[1] FLOPs of the reference's per-term
+ * schedule, info[2] algorithmic bytes 8*(|L|+|R|+2|theta|), info[3] kernel launches per application. */
+mpsg_status mpsg_matvec2_plan_info(mpsg_matvec_plan plan, double* info4);
+void mpsg_matvec2_plan_destroy(mpsg_matvec_plan plan);
+/* Smallest superset of theta's blocks closed under the matvec (the structure the reference's
+ * Lanczos vectors reach); out holds zeros in the added blocks and theta's values elsewhere. */
+mpsg_status mpsg_theta_closure(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta, const mpsg_mpo* Wl,
+                               const mpsg_mpo* Wr, const mpsg_itokey* ikl, const mpsg_itokey* ikr,
+                               mpsg_tensor* out);
+
 /* BlockMatrix<2>(A1, A2): theta formation  -- src/BlockTensor.hpp:285-301. */
 mpsg_status mpsg_theta(mpsg_ctx ctx, mpsg_tensor A1, mpsg_tensor A2, mpsg_tensor* out);
 
@@ -141,14 +161,21 @@ mpsg_status mpsg_dmrg_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, ui
 mpsg_status mpsg_dmrg_prepare(mpsg_dmrg e);
 mpsg_status mpsg_dmrg_do_step(mpsg_dmrg e, int32_t site, int32_t dir, uint32_t chimax, int32_t doTrunc,
                               double tr_weight, double delta, int32_t testenergy, double* E);
+/* Environments of the current MPS without canonicalising it: L[-1..center-1] from the left
+ * edge and R[N..center+2] from the right edge (getLMin / getRMax / addContractionLayer), so a
+ * mixed-canonical state (e.g. a checkpoint) can be resumed at bond (center, center+1). */
+mpsg_status mpsg_dmrg_build_environments(mpsg_dmrg e, int32_t center);
+/* Copy of an environment: which = 0 for L[site], 1 for R[site]. */
+mpsg_status mpsg_dmrg_env(mpsg_dmrg e, int32_t which, int32_t site, mpsg_tensor* out);
 /* Step records appended by every doStep. */
 int32_t mpsg_dmrg_nsteps(mpsg_dmrg e);
 mpsg_status mpsg_dmrg_steps(mpsg_dmrg e, int32_t* site, int32_t* dir, int32_t* iters, int32_t* chi,
                             double* E, double* tw);
-/* Accumulated counters: [0] matvecs, [1] matvec FLOPs (algorithmic), [2] matvec seconds
- * (device events), [3] env-update seconds, [4] split seconds, [5] lanczos seconds (total),
- * [6] theta FLOPs in env updates, [7] wall seconds of simulate. */
-mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* stats8);
+/* Accumulated counters: [0] matvecs, [1] matvec FLOPs (algorithmic), [2] Lanczos iteration
+ * seconds (device events around the batched iterations), [3] env-update seconds, [4] split
+ * seconds, [5] Lanczos seconds (wall), [6] env-update FLOPs, [7] wall seconds of simulate,
+ * [8] device seconds of all doStep calls (events), [9] number of doStep calls. */
+mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* stats10);
 mpsg_status mpsg_dmrg_site(mpsg_dmrg e, int32_t site, mpsg_tensor* out);
 mpsg_status mpsg_dmrg_lambda(mpsg_dmrg e, int32_t bond, mpsg_tensor* out);
 /* MPO::measure(mps) in FP64 on the GPU  -- src/MPOTypes.hpp:990-1020. */

@@ -154,11 +154,24 @@ class DMRGengine:
                      tw=float(tw[i])) for i in range(n)]
 
     def stats(self):
-        s = np.zeros(8)
+        s = np.zeros(10)
         check(self.ctx.L.mpsg_dmrg_stats(self.h, lib.ptr(s)))
-        keys = ["matvecs", "matvec_flops", "matvec_seconds", "env_seconds", "split_seconds", "lanczos_seconds",
-                "env_flops", "wall_seconds"]
+        keys = ["matvecs", "matvec_flops", "lanczos_iter_seconds", "env_seconds", "split_seconds",
+                "lanczos_seconds", "env_flops", "wall_seconds", "step_device_seconds", "step_calls"]
         return dict(zip(keys, s.tolist()))
+
+    def build_environments(self, center):
+        check(self.ctx.L.mpsg_dmrg_build_environments(self.h, int(center)))
+
+    def env_tensor(self, which, site):
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_dmrg_env(self.h, 1 if which == "R" else 0, int(site), C.byref(h)))
+        return Tensor(self.ctx, h)
+
+    def site_tensor(self, s):
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_dmrg_site(self.h, int(s), C.byref(h)))
+        return Tensor(self.ctx, h)
 
     def site(self, s):
         h = C.c_void_p()

@@ -81,7 +81,45 @@ struct Engine {
     L[-1] = lmin(ctx);
   }
 
+  void build_environments(int c) {
+    MPSG_CHECK(c >= 0 && c + 1 < N, "center out of range");
+    auto t0 = std::chrono::steady_clock::now();
+    L.clear();
+    L[-1] = lmin(ctx);
+    for (int s = 0; s < c; ++s) L[s] = env_update(ctx, *L[s - 1], *mps[s], mpo[s], ik[s], 1, &env_flops);
+    R.clear();
+    R[N] = rmax(ctx, *mps[N - 1]);
+    for (int s = N - 1; s >= c + 2; --s) R[s] = env_update(ctx, *R[s + 1], *mps[s], mpo[s], ik[s], 0, &env_flops);
+    ctx->sync();
+    env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double step_device_seconds = 0;
+  int64_t nstep_calls = 0;
+
   StepRec do_step(int site, int dir, int chimax, bool doTrunc, double tr_weight, double delta, bool testenergy) {
+    if (!ev0) {
+      MPSG_CUDA(cudaEventCreate(&ev0));
+      MPSG_CUDA(cudaEventCreate(&ev1));
+    }
+    MPSG_CUDA(cudaEventRecord(ev0, ctx->stream));
+    StepRec r = do_step_impl(site, dir, chimax, doTrunc, tr_weight, delta, testenergy);
+    MPSG_CUDA(cudaEventRecord(ev1, ctx->stream));
+    MPSG_CUDA(cudaEventSynchronize(ev1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    step_device_seconds += ms * 1e-3;
+    ++nstep_calls;
+    return r;
+  }
+  ~Engine() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+
+  StepRec do_step_impl(int site, int dir, int chimax, bool doTrunc, double tr_weight, double delta,
+                       bool testenergy) {
     MPSG_CHECK(site >= 0 && site + 1 < N, "site out of range");
     MPSG_CHECK(L.count(site - 1) && R.count(site + 2), "environments missing (call prepare first)");
     const Tensor& Le = *L[site - 1];
@@ -167,6 +205,9 @@ struct Engine {
 
 struct mpsg_dmrg_s {
   Engine* e = nullptr;
+};
+struct mpsg_matvec_plan_s {
+  std::unique_ptr<MatvecPlan> p;
 };
 
 // ============================================================================ error plumbing
@@ -463,6 +504,87 @@ mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* st) {
   st[5] = g.lst.seconds;
   st[6] = g.env_flops;
   st[7] = g.wall;
+  st[8] = g.step_device_seconds;
+  st[9] = (double)g.nstep_calls;
+  API_END
+}
+mpsg_status mpsg_dmrg_build_environments(mpsg_dmrg e, int32_t center) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e, "null engine");
+  e->e->build_environments(center);
+  API_END
+}
+mpsg_status mpsg_dmrg_env(mpsg_dmrg e, int32_t which, int32_t site, mpsg_tensor* out) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e && out, "null argument");
+  auto& m = which ? e->e->R : e->e->L;
+  auto it = m.find(site);
+  MPSG_CHECK(it != m.end() && it->second, "environment not available");
+  *out = wrap(tensor_copy(*it->second));
+  e->e->ctx->sync();
+  API_END
+}
+
+mpsg_status mpsg_matvec2_plan_create(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta_layout,
+                                     const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
+                                     const mpsg_itokey* ikr, mpsg_prec prec, mpsg_matvec_plan* out) {
+  API_BEGIN
+  MPSG_CHECK(out, "null output");
+  check_prec(prec);
+  Ctx* c = C(ctx);
+  const Tensor& th = T(theta_layout);
+  MPSG_CHECK(th.nphys == 2, "theta_layout must be a two-site tensor");
+  Layout lay = layout_of(th);
+  auto P = build_matvec(c, T(L), T(R), lay, mpo_from_c(Wl), mpo_from_c(Wr), itokey_from_c(ikl), itokey_from_c(ikr),
+                        &lay);
+  mpsg_matvec_plan p = new mpsg_matvec_plan_s;
+  p->p = std::move(P);
+  *out = p;
+  API_END
+}
+mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta_in, double* theta_out) {
+  API_BEGIN
+  MPSG_CHECK(plan && plan->p, "null plan");
+  MPSG_CHECK(theta_in && theta_out && theta_in != theta_out, "matvec needs distinct input and output arenas");
+  plan->p->run(theta_in, theta_out);
+  MPSG_CUDA(cudaGetLastError());
+  API_END
+}
+mpsg_status mpsg_matvec2_plan_info(mpsg_matvec_plan plan, double* info) {
+  API_BEGIN
+  MPSG_CHECK(plan && plan->p && info, "null argument");
+  info[0] = plan->p->flops;
+  info[1] = plan->p->flops_ref;
+  info[2] = (double)plan->p->bytes_alg;
+  info[3] = (double)plan->p->launches_per_run();
+  API_END
+}
+void mpsg_matvec2_plan_destroy(mpsg_matvec_plan plan) {
+  if (!plan) return;
+  try {
+    plan->p.reset();
+  } catch (...) {
+  }
+  delete plan;
+}
+mpsg_status mpsg_theta_closure(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta, const mpsg_mpo* Wl,
+                               const mpsg_mpo* Wr, const mpsg_itokey* ikl, const mpsg_itokey* ikr,
+                               mpsg_tensor* out) {
+  API_BEGIN
+  MPSG_CHECK(out, "null output");
+  Ctx* c = C(ctx);
+  const Tensor& th = T(theta);
+  Layout sx = theta_closure(T(L), T(R), layout_of(th), mpo_from_c(Wl), mpo_from_c(Wr), itokey_from_c(ikl),
+                            itokey_from_c(ikr));
+  TensorP o = make_tensor(c, 2, sx, true);
+  std::vector<CopyOp> ops;
+  for (auto& b : th.b) {
+    const Block& nb = o->b[o->find(b.k)];
+    ops.push_back(CopyOp{th.d + b.off, o->d + nb.off, nullptr, nullptr, b.r, b.c, b.r, b.r, 0, 1.0});
+  }
+  run_copyops(c, ops);
+  c->sync();
+  *out = wrap(o);
   API_END
 }
 mpsg_status mpsg_dmrg_site(mpsg_dmrg e, int32_t site, mpsg_tensor* out) {

@@ -56,6 +56,7 @@ struct MatvecPlan {
   double flops_survey = 0;   // F_A + F_B + F_C of the factored (L.theta first) schedule
   int64_t bytes_alg = 0;     // 8*(|L|+|R|+2|theta|)
   void run(const double* theta_in, double* theta_out);
+  int launches_per_run() const { return (stageA.hprob.empty() ? 0 : 1) + (stageC.hprob.empty() ? 0 : 1); }
   ~MatvecPlan();
 };
 std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th_in,

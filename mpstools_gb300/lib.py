@@ -65,6 +65,14 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_measure_energy.argtypes = [vp, P(f64)]
     L.mpsg_dmrg_destroy.argtypes = [vp]
     L.mpsg_dmrg_destroy.restype = None
+    L.mpsg_dmrg_build_environments.argtypes = [vp, i32]
+    L.mpsg_dmrg_env.argtypes = [vp, i32, i32, P(vp)]
+    L.mpsg_matvec2_plan_create.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i32, P(vp)]
+    L.mpsg_matvec2_plan_execute.argtypes = [vp, vp, vp]
+    L.mpsg_matvec2_plan_info.argtypes = [vp, vp]
+    L.mpsg_matvec2_plan_destroy.argtypes = [vp]
+    L.mpsg_matvec2_plan_destroy.restype = None
+    L.mpsg_theta_closure.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, P(vp)]
     _L = L
     return L
 
@@ -142,6 +150,33 @@ class Tensor:
                                        C.byref(h)))
         return Tensor(ctx, h)
 
+    @staticmethod
+    def from_flat(ctx: Context, flat) -> "Tensor":
+        """flat = (nphys, q, p, rows, cols, data) as produced by pack_flat (no Python loops)."""
+        nphys, q, p, rows, cols, data = flat
+        h = C.c_void_p()
+        check(ctx.L.mpsg_tensor_create(ctx.h, nphys, len(rows), ptr(q), ptr(p), ptr(rows), ptr(cols), ptr(data),
+                                       C.byref(h)))
+        return Tensor(ctx, h)
+
+    def device_view(self):
+        """(device base pointer, element offsets of the blocks in key order)."""
+        _, nb, _ = self.shape()
+        d = C.c_void_p()
+        offs = np.zeros(max(nb, 1), np.int64)
+        check(self.ctx.L.mpsg_tensor_device_view(self.h, C.byref(d), ptr(offs)))
+        return d.value, offs[:nb]
+
+    def export_flat(self):
+        nphys, n, ne = self.shape()
+        q = np.zeros(2 * max(n, 1), np.uint64)
+        p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+        rows = np.zeros(max(n, 1), np.int32)
+        cols = np.zeros(max(n, 1), np.int32)
+        data = np.zeros(max(ne, 1))
+        check(self.ctx.L.mpsg_tensor_export(self.h, ptr(q), ptr(p), ptr(rows), ptr(cols), ptr(data)))
+        return (nphys, q, p, rows[:n], cols[:n], data)
+
     def shape(self):
         nphys, nb, ne = C.c_int32(), C.c_int32(), C.c_int64()
         check(self.ctx.L.mpsg_tensor_shape(self.h, C.byref(nphys), C.byref(nb), C.byref(ne)))
@@ -171,6 +206,62 @@ class Tensor:
     def close(self):
         if self.h:
             self.ctx.L.mpsg_tensor_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def pack_flat(bm: dict, nphys: int):
+    """dict block matrix -> (nphys, q, p, rows, cols, data) in key order."""
+    keys = sorted(bm.keys())
+    n = len(keys)
+    q = np.zeros(2 * max(n, 1), np.uint64)
+    p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
+    rows = np.zeros(max(n, 1), np.int32)
+    cols = np.zeros(max(n, 1), np.int32)
+    chunks = []
+    for i, k in enumerate(keys):
+        a = np.asarray(bm[k], dtype=np.float64)
+        if nphys == 0:
+            q[2 * i] = q[2 * i + 1] = k
+            a = a.reshape(-1, 1)
+        else:
+            q[2 * i], q[2 * i + 1] = k[0], k[1]
+            for j in range(nphys):
+                p[nphys * i + j] = k[2 + j]
+        rows[i], cols[i] = a.shape
+        chunks.append(a.ravel(order="F"))
+    data = np.ascontiguousarray(np.concatenate(chunks)) if chunks else np.zeros(1)
+    return (nphys, q, p, rows[:n], cols[:n], data)
+
+
+class MatvecPlan:
+    """mpsg_matvec_plan: persistent two-site matvec on device arenas laid out like `layout`."""
+
+    def __init__(self, ctx, L, R, layout, W1, W2, ik0, ik1, prec=0):
+        self.ctx = ctx
+        self._keep = (MPOArg(W1), MPOArg(W2), ItoKeyArg(ik0), ItoKeyArg(ik1))
+        w1, w2, k0, k1 = self._keep
+        h = C.c_void_p()
+        check(ctx.L.mpsg_matvec2_plan_create(ctx.h, L.h, R.h, layout.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(),
+                                             int(prec), C.byref(h)))
+        self.h = h
+
+    def execute(self, din: int, dout: int):
+        check(self.ctx.L.mpsg_matvec2_plan_execute(self.h, C.c_void_p(din), C.c_void_p(dout)))
+
+    def info(self):
+        a = np.zeros(4)
+        check(self.ctx.L.mpsg_matvec2_plan_info(self.h, ptr(a)))
+        return dict(flops=a[0], flops_ref=a[1], bytes=a[2], launches=int(a[3]))
+
+    def close(self):
+        if self.h:
+            self.ctx.L.mpsg_matvec2_plan_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -245,6 +245,52 @@ def random_u1_mps(N, Nup, chi, seed, itokeys=None):
     return sites
 
 
+def random_mixed_canonical_mps(N, Nup, chi, seed, center, itokeys=None):
+    """Random U(1) MPS in mixed-canonical form around bond (center, center+1).
+
+    Sites left of `center` are left isometries (for every right charge b the stacked blocks
+    [A(a,b;s)] over (a,s) have orthonormal columns), sites right of center+1 are right
+    isometries (for every left charge a the blocks [B(a,b;s)] over (b,s) have orthonormal
+    rows); the two centre sites keep their N(0,1) entries.  Where a charge group has fewer
+    rows than columns the orthonormal side is swapped (the bond is larger than the sector's
+    exact dimension).  Isometries come from the QR factorisation of the seeded N(0,1) blocks.
+    """
+    sites = random_u1_mps(N, Nup, chi, seed, itokeys)
+    for x in list(range(center)) + list(range(center + 2, N)):
+        blocks = sites[x]
+        left = x < center
+        groups = {}
+        for k in sorted(blocks):
+            groups.setdefault(k[1] if left else k[0], []).append(k)
+        for _, ks in groups.items():
+            if left:
+                M = np.vstack([blocks[k] for k in ks])
+            else:
+                M = np.hstack([blocks[k] for k in ks]).T
+            r, c = M.shape
+            if r >= c:
+                Qm, _ = np.linalg.qr(M)
+            else:
+                Qm, _ = np.linalg.qr(M.T)
+                Qm = Qm.T
+            if not left:
+                Qm = Qm.T
+            off = 0
+            for k in ks:
+                if left:
+                    n = blocks[k].shape[0]
+                    blocks[k] = np.ascontiguousarray(Qm[off:off + n, :])
+                else:
+                    n = blocks[k].shape[1]
+                    blocks[k] = np.ascontiguousarray(Qm[:, off:off + n])
+                off += n
+    for x in (center, center + 1):
+        nrm = np.sqrt(sum(float(np.vdot(v, v)) for v in sites[x].values()))
+        for k in sites[x]:
+            sites[x][k] = sites[x][k] / nrm
+    return sites
+
+
 def xxz_couplings(N, seed, lo=0.5, hi=1.5):
     """Delta_i ~ U[lo,hi] per bond (N-1 values) from splitmix64(seed)."""
     return lo + (hi - lo) * uniform01(seed, N - 1)

@@ -1100,6 +1100,21 @@ int orc_dmrg_prepare(void* ee) {
   g.L[-1] = get_lmin();
   return 0;
 }
+// environments of the current (mixed-canonical) MPS around bond (center, center+1)
+int orc_dmrg_build_envs(void* ee, int center) {
+  DMRG& g = ((orc_dmrg_t*)ee)->g;
+  MPS& mps = g.mps;
+  const int N = (int)mps.s.size();
+  g.L.clear();
+  g.L[-1] = get_lmin();
+  for (int s = 0; s < center; ++s)
+    g.L[s] = add_contraction_layer(g.L[s - 1], mps.s[s], g.mpo[s], mps.ik[s], 1, g.maxthreads);
+  g.R.clear();
+  g.R[N] = get_rmax(mps.s[N - 1]);
+  for (int s = N - 1; s >= center + 2; --s)
+    g.R[s] = add_contraction_layer(g.R[s + 1], mps.s[s], g.mpo[s], mps.ik[s], 0, g.maxthreads);
+  return 0;
+}
 double orc_dmrg_do_step(void* ee, int site, int dir, int chimax, int doTrunc, double tr_weight,
                         double delta, int testenergy) {
   return dmrg_step(((orc_dmrg_t*)ee)->g, site, dir, chimax, doTrunc != 0, tr_weight, delta, testenergy != 0).E;

@@ -85,6 +85,7 @@ def lib():
     L.orc_dmrg_simulate.restype = f64
     L.orc_dmrg_simulate.argtypes = [vp, i32, f64, i32, i32, f64, f64, i32]
     L.orc_dmrg_prepare.argtypes = [vp]
+    L.orc_dmrg_build_envs.argtypes = [vp, i32]
     L.orc_dmrg_do_step.restype = f64
     L.orc_dmrg_do_step.argtypes = [vp, i32, i32, i32, i32, f64, f64, i32]
     L.orc_dmrg_nsteps.argtypes = [vp]
@@ -295,6 +296,9 @@ class DMRG:
 
     def prepare(self):
         lib().orc_dmrg_prepare(self.h)
+
+    def build_environments(self, center):
+        lib().orc_dmrg_build_envs(self.h, int(center))
 
     def do_step(self, site, direction, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
         return lib().orc_dmrg_do_step(self.h, site, direction, chimax, int(doTrunc), tr_weight, delta,

@@ -95,7 +95,8 @@ def test_split_matches_oracle(ctx, chimax):
     g, W, ik = _case(chi=12)
     site = 4
     L, R = g.env("L", site - 1), g.env("R", site + 2)
-    _, _, psi = O.lanczos(L, R, g.site(site), g.site(site + 1), W[site], W[site + 1], ik[site], ik[site + 1])
+    th = O.theta(g.site(site), g.site(site + 1))
+    _, _, psi = O.lanczos(L, R, th, W[site], W[site + 1], ik[site], ik[site + 1])
     U0, V0, l0, tw0, chi0 = O.split(psi, ik[site], ik[site + 1], chimax)
     U1, V1, l1, tw1, chi1 = api.split(psi, (ik[site], ik[site + 1]), chimax, ctx=ctx)
     assert chi1 == chi0
@@ -111,7 +112,8 @@ def test_lanczos_matches_oracle(ctx):
     g, W, ik = _case(chi=12)
     site = 4
     L, R = g.env("L", site - 1), g.env("R", site + 2)
-    E0, it0, psi0 = O.lanczos(L, R, g.site(site), g.site(site + 1), W[site], W[site + 1], ik[site], ik[site + 1])
+    th = O.theta(g.site(site), g.site(site + 1))
+    E0, it0, psi0 = O.lanczos(L, R, th, W[site], W[site + 1], ik[site], ik[site + 1])
     lan = api.TSLanzcosEngine(L, R, g.site(site), g.site(site + 1), W[site], W[site + 1], ik[site], ik[site + 1],
                               ctx=ctx)
     lan.simulate(500, 1e-12, True)
