@@ -122,28 +122,6 @@ def fp64_peak_tflops(torch):
 
 
 # ----------------------------------------------------------------------------- CPU oracle leg
-def cpu_update_seconds(W, ik, sites, center, chi, nsteps, threads, envs=None):
-    """Time `nsteps` two-site updates of the CPU oracle at the centre bond (setup untimed)."""
-    from oracle import pyoracle as O
-    N = len(sites)
-    window = [sites[i] if i in (center, center + 1) or envs is None else sites[i] for i in range(N)]
-    if envs is not None:
-        window = [sites[i] if i in (center, center + 1) else {} for i in range(N)]
-    g = O.DMRG(window, W, ik, maxthreads=threads, matvec_threads=threads)
-    if envs is None:
-        g.build_environments(center)
-    else:
-        g.set_env("L", center - 1, envs[0])
-        g.set_env("R", center + 2, envs[1])
-    ts = []
-    for i in range(nsteps):
-        t0 = time.perf_counter()
-        g.do_step(center, 1 if i % 2 == 0 else -1, chi)
-        ts.append(time.perf_counter() - t0)
-    st = g.steps()
-    return ts, st
-
-
 def reference_arm(args):
     """--impl reference: the CPU oracle on the same workload, all host threads."""
     rank = int(os.environ.get("RANK", "0"))
@@ -239,7 +217,9 @@ def gpu_arm(args):
     prec = args.prec
     W, ik, sites, center = workload(args.chi, args.L)
     ctx = lib.Context(local)
-    stream = torch.cuda.current_stream()
+    # one explicit stream shared by the library, the L2 flush and the timing events
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
     eng.build_environments(center)
@@ -329,7 +309,12 @@ def gpu_arm(args):
                 "matvec_seconds": mv_avg}
 
     # --------------------------------------------------------------- e2e through the C ABI, host buffers
-    e2e = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)
+    e2e_raw = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)
+    e2e = {"value": info["flops"] * e2e_raw["matvecs"] * world / e2e_raw["seconds"] / 1e12, "unit": "TFLOP/s",
+           "h2d_bytes_per_step": e2e_raw["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e_raw["d2h_bytes_per_step"],
+           "ms_per_step": e2e_raw["seconds"] / e2e_raw["steps"] * 1e3, "steps": e2e_raw["steps"],
+           "path": "mpsg_tensor_create x4 -> mpsg_lanczos2 -> mpsg_split2 -> mpsg_add_contraction_layer -> "
+                   "mpsg_tensor_export x4 (host buffers, wall clock with device sync)"}
 
     # --------------------------------------------------------------- CPU baseline (bounded sample)
     cpu = None
@@ -412,19 +397,16 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
     for i in range(2):
         step(i)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
     n = max(2, min(args.steps, 5))
-    mvs = 0
+    mvs, secs = 0, 0.0
     for i in range(n):
         flush.zero_()
         torch.cuda.synchronize()
         a = time.perf_counter()
         mvs += step(i)
         torch.cuda.synchronize()
-        t0 += 0
-        flops[0] += time.perf_counter() - a
-    # FLOPs of the e2e updates: same centre-bond matvec as the device-resident leg
-    return {"mvs": mvs, "seconds": flops[0], "steps": n, "h2d_bytes_per_step": int(h2d),
+        secs += time.perf_counter() - a
+    return {"matvecs": mvs, "seconds": secs, "steps": n, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h[0])}
 
 

@@ -141,10 +141,9 @@ struct Engine {
     }
     Layout sx = theta_closure(Le, Re, s0, mpo[site], mpo[site + 1], ik[site], ik[site + 1]);
     TensorP th = theta_form(ctx, *mps[site], *mps[site + 1], &sx);
-    auto mv = build_matvec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], &sx);
     TensorP psi = make_tensor(ctx, 2, sx, true);
-    LanczosResult lr = lanczos(ctx, *mv, *th, *psi, lanmax, delta, testenergy, reorth, &lst);
-    mv.reset();
+    LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], *th, *psi,
+                                    lanmax, delta, testenergy, reorth, (int)prec, &lst);
     th.reset();
     auto t0 = std::chrono::steady_clock::now();
     SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
@@ -336,8 +335,14 @@ void mpsg_tensor_destroy(mpsg_tensor t) {
   delete t;
 }
 
-static void check_prec(mpsg_prec prec) {
+static void check_prec(mpsg_prec prec) {  // FP64 only (environment update, split)
   MPSG_CHECK(prec == MPSG_PREC_FP64, "only MPSG_PREC_FP64 is available for this entry point");
+}
+static void check_matvec_prec(mpsg_prec prec) {
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "matvec precision must be FP64, TF32(X3) or BF16(X3)");
+}
+static void check_lanczos_prec(mpsg_prec prec) {
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_AUTO, "unknown precision mode");
 }
 
 mpsg_status mpsg_contract_twosite(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta, const mpsg_mpo* Wl,
@@ -345,15 +350,16 @@ mpsg_status mpsg_contract_twosite(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mp
                                   mpsg_tensor* out) {
   API_BEGIN
   MPSG_CHECK(out, "null output");
-  check_prec(prec);
+  check_matvec_prec(prec);
   Ctx* c = C(ctx);
   const Tensor& th = T(theta);
   MPSG_CHECK(th.nphys == 2 && T(L).nphys == 1 && T(R).nphys == 1, "tensor kinds do not match");
   Layout lin = layout_of(th);
   auto P = build_matvec(c, T(L), T(R), lin, mpo_from_c(Wl), mpo_from_c(Wr), itokey_from_c(ikl), itokey_from_c(ikr),
-                        nullptr);
+                        nullptr, prec);
   TensorP o = make_tensor(c, 2, P->out, true);
   P->run(th.d, o->d);
+  P->check_error();
   c->sync();
   *out = wrap(o);
   API_END
@@ -402,16 +408,16 @@ mpsg_status mpsg_lanczos2(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tenso
                           mpsg_tensor* state, double* E0, int32_t* iterations) {
   API_BEGIN
   MPSG_CHECK(state, "null output");
-  check_prec(prec);
+  check_lanczos_prec(prec);
   Ctx* c = C(ctx);
   MPO w1 = mpo_from_c(Wl), w2 = mpo_from_c(Wr);
   ItoKey k0 = itokey_from_c(ikl), k1 = itokey_from_c(ikr);
   TensorP th0 = theta_form(c, T(mpsl), T(mpsr), nullptr);
   Layout sx = theta_closure(T(L), T(R), layout_of(*th0), w1, w2, k0, k1);
   TensorP th = theta_form(c, T(mpsl), T(mpsr), &sx);
-  auto P = build_matvec(c, T(L), T(R), sx, w1, w2, k0, k1, &sx);
   TensorP psi = make_tensor(c, 2, sx, true);
-  LanczosResult r = lanczos(c, *P, *th, *psi, itmax, delta, testenergy != 0, reorth != 0, nullptr);
+  LanczosResult r = lanczos_prec(c, T(L), T(R), sx, w1, w2, k0, k1, *th, *psi, itmax, delta, testenergy != 0,
+                                 reorth != 0, (int)prec, nullptr);
   c->sync();
   *state = wrap(psi);
   if (E0) *E0 = r.E0;
@@ -446,7 +452,7 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
 mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax) {
   API_BEGIN
   MPSG_CHECK(e && e->e, "null engine");
-  check_prec(prec);
+  check_lanczos_prec(prec);
   MPSG_CHECK(lanmax >= 1 && lanmax <= 1000, "lanmax must be in [1, 1000]");
   e->e->prec = prec;
   e->e->reorth = reorth != 0;
@@ -530,13 +536,13 @@ mpsg_status mpsg_matvec2_plan_create(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R,
                                      const mpsg_itokey* ikr, mpsg_prec prec, mpsg_matvec_plan* out) {
   API_BEGIN
   MPSG_CHECK(out, "null output");
-  check_prec(prec);
+  check_matvec_prec(prec);
   Ctx* c = C(ctx);
   const Tensor& th = T(theta_layout);
   MPSG_CHECK(th.nphys == 2, "theta_layout must be a two-site tensor");
   Layout lay = layout_of(th);
   auto P = build_matvec(c, T(L), T(R), lay, mpo_from_c(Wl), mpo_from_c(Wr), itokey_from_c(ikl), itokey_from_c(ikr),
-                        &lay);
+                        &lay, prec);
   mpsg_matvec_plan p = new mpsg_matvec_plan_s;
   p->p = std::move(P);
   *out = p;

@@ -76,20 +76,230 @@ MatvecPlan::~MatvecPlan() {
     ctx->dfree(dLt);
     ctx->dfree(dRt);
     ctx->dfree(dX);
+    for (int i = 0; i < 4; ++i) ctx->dfree(dimg[i]);
+    for (int i = 0; i < 2; ++i) {
+      ctx->dfree(dprob[i]);
+      ctx->dfree(dseg[i]);
+      ctx->dfree(dtile[i]);
+    }
+    ctx->dfree(dconv_theta);
+    ctx->dfree(derr);
   }
 }
 
+static TcBases tc_bases(MatvecPlan& P, const double* theta_in, double* theta_out) {
+  TcBases B;
+  for (int i = 0; i < 6; ++i) {
+    B.img[i] = nullptr;
+    B.lo_off[i] = 0;
+    B.f64[i] = nullptr;
+  }
+  for (int i = 0; i < 4; ++i) {
+    B.img[i] = P.dimg[i];
+    B.lo_off[i] = P.img_hi[i];
+  }
+  B.f64[0] = const_cast<double*>(theta_in);
+  B.f64[1] = theta_out;
+  B.f64[2] = P.dLt;
+  B.f64[3] = P.dRt;
+  B.err = P.derr;
+  return B;
+}
+
 void MatvecPlan::run(const double* theta_in, double* theta_out) {
-  const double* bases[8] = {dLt, theta_in, dX, dRt, theta_out, nullptr, nullptr, nullptr};
-  stageA.run(bases);
-  stageC.run(bases);
+  if (prec == MPSG_PREC_FP64) {
+    const double* bases[8] = {dLt, theta_in, dX, dRt, theta_out, nullptr, nullptr, nullptr};
+    stageA.run(bases);
+    stageC.run(bases);
+    return;
+  }
+  const TcBases B = tc_bases(*this, theta_in, theta_out);
+  launch_tc_convert(kind, nprod == 3 ? 2 : 1, dconv_theta, nconv_theta, nimg_theta, B, ctx->stream);
+  launch_tc_gemm(kind, nprod, dprob[0], dseg[0], dtile[0], ntile[0], B, nsm, ctx->stream);
+  launch_tc_gemm(kind, nprod, dprob[1], dseg[1], dtile[1], ntile[1], B, nsm, ctx->stream);
+}
+
+void MatvecPlan::check_error() {
+  if (!derr) return;
+  int e = 0;
+  MPSG_CUDA(cudaMemcpyAsync(&e, derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  ctx->sync();
+  if (e) throw Err(5, "tensor-core matvec: a bounded device wait expired (code " + std::to_string(e) + ")");
+}
+
+// Tile-image arenas, conversion ops and tcgen05 work lists of the mixed-precision matvec.
+template <class K>
+static int64_t add_images(std::map<K, int64_t>& off, const K& key, int rows, int cols, int KC, int64_t& total) {
+  auto it = off.find(key);
+  if (it != off.end()) return it->second;
+  const int64_t nimg = (int64_t)((rows + 127) / 128) * ((cols + KC - 1) / KC);
+  off[key] = total;
+  total += nimg * 16384;
+  return off[key];
+}
+
+static void build_tc(MatvecPlan& P, Ctx* ctx, const Layout& th,
+                     const std::map<K5, std::map<uint32_t, std::pair<K5, int>>>& xterms,
+                     const std::map<BKey, std::set<std::pair<K5, K5>>>& oterms) {
+  P.kind = (P.prec == MPSG_PREC_TF32 || P.prec == MPSG_PREC_TF32X3) ? 0 : 1;
+  P.nprod = (P.prec == MPSG_PREC_TF32X3 || P.prec == MPSG_PREC_BF16X3) ? 3 : 1;
+  const int KC = P.kind == 0 ? 32 : 64;
+  const int ncomp = P.nprod == 3 ? 2 : 1;
+  int dev = 0;
+  MPSG_CUDA(cudaGetDevice(&dev));
+  MPSG_CUDA(cudaDeviceGetAttribute(&P.nsm, cudaDevAttrMultiProcessorCount, dev));
+  auto nkc = [&](int k) { return (k + KC - 1) / KC; };
+  std::map<K5, int64_t> lt_img, rt_img, x_img;
+  std::map<int, int64_t> th_img;
+  int64_t tot[4] = {0, 0, 0, 0};
+  std::vector<TcConv> conv_env, conv_th;
+  int img_env = 0, img_th = 0;
+  auto conv = [&](std::vector<TcConv>& v, int& img, int src_slot, int64_t src_off, int R, int K, int rs, int ks,
+                  int dst_slot, int64_t dst_off) {
+    TcConv c;
+    c.src_off = src_off;
+    c.dst_off = dst_off;
+    c.R = R;
+    c.K = K;
+    c.rs = rs;
+    c.ks = ks;
+    c.nkc = nkc(K);
+    c.img0 = img;
+    c.scale = 1.0;
+    c.src_slot = (int8_t)src_slot;
+    c.dst_slot = (int8_t)dst_slot;
+    img += ((R + 127) / 128) * c.nkc;
+    v.push_back(c);
+  };
+  for (auto& x : P.lt.m) {  // A operand of stage A: rows a', K = a (column-major source)
+    const int64_t o = add_images(lt_img, x.first, x.second.r, x.second.c, KC, tot[0]);
+    conv(conv_env, img_env, 2, x.second.off, x.second.r, x.second.c, 1, x.second.r, 0, o);
+  }
+  for (auto& x : P.rt.m) {  // B operand of stage C: rows b', K = b (column-major source)
+    const int64_t o = add_images(rt_img, x.first, x.second.r, x.second.c, KC, tot[3]);
+    conv(conv_env, img_env, 3, x.second.off, x.second.r, x.second.c, 1, x.second.r, 3, o);
+  }
+  for (int i = 0; i < (int)th.b.size(); ++i) {  // B operand of stage A: rows b (columns of theta), K = a
+    const Block& b = th.b[i];
+    const int64_t o = add_images(th_img, i, b.c, b.r, KC, tot[1]);
+    conv(conv_th, img_th, 0, b.off, b.c, b.r, b.r, 1, 1, o);
+  }
+  for (auto& x : P.xa.m) add_images(x_img, x.first, x.second.r, x.second.c, KC, tot[2]);
+  for (int i = 0; i < 4; ++i) {
+    P.img_hi[i] = std::max<int64_t>(tot[i], 16384);
+    const size_t bytes = (size_t)P.img_hi[i] * ncomp;
+    P.dimg[i] = (uint8_t*)ctx->dmalloc(bytes);
+    MPSG_CUDA(cudaMemsetAsync(P.dimg[i], 0, bytes, ctx->stream));
+  }
+  P.derr = (int*)ctx->dmalloc(sizeof(int));
+  MPSG_CUDA(cudaMemsetAsync(P.derr, 0, sizeof(int), ctx->stream));
+  // work lists
+  for (int st = 0; st < 2; ++st) {
+    std::vector<TcProb> probs;
+    std::vector<TcSeg> segs;
+    std::vector<std::pair<int, TcTile>> tiles;  // (K chunks, tile)
+    auto add_prob = [&](TcProb p, const std::vector<TcSeg>& ss) {
+      p.seg0 = (int32_t)segs.size();
+      int work = 0;
+      for (auto& s : ss) {
+        segs.push_back(s);
+        work += s.nkc;
+      }
+      p.seg1 = (int32_t)segs.size();
+      const int pi = (int)probs.size();
+      probs.push_back(p);
+      for (int mt = 0; mt < (p.M + 127) / 128; ++mt)
+        for (int nt = 0; nt < (p.N + 127) / 128; ++nt) tiles.push_back({work, TcTile{pi, mt, nt}});
+    };
+    if (st == 0) {
+      for (auto& x : xterms) {
+        const auto& XB = P.xa.at(x.first);
+        TcProb p{};
+        p.c_off = x_img.at(x.first);
+        p.ldc = 0;
+        p.M = XB.r;
+        p.N = XB.c;
+        p.c_nkc = nkc(XB.c);
+        p.mode = 1;
+        p.c_slot = 2;
+        p.beta = 0;
+        std::vector<TcSeg> ss;
+        for (auto& s : x.second) {
+          const auto& LB = P.lt.at(s.second.first);
+          TcSeg g{};
+          g.a_off = lt_img.at(s.second.first);
+          g.b_off = th_img.at(s.second.second);
+          g.nkc = nkc(LB.c);
+          g.a_slot = 0;
+          g.b_slot = 1;
+          ss.push_back(g);
+        }
+        add_prob(p, ss);
+      }
+    } else {
+      for (auto& o : oterms) {
+        const Block& OB = P.out.b[P.out.idx.at(o.first)];
+        TcProb p{};
+        p.c_off = OB.off;
+        p.ldc = OB.r;
+        p.M = OB.r;
+        p.N = OB.c;
+        p.c_nkc = 0;
+        p.mode = 0;
+        p.c_slot = 1;
+        p.beta = 0;
+        std::vector<TcSeg> ss;
+        for (auto& pr : o.second) {
+          const auto& XB = P.xa.at(pr.first);
+          TcSeg g{};
+          g.a_off = x_img.at(pr.first);
+          g.b_off = rt_img.at(pr.second);
+          g.nkc = nkc(XB.c);
+          g.a_slot = 2;
+          g.b_slot = 3;
+          ss.push_back(g);
+        }
+        add_prob(p, ss);
+      }
+    }
+    std::stable_sort(tiles.begin(), tiles.end(),
+                     [](const std::pair<int, TcTile>& a, const std::pair<int, TcTile>& b) { return a.first > b.first; });
+    std::vector<TcTile> tl;
+    for (auto& t : tiles) tl.push_back(t.second);
+    P.ntile[st] = (int)tl.size();
+    P.dprob[st] = (TcProb*)ctx->dmalloc(sizeof(TcProb) * std::max<size_t>(probs.size(), 1));
+    P.dseg[st] = (TcSeg*)ctx->dmalloc(sizeof(TcSeg) * std::max<size_t>(segs.size(), 1));
+    P.dtile[st] = (TcTile*)ctx->dmalloc(sizeof(TcTile) * std::max<size_t>(tl.size(), 1));
+    if (!probs.empty())
+      MPSG_CUDA(cudaMemcpyAsync(P.dprob[st], probs.data(), sizeof(TcProb) * probs.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if (!segs.empty())
+      MPSG_CUDA(cudaMemcpyAsync(P.dseg[st], segs.data(), sizeof(TcSeg) * segs.size(), cudaMemcpyHostToDevice, ctx->stream));
+    if (!tl.empty())
+      MPSG_CUDA(cudaMemcpyAsync(P.dtile[st], tl.data(), sizeof(TcTile) * tl.size(), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  P.nconv_theta = (int)conv_th.size();
+  P.nimg_theta = img_th;
+  P.dconv_theta = (TcConv*)ctx->dmalloc(sizeof(TcConv) * std::max<size_t>(conv_th.size(), 1));
+  if (!conv_th.empty())
+    MPSG_CUDA(cudaMemcpyAsync(P.dconv_theta, conv_th.data(), sizeof(TcConv) * conv_th.size(), cudaMemcpyHostToDevice,
+                              ctx->stream));
+  // environments -> images, once per plan
+  if (!conv_env.empty()) {
+    TcConv* d = (TcConv*)ctx->dmalloc(sizeof(TcConv) * conv_env.size());
+    MPSG_CUDA(cudaMemcpyAsync(d, conv_env.data(), sizeof(TcConv) * conv_env.size(), cudaMemcpyHostToDevice, ctx->stream));
+    const TcBases B = tc_bases(P, nullptr, nullptr);
+    launch_tc_convert(P.kind, ncomp, d, (int)conv_env.size(), img_env, B, ctx->stream);
+    ctx->dfree(d);
+  }
 }
 
 std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th, const MPO& W1,
                                          const MPO& W2, const ItoKey& ik0, const ItoKey& ik1,
-                                         const Layout* out_layout) {
+                                         const Layout* out_layout, int prec) {
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "unsupported matvec precision");
   std::unique_ptr<MatvecPlan> P(new MatvecPlan());
   P->ctx = ctx;
+  P->prec = prec;
   std::map<K5, std::map<std::tuple<int, int, int>, double>> ltc, rtc;
   std::map<K5, std::map<uint32_t, std::pair<K5, int>>> xterms;
   std::map<BKey, std::set<std::pair<K5, K5>>> oterms;
@@ -158,7 +368,7 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
   }
   P->dLt = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->lt.nelem, 2));
   P->dRt = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->rt.nelem, 2));
-  P->dX = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->xa.nelem, 2));
+  if (prec == MPSG_PREC_FP64) P->dX = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P->xa.nelem, 2));
   // combined environments
   for (auto& x : ltc) {
     std::vector<std::pair<const double*, double>> terms;
@@ -206,6 +416,7 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
   for (auto& b : R.b) nr += (int64_t)b.r * b.c;
   for (auto& b : th.b) nt += (int64_t)b.r * b.c;
   P->bytes_alg = 8 * (nl + nr + 2 * nt);
+  if (prec != MPSG_PREC_FP64) build_tc(*P, ctx, th, xterms, oterms);
   return P;
 }
 
@@ -783,7 +994,8 @@ void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, do
 
 // ============================================================================ Lanczos
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
-                      bool testenergy, bool reorth, LanczosStats* st) {
+                      bool testenergy, bool reorth, LanczosStats* st, double tol_rel, int ndiag, double stall_rel) {
+  MPSG_CHECK(ndiag >= 1, "ndiag must be >= 1");
   auto t_start = std::chrono::steady_clock::now();
   const int64_t n = th_init.nelem;
   MPSG_CHECK(psi.nelem == n, "Lanczos state layout mismatch");
@@ -816,20 +1028,21 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   MPSG_CUDA(cudaEventCreate(&e1));
   std::vector<double> ha(na), hb(na), hn(na), hE(na);
   int it = 0, n_es = 0;
-  double eold = 1e100;
+  double eold = 1e100, dE_prev = 1e100;
   bool done = false;
   float mv_ms_total = 0;
   while (!done) {
-    // batch up to the next energy checkpoint (it % 5 == 0, it != 0) or itmax-1
+    // batch up to the next energy checkpoint (it % ndiag == 0, it != 0) or itmax-1
     int ck = it;
-    while (!((ck % 5 == 0 && ck != 0) || ck >= itmax - 1)) ++ck;
+    while (!((ck % ndiag == 0 && ck != 0) || ck >= itmax - 1)) ++ck;
     MPSG_CUDA(cudaEventRecord(e0, s));
     for (int j = it; j <= ck; ++j) {
       slot(j + 1);
       launch_scale_by_norm(V[j], n, d_norm2 + j, delta, d_beta + j, s);
       mv.run(V[j], w);
       launch_dot(w, V[j], n, ctx->part, d_alpha + j, s);
-      if (testenergy && j % 5 == 0 && j != 0) launch_tri_lowest(d_alpha, d_beta, j + 1, d_E + j / 5, nullptr, s);
+      if (testenergy && j % ndiag == 0 && j != 0)
+        launch_tri_lowest(d_alpha, d_beta, j + 1, d_E + j / ndiag, nullptr, s);
       launch_axpy3(V[j + 1], w, V[j], j > 0 ? V[j - 1] : nullptr, d_alpha + j, d_beta + j, n, ctx->part,
                    d_norm2 + j + 1, s);
       if (reorth) {
@@ -843,6 +1056,7 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
     MPSG_CUDA(cudaEventRecord(e1, s));
     MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dsc, sizeof(double) * (size_t)na * 4, cudaMemcpyDeviceToHost, s));
     ctx->sync();
+    mv.check_error();
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
     mv_ms_total += ms;
@@ -858,9 +1072,13 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
       const double k = std::sqrt(hn[j]);
       if (std::fabs(k) < delta) { n_es = j; done = true; break; }
       n_es = j + 1;
-      if (testenergy && j % 5 == 0 && j != 0) {
-        if (std::fabs(hE[j / 5] - eold) < delta) { done = true; break; }
-        eold = hE[j / 5];
+      if (testenergy && j % ndiag == 0 && j != 0) {
+        const double E = hE[j / ndiag], dE = std::fabs(E - eold);
+        if (dE < std::max(delta, tol_rel * std::fabs(E))) { done = true; break; }
+        // stall: below the stall level and no longer shrinking (noise floor of a low-precision matvec)
+        if (stall_rel > 0 && dE < stall_rel * std::fabs(E) && dE > 0.5 * dE_prev) { done = true; break; }
+        dE_prev = dE;
+        eold = E;
       }
       if (j + 1 >= itmax) { done = true; break; }
     }
@@ -887,6 +1105,49 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   ctx->sync();
   if (st) st->seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   return res;
+}
+
+// Relative energy-change floor of the Lanczos energy test per matvec precision (FP32 accumulation
+// bounds the hi/lo modes; single-product modes are limited by the 10 / 7 bit operands).
+static double prec_tol(int prec) {
+  switch (prec) {
+    case MPSG_PREC_TF32X3: return 1e-11;
+    case MPSG_PREC_BF16X3: return 1e-9;
+    case MPSG_PREC_TF32: return 1e-7;
+    case MPSG_PREC_BF16: return 1e-6;
+    default: return 0.0;
+  }
+}
+static double prec_stall(int prec) {
+  switch (prec) {
+    case MPSG_PREC_TF32X3: return 1e-9;
+    case MPSG_PREC_BF16X3: return 1e-7;
+    case MPSG_PREC_TF32: return 1e-5;
+    case MPSG_PREC_BF16: return 1e-4;
+    default: return 0.0;
+  }
+}
+
+LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
+                           const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
+                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st) {
+  if (prec == MPSG_PREC_FP64) {
+    auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
+    return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st);
+  }
+  const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_BF16X3 : prec;
+  LanczosResult r;
+  {
+    auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
+    r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo));
+  }
+  if (prec != MPSG_PREC_AUTO) return r;
+  // FP64 finish: Lanczos restarted from the mixed-precision ground state, energy test every iteration
+  auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
+  TensorP start = tensor_copy(psi);
+  LanczosResult r2 = lanczos(ctx, *mv64, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0);
+  r2.iterations += r.iterations;
+  return r2;
 }
 
 }  // namespace mpsg

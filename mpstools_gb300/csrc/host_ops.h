@@ -3,6 +3,7 @@
 #include <memory>
 
 #include "host_core.h"
+#include "tc_types.h"
 
 namespace mpsg {
 
@@ -55,13 +56,29 @@ struct MatvecPlan {
   double flops_ref = 0;      // FLOPs of the reference's per-term schedule (2 GEMMs per term)
   double flops_survey = 0;   // F_A + F_B + F_C of the factored (L.theta first) schedule
   int64_t bytes_alg = 0;     // 8*(|L|+|R|+2|theta|)
+  // tensor-core path (prec != FP64): operands as hi/lo tile images
+  int prec = MPSG_PREC_FP64;
+  int kind = 0, nprod = 3, nsm = 148;
+  uint8_t* dimg[4] = {nullptr, nullptr, nullptr, nullptr};  // L~, theta, X, R~ images
+  int64_t img_hi[4] = {0, 0, 0, 0};                         // bytes of the hi component per arena
+  TcProb* dprob[2] = {nullptr, nullptr};
+  TcSeg* dseg[2] = {nullptr, nullptr};
+  TcTile* dtile[2] = {nullptr, nullptr};
+  int ntile[2] = {0, 0};
+  TcConv* dconv_theta = nullptr;
+  int nconv_theta = 0, nimg_theta = 0;
+  int* derr = nullptr;
   void run(const double* theta_in, double* theta_out);
-  int launches_per_run() const { return (stageA.hprob.empty() ? 0 : 1) + (stageC.hprob.empty() ? 0 : 1); }
+  void check_error();  // throws MPSG_ERR_TIMEOUT when a bounded device wait expired
+  int launches_per_run() const {
+    if (prec != MPSG_PREC_FP64) return 3;
+    return (stageA.hprob.empty() ? 0 : 1) + (stageC.hprob.empty() ? 0 : 1);
+  }
   ~MatvecPlan();
 };
 std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th_in,
                                          const MPO& W1, const MPO& W2, const ItoKey& ik0, const ItoKey& ik1,
-                                         const Layout* out_layout);
+                                         const Layout* out_layout, int prec = MPSG_PREC_FP64);
 // Block keys reachable from `th` by repeated application of the matvec (reference semantics).
 Layout theta_closure(const Tensor& L, const Tensor& R, const Layout& th, const MPO& W1, const MPO& W2,
                      const ItoKey& ik0, const ItoKey& ik1);
@@ -113,8 +130,18 @@ struct LanczosResult {
   int iterations = 0;
   int n = 0;
 };
-// TSLanzcosEngine::simulate + getState(0): psi receives the ground state (layout of th_init)
+// TSLanzcosEngine::simulate + getState(0): psi receives the ground state (layout of th_init).
+// The energy test runs every ndiag iterations (reference: 5) and passes when
+// |E - E_prev| < max(delta, tol_rel*|E|); stall_rel > 0 also stops once |E - E_prev| is below
+// stall_rel*|E| and stopped shrinking (the noise floor of a low-precision matvec).
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
-                      bool testenergy, bool reorth, LanczosStats* st);
+                      bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
+                      double stall_rel = 0.0);
+// Lanczos in precision `prec` (mpsg_prec): FP64 is the reference loop; TF32/TF32X3/BF16/BF16X3 run
+// the loop with the tensor-core matvec and a precision-adapted energy test; AUTO runs BF16X3 first
+// and finishes with FP64 iterations restarted from the mixed-precision ground state.
+LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
+                           const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
+                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st);
 
 }  // namespace mpsg

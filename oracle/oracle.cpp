@@ -1100,6 +1100,12 @@ int orc_dmrg_prepare(void* ee) {
   g.L[-1] = get_lmin();
   return 0;
 }
+// replace one environment (which = 0: L[site], 1: R[site]) with a given block matrix
+int orc_dmrg_set_env(void* ee, int which, int site, void* bm) {
+  DMRG& g = ((orc_dmrg_t*)ee)->g;
+  (which ? g.R : g.L)[site] = ((orc_bm_t*)bm)->m;
+  return 0;
+}
 // environments of the current (mixed-canonical) MPS around bond (center, center+1)
 int orc_dmrg_build_envs(void* ee, int center) {
   DMRG& g = ((orc_dmrg_t*)ee)->g;

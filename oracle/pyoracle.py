@@ -86,6 +86,7 @@ def lib():
     L.orc_dmrg_simulate.argtypes = [vp, i32, f64, i32, i32, f64, f64, i32]
     L.orc_dmrg_prepare.argtypes = [vp]
     L.orc_dmrg_build_envs.argtypes = [vp, i32]
+    L.orc_dmrg_set_env.argtypes = [vp, i32, i32, vp]
     L.orc_dmrg_do_step.restype = f64
     L.orc_dmrg_do_step.argtypes = [vp, i32, i32, i32, i32, f64, f64, i32]
     L.orc_dmrg_nsteps.argtypes = [vp]
@@ -299,6 +300,11 @@ class DMRG:
 
     def build_environments(self, center):
         lib().orc_dmrg_build_envs(self.h, int(center))
+
+    def set_env(self, which, site, bm):
+        h = bm_to_handle(bm, 1)
+        lib().orc_dmrg_set_env(self.h, 1 if which == "R" else 0, int(site), h)
+        lib().orc_bm_free(h)
 
     def do_step(self, site, direction, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
         return lib().orc_dmrg_do_step(self.h, site, direction, chimax, int(doTrunc), tr_weight, delta,

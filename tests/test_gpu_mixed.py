@@ -1,0 +1,88 @@
+"""GPU tests of the tensor-core (tcgen05) matvec and the mixed-precision Lanczos / DMRG paths.
+
+Tolerances: max |mixed - FP64| relative to the largest |FP64| entry of the output:
+TF32X3 2e-5, BF16X3 3e-4, TF32 5e-3, BF16 4e-2 (FP32 accumulation over K <= a few hundred;
+hi/lo splits carry ~22 / ~16 significant bits, single TF32 / BF16 operands 11 / 8 bits).
+Energies of the AUTO path (BF16X3 Lanczos finished in FP64) agree with the FP64 oracle to 1e-10.
+"""
+import numpy as np
+import pytest
+
+from mpstools_gb300 import api, models as M
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"tf32x3": 2e-5, "bf16x3": 3e-4, "tf32": 5e-3, "bf16": 4e-2}
+
+
+def _case(N=16, chi=48, seed=7, site=6, model="xxz"):
+    if model == "xxz":
+        W = M.heisenberg_mpo(M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N))
+    else:
+        W = M.spinless_fermions_mpo(2.0 * M.uniform01(2, N - 1), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    g = O.DMRG(M.random_u1_mps(N, N // 2, chi, seed), W, ik, maxthreads=4)
+    g.prepare()
+    for s in range(site):
+        g.do_step(s, 1, chi)
+    return g, W, ik
+
+
+def _max_rel(a, b):
+    scale = max(np.abs(v).max() for v in b.values())
+    return max(np.abs(a[k] - b[k]).max() for k in b) / scale
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3", "tf32", "bf16"])
+@pytest.mark.parametrize("model", ["xxz", "tv"])
+def test_tc_matvec_matches_fp64(ctx, prec, model):
+    g, W, ik = _case(model=model)
+    site = 6
+    L, R = g.env("L", site - 1), g.env("R", site + 2)
+    th = O.theta(g.site(site), g.site(site + 1))
+    rng = np.random.default_rng(3)
+    th = {k: rng.standard_normal(v.shape) for k, v in th.items()}
+    ref = api.contractTwosite(L, R, th, W[site], W[site + 1], (ik[site], ik[site + 1]), prec="fp64", ctx=ctx)
+    got = api.contractTwosite(L, R, th, W[site], W[site + 1], (ik[site], ik[site + 1]), prec=prec, ctx=ctx)
+    assert set(got) == set(ref)
+    err = _max_rel(got, ref)
+    print(f"{model} {prec}: max rel err {err:.2e}")
+    assert err < TOL[prec], err
+
+
+def test_tc_matvec_large_blocks(ctx):
+    """Blocks larger than one 128x128 tile and K spanning several chunks (chi = 300)."""
+    g, W, ik = _case(N=14, chi=300, site=5)
+    site = 5
+    L, R = g.env("L", site - 1), g.env("R", site + 2)
+    th = O.theta(g.site(site), g.site(site + 1))
+    rng = np.random.default_rng(4)
+    th = {k: rng.standard_normal(v.shape) for k, v in th.items()}
+    ref = api.contractTwosite(L, R, th, W[site], W[site + 1], (ik[site], ik[site + 1]), prec="fp64", ctx=ctx)
+    assert max(v.shape[0] for v in th.values()) > 128
+    for prec in ("tf32x3", "bf16x3"):
+        got = api.contractTwosite(L, R, th, W[site], W[site + 1], (ik[site], ik[site + 1]), prec=prec, ctx=ctx)
+        err = _max_rel(got, ref)
+        print(f"large {prec}: {err:.2e}")
+        assert err < TOL[prec], (prec, err)
+
+
+@pytest.mark.parametrize("prec", ["auto", "tf32x3"])
+def test_mixed_dmrg_energy(ctx, prec):
+    N = 20
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    sites = M.random_u1_mps(N, N // 2, 32, 12345)
+    go = O.DMRG(sites, W, ik, maxthreads=8)
+    Eo = go.simulate(maxsteps=4, EnConv=1e-300, chimax=32, delta=1e-12)
+    gg = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
+    Eg = gg.simulate(maxsteps=4, EnConv=1e-300, chimax=32, delta=1e-12)
+    Em = gg.measure_energy()
+    rel = abs(Em - go.measure()) / abs(Eo)
+    print(f"{prec}: E_lanczos {Eg:.15f} E_measured {Em:.15f} oracle {Eo:.15f} rel {rel:.2e}")
+    if prec == "auto":
+        assert abs(Eg - Eo) <= 1e-10 * abs(Eo)
+        assert rel <= 1e-10
+    else:
+        assert rel <= 1e-7
