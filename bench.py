@@ -47,12 +47,12 @@ def workload(chi=CHI, L=L_SITES):
     return W, ik, sites, center
 
 
-def config_dict(chi, L, prec):
+def config_dict(chi, L, prec, svd="density"):
     return {"workload": f"xxz_L{L}_chi{chi}_centre_bond_two_site_update",
             "model": "XXZ (Heisenberg MPO D=5), Jxy=1, Delta~U[0.5,1.5] seed 1",
             "L": L, "Sz_total": 0, "chi": chi, "mpo_bond_dim": 5, "state": "seeded random U(1) MPS, mixed canonical",
             "lanczos": "delta=1e-12, energy test every 5 iterations, itmax 500", "matvec_precision": prec,
-            "l2": "flushed (512 MiB write) before every timed step and every roofline launch"}
+            "svd": svd, "l2": "flushed (512 MiB write) before every timed step and every roofline launch"}
 
 
 class ClockSampler:
@@ -221,6 +221,7 @@ def gpu_arm(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
+    ctx.set_svd_method(args.svd)
     eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
     eng.build_environments(center)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -333,7 +334,7 @@ def gpu_arm(args):
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else prec,
-                "data": "synthetic", "config": config_dict(args.chi, args.L, prec), "clocks": clocks,
+                "data": "synthetic", "config": config_dict(args.chi, args.L, prec, args.svd), "clocks": clocks,
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
                 "lanczos_matvecs_per_step": matvecs / args.steps,
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
@@ -419,6 +420,7 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--prec", default="fp64")
+    ap.add_argument("--svd", default="density", choices=["density", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
     args = ap.parse_args()

@@ -73,6 +73,11 @@ mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
 mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
+/* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
+ * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default),
+ * 1 = eigen-decomposition of the sector's reduced density matrix (FP64 Gram GEMM + syevd);
+ *     singular values below ~1e-8 of their sector's largest lose relative accuracy. */
+mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method);
 
 /* ------------------------------------------------------------------ tensors
  * nphys: 0 = lambda (DiagBlockMatrix: keys (q,q), blocks are n x 1 vectors),

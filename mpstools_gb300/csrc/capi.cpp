@@ -274,7 +274,13 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   C(ctx)->sync();
   API_END
 }
-int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count(); }
+int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count(); }
+mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
+  API_BEGIN
+  MPSG_CHECK(method == 0 || method == 1, "svd method must be 0 (Jacobi SVD) or 1 (density matrix)");
+  C(ctx)->svd_method = method;
+  API_END
+}
 
 mpsg_status mpsg_tensor_create(mpsg_ctx ctx, int32_t nphys, int32_t nblocks, const uint64_t* q, const uint32_t* p,
                                const int32_t* rows, const int32_t* cols, const double* host_data,

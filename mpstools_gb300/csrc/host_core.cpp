@@ -24,6 +24,7 @@ Ctx::Ctx(int dev) : device(dev) {
 Ctx::~Ctx() {
   if (solver) cusolverDnDestroy(solver);
   if (svdp) cusolverDnDestroyGesvdjInfo(svdp);
+  if (params) cusolverDnDestroyParams(params);
   if (part) cudaFreeAsync(part, stream);
   cudaStreamSynchronize(stream);
   if (hscal) cudaFreeHost(hscal);
@@ -48,6 +49,10 @@ cusolverDnHandle_t Ctx::svd_handle() {
   }
   cusolverDnSetStream(solver, stream);
   return solver;
+}
+cusolverDnParams_t Ctx::solver_params() {
+  if (!params && cusolverDnCreateParams(&params) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreateParams failed");
+  return params;
 }
 void Ctx::sync() { MPSG_CUDA(cudaStreamSynchronize(stream)); }
 

@@ -17,11 +17,14 @@ struct Ctx {
   gesvdjInfo_t svdp = nullptr;
   double* part = nullptr;     // reduction partials (kRedBlocks) + 64 scalars
   double* hscal = nullptr;    // pinned host scalars
+  int svd_method = 0;         // 0: Jacobi SVD (gesvdj), 1: density matrix (Gram + syevd)
   explicit Ctx(int dev);
   ~Ctx();
   void* dmalloc(size_t bytes);
   void dfree(void* p);
   cusolverDnHandle_t svd_handle();
+  cusolverDnParams_t params = nullptr;
+  cusolverDnParams_t solver_params();
   void sync();
 };
 

@@ -679,7 +679,200 @@ struct SvdBatch {
     if (!x.trans) { *ld = x.ns; return dV + x.offV; }
     *ld = x.ms; return dU + x.offU;
   }
-  void run() {
+  // Density-matrix route: G = Mst^T Mst (grouped FP64 GEMM), eigenpairs of G (cuSOLVER syevd, FP64),
+  // s = sqrt(lambda) descending, Vst = eigenvectors, Ust = Mst Vst / s.  Singular values below about
+  // 1e-8 of the sector's largest carry absolute errors ~1e-16/s (squared condition number).
+  // Batched density-matrix route: sectors are grouped by size class (next power of two >= ns, at
+  // least 32); each G_i = Mst_i^T Mst_i is written into the top-left corner of its class slot and the
+  // padding diagonal is set to -1, so the padded eigenvalues sort below the (non-negative) spectrum.
+  // One cusolverDnXsyevBatched call per class.
+  void run_gram() {
+    cusolverDnHandle_t h = ctx->svd_handle();
+    std::map<int, std::vector<int>> cls;  // class size -> sectors
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (s[i].k == 0) continue;
+      int c = 32;
+      while (c < s[i].ns) c <<= 1;
+      cls[c].push_back((int)i);
+    }
+    std::vector<int64_t> slot_off(s.size(), 0), lam_off(s.size(), 0), cls_of(s.size(), 0);
+    int64_t oB = 0, oW = 0;
+    for (auto& c : cls)
+      for (int i : c.second) {
+        slot_off[i] = oB;
+        lam_off[i] = oW;
+        cls_of[i] = c.first;
+        oB += (int64_t)c.first * c.first;
+        oW += c.first;
+      }
+    double* dB = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oB, 2));
+    double* dWv = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oW, 2));
+    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
+    int* dinf = (int*)ctx->dmalloc(sizeof(int) * (s.size() + 1));
+    MPSG_CUDA(cudaMemsetAsync(dB, 0, sizeof(double) * std::max<int64_t>(oB, 2), ctx->stream));
+    {  // G_i into the class slots, padding diagonal -1
+      GemmPlan g;
+      std::vector<double*> pads;
+      std::vector<GramPad> pd;
+      for (size_t i = 0; i < s.size(); ++i) {
+        const Sec& x = s[i];
+        if (x.k == 0) continue;
+        g.add_problem(2, slot_off[i], (int)cls_of[i], x.ns, x.ns, false,
+                      {GSegH{0, 0, x.offM, x.offM, x.ms, x.ms, x.ms, 1, 0, 1.0}});
+        pd.push_back(GramPad{dB + slot_off[i], (int32_t)cls_of[i], x.ns});
+      }
+      g.upload(ctx);
+      const double* bases[8] = {dM, nullptr, dB, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+      if (!pd.empty()) {
+        GramPad* d = (GramPad*)ctx->dmalloc(sizeof(GramPad) * pd.size());
+        MPSG_CUDA(cudaMemcpyAsync(d, pd.data(), sizeof(GramPad) * pd.size(), cudaMemcpyHostToDevice, ctx->stream));
+        launch_gram_pad(d, (int)pd.size(), ctx->stream);
+        ctx->dfree(d);
+      }
+    }
+    int ib = 0;
+    for (auto& c : cls) {
+      const int64_t n = c.first, batch = (int64_t)c.second.size();
+      double* A = dB + slot_off[c.second[0]];
+      double* W = dWv + lam_off[c.second[0]];
+      size_t wd = 0, wh = 0;
+      if (cusolverDnXsyevBatched_bufferSize(h, ctx->solver_params(), CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                            CUDA_R_64F, A, n, CUDA_R_64F, W, CUDA_R_64F, &wd, &wh, batch) !=
+          CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "syevBatched_bufferSize failed");
+      void* dwork = ctx->dmalloc(wd + 16);
+      std::vector<char> hwork(wh + 16);
+      if (cusolverDnXsyevBatched(h, ctx->solver_params(), CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, CUDA_R_64F,
+                                 A, n, CUDA_R_64F, W, CUDA_R_64F, dwork, wd, hwork.data(), wh, dinf + ib, batch) !=
+          CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "syevBatched failed");
+      ctx->sync();  // host workspace must outlive the call
+      ctx->dfree(dwork);
+      ib += (int)batch;
+    }
+    {
+      std::vector<int> inf(ib + 1, 0);
+      MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * (ib + 1), cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->sync();
+      for (int i = 0; i < ib; ++i)
+        if (inf[i] != 0) throw Err(3, "batched eigensolver failed (info=" + std::to_string(inf[i]) + ")");
+      MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(s.size(), 1), ctx->stream));
+    }
+    std::vector<GramPost> post;
+    for (size_t i = 0; i < s.size(); ++i) {
+      const Sec& x = s[i];
+      if (x.k == 0) continue;
+      const int64_t nc = cls_of[i], pad = nc - x.ns;
+      post.push_back(GramPost{dB + slot_off[i] + pad * nc, dWv + lam_off[i] + pad, dV + x.offV, dS + x.offS,
+                              dI + x.offS, x.ns, (int32_t)nc});
+    }
+    if (!post.empty()) {
+      GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, post.data(), sizeof(GramPost) * post.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_gram_post(d, (int)post.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    {  // Ust = Mst Vst, then columns scaled by 1/s
+      GemmPlan g;
+      std::vector<CopyOp> sc;
+      for (size_t i = 0; i < s.size(); ++i) {
+        const Sec& x = s[i];
+        if (x.k == 0) continue;
+        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
+        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
+      }
+      g.upload(ctx);
+      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+      run_copyops(ctx, sc);
+    }
+    ctx->dfree(dB);
+    ctx->dfree(dWv);
+    ctx->dfree(dI);
+    ctx->dfree(dinf);
+    fixphase();
+  }
+
+  // density-matrix route with one cuSOLVER syevd per sector (kept for comparison)
+  void run_gram_seq() {
+    cusolverDnHandle_t h = ctx->svd_handle();
+    int64_t oG = 0;
+    std::vector<int64_t> offG(s.size());
+    for (size_t i = 0; i < s.size(); ++i) {
+      offG[i] = oG;
+      oG += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+    }
+    double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
+    double* dL = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
+    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
+    {  // G_i = Mst_i^T Mst_i
+      GemmPlan g;
+      for (size_t i = 0; i < s.size(); ++i) {
+        const Sec& x = s[i];
+        if (x.k == 0) continue;
+        g.add_problem(2, offG[i], x.ns, x.ns, x.ns, false, {GSegH{0, 0, x.offM, x.offM, x.ms, x.ms, x.ms, 1, 0, 1.0}});
+      }
+      g.upload(ctx);
+      const double* bases[8] = {dM, nullptr, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+    }
+    int lwork = 0;
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (s[i].k == 0) continue;
+      int lw = 0;
+      if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, s[i].ns, dG + offG[i], s[i].ns,
+                                      dL + s[i].offS, &lw) != CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "syevd_bufferSize failed");
+      lwork = std::max(lwork, lw);
+    }
+    double* work = (double*)ctx->dmalloc(sizeof(double) * std::max(lwork, 2));
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (s[i].k == 0) continue;
+      if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, s[i].ns, dG + offG[i], s[i].ns,
+                           dL + s[i].offS, work, lwork, dinfo + i) != CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "syevd failed");
+    }
+    ctx->dfree(work);
+    // s, 1/s and Vst (eigenvectors in descending order)
+    std::vector<GramPost> post;
+    for (size_t i = 0; i < s.size(); ++i) {
+      if (s[i].k == 0) continue;
+      post.push_back(
+          GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns, s[i].ns});
+    }
+    if (!post.empty()) {
+      GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, post.data(), sizeof(GramPost) * post.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_gram_post(d, (int)post.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    {  // Ust = Mst Vst, then columns scaled by 1/s
+      GemmPlan g;
+      std::vector<CopyOp> sc;
+      for (size_t i = 0; i < s.size(); ++i) {
+        const Sec& x = s[i];
+        if (x.k == 0) continue;
+        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
+        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
+      }
+      g.upload(ctx);
+      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+      run_copyops(ctx, sc);
+    }
+    ctx->dfree(dG);
+    ctx->dfree(dL);
+    ctx->dfree(dI);
+    fixphase();
+  }
+
+  void run(int method) {
+    if (method == 1) run_gram();
+    else run_jacobi();
+  }
+
+  void run_jacobi() {
     cusolverDnHandle_t h = ctx->svd_handle();
     int lwork = 0;
     for (auto& x : s) {
@@ -701,6 +894,9 @@ struct SvdBatch {
       if (st != CUSOLVER_STATUS_SUCCESS) throw Err(3, "gesvdj failed");
     }
     ctx->dfree(work);
+    fixphase();
+  }
+  void fixphase() {
     std::vector<PhaseOp> ph;
     int maxk = 0;
     for (size_t i = 0; i < s.size(); ++i) {
@@ -731,7 +927,7 @@ struct SvdBatch {
     ctx->sync();
     for (size_t i = 0; i < s.size(); ++i)
       if (s[i].k > 0 && info[i] != 0)
-        throw Err(3, "gesvdj did not converge (info=" + std::to_string(info[i]) + ")");
+        throw Err(3, "SVD solver did not converge (info=" + std::to_string(info[i]) + ")");
   }
 };
 
@@ -775,7 +971,7 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
     }
   }
   run_copyops(ctx, gops);
-  sv.run();
+  sv.run(ctx->svd_method);
   // global truncation
   std::vector<int32_t> sec_of(sv.nS);
   for (size_t si = 0; si < qcs.size(); ++si)
@@ -903,7 +1099,7 @@ void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, do
     }
   }
   run_copyops(ctx, gops);
-  sv.run();
+  sv.run(ctx->svd_method);
   sv.check_info();
   std::vector<double> S(std::max<int64_t>(sv.nS, 1));
   if (sv.nS) MPSG_CUDA(cudaMemcpyAsync(S.data(), sv.dS, sizeof(double) * sv.nS, cudaMemcpyDeviceToHost, ctx->stream));

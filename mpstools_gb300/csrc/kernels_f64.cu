@@ -172,6 +172,37 @@ void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s) {
   LAUNCHED();
 }
 
+// ============================================================================ density-matrix SVD post-processing
+// s_i = sqrt(max(lambda_{n-1-i}, 0)), 1/s_i (0 for s_i = 0), V(:, i) = W(:, n-1-i)
+__global__ void k_gram_post(const GramPost* __restrict__ ops) {
+  const GramPost o = ops[blockIdx.x];
+  const int n = o.n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double l = o.lam[n - 1 - i];
+    const double sv = l > 0.0 ? sqrt(l) : 0.0;
+    o.S[i] = sv;
+    o.invS[i] = sv > 0.0 ? 1.0 / sv : 0.0;
+  }
+  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
+    const int r = (int)(e % n), c = (int)(e / n);
+    o.V[r + (int64_t)c * n] = o.W[r + (int64_t)(n - 1 - c) * o.ldw];
+  }
+}
+void launch_gram_post(const GramPost* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_gram_post<<<nops, 256, 0, s>>>(ops);
+  LAUNCHED();
+}
+__global__ void k_gram_pad(const GramPad* __restrict__ ops) {
+  const GramPad o = ops[blockIdx.x];
+  for (int i = o.n + threadIdx.x; i < o.nc; i += blockDim.x) o.A[i + (int64_t)i * o.nc] = -1.0;
+}
+void launch_gram_pad(const GramPad* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_gram_pad<<<nops, 128, 0, s>>>(ops);
+  LAUNCHED();
+}
+
 // ============================================================================ reductions
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -125,6 +125,18 @@ struct CopyOp {  // dst(i,j) = scale * rs[i] * cs[j] * (trans ? src(j,i) : src(i
   int32_t rows, cols, lds, ldd, trans;
   double scale;
 };
+struct GramPost {  // eigenpairs of G (ascending) -> s descending, 1/s, V = reversed eigenvectors (n x n)
+  const double* W;  // eigenvectors, column j at W + j*ldw
+  const double* lam;
+  double* V;
+  double* S;
+  double* invS;
+  int32_t n, ldw;
+};
+struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
+  double* A;
+  int32_t nc, n;
+};
 struct PhaseOp {  // FixPhase on one sector: Q (m x k, ldq) and P (n x k, ldp); sign from P columns
   double* Qm;
   double* Pm;
@@ -137,6 +149,8 @@ void launch_gemm_f64(const GProb* prob, const GSeg* seg, const GTile* tile, int 
 void launch_lincomb(const LCOut* outs, const LCTerm* terms, int nout, int64_t maxn, cudaStream_t s);
 void launch_copyops(const CopyOp* ops, int nops, cudaStream_t s);
 void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s);
+void launch_gram_post(const GramPost* ops, int nops, cudaStream_t s);
+void launch_gram_pad(const GramPad* ops, int nops, cudaStream_t s);
 // Lanczos vector kernels; `part` is a scratch array of kRedBlocks doubles
 constexpr int kRedBlocks = 608;
 void launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t s);

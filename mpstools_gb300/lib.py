@@ -41,6 +41,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_ctx_sync.argtypes = [vp]
     L.mpsg_ctx_kernel_launches.argtypes = [vp]
     L.mpsg_ctx_kernel_launches.restype = i64
+    L.mpsg_ctx_set_svd_method.argtypes = [vp, i32]
     L.mpsg_tensor_create.argtypes = [vp, i32, i32, vp, vp, vp, vp, vp, P(vp)]
     L.mpsg_tensor_shape.argtypes = [vp, P(i32), P(i32), P(i64)]
     L.mpsg_tensor_export.argtypes = [vp, vp, vp, vp, vp, vp]
@@ -101,6 +102,11 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.L.mpsg_ctx_kernel_launches(self.h))
+
+    def set_svd_method(self, method):
+        """'jacobi' (0, default) or 'density' (1): see mpsg_ctx_set_svd_method."""
+        m = {"jacobi": 0, "density": 1}.get(method, method)
+        check(self.L.mpsg_ctx_set_svd_method(self.h, int(m)))
 
     def set_stream(self, stream_ptr: int | None):
         check(self.L.mpsg_ctx_set_stream(self.h, C.c_void_p(stream_ptr) if stream_ptr else None))

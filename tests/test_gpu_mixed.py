@@ -52,9 +52,9 @@ def test_tc_matvec_matches_fp64(ctx, prec, model):
 
 
 def test_tc_matvec_large_blocks(ctx):
-    """Blocks larger than one 128x128 tile and K spanning several chunks (chi = 300)."""
-    g, W, ik = _case(N=14, chi=300, site=5)
-    site = 5
+    """Blocks larger than one 128x128 tile and K spanning several chunks (N = 20, chi = 1000)."""
+    g, W, ik = _case(N=20, chi=1000, site=9)
+    site = 9
     L, R = g.env("L", site - 1), g.env("R", site + 2)
     th = O.theta(g.site(site), g.site(site + 1))
     rng = np.random.default_rng(4)

@@ -170,3 +170,43 @@ def test_dmrg_tv_product_state_matches_oracle(ctx):
     sites = M.product_state(M.filling_state(N, N // 2), ik)
     go, Eo, gg, Eg = _run_both(W, sites, ik, 32, 3, ctx)
     assert abs(Eg - Eo) <= 1e-10 * abs(Eo)
+
+
+def test_split_density_method_matches_oracle(ctx):
+    """Density-matrix SVD (Gram + syevd): same kept structure and lambdas within 1e-10 (chi cut)."""
+    g, W, ik = _case(chi=12)
+    site = 4
+    L, R = g.env("L", site - 1), g.env("R", site + 2)
+    th = O.theta(g.site(site), g.site(site + 1))
+    _, _, psi = O.lanczos(L, R, th, W[site], W[site + 1], ik[site], ik[site + 1])
+    U0, V0, l0, tw0, chi0 = O.split(psi, ik[site], ik[site + 1], 8)
+    ctx.set_svd_method("density")
+    try:
+        U1, V1, l1, tw1, chi1 = api.split(psi, (ik[site], ik[site + 1]), 8, ctx=ctx)
+    finally:
+        ctx.set_svd_method("jacobi")
+    assert chi1 == chi0 and abs(tw1 - tw0) < 1e-10
+    assert set(l1) == set(l0)
+    for q in l0:
+        assert np.abs(l1[q] - l0[q]).max() < 1e-10
+    _close_bm(_recompose(U1, l1, V1), _recompose(U0, l0, V0), rtol=1e-8)
+
+
+def test_dmrg_config1_density_svd(ctx):
+    """Config 1 with the density-matrix SVD: energy within 1e-10 relative of the oracle."""
+    N = 32
+    W = M.heisenberg_mpo(np.ones(N - 1), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    sites = M.random_u1_mps(N, N // 2, 64, 12345)
+    go = O.DMRG(sites, W, ik, maxthreads=8)
+    Eo = go.simulate(maxsteps=6, EnConv=1e-300, chimax=64, delta=1e-12)
+    ctx.set_svd_method("density")
+    try:
+        gg = api.DMRGengine(sites, W, ik, ctx=ctx)
+        Eg = gg.simulate(maxsteps=6, EnConv=1e-300, chimax=64, delta=1e-12)
+        Em = gg.measure_energy()
+    finally:
+        ctx.set_svd_method("jacobi")
+    print(f"density svd: E {Eg:.15f} measured {Em:.15f} oracle {Eo:.15f}")
+    assert abs(Eg - Eo) <= 1e-10 * abs(Eo)
+    assert abs(Em - go.measure()) <= 1e-10 * abs(Eo)
