@@ -278,7 +278,8 @@ def gpu_arm(args):
     thout = C.c_void_p()
     lib.check(ctx.L.mpsg_theta_closure(ctx.h, L.h, R.h, th0.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), C.byref(thout)))
     thout = lib.Tensor(ctx, thout)
-    plan = lib.MatvecPlan(ctx, L, R, thc, W[center], W[center + 1], ik[center], ik[center + 1], lib.PREC[prec])
+    mv_prec = "bf16x3" if prec == "auto" else prec  # the matvec kernel that dominates the timed steps
+    plan = lib.MatvecPlan(ctx, L, R, thc, W[center], W[center + 1], ik[center], ik[center + 1], lib.PREC[mv_prec])
     info = plan.info()
     din, _ = thc.device_view()
     dout, _ = thout.device_view()
@@ -304,10 +305,15 @@ def gpu_arm(args):
                 "matvec_seconds": mv_avg}
     else:
         peak = pk["bf16_tflops"]
-        roof = {"bound": "tensor", "achieved": info["flops"] / mv_avg / 1e12, "peak": peak, "unit": "TFLOP/s",
-                "frac": info["flops"] / mv_avg / 1e12 / peak, "traffic": args.traffic_bytes,
-                "peak_source": f"bf16_tflops ({pk_kind})", "flops_per_matvec": info["flops"],
-                "matvec_seconds": mv_avg}
+        # hardware MMA work per algorithmic FLOP: 3 for hi/lo splits, x2 for TF32 (half the BF16 rate)
+        mma_per_flop = (3 if mv_prec.endswith("x3") else 1) * (2 if mv_prec.startswith("tf32") else 1)
+        ach = info["flops"] / mv_avg / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "traffic": args.traffic_bytes, "peak_source": f"bf16_tflops ({pk_kind} dense BF16 cuBLAS)",
+                "kernel": f"k_tc_gemm<{mv_prec}> (conversion + stage A + stage C of one matvec)",
+                "flops_per_matvec": info["flops"], "matvec_seconds": mv_avg,
+                "bf16_equivalent_mma_per_algorithmic_flop": mma_per_flop,
+                "tensor_issue_frac": ach * mma_per_flop / peak}
 
     # --------------------------------------------------------------- e2e through the C ABI, host buffers
     e2e_raw = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)
@@ -388,7 +394,7 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
                                     C.byref(lam), C.byref(tw), C.byref(chi)))
         U, V, lam = lib.Tensor(ctx, U), lib.Tensor(ctx, V), lib.Tensor(ctx, lam)
         Lo = C.c_void_p()
-        lib.check(ctx.L.mpsg_add_contraction_layer(ctx.h, tL.h, U.h, w1.ref(), k0.ref(), 1, lib.PREC[prec],
+        lib.check(ctx.L.mpsg_add_contraction_layer(ctx.h, tL.h, U.h, w1.ref(), k0.ref(), 1, lib.PREC["fp64"],
                                                    C.byref(Lo)))
         Lo = lib.Tensor(ctx, Lo)
         outs = [U.export_flat(), V.export_flat(), lam.export_flat(), Lo.export_flat()]

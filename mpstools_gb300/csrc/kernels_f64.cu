@@ -174,12 +174,16 @@ void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s) {
 
 // ============================================================================ density-matrix SVD post-processing
 // s_i = sqrt(max(lambda_{n-1-i}, 0)), 1/s_i (0 for s_i = 0), V(:, i) = W(:, n-1-i)
+// Eigenvalues at or below the eigensolver's noise level (8 n eps lambda_max) are not resolved by
+// the Gram route; they are reported as exact zeros so that truncation never keeps their vectors.
 __global__ void k_gram_post(const GramPost* __restrict__ ops) {
   const GramPost o = ops[blockIdx.x];
   const int n = o.n;
+  const double lmax = n > 0 ? o.lam[n - 1] : 0.0;
+  const double floor_l = 8.0 * n * DBL_EPSILON * fmax(lmax, 0.0);
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const double l = o.lam[n - 1 - i];
-    const double sv = l > 0.0 ? sqrt(l) : 0.0;
+    const double sv = l > floor_l ? sqrt(l) : 0.0;
     o.S[i] = sv;
     o.invS[i] = sv > 0.0 ? 1.0 / sv : 0.0;
   }
