@@ -426,7 +426,7 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--prec", default="fp64")
-    ap.add_argument("--svd", default="density", choices=["density", "jacobi"])
+    ap.add_argument("--svd", default="density", choices=["density", "density_mt", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
     args = ap.parse_args()

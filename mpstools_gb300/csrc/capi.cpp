@@ -8,7 +8,7 @@
 using namespace mpsg;
 
 struct mpsg_ctx_s {
-  Ctx* c = nullptr;
+  std::shared_ptr<Ctx> c;  // tensors, plans and engines hold further references
 };
 struct mpsg_tensor_s {
   TensorP t;
@@ -24,6 +24,7 @@ struct StepRec {
 // DMRGengine (src/container.hpp:236-438) with all tensors resident on the device.
 struct Engine {
   Ctx* ctx;
+  std::shared_ptr<Ctx> keep;
   int N;
   std::vector<TensorP> mps;
   std::vector<MPO> mpo;
@@ -225,7 +226,7 @@ struct mpsg_matvec_plan_s {
 
 static Ctx* C(mpsg_ctx c) {
   MPSG_CHECK(c && c->c, "null context");
-  return c->c;
+  return c->c.get();
 }
 static const Tensor& T(mpsg_tensor t) {
   MPSG_CHECK(t && t->t, "null tensor");
@@ -246,7 +247,7 @@ mpsg_status mpsg_ctx_create(int32_t device, mpsg_ctx* out) {
   MPSG_CHECK(out, "null output");
   mpsg_ctx c = new mpsg_ctx_s;
   try {
-    c->c = new Ctx(device);
+    c->c = std::make_shared<Ctx>(device);
   } catch (...) {
     delete c;
     throw;
@@ -257,7 +258,7 @@ mpsg_status mpsg_ctx_create(int32_t device, mpsg_ctx* out) {
 void mpsg_ctx_destroy(mpsg_ctx ctx) {
   if (!ctx) return;
   try {
-    delete ctx->c;
+    ctx->c.reset();  // the Ctx lives on while tensors, plans or engines still use it
   } catch (...) {
   }
   delete ctx;
@@ -277,7 +278,8 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count(); }
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
   API_BEGIN
-  MPSG_CHECK(method == 0 || method == 1, "svd method must be 0 (Jacobi SVD) or 1 (density matrix)");
+  MPSG_CHECK(method >= 0 && method <= 2,
+             "svd method must be 0 (Jacobi SVD), 1 (density matrix, batched) or 2 (density matrix, concurrent)");
   C(ctx)->svd_method = method;
   API_END
 }
@@ -438,6 +440,7 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
   MPSG_CHECK(N >= 3, "DMRG needs at least 3 sites");
   Engine* e = new Engine();
   e->ctx = C(ctx);
+  e->keep = e->ctx->shared_from_this();
   e->N = N;
   try {
     for (int i = 0; i < N; ++i) {

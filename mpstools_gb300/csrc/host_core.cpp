@@ -25,6 +25,8 @@ Ctx::~Ctx() {
   if (solver) cusolverDnDestroy(solver);
   if (svdp) cusolverDnDestroyGesvdjInfo(svdp);
   if (params) cusolverDnDestroyParams(params);
+  for (auto h : whandles) cusolverDnDestroy(h);
+  for (auto s : wstreams) cudaStreamDestroy(s);
   if (part) cudaFreeAsync(part, stream);
   cudaStreamSynchronize(stream);
   if (hscal) cudaFreeHost(hscal);
@@ -54,6 +56,19 @@ cusolverDnParams_t Ctx::solver_params() {
   if (!params && cusolverDnCreateParams(&params) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreateParams failed");
   return params;
 }
+int Ctx::nworkers() {
+  constexpr int kWorkers = 8;
+  while ((int)wstreams.size() < kWorkers) {
+    cudaStream_t s;
+    MPSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cusolverDnHandle_t h;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreate failed");
+    cusolverDnSetStream(h, s);
+    wstreams.push_back(s);
+    whandles.push_back(h);
+  }
+  return kWorkers;
+}
 void Ctx::sync() { MPSG_CUDA(cudaStreamSynchronize(stream)); }
 
 // ============================================================================ layouts and tensors
@@ -77,6 +92,7 @@ Tensor::~Tensor() {
 TensorP make_tensor(Ctx* ctx, int nphys, const Layout& lay, bool zero) {
   TensorP t = std::make_shared<Tensor>();
   t->ctx = ctx;
+  t->keep = ctx->shared_from_this();
   t->nphys = nphys;
   t->b = lay.b;
   t->idx = lay.idx;
@@ -185,6 +201,7 @@ void GemmPlan::add_problem(int baseC, int64_t offC, int ldc, int M, int N, bool 
 }
 void GemmPlan::upload(Ctx* ctx) {
   this->ctx = ctx;
+  keep = ctx->shared_from_this();
   std::vector<GTile> tiles;
   for (size_t i = 0; i < hprob.size(); ++i)
     for (int m0 = 0; m0 < hprob[i].M; m0 += 64)

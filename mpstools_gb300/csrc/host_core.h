@@ -9,7 +9,7 @@ namespace mpsg {
 
 extern thread_local std::string g_last_error;
 
-struct Ctx {
+struct Ctx : std::enable_shared_from_this<Ctx> {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t own = nullptr;
@@ -25,6 +25,10 @@ struct Ctx {
   cusolverDnHandle_t svd_handle();
   cusolverDnParams_t params = nullptr;
   cusolverDnParams_t solver_params();
+  // worker streams / solver handles for concurrent per-sector eigen-solves (created on first use)
+  std::vector<cudaStream_t> wstreams;
+  std::vector<cusolverDnHandle_t> whandles;
+  int nworkers();
   void sync();
 };
 
@@ -68,6 +72,7 @@ struct GProbH {
 };
 struct GemmPlan {
   Ctx* ctx = nullptr;
+  std::shared_ptr<Ctx> keep;
   std::vector<GProbH> hprob;
   std::vector<GSegH> hseg;
   GProb* dprob = nullptr;

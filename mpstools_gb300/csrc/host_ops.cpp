@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstring>
 #include <set>
+#include <thread>
 #include <tuple>
 
 namespace mpsg {
@@ -299,6 +300,7 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
   MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "unsupported matvec precision");
   std::unique_ptr<MatvecPlan> P(new MatvecPlan());
   P->ctx = ctx;
+  P->keep = ctx->shared_from_this();
   P->prec = prec;
   std::map<K5, std::map<std::tuple<int, int, int>, double>> ltc, rtc;
   std::map<K5, std::map<uint32_t, std::pair<K5, int>>> xterms;
@@ -437,6 +439,7 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
                                    int direction) {
   std::unique_ptr<EnvPlan> P(new EnvPlan());
   P->ctx = ctx;
+  P->keep = ctx->shared_from_this();
   const bool left = direction > 0;
   std::map<std::pair<uint32_t, Q>, std::vector<int>> envby;  // (w, lower charge) -> env blocks
   for (int i = 0; i < (int)BL.b.size(); ++i) envby[{BL.b[i].k.p0, BL.b[i].k.q1}].push_back(i);
@@ -764,8 +767,9 @@ struct SvdBatch {
       const Sec& x = s[i];
       if (x.k == 0) continue;
       const int64_t nc = cls_of[i], pad = nc - x.ns;
-      post.push_back(GramPost{dB + slot_off[i] + pad * nc, dWv + lam_off[i] + pad, dV + x.offV, dS + x.offS,
-                              dI + x.offS, x.ns, (int32_t)nc});
+      (void)pad;
+      post.push_back(GramPost{dB + slot_off[i], dWv + lam_off[i], dV + x.offV, dS + x.offS, dI + x.offS, x.ns,
+                              (int32_t)nc, (int32_t)nc});
     }
     if (!post.empty()) {
       GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
@@ -791,6 +795,101 @@ struct SvdBatch {
     ctx->dfree(dWv);
     ctx->dfree(dI);
     ctx->dfree(dinf);
+    fixphase();
+  }
+
+  // Density-matrix route with one cuSOLVER syevd per sector, sectors spread over worker threads
+  // that each own a stream and a solver handle (largest sectors first), so the solver's per-call
+  // latency overlaps across sectors.
+  void run_gram_mt() {
+    const int nw = ctx->nworkers();
+    int64_t oG = 0;
+    std::vector<int64_t> offG(s.size());
+    std::vector<int> order;
+    for (size_t i = 0; i < s.size(); ++i) {
+      offG[i] = oG;
+      oG += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+      if (s[i].k > 0) order.push_back((int)i);
+    }
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return s[a].ns > s[b].ns; });
+    double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
+    double* dL = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
+    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
+    {
+      GemmPlan g;
+      for (int i : order)
+        g.add_problem(2, offG[i], s[i].ns, s[i].ns, s[i].ns, false,
+                      {GSegH{0, 0, s[i].offM, s[i].offM, s[i].ms, s[i].ms, s[i].ms, 1, 0, 1.0}});
+      g.upload(ctx);
+      const double* bases[8] = {dM, nullptr, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+    }
+    cudaEvent_t ready;
+    MPSG_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    MPSG_CUDA(cudaEventRecord(ready, ctx->stream));
+    ctx->sync();  // G complete before the workers allocate workspaces on their streams
+    std::vector<std::vector<int>> part(nw);
+    for (size_t t = 0; t < order.size(); ++t) part[t % nw].push_back(order[t]);
+    std::vector<std::string> errs(nw);
+    std::vector<std::thread> th;
+    for (int w = 0; w < nw; ++w) {
+      if (part[w].empty()) continue;
+      th.emplace_back([&, w]() {
+        try {
+          cudaStream_t st = ctx->wstreams[w];
+          cusolverDnHandle_t h = ctx->whandles[w];
+          MPSG_CUDA(cudaSetDevice(ctx->device));
+          int lwork = 0;
+          for (int i : part[w]) {
+            int lw = 0;
+            if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, s[i].ns, dG + offG[i],
+                                            s[i].ns, dL + s[i].offS, &lw) != CUSOLVER_STATUS_SUCCESS)
+              throw Err(3, "syevd_bufferSize failed");
+            lwork = std::max(lwork, lw);
+          }
+          double* work = nullptr;
+          MPSG_CUDA(cudaMallocAsync(&work, sizeof(double) * std::max(lwork, 2), st));
+          for (int i : part[w])
+            if (cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, s[i].ns, dG + offG[i], s[i].ns,
+                                 dL + s[i].offS, work, lwork, dinfo + i) != CUSOLVER_STATUS_SUCCESS)
+              throw Err(3, "syevd failed");
+          MPSG_CUDA(cudaFreeAsync(work, st));
+          MPSG_CUDA(cudaStreamSynchronize(st));
+        } catch (const std::exception& e) {
+          errs[w] = e.what();
+        }
+      });
+    }
+    for (auto& t : th) t.join();
+    cudaEventDestroy(ready);
+    for (auto& e : errs)
+      if (!e.empty()) throw Err(3, e);
+    std::vector<GramPost> post;
+    for (int i : order)
+      post.push_back(GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns,
+                              s[i].ns, s[i].ns});
+    if (!post.empty()) {
+      GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, post.data(), sizeof(GramPost) * post.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_gram_post(d, (int)post.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    {
+      GemmPlan g;
+      std::vector<CopyOp> sc;
+      for (int i : order) {
+        const Sec& x = s[i];
+        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
+        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
+      }
+      g.upload(ctx);
+      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+      run_copyops(ctx, sc);
+    }
+    ctx->dfree(dG);
+    ctx->dfree(dL);
+    ctx->dfree(dI);
     fixphase();
   }
 
@@ -839,7 +938,8 @@ struct SvdBatch {
     for (size_t i = 0; i < s.size(); ++i) {
       if (s[i].k == 0) continue;
       post.push_back(
-          GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns, s[i].ns});
+          GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns, s[i].ns,
+                   s[i].ns});
     }
     if (!post.empty()) {
       GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
@@ -869,6 +969,7 @@ struct SvdBatch {
 
   void run(int method) {
     if (method == 1) run_gram();
+    else if (method == 2) run_gram_mt();
     else run_jacobi();
   }
 

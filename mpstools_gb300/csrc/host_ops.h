@@ -45,6 +45,7 @@ struct K5 {
 //   theta'(a',b';s1',s2') = sum_{wm,s2,b} X(a',b;wm,s1',s2) R~(b',b;wm,s2',s2)^T   (stage C)
 struct MatvecPlan {
   Ctx* ctx = nullptr;
+  std::shared_ptr<Ctx> keep;
   KeyedArena<K5> lt, rt, xa;
   double* dLt = nullptr;
   double* dRt = nullptr;
@@ -86,6 +87,7 @@ Layout theta_closure(const Tensor& L, const Tensor& R, const Layout& th, const M
 // Environment update (addContractionLayer) factored as two grouped GEMM stages.
 struct EnvPlan {
   Ctx* ctx = nullptr;
+  std::shared_ptr<Ctx> keep;
   KeyedArena<K5> ct;      // combined environment (L~ or R~)
   KeyedArena<K5> tt;      // intermediate T
   double* dCt = nullptr;

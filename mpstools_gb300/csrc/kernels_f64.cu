@@ -174,22 +174,37 @@ void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s) {
 
 // ============================================================================ density-matrix SVD post-processing
 // s_i = sqrt(max(lambda_{n-1-i}, 0)), 1/s_i (0 for s_i = 0), V(:, i) = W(:, n-1-i)
-// Eigenvalues at or below the eigensolver's noise level (8 n eps lambda_max) are not resolved by
-// the Gram route; they are reported as exact zeros so that truncation never keeps their vectors.
+// The eigenpairs come from an nc x nc slot whose padding eigenvalues are -1; the n eigenvalues
+// >= -0.5 are the sector's, in any order.  They are ranked descending (ties by index) without
+// relying on the solver's ordering.  Eigenvalues at or below the eigensolver's noise level
+// (8 n eps lambda_max) are not resolved by the Gram route and are reported as exact zeros, so
+// truncation never keeps their vectors.
 __global__ void k_gram_post(const GramPost* __restrict__ ops) {
   const GramPost o = ops[blockIdx.x];
-  const int n = o.n;
-  const double lmax = n > 0 ? o.lam[n - 1] : 0.0;
-  const double floor_l = 8.0 * n * DBL_EPSILON * fmax(lmax, 0.0);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double l = o.lam[n - 1 - i];
-    const double sv = l > floor_l ? sqrt(l) : 0.0;
-    o.S[i] = sv;
-    o.invS[i] = sv > 0.0 ? 1.0 / sv : 0.0;
+  const int n = o.n, nc = o.nc;
+  __shared__ double lmax_s;
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int j = 0; j < nc; ++j) m = fmax(m, o.lam[j]);
+    lmax_s = m;
   }
-  for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += blockDim.x) {
-    const int r = (int)(e % n), c = (int)(e / n);
-    o.V[r + (int64_t)c * n] = o.W[r + (int64_t)(n - 1 - c) * o.ldw];
+  __syncthreads();
+  const double floor_l = 8.0 * n * DBL_EPSILON * lmax_s;
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+    const double lj = o.lam[j];
+    if (!(lj > -0.5)) continue;  // padding
+    int rank = 0;
+    for (int l = 0; l < nc; ++l) {
+      const double ll = o.lam[l];
+      rank += (ll > -0.5) && (ll > lj || (ll == lj && l < j));
+    }
+    if (rank >= n) continue;  // defensive: more than n non-padding eigenvalues
+    const double sv = lj > floor_l ? sqrt(lj) : 0.0;
+    o.S[rank] = sv;
+    o.invS[rank] = sv > 0.0 ? 1.0 / sv : 0.0;
+    const double* w = o.W + (int64_t)j * o.ldw;
+    double* v = o.V + (int64_t)rank * n;
+    for (int r = 0; r < n; ++r) v[r] = w[r];
   }
 }
 void launch_gram_post(const GramPost* ops, int nops, cudaStream_t s) {

@@ -57,6 +57,7 @@ struct Ctx;
 // Block-sparse tensor with a device arena.  Padding between blocks is kept zero.
 struct Tensor {
   Ctx* ctx = nullptr;
+  std::shared_ptr<Ctx> keep;  // keeps the context (memory pool, stream) alive
   int nphys = 1;
   std::vector<Block> b;         // sorted by key
   std::map<BKey, int> idx;      // key -> position in b
@@ -125,13 +126,13 @@ struct CopyOp {  // dst(i,j) = scale * rs[i] * cs[j] * (trans ? src(j,i) : src(i
   int32_t rows, cols, lds, ldd, trans;
   double scale;
 };
-struct GramPost {  // eigenpairs of G (ascending) -> s descending, 1/s, V = reversed eigenvectors (n x n)
-  const double* W;  // eigenvectors, column j at W + j*ldw
-  const double* lam;
+struct GramPost {  // eigenpairs of an nc x nc slot (padding eigenvalues -1) -> s descending, 1/s, V (n x n)
+  const double* W;   // eigenvectors, column j at W + j*ldw (rows 0..n-1 belong to the sector)
+  const double* lam; // nc eigenvalues, any order
   double* V;
   double* S;
   double* invS;
-  int32_t n, ldw;
+  int32_t n, ldw, nc;
 };
 struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
   double* A;

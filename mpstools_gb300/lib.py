@@ -105,7 +105,7 @@ class Context:
 
     def set_svd_method(self, method):
         """'jacobi' (0, default) or 'density' (1): see mpsg_ctx_set_svd_method."""
-        m = {"jacobi": 0, "density": 1}.get(method, method)
+        m = {"jacobi": 0, "density": 1, "density_mt": 2}.get(method, method)
         check(self.L.mpsg_ctx_set_svd_method(self.h, int(m)))
 
     def set_stream(self, stream_ptr: int | None):
