@@ -120,6 +120,18 @@ mpsg_status mpsg_matvec2_plan_create(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R,
                                      const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
                                      const mpsg_itokey* ikr, mpsg_prec prec, mpsg_matvec_plan* out);
 mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta_in, double* theta_out);
+/* mpsg_matvec2_plan_execute for callers that may not allocate device memory: code running while a
+ * stream is captured into a CUDA graph, hosts whose own allocator owns the whole GPU memory
+ * budget, latency-bound loops.  No counterpart in MPSTools (the reference runs on the CPU).
+ * It calls no cudaMalloc / cudaFree or other allocating routine: the stage-A intermediate is
+ * kept in a fixed 8 MiB device array inside the library (held by every GPU that loads it until
+ * the process exits).  FP64 plans only; plans whose intermediate exceeds 1 Mi FP64 elements are
+ * rejected with MPSG_ERR_ARG.  The first call on a device resolves the array's device address
+ * (cudaGetSymbolAddress) -- make that first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU (other streams, other threads) race; nothing in
+ * it needs clearing, every intermediate block is overwritten before it is read.  Runs on the
+ * context's stream, the current device must be the plan's device. */
+mpsg_status mpsg_matvec2_plan_execute_noalloc(mpsg_matvec_plan plan, const double* theta_in, double* theta_out);
 /* info[0] algorithmic FLOPs of one application, info[1] FLOPs of the reference's per-term
  * schedule, info[2] algorithmic bytes 8*(|L|+|R|+2|theta|), info[3] kernel launches per application. */
 mpsg_status mpsg_matvec2_plan_info(mpsg_matvec_plan plan, double* info4);

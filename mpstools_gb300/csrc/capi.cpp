@@ -565,6 +565,13 @@ mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta
   MPSG_CUDA(cudaGetLastError());
   API_END
 }
+mpsg_status mpsg_matvec2_plan_execute_noalloc(mpsg_matvec_plan plan, const double* theta_in, double* theta_out) {
+  API_BEGIN
+  MPSG_CHECK(plan && plan->p, "null plan");
+  MPSG_CHECK(theta_in && theta_out && theta_in != theta_out, "matvec needs distinct input and output arenas");
+  matvec_noalloc(*plan->p, theta_in, theta_out);
+  API_END
+}
 mpsg_status mpsg_matvec2_plan_info(mpsg_matvec_plan plan, double* info) {
   API_BEGIN
   MPSG_CHECK(plan && plan->p && info, "null argument");

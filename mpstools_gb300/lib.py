@@ -70,6 +70,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_env.argtypes = [vp, i32, i32, P(vp)]
     L.mpsg_matvec2_plan_create.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i32, P(vp)]
     L.mpsg_matvec2_plan_execute.argtypes = [vp, vp, vp]
+    L.mpsg_matvec2_plan_execute_noalloc.argtypes = [vp, vp, vp]
     L.mpsg_matvec2_plan_info.argtypes = [vp, vp]
     L.mpsg_matvec2_plan_destroy.argtypes = [vp]
     L.mpsg_matvec2_plan_destroy.restype = None
