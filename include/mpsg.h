@@ -120,9 +120,9 @@ mpsg_status mpsg_matvec2_plan_create(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R,
                                      const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
                                      const mpsg_itokey* ikr, mpsg_prec prec, mpsg_matvec_plan* out);
 mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta_in, double* theta_out);
-/* mpsg_matvec2_plan_execute for callers that may not allocate device memory: code running while a
- * stream is captured into a CUDA graph, hosts whose own allocator owns the whole GPU memory
- * budget, latency-bound loops.  No counterpart in MPSTools (the reference runs on the CPU).
+/* mpsg_matvec2_plan_execute for callers that may not allocate device memory: hosts whose own
+ * allocator owns the whole GPU memory budget and forbids libraries from allocating, and
+ * latency-bound loops that may not block on an allocation.  No counterpart in MPSTools (the reference runs on the CPU).
  * It calls no cudaMalloc / cudaFree or other allocating routine: the stage-A intermediate is
  * kept in a fixed 8 MiB device array inside the library (held by every GPU that loads it until
  * the process exits).  FP64 plans only; plans whose intermediate exceeds 1 Mi FP64 elements are

@@ -1,9 +1,8 @@
 // Two-site matvec that allocates no device memory.
 //
-// Some callers cannot allocate device memory at the point where they need a matvec: code that
-// runs while a stream is being captured into a CUDA graph (cudaMalloc / cudaFree are not allowed
-// there), host applications that hand the whole GPU memory budget to their own allocator and
-// forbid libraries from allocating, and latency-bound loops that may not block on an allocation.
+// Some callers cannot allocate device memory at the point where they need a matvec: host
+// applications that hand the whole GPU memory budget to their own allocator and forbid libraries
+// from allocating, and latency-bound loops that may not block on an allocation.
 // For them the FP64 matvec can run with its stage-A intermediate X in a fixed device array that
 // lives inside this library instead of the plan's own arena.
 #include <cuda_runtime.h>

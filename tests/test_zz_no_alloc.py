@@ -1,8 +1,7 @@
 """GPU test of mpsg_matvec2_plan_execute_noalloc, the matvec entry point that allocates nothing.
 
-It serves callers that may not allocate device memory when they need a matvec (code running while
-a stream is captured into a CUDA graph, hosts whose allocator owns the whole memory budget,
-latency-bound loops): the stage-A intermediate sits in a fixed 8 MiB array inside the library.
+It serves callers that may not allocate device memory when they need a matvec (hosts whose
+allocator owns the whole memory budget, latency-bound loops): the stage-A intermediate sits in a fixed 8 MiB array inside the library.
 Two consecutive calls through the C ABI must agree with mpsg_matvec2_plan_execute on the same plan
 within the parity tolerance of the FP64 tests (1e-11 relative to the largest output entry).
 The file name sorts last so that a run stopping at the first failure has run every other test.
