@@ -261,6 +261,18 @@ def gpu_arm(args):
     matvecs = st1["matvecs"] - st0["matvecs"]
     value = mv_flops * world / total / 1e12
     steps_rec = eng.steps()[n_steps0:]
+    lam_c = eng.lam(center)
+    lam_all = np.sort(np.concatenate([np.asarray(v) for v in lam_c.values() if len(v)]))[::-1]
+    spectrum = {"chi": int(lam_all.size), "s_max": float(lam_all[0]), "s_min_kept": float(lam_all[-1]),
+                "sectors": {int(q): len(v) for q, v in lam_c.items()}}
+
+    if args.steps_only:  # profiling runs: only warm-up + timed steps (few launches under a profiler)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "steps_only": True, "ms_per_step": total / args.steps * 1e3,
+                              "gpu_launches": int(launches), "config": config_dict(args.chi, args.L, prec, args.svd),
+                              "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
+                              "energies": [s["E"] for s in steps_rec]}), flush=True)
+        return
 
     # --------------------------------------------------------------- roofline: matvec kernel alone
     L = eng.env_tensor("L", center - 1)
@@ -346,6 +358,7 @@ def gpu_arm(args):
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
                 "env_seconds_per_step": (st1["env_seconds"] - st0["env_seconds"]) / args.steps,
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
+                "centre_bond_spectrum": spectrum,
                 "matvec_flops_reference_schedule": info["flops_ref"]}
         print(json.dumps(line), flush=True)
     if dist:
@@ -426,9 +439,11 @@ def main():
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--L", type=int, default=L_SITES)
     ap.add_argument("--prec", default="fp64")
-    ap.add_argument("--svd", default="density", choices=["density", "density_mt", "jacobi"])
+    ap.add_argument("--svd", default="density", choices=["density", "density_mt", "density_eig", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
+    ap.add_argument("--steps-only", action="store_true",
+                    help="time the DMRG steps only (no roofline / e2e / CPU legs); for profiler launch lists")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)

@@ -38,8 +38,8 @@ typedef enum {
   MPSG_PREC_TF32X3 = 2,  /* tcgen05 kind::tf32 with hi/lo split (3 products), FP32 accumulate */
   MPSG_PREC_BF16 = 3,    /* tcgen05 kind::f16 (bf16), FP32 accumulate */
   MPSG_PREC_BF16X3 = 4,  /* tcgen05 kind::f16 (bf16) hi/lo split (3 products), FP32 accumulate */
-  MPSG_PREC_AUTO = 5     /* Lanczos only: cheapest precision first, hi/lo split when the
-                            Ritz residual stalls, FP64 for the final Rayleigh quotient */
+  MPSG_PREC_AUTO = 5     /* Lanczos only: TF32X3 Lanczos to its precision floor, then the reference's
+                            FP64 Lanczos restarted from that state (energy test every iteration) */
 } mpsg_prec;
 
 typedef struct mpsg_ctx_s* mpsg_ctx;
@@ -74,9 +74,12 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
- * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default),
- * 1 = eigen-decomposition of the sector's reduced density matrix (FP64 Gram GEMM + syevd);
- *     singular values below ~1e-8 of their sector's largest lose relative accuracy. */
+ * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default, exact),
+ * 1, 2, 3 = eigen-decomposition of each sector's reduced density matrix G = M^T M (FP64) with the
+ *     eigensolver of cuSOLVER batched by size class (1), cuSOLVER per sector on concurrent streams (2)
+ *     or the library's own batched eigensolver (3).  The left vectors are re-orthonormalised
+ *     (CholeskyQR); singular values below sqrt(32 n eps) of their sector's largest are not resolved
+ *     by G and are dropped, and a kept value s carries an absolute error up to ~n eps s_max^2 / s. */
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method);
 
 /* ------------------------------------------------------------------ tensors
@@ -142,6 +145,20 @@ mpsg_status mpsg_theta_closure(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_
                                const mpsg_mpo* Wr, const mpsg_itokey* ikl, const mpsg_itokey* ikr,
                                mpsg_tensor* out);
 
+/* Two-tensor addContractionLayer(BL, A, mpo, Ap, itokey, direction): A is the lower (ket) tensor,
+ * Ap the upper (bra) one -- src/MPSfunctions.hpp:500-556 (add_out_sub :360-434). */
+mpsg_status mpsg_add_contraction_layer2(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor A, mpsg_tensor Ap,
+                                        const mpsg_mpo* W, const mpsg_itokey* ik, int32_t direction, mpsg_prec prec,
+                                        mpsg_tensor* out);
+/* computeOverlap(a, b): identity-MPO layers over N sites, a lower and b upper; entry (0,0) of the first
+ * block of the final environment -- src/MPSfunctions.hpp:2066-2085. */
+mpsg_status mpsg_overlap(mpsg_ctx ctx, int32_t N, const mpsg_tensor* a, const mpsg_tensor* b, const mpsg_itokey* ik,
+                         double* out);
+/* MPO::measure(mps) for N site tensors and N MPO tensors (energies, local operators as D = 1 MPOs)
+ * -- src/MPOTypes.hpp:990-1020. */
+mpsg_status mpsg_mpo_measure(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
+                             const mpsg_itokey* ik, double* out);
+
 /* BlockMatrix<2>(A1, A2): theta formation  -- src/BlockTensor.hpp:285-301. */
 mpsg_status mpsg_theta(mpsg_ctx ctx, mpsg_tensor A1, mpsg_tensor A2, mpsg_tensor* out);
 
@@ -197,6 +214,9 @@ mpsg_status mpsg_dmrg_site(mpsg_dmrg e, int32_t site, mpsg_tensor* out);
 mpsg_status mpsg_dmrg_lambda(mpsg_dmrg e, int32_t bond, mpsg_tensor* out);
 /* MPO::measure(mps) in FP64 on the GPU  -- src/MPOTypes.hpp:990-1020. */
 mpsg_status mpsg_dmrg_measure_energy(mpsg_dmrg e, double* E);
+/* MPO::measure of the engine's state with another MPO (N tensors), e.g. a local operator
+ * -- src/MPOTypes.hpp:990-1020. */
+mpsg_status mpsg_dmrg_measure_mpo(mpsg_dmrg e, const mpsg_mpo* W, double* out);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
 
 #ifdef __cplusplus

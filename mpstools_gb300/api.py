@@ -6,6 +6,8 @@ Names and argument meaning follow MPSTools:
   split                src/MPSfunctions.hpp:1142-1278
   TSLanzcosEngine      src/lanzcos.hpp:96-278
   DMRGengine           src/container.hpp:236-438
+  computeOverlap       src/MPSfunctions.hpp:2066-2085
+  MPO::measure         src/MPOTypes.hpp:990-1020
 Block matrices are dicts keyed like TensorKeyType ((q0, q1, p0) or (q0, q1, p0, p1));
 lambdas are dicts {q: 1-D array}; MPO matrices are (terms, Dl, Dr) with
 terms (wl, wr, out, in, value).  All arithmetic runs on the GPU.
@@ -17,7 +19,7 @@ import ctypes as C
 import numpy as np
 
 from . import lib
-from .lib import Context, ItoKeyArg, MPOArg, Tensor, check
+from .lib import Context, ItoKeyArg, ItoKeyArray, MPOArg, MPOArray, Tensor, check, handle_array
 
 _CTX = None
 
@@ -61,6 +63,39 @@ def theta(A1, A2, ctx=None):
     h = C.c_void_p()
     check(ctx.L.mpsg_theta(ctx.h, t1.h, t2.h, C.byref(h)))
     return Tensor(ctx, h).to_dict()
+
+
+def addContractionLayer2(BL, A, mpo, Ap, itokey, direction, prec="fp64", ctx=None):
+    """Two-tensor addContractionLayer(BL, A, mpo, Ap, itokey, direction): A lower, Ap upper."""
+    ctx = ctx or default_context()
+    tB, tA, tP = Tensor.from_dict(ctx, BL, 1), Tensor.from_dict(ctx, A, 1), Tensor.from_dict(ctx, Ap, 1)
+    w = MPOArg(mpo)
+    k = ItoKeyArg(itokey)
+    h = C.c_void_p()
+    check(ctx.L.mpsg_add_contraction_layer2(ctx.h, tB.h, tA.h, tP.h, w.ref(), k.ref(), int(direction),
+                                            _prec(prec), C.byref(h)))
+    return Tensor(ctx, h).to_dict()
+
+
+def computeOverlap(a, b, itokeys, ctx=None):
+    """computeOverlap(a, b) for two MPS given as lists of site dicts (a lower, b upper)."""
+    ctx = ctx or default_context()
+    ta = [Tensor.from_dict(ctx, x, 1) for x in a]
+    tb = [Tensor.from_dict(ctx, x, 1) for x in b]
+    ks = ItoKeyArray(itokeys)
+    out = C.c_double()
+    check(ctx.L.mpsg_overlap(ctx.h, len(ta), handle_array(ta), handle_array(tb), ks.ptr(), C.byref(out)))
+    return out.value
+
+
+def measureMPO(sites, mpo, itokeys, ctx=None):
+    """MPO::measure(mps): <psi|W|psi> for site dicts and one MPO tensor per site."""
+    ctx = ctx or default_context()
+    ts = [Tensor.from_dict(ctx, x, 1) for x in sites]
+    ws, ks = MPOArray(mpo), ItoKeyArray(itokeys)
+    out = C.c_double()
+    check(ctx.L.mpsg_mpo_measure(ctx.h, len(ts), handle_array(ts), ws.ptr(), ks.ptr(), C.byref(out)))
+    return out.value
 
 
 def split(A, itokey, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, ctx=None):
@@ -187,6 +222,13 @@ class DMRGengine:
         E = C.c_double()
         check(self.ctx.L.mpsg_dmrg_measure_energy(self.h, C.byref(E)))
         return E.value
+
+    def measure(self, mpo):
+        """MPO::measure of the current state with another MPO (one tensor per site)."""
+        ws = MPOArray(mpo)
+        out = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_measure_mpo(self.h, ws.ptr(), C.byref(out)))
+        return out.value
 
     def close(self):
         if getattr(self, "h", None):

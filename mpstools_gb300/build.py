@@ -72,7 +72,7 @@ def build(force: bool = False, verbose: bool = False, extra_nvcc=None) -> str:
         if not os.path.exists(libdir):
             libdir = os.path.join(cuda, "lib")
         _run(["g++", "-shared", "-o", LIB] + objs +
-             ["-L", libdir, "-lcusolver", "-lcudart", f"-Wl,-rpath,{libdir}"])
+             ["-L", libdir, "-lcusolver", "-lcublas", "-lcudart", f"-Wl,-rpath,{libdir}"])
     return LIB
 
 

@@ -185,9 +185,19 @@ struct Engine {
     return out.E;
   }
 
-  double measure_energy() {  // MPO::measure (src/MPOTypes.hpp:990-1020)
+  double measure_energy() { return measure(mpo); }
+
+  // MPO::measure (src/MPOTypes.hpp:990-1020): left environments through the chain, then the sum of
+  // the diagonals of the charge-diagonal blocks.
+  double measure(const std::vector<MPO>& W) {
+    std::vector<const Tensor*> s;
+    for (auto& t : mps) s.push_back(t.get());
+    return mpo_expectation(ctx, s, W, ik);
+  }
+  static double mpo_expectation(Ctx* ctx, const std::vector<const Tensor*>& sites, const std::vector<MPO>& W,
+                                const std::vector<ItoKey>& ik) {
     TensorP l = lmin(ctx);
-    for (int s = 0; s < N; ++s) l = env_update(ctx, *l, *mps[s], mpo[s], ik[s], 1, nullptr);
+    for (size_t s = 0; s < sites.size(); ++s) l = env_update(ctx, *l, *sites[s], W[s], ik[s], 1, nullptr);
     std::vector<double> h;
     tensor_to_host(*l, h);
     double e = 0;
@@ -198,6 +208,26 @@ struct Engine {
       off += (int64_t)b.r * b.c;
     }
     return e;
+  }
+  // computeOverlap(a, b) (src/MPSfunctions.hpp:2066-2085): identity MPO layers with a lower and b upper;
+  // the value is entry (0,0) of the first block of the last environment (0 if there is none).
+  static double overlap(Ctx* ctx, const std::vector<const Tensor*>& a, const std::vector<const Tensor*>& b,
+                        const std::vector<ItoKey>& ik) {
+    TensorP l = lmin(ctx);
+    for (size_t s = 0; s < a.size(); ++s) {
+      MPO id;
+      id.Dl = id.Dr = 1;
+      MPOEntry en;
+      en.wl = en.wr = 0;
+      for (uint32_t i = 0; i < (uint32_t)ik[s].size(); ++i) en.ops.push_back(OpEl{i, i, 1.0});
+      id.e.push_back(en);
+      l = env_update(ctx, *l, *a[s], id, ik[s], 1, nullptr, b[s]);
+    }
+    if (l->b.empty()) return 0.0;
+    double v = 0;
+    MPSG_CUDA(cudaMemcpyAsync(&v, l->d + l->b[0].off, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    return v;
   }
 };
 
@@ -275,11 +305,12 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   C(ctx)->sync();
   API_END
 }
-int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count(); }
+int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count() + eig_launch_count(); }
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
   API_BEGIN
-  MPSG_CHECK(method >= 0 && method <= 2,
-             "svd method must be 0 (Jacobi SVD), 1 (density matrix, batched) or 2 (density matrix, concurrent)");
+  MPSG_CHECK(method >= 0 && method <= 3,
+             "svd method must be 0 (Jacobi SVD), 1 (density matrix, cuSOLVER batched), 2 (density matrix, "
+             "cuSOLVER concurrent) or 3 (density matrix, own batched eigensolver)");
   C(ctx)->svd_method = method;
   API_END
 }
@@ -383,6 +414,55 @@ mpsg_status mpsg_add_contraction_layer(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor
   TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr);
   c->sync();
   *out = wrap(o);
+  API_END
+}
+
+mpsg_status mpsg_add_contraction_layer2(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor A, mpsg_tensor Ap,
+                                        const mpsg_mpo* W, const mpsg_itokey* ik, int32_t direction, mpsg_prec prec,
+                                        mpsg_tensor* out) {
+  API_BEGIN
+  MPSG_CHECK(out, "null output");
+  check_prec(prec);
+  Ctx* c = C(ctx);
+  MPSG_CHECK(T(A).b.size() > 0, "Error in addContractionLayer: A is empty.");
+  MPSG_CHECK(T(Ap).b.size() > 0, "Error in addContractionLayer: Ap is empty.");
+  TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr, &T(Ap));
+  c->sync();
+  *out = wrap(o);
+  API_END
+}
+
+mpsg_status mpsg_overlap(mpsg_ctx ctx, int32_t N, const mpsg_tensor* a, const mpsg_tensor* b, const mpsg_itokey* ik,
+                         double* out) {
+  API_BEGIN
+  MPSG_CHECK(N >= 1 && a && b && ik && out, "null argument or N < 1");
+  std::vector<const Tensor*> ta, tb;
+  std::vector<ItoKey> k;
+  for (int s = 0; s < N; ++s) {
+    MPSG_CHECK(a[s] && b[s], "null site tensor");
+    ta.push_back(&T(a[s]));
+    tb.push_back(&T(b[s]));
+    k.push_back(itokey_from_c(&ik[s]));
+  }
+  *out = mpsg::Engine::overlap(C(ctx), ta, tb, k);
+  API_END
+}
+
+mpsg_status mpsg_mpo_measure(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
+                             const mpsg_itokey* ik, double* out) {
+  API_BEGIN
+  MPSG_CHECK(N >= 1 && sites && W && ik && out, "null argument or N < 1");
+  std::vector<const Tensor*> ts;
+  std::vector<MPO> w;
+  std::vector<ItoKey> k;
+  for (int s = 0; s < N; ++s) {
+    MPSG_CHECK(sites[s], "null site tensor");
+    MPSG_CHECK(T(sites[s]).b.size() > 0, "Error in addContractionLayer: A is empty.");
+    ts.push_back(&T(sites[s]));
+    w.push_back(mpo_from_c(&W[s]));
+    k.push_back(itokey_from_c(&ik[s]));
+  }
+  *out = mpsg::Engine::mpo_expectation(C(ctx), ts, w, k);
   API_END
 }
 
@@ -630,6 +710,14 @@ mpsg_status mpsg_dmrg_measure_energy(mpsg_dmrg e, double* E) {
   API_BEGIN
   MPSG_CHECK(e && e->e && E, "null argument");
   *E = e->e->measure_energy();
+  API_END
+}
+mpsg_status mpsg_dmrg_measure_mpo(mpsg_dmrg e, const mpsg_mpo* W, double* out) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e && W && out, "null argument");
+  std::vector<MPO> w;
+  for (int s = 0; s < e->e->N; ++s) w.push_back(mpo_from_c(&W[s]));
+  *out = e->e->measure(w);
   API_END
 }
 void mpsg_dmrg_destroy(mpsg_dmrg e) {

@@ -26,6 +26,7 @@ Ctx::~Ctx() {
   if (svdp) cusolverDnDestroyGesvdjInfo(svdp);
   if (params) cusolverDnDestroyParams(params);
   for (auto h : whandles) cusolverDnDestroy(h);
+  for (auto h : wblas) cublasDestroy(h);
   for (auto s : wstreams) cudaStreamDestroy(s);
   if (part) cudaFreeAsync(part, stream);
   cudaStreamSynchronize(stream);
@@ -64,8 +65,12 @@ int Ctx::nworkers() {
     cusolverDnHandle_t h;
     if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreate failed");
     cusolverDnSetStream(h, s);
+    cublasHandle_t b;
+    if (cublasCreate(&b) != CUBLAS_STATUS_SUCCESS) throw Err(3, "cublasCreate failed");
+    cublasSetStream(b, s);
     wstreams.push_back(s);
     whandles.push_back(h);
+    wblas.push_back(b);
   }
   return kWorkers;
 }

@@ -1,5 +1,6 @@
 // Host-side core types of libmpsg (context, MPO terms, GEMM / lincomb plans).
 #pragma once
+#include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include "../../include/mpsg.h"
@@ -28,6 +29,7 @@ struct Ctx : std::enable_shared_from_this<Ctx> {
   // worker streams / solver handles for concurrent per-sector eigen-solves (created on first use)
   std::vector<cudaStream_t> wstreams;
   std::vector<cusolverDnHandle_t> whandles;
+  std::vector<cublasHandle_t> wblas;
   int nworkers();
   void sync();
 };

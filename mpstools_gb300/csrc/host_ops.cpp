@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -429,14 +430,15 @@ EnvPlan::~EnvPlan() {
     ctx->dfree(dT);
   }
 }
-void EnvPlan::run(const double* A, double* out_d) {
-  const double* bases[8] = {dCt, A, dT, out_d, nullptr, nullptr, nullptr, nullptr};
+void EnvPlan::run(const double* A, double* out_d, const double* Aup) {
+  const double* bases[8] = {dCt, A, dT, out_d, Aup ? Aup : A, nullptr, nullptr, nullptr};
   st1.run(bases);
   st2.run(bases);
 }
 
 std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
-                                   int direction) {
+                                   int direction, const Tensor* Aup) {
+  const Tensor& U = Aup ? *Aup : A;  // upper tensor (add_out_sub, src/MPSfunctions.hpp:360-434)
   std::unique_ptr<EnvPlan> P(new EnvPlan());
   P->ctx = ctx;
   P->keep = ctx->shared_from_this();
@@ -464,7 +466,7 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
           for (int i : it->second) {
             const Q a1 = BL.b[i].k.q0;
             const Q b1 = a1 + qat(ik, si);
-            const int au = A.find(K1(a1, b1, si));
+            const int au = U.find(K1(a1, b1, si));
             if (au < 0) continue;
             K5 ck{a1, a, en.wr, si, so};
             ctc[ck][std::make_tuple(i, e, o)] = op.v;
@@ -479,7 +481,7 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
           for (int i : it->second) {
             const Q b1 = BL.b[i].k.q0;
             const Q a1 = b1 - qat(ik, si);
-            const int au = A.find(K1(a1, b1, si));
+            const int au = U.find(K1(a1, b1, si));
             if (au < 0) continue;
             K5 ck{b1, b, en.wl, si, so};
             ctc[ck][std::make_tuple(i, e, o)] = op.v;
@@ -504,7 +506,7 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
   }
   for (auto& o : oterms) {
     const auto& f = o.second.begin()->second;
-    const Block& au = A.b[f.first];
+    const Block& au = U.b[f.first];
     const auto& TB = P->tt.at(f.second);
     if (left) P->out.add(o.first, au.c, TB.c);  // (chi_b' x chi_b)
     else P->out.add(o.first, au.r, TB.r);       // (chi_a' x chi_a)
@@ -519,7 +521,7 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
     P->build_ct.add(P->dCt + B.off, (int64_t)B.r * B.c, terms);
   }
   P->build_ct.run(ctx);
-  // bases: 0 = Ct, 1 = A, 2 = T, 3 = out
+  // bases: 0 = Ct, 1 = A (lower), 2 = T, 3 = out, 4 = upper tensor
   for (auto& x : tterms) {
     const auto& TB = P->tt.at(x.first);
     std::vector<GSegH> segs;
@@ -540,14 +542,14 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
     const Block& OB = P->out.b[P->out.idx.at(o.first)];
     std::vector<GSegH> segs;
     for (auto& s : o.second) {
-      const Block& au = A.b[s.second.first];
+      const Block& au = U.b[s.second.first];
       const auto& TB = P->tt.at(s.second.second);
-      if (left) {  // out(b',b) += A(a',b')^T T(a',b)
+      if (left) {  // out(b',b) += Aup(a',b')^T T(a',b)
         MPSG_CHECK(au.r == TB.r && au.c == OB.r && TB.c == OB.c, "inconsistent block sizes (env, stage 2)");
-        segs.push_back(GSegH{1, 2, au.off, TB.off, au.r, TB.r, au.r, 1, 0, 1.0});
-      } else {     // out(a',a) += A(a',b') T(a,b')^T
+        segs.push_back(GSegH{4, 2, au.off, TB.off, au.r, TB.r, au.r, 1, 0, 1.0});
+      } else {     // out(a',a) += Aup(a',b') T(a,b')^T
         MPSG_CHECK(au.c == TB.c && au.r == OB.r && TB.r == OB.c, "inconsistent block sizes (env, stage 2)");
-        segs.push_back(GSegH{1, 2, au.off, TB.off, au.r, TB.r, au.c, 0, 1, 1.0});
+        segs.push_back(GSegH{4, 2, au.off, TB.off, au.r, TB.r, au.c, 0, 1, 1.0});
       }
     }
     P->st2.add_problem(3, OB.off, OB.r, OB.r, OB.c, false, segs);
@@ -559,10 +561,10 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
 }
 
 TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
-                   double* flops_out) {
-  auto P = build_env(ctx, BL, A, W, ik, direction);
+                   double* flops_out, const Tensor* Aup) {
+  auto P = build_env(ctx, BL, A, W, ik, direction, Aup);
   TensorP out = make_tensor(ctx, 1, P->out, true);
-  P->run(A.d, out->d);
+  P->run(A.d, out->d, Aup ? Aup->d : nullptr);
   if (flops_out) *flops_out += P->flops;
   return out;
 }
@@ -682,9 +684,11 @@ struct SvdBatch {
     if (!x.trans) { *ld = x.ns; return dV + x.offV; }
     *ld = x.ms; return dU + x.offU;
   }
-  // Density-matrix route: G = Mst^T Mst (grouped FP64 GEMM), eigenpairs of G (cuSOLVER syevd, FP64),
-  // s = sqrt(lambda) descending, Vst = eigenvectors, Ust = Mst Vst / s.  Singular values below about
-  // 1e-8 of the sector's largest carry absolute errors ~1e-16/s (squared condition number).
+  // Density-matrix route: G = Mst^T Mst (grouped FP64 GEMM), eigenpairs of G (FP64), Vst = eigenvectors
+  // in descending order, Ust = Mst Vst with unit columns, s_j = |Mst v_j|.  The Gram matrix squares the
+  // condition number: eigenvalues below 32 n eps lambda_max are not resolved and their pairs are dropped
+  // (s_j = 0); above that floor u_i . u_j ~ n eps lambda_max / (s_i s_j), which CholeskyQR removes
+  // (orthonormalize_left), so the kept left vectors are orthonormal to rounding.
   // Batched density-matrix route: sectors are grouped by size class (next power of two >= ns, at
   // least 32); each G_i = Mst_i^T Mst_i is written into the top-left corner of its class slot and the
   // padding diagonal is set to -1, so the padded eigenvalues sort below the (non-negative) spectrum.
@@ -710,7 +714,6 @@ struct SvdBatch {
       }
     double* dB = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oB, 2));
     double* dWv = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oW, 2));
-    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
     int* dinf = (int*)ctx->dmalloc(sizeof(int) * (s.size() + 1));
     MPSG_CUDA(cudaMemsetAsync(dB, 0, sizeof(double) * std::max<int64_t>(oB, 2), ctx->stream));
     {  // G_i into the class slots, padding diagonal -1
@@ -768,8 +771,8 @@ struct SvdBatch {
       if (x.k == 0) continue;
       const int64_t nc = cls_of[i], pad = nc - x.ns;
       (void)pad;
-      post.push_back(GramPost{dB + slot_off[i], dWv + lam_off[i], dV + x.offV, dS + x.offS, dI + x.offS, x.ns,
-                              (int32_t)nc, (int32_t)nc});
+      post.push_back(GramPost{dB + slot_off[i], dWv + lam_off[i], dV + x.offV, dS + x.offS, x.ns, (int32_t)nc,
+                              (int32_t)nc});
     }
     if (!post.empty()) {
       GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
@@ -777,24 +780,147 @@ struct SvdBatch {
       launch_gram_post(d, (int)post.size(), ctx->stream);
       ctx->dfree(d);
     }
-    {  // Ust = Mst Vst, then columns scaled by 1/s
-      GemmPlan g;
-      std::vector<CopyOp> sc;
-      for (size_t i = 0; i < s.size(); ++i) {
-        const Sec& x = s[i];
-        if (x.k == 0) continue;
-        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
-        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
-      }
-      g.upload(ctx);
-      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
-      g.run(bases);
-      run_copyops(ctx, sc);
-    }
+    left_vectors();
+    orthonormalize_left();
     ctx->dfree(dB);
     ctx->dfree(dWv);
-    ctx->dfree(dI);
     ctx->dfree(dinf);
+    fixphase();
+  }
+
+  // Density-matrix route on the library's own batched eigensolver (eig_f64.cu): Gram matrices by the
+  // grouped FP64 GEMM, cluster-parallel Householder tridiagonalisation, bisection and inverse
+  // iteration for the eigenpairs above the resolution floor, reflector back-transformation, one
+  // Newton-Schulz step that re-orthonormalises the eigenvectors (inverse iteration leaves
+  // ~eps lambda_max / gap between eigenvalues that are not grouped), then the left vectors as in the
+  // other density routes.  Sectors wider than the cluster kernel's limit use run_gram.
+  void run_gram_custom() {
+    std::vector<int> idx;
+    int nmax = 0;
+    for (size_t i = 0; i < s.size(); ++i)
+      if (s[i].k > 0) {
+        idx.push_back((int)i);
+        nmax = std::max(nmax, s[i].ns);
+      }
+    if (idx.empty()) return;
+    if (nmax > sytrd_max_n()) { run_gram(); return; }
+    cudaStream_t st = ctx->stream;
+    MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(s.size(), 1), st));  // no solver status
+    std::vector<int64_t> offG(s.size(), 0);
+    int64_t oG = 0;
+    for (int i : idx) {
+      offG[i] = oG;
+      oG += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+    }
+    double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
+    // per sector: d (n), e (n), tau (n), W (n), meta (4)
+    double* dT = (double*)ctx->dmalloc(sizeof(double) * (size_t)(4 * nS + 4 * (int64_t)idx.size() + 2));
+    double *dd = dT, *de = dT + nS, *dtau = dT + 2 * nS, *dW = dT + 3 * nS, *dmeta = dT + 4 * nS;
+    {
+      GemmPlan g;
+      for (int i : idx)
+        g.add_problem(2, offG[i], s[i].ns, s[i].ns, s[i].ns, false,
+                      {GSegH{0, 0, s[i].offM, s[i].offM, s[i].ms, s[i].ms, s[i].ms, 1, 0, 1.0}});
+      g.upload(ctx);
+      const double* bases[8] = {dM, nullptr, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+    }
+    // 1. tridiagonalisation, one launch per cluster size
+    {
+      std::map<int, std::vector<SytrdOp>> byCL;
+      std::map<int, int> nmaxCL;
+      for (int i : idx) {
+        const int CL = sytrd_cluster_size(s[i].ns);
+        byCL[CL].push_back(SytrdOp{dG + offG[i], dd + s[i].offS, de + s[i].offS, dtau + s[i].offS, s[i].ns, s[i].ns});
+        nmaxCL[CL] = std::max(nmaxCL[CL], s[i].ns);
+      }
+      std::vector<void*> bufs;
+      for (auto& g : byCL) {
+        SytrdOp* d = (SytrdOp*)ctx->dmalloc(sizeof(SytrdOp) * g.second.size());
+        MPSG_CUDA(cudaMemcpyAsync(d, g.second.data(), sizeof(SytrdOp) * g.second.size(), cudaMemcpyHostToDevice, st));
+        launch_sytrd(d, (int)g.second.size(), g.first, nmaxCL[g.first], st);
+        bufs.push_back(d);
+      }
+      for (void* b : bufs) ctx->dfree(b);
+    }
+    // 2./3. eigenvalues and eigenvectors of T, written in descending order into V's columns
+    std::vector<TriOp> tops;
+    std::vector<int> op_of, k_of;
+    std::vector<int64_t> soff;
+    int64_t scratch = 0;
+    for (size_t t = 0; t < idx.size(); ++t) {
+      const Sec& x = s[idx[t]];
+      tops.push_back(TriOp{dd + x.offS, de + x.offS, dW + x.offS, dV + x.offV, dmeta + 4 * t,
+                           32.0 * x.ns * DBL_EPSILON, x.ns, x.ns});
+      for (int k = 0; k < x.ns; ++k) {
+        op_of.push_back((int)t);
+        k_of.push_back(k);
+        soff.push_back(scratch);
+        scratch += 5 * (int64_t)x.ns;
+      }
+    }
+    const int nthreads = (int)op_of.size();
+    TriOp* dtops = (TriOp*)ctx->dmalloc(sizeof(TriOp) * tops.size());
+    int* dmap = (int*)ctx->dmalloc(sizeof(int) * 2 * (size_t)nthreads);
+    int64_t* dsoff = (int64_t*)ctx->dmalloc(sizeof(int64_t) * (size_t)nthreads);
+    double* dscr = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(scratch, 2));
+    MPSG_CUDA(cudaMemcpyAsync(dtops, tops.data(), sizeof(TriOp) * tops.size(), cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int) * nthreads, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap + nthreads, k_of.data(), sizeof(int) * nthreads, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dsoff, soff.data(), sizeof(int64_t) * nthreads, cudaMemcpyHostToDevice, st));
+    launch_tri_bounds(dtops, (int)tops.size(), st);
+    launch_tri_bisect(dtops, dmap, dmap + nthreads, nthreads, 0.0, st);
+    launch_tri_invit(dtops, dmap, dmap + nthreads, nthreads, 1e-12, dscr, dsoff, st);
+    // 4. back-transformation V = Q Z, blocks of 8 columns
+    {
+      std::vector<OrmtrOp> oo;
+      for (int i : idx)
+        for (int c0 = 0; c0 < s[i].ns; c0 += 8)
+          oo.push_back(OrmtrOp{dG + offG[i], dtau + s[i].offS, dV + s[i].offV, s[i].ns, s[i].ns, s[i].ns, c0,
+                               std::min(c0 + 8, s[i].ns)});
+      OrmtrOp* d = (OrmtrOp*)ctx->dmalloc(sizeof(OrmtrOp) * oo.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, oo.data(), sizeof(OrmtrOp) * oo.size(), cudaMemcpyHostToDevice, st));
+      launch_ormtr(d, (int)oo.size(), nmax, st);
+      ctx->dfree(d);
+    }
+    // 5. S = sqrt(W); one Newton-Schulz step V <- V (1.5 I - 0.5 V^T V) (G's storage reused for C)
+    {
+      GemmPlan gc;
+      for (int i : idx)
+        gc.add_problem(2, offG[i], s[i].ns, s[i].ns, s[i].ns, false,
+                       {GSegH{1, 1, s[i].offV, s[i].offV, s[i].ns, s[i].ns, s[i].ns, 1, 0, 1.0}});
+      gc.upload(ctx);
+      const double* bases[8] = {nullptr, dV, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
+      gc.run(bases);
+      std::vector<EigPostOp> po;
+      for (size_t t = 0; t < idx.size(); ++t) {
+        const Sec& x = s[idx[t]];
+        po.push_back(EigPostOp{dW + x.offS, dS + x.offS, dG + offG[idx[t]], x.ns, x.ns});
+      }
+      EigPostOp* d = (EigPostOp*)ctx->dmalloc(sizeof(EigPostOp) * po.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, po.data(), sizeof(EigPostOp) * po.size(), cudaMemcpyHostToDevice, st));
+      launch_eig_post(d, (int)po.size(), st);
+      ctx->dfree(d);
+      GemmPlan gv;  // U's storage holds V P, copied back into V
+      std::vector<CopyOp> cp;
+      for (int i : idx) {
+        const Sec& x = s[i];
+        gv.add_problem(2, x.offU, x.ns, x.ns, x.ns, false, {GSegH{1, 0, x.offV, offG[i], x.ns, x.ns, x.ns, 0, 0, 1.0}});
+        cp.push_back(CopyOp{dU + x.offU, dV + x.offV, nullptr, nullptr, x.ns, x.ns, x.ns, x.ns, 0, 1.0});
+      }
+      gv.upload(ctx);
+      const double* bv[8] = {dG, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
+      gv.run(bv);
+      run_copyops(ctx, cp);
+    }
+    ctx->dfree(dscr);
+    ctx->dfree(dsoff);
+    ctx->dfree(dmap);
+    ctx->dfree(dtops);
+    ctx->dfree(dT);
+    ctx->dfree(dG);
+    left_vectors();
+    orthonormalize_left();
     fixphase();
   }
 
@@ -814,7 +940,6 @@ struct SvdBatch {
     std::sort(order.begin(), order.end(), [&](int a, int b) { return s[a].ns > s[b].ns; });
     double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
     double* dL = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
-    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
     {
       GemmPlan g;
       for (int i : order)
@@ -866,30 +991,18 @@ struct SvdBatch {
       if (!e.empty()) throw Err(3, e);
     std::vector<GramPost> post;
     for (int i : order)
-      post.push_back(GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns,
-                              s[i].ns, s[i].ns});
+      post.push_back(GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, s[i].ns, s[i].ns,
+                              s[i].ns});
     if (!post.empty()) {
       GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
       MPSG_CUDA(cudaMemcpyAsync(d, post.data(), sizeof(GramPost) * post.size(), cudaMemcpyHostToDevice, ctx->stream));
       launch_gram_post(d, (int)post.size(), ctx->stream);
       ctx->dfree(d);
     }
-    {
-      GemmPlan g;
-      std::vector<CopyOp> sc;
-      for (int i : order) {
-        const Sec& x = s[i];
-        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
-        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
-      }
-      g.upload(ctx);
-      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
-      g.run(bases);
-      run_copyops(ctx, sc);
-    }
+    left_vectors();
+    orthonormalize_left();
     ctx->dfree(dG);
     ctx->dfree(dL);
-    ctx->dfree(dI);
     fixphase();
   }
 
@@ -904,7 +1017,6 @@ struct SvdBatch {
     }
     double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
     double* dL = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
-    double* dI = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));
     {  // G_i = Mst_i^T Mst_i
       GemmPlan g;
       for (size_t i = 0; i < s.size(); ++i) {
@@ -938,8 +1050,7 @@ struct SvdBatch {
     for (size_t i = 0; i < s.size(); ++i) {
       if (s[i].k == 0) continue;
       post.push_back(
-          GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, dI + s[i].offS, s[i].ns, s[i].ns,
-                   s[i].ns});
+          GramPost{dG + offG[i], dL + s[i].offS, dV + s[i].offV, dS + s[i].offS, s[i].ns, s[i].ns, s[i].ns});
     }
     if (!post.empty()) {
       GramPost* d = (GramPost*)ctx->dmalloc(sizeof(GramPost) * post.size());
@@ -947,29 +1058,121 @@ struct SvdBatch {
       launch_gram_post(d, (int)post.size(), ctx->stream);
       ctx->dfree(d);
     }
-    {  // Ust = Mst Vst, then columns scaled by 1/s
-      GemmPlan g;
-      std::vector<CopyOp> sc;
-      for (size_t i = 0; i < s.size(); ++i) {
-        const Sec& x = s[i];
-        if (x.k == 0) continue;
-        g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
-        sc.push_back(CopyOp{dU + x.offU, dU + x.offU, nullptr, dI + x.offS, x.ms, x.k, x.ms, x.ms, 0, 1.0});
-      }
-      g.upload(ctx);
-      const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
-      g.run(bases);
-      run_copyops(ctx, sc);
-    }
+    left_vectors();
+    orthonormalize_left();
     ctx->dfree(dG);
     ctx->dfree(dL);
-    ctx->dfree(dI);
     fixphase();
+  }
+
+  // Ust = Mst Vst with unit columns; s_j = |Mst v_j| (columns whose eigenvalue was below the Gram
+  // route's resolution keep s_j = 0 and a zero column).
+  void left_vectors() {
+    GemmPlan g;
+    std::vector<ColNorm> cn;
+    for (size_t i = 0; i < s.size(); ++i) {
+      const Sec& x = s[i];
+      if (x.k == 0) continue;
+      g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
+      cn.push_back(ColNorm{dU + x.offU, dS + x.offS, x.ms, x.k, x.ms});
+    }
+    g.upload(ctx);
+    const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
+    g.run(bases);
+    if (!cn.empty()) {
+      ColNorm* d = (ColNorm*)ctx->dmalloc(sizeof(ColNorm) * cn.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, cn.data(), sizeof(ColNorm) * cn.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_colnorm(d, (int)cn.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+  }
+
+  // CholeskyQR of every sector's Ust (columns in descending s order): C = U^T U, C = R^T R (cuSOLVER
+  // potrf), U <- U R^-1 (cuBLAS trsm); s_j is multiplied by R_jj (the norm of y_j after removing its
+  // components along the larger pairs).  The resolution floor bounds |C - I| well below 1, so one
+  // pass leaves U orthonormal to rounding (error ~ eps cond(U)^2).  Sectors are spread over the
+  // worker streams, largest first; the context stream waits for all of them.
+  void orthonormalize_left() {
+    const int nw = ctx->nworkers();
+    std::vector<int> idx;
+    for (size_t i = 0; i < s.size(); ++i)
+      if (s[i].k > 0) idx.push_back((int)i);
+    if (idx.empty()) return;
+    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return s[a].ns > s[b].ns; });
+    std::vector<int64_t> offC(s.size(), 0);
+    int64_t oC = 0;
+    int lwork = 0;
+    for (int i : idx) {
+      offC[i] = oC;
+      oC += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+    }
+    double* dC = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
+    for (int i : idx) {
+      int lw = 0;
+      if (cusolverDnDpotrf_bufferSize(ctx->whandles[0], CUBLAS_FILL_MODE_UPPER, s[i].ns, dC + offC[i], s[i].ns, &lw) !=
+          CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "potrf_bufferSize failed");
+      lwork = std::max(lwork, lw);
+    }
+    lwork = std::max(lwork, 2);
+    double* work = (double*)ctx->dmalloc(sizeof(double) * (size_t)lwork * nw);
+    int* dinf = (int*)ctx->dmalloc(sizeof(int) * idx.size());
+    std::vector<CholOp> ops;
+    for (int i : idx) ops.push_back(CholOp{dC + offC[i], dS + s[i].offS, s[i].ns, s[i].ns});
+    CholOp* dops = (CholOp*)ctx->dmalloc(sizeof(CholOp) * ops.size());
+    MPSG_CUDA(cudaMemcpyAsync(dops, ops.data(), sizeof(CholOp) * ops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    GemmPlan g;
+    for (int i : idx)
+      g.add_problem(2, offC[i], s[i].ns, s[i].ns, s[i].ns, false,
+                    {GSegH{0, 0, s[i].offU, s[i].offU, s[i].ms, s[i].ms, s[i].ms, 1, 0, 1.0}});
+    g.upload(ctx);
+    cudaEvent_t fork;
+    std::vector<cudaEvent_t> join(nw);
+    MPSG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    for (auto& e : join) MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    const double one = 1.0;
+    std::string err;
+    for (int pass = 0; pass < 1 && err.empty(); ++pass) {
+      const double* bases[8] = {dU, nullptr, dC, nullptr, nullptr, nullptr, nullptr, nullptr};
+      g.run(bases);
+      launch_chol_unit_zero_diag(dops, (int)ops.size(), ctx->stream);
+      MPSG_CUDA(cudaEventRecord(fork, ctx->stream));
+      for (int w = 0; w < nw; ++w) MPSG_CUDA(cudaStreamWaitEvent(ctx->wstreams[w], fork, 0));
+      for (size_t t = 0; t < idx.size() && err.empty(); ++t) {
+        const int i = idx[t], w = (int)(t % nw);
+        const Sec& x = s[i];
+        if (cusolverDnDpotrf(ctx->whandles[w], CUBLAS_FILL_MODE_UPPER, x.ns, dC + offC[i], x.ns,
+                             work + (size_t)w * lwork, lwork, dinf + pass * idx.size() + t) != CUSOLVER_STATUS_SUCCESS)
+          err = "potrf failed";
+        else if (cublasDtrsm(ctx->wblas[w], CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
+                             CUBLAS_DIAG_NON_UNIT, x.ms, x.ns, &one, dC + offC[i], x.ns, dU + x.offU, x.ms) !=
+                 CUBLAS_STATUS_SUCCESS)
+          err = "trsm failed";
+      }
+      for (int w = 0; w < nw; ++w) {
+        MPSG_CUDA(cudaEventRecord(join[w], ctx->wstreams[w]));
+        MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, join[w], 0));
+      }
+      if (pass == 0) launch_chol_scale_s(dops, (int)ops.size(), ctx->stream);
+    }
+    std::vector<int> inf(idx.size(), 0);
+    MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * inf.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    cudaEventDestroy(fork);
+    for (auto& e : join) cudaEventDestroy(e);
+    ctx->dfree(dops);
+    ctx->dfree(dinf);
+    ctx->dfree(work);
+    ctx->dfree(dC);
+    if (!err.empty()) throw Err(3, err);
+    for (int v : inf)
+      if (v != 0) throw Err(3, "Cholesky of the left-vector overlap failed (info=" + std::to_string(v) + ")");
   }
 
   void run(int method) {
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
+    else if (method == 3) run_gram_custom();
     else run_jacobi();
   }
 
@@ -1432,14 +1635,15 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
     return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st);
   }
-  const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_BF16X3 : prec;
+  const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_TF32X3 : prec;
   LanczosResult r;
   {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
     r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo));
   }
   if (prec != MPSG_PREC_AUTO) return r;
-  // FP64 finish: Lanczos restarted from the mixed-precision ground state, energy test every iteration
+  // FP64 finish: the reference's Lanczos restarted from the mixed-precision ground state, energy test
+  // every iteration, so the final energy carries the same convergence criterion as the FP64 path
   auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
   TensorP start = tensor_copy(psi);
   LanczosResult r2 = lanczos(ctx, *mv64, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0);

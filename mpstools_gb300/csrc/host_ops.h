@@ -98,13 +98,15 @@ struct EnvPlan {
   GemmPlan st1, st2;
   LincombPlan build_ct;
   double flops = 0;
-  void run(const double* A, double* out_d);
+  // A: lower tensor data; Aup: upper tensor data (nullptr: the lower tensor is also the upper one)
+  void run(const double* A, double* out_d, const double* Aup = nullptr);
   ~EnvPlan();
 };
+// Aup (optional): separate upper tensor, the two-tensor addContractionLayer(BL, A, mpo, Ap, ...)
 std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
-                                   int direction);
+                                   int direction, const Tensor* Aup = nullptr);
 TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
-                   double* flops_out);
+                   double* flops_out, const Tensor* Aup = nullptr);
 
 // theta(a,b;s1,s2) = A1(a,c;s1) A2(c,b;s2)
 TensorP theta_form(Ctx* ctx, const Tensor& A1, const Tensor& A2, const Layout* layout);

@@ -173,11 +173,11 @@ void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s) {
 }
 
 // ============================================================================ density-matrix SVD post-processing
-// s_i = sqrt(max(lambda_{n-1-i}, 0)), 1/s_i (0 for s_i = 0), V(:, i) = W(:, n-1-i)
+// s_i = sqrt(lambda_(i)) for the i-th largest eigenvalue, V(:, i) = its eigenvector
 // The eigenpairs come from an nc x nc slot whose padding eigenvalues are -1; the n eigenvalues
 // >= -0.5 are the sector's, in any order.  They are ranked descending (ties by index) without
 // relying on the solver's ordering.  Eigenvalues at or below the eigensolver's noise level
-// (8 n eps lambda_max) are not resolved by the Gram route and are reported as exact zeros, so
+// (32 n eps lambda_max) are not resolved by the Gram route and are reported as exact zeros, so
 // truncation never keeps their vectors.
 __global__ void k_gram_post(const GramPost* __restrict__ ops) {
   const GramPost o = ops[blockIdx.x];
@@ -189,7 +189,7 @@ __global__ void k_gram_post(const GramPost* __restrict__ ops) {
     lmax_s = m;
   }
   __syncthreads();
-  const double floor_l = 8.0 * n * DBL_EPSILON * lmax_s;
+  const double floor_l = 32.0 * n * DBL_EPSILON * lmax_s;
   for (int j = threadIdx.x; j < nc; j += blockDim.x) {
     const double lj = o.lam[j];
     if (!(lj > -0.5)) continue;  // padding
@@ -201,7 +201,6 @@ __global__ void k_gram_post(const GramPost* __restrict__ ops) {
     if (rank >= n) continue;  // defensive: more than n non-padding eigenvalues
     const double sv = lj > floor_l ? sqrt(lj) : 0.0;
     o.S[rank] = sv;
-    o.invS[rank] = sv > 0.0 ? 1.0 / sv : 0.0;
     const double* w = o.W + (int64_t)j * o.ldw;
     double* v = o.V + (int64_t)rank * n;
     for (int r = 0; r < n; ++r) v[r] = w[r];
@@ -210,6 +209,55 @@ __global__ void k_gram_post(const GramPost* __restrict__ ops) {
 void launch_gram_post(const GramPost* ops, int nops, cudaStream_t s) {
   if (nops <= 0) return;
   k_gram_post<<<nops, 256, 0, s>>>(ops);
+  LAUNCHED();
+}
+// Left vectors of the density-matrix route: y_j = M v_j has norm s_j (the singular value the pair
+// (u_j, v_j) actually carries, free of the Gram eigenvalue's absolute error), u_j = y_j / s_j is unit
+// length; unresolved columns (S already 0) are cleared so truncation never keeps them.
+// One block per sector, one warp per column at a time.
+__global__ void k_colnorm(const ColNorm* __restrict__ ops) {
+  const ColNorm o = ops[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int j = warp; j < o.k; j += nwarp) {
+    double* u = o.U + (int64_t)j * o.ldu;
+    if (o.S[j] == 0.0) {
+      for (int r = lane; r < o.m; r += 32) u[r] = 0.0;
+      continue;
+    }
+    double acc = 0.0;
+    for (int r = lane; r < o.m; r += 32) acc = fma(u[r], u[r], acc);
+    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    const double nrm = sqrt(acc);
+    const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    for (int r = lane; r < o.m; r += 32) u[r] *= inv;
+    __syncwarp();
+    if (lane == 0) o.S[j] = nrm;
+  }
+}
+void launch_colnorm(const ColNorm* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_colnorm<<<nops, 256, 0, s>>>(ops);
+  LAUNCHED();
+}
+__global__ void k_chol_unit_zero_diag(const CholOp* __restrict__ ops) {
+  const CholOp o = ops[blockIdx.x];
+  for (int j = threadIdx.x; j < o.n; j += blockDim.x) {
+    double* c = o.C + j + (int64_t)j * o.ld;
+    if (*c == 0.0) *c = 1.0;
+  }
+}
+void launch_chol_unit_zero_diag(const CholOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_chol_unit_zero_diag<<<nops, 128, 0, s>>>(ops);
+  LAUNCHED();
+}
+__global__ void k_chol_scale_s(const CholOp* __restrict__ ops) {
+  const CholOp o = ops[blockIdx.x];
+  for (int j = threadIdx.x; j < o.n; j += blockDim.x) o.S[j] *= fabs(o.C[j + (int64_t)j * o.ld]);
+}
+void launch_chol_scale_s(const CholOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_chol_scale_s<<<nops, 128, 0, s>>>(ops);
   LAUNCHED();
 }
 __global__ void k_gram_pad(const GramPad* __restrict__ ops) {

@@ -126,13 +126,51 @@ struct CopyOp {  // dst(i,j) = scale * rs[i] * cs[j] * (trans ? src(j,i) : src(i
   int32_t rows, cols, lds, ldd, trans;
   double scale;
 };
-struct GramPost {  // eigenpairs of an nc x nc slot (padding eigenvalues -1) -> s descending, 1/s, V (n x n)
+struct GramPost {  // eigenpairs of an nc x nc slot (padding eigenvalues -1) -> s descending (0 if unresolved), V
   const double* W;   // eigenvectors, column j at W + j*ldw (rows 0..n-1 belong to the sector)
   const double* lam; // nc eigenvalues, any order
   double* V;
   double* S;
-  double* invS;
   int32_t n, ldw, nc;
+};
+struct ColNorm {  // U (m x k, column j at U + j*ldu): s_j = |U(:, j)|, U(:, j) /= s_j; columns with S[j] == 0 zeroed
+  double* U;
+  double* S;
+  int32_t m, k, ldu;
+};
+struct CholOp {  // square n x n matrix C (leading dimension ld) of one sector, and its singular values S
+  double* C;
+  double* S;
+  int32_t n, ld;
+};
+// ---- batched FP64 symmetric eigensolver (eig_f64.cu)
+struct SytrdOp {  // n x n symmetric matrix A (full storage); out: diagonal d, off-diagonal e, reflectors in A
+  double* A;
+  double* d;
+  double* e;
+  double* tau;
+  int32_t n, lda;
+};
+struct TriOp {  // tridiagonal (d, e) of one sector -> W (eigenvalues, descending; -1 below the floor), Z
+  const double* d;
+  const double* e;
+  double* W;
+  double* Z;
+  double* meta;  // 4 doubles: lambda_max, pivmin, Gershgorin lo, hi
+  double floor_rel;
+  int32_t n, ldz;
+};
+struct OrmtrOp {  // columns [c0, c1) of Z <- Q Z with the reflectors of SytrdOp
+  const double* A;
+  const double* tau;
+  double* Z;
+  int32_t n, lda, ldz, c0, c1;
+};
+struct EigPostOp {  // S = sqrt(W) (0 below the floor); C <- 1.5 I - 0.5 C (n x n, leading dimension ldc)
+  const double* W;
+  double* S;
+  double* C;
+  int32_t n, ldc;
 };
 struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
   double* A;
@@ -152,6 +190,11 @@ void launch_copyops(const CopyOp* ops, int nops, cudaStream_t s);
 void launch_fixphase(const PhaseOp* ops, int nops, int maxk, cudaStream_t s);
 void launch_gram_post(const GramPost* ops, int nops, cudaStream_t s);
 void launch_gram_pad(const GramPad* ops, int nops, cudaStream_t s);
+void launch_colnorm(const ColNorm* ops, int nops, cudaStream_t s);
+// C_jj = 1 where C_jj == 0 (zero columns of U stay zero through C = R^T R, U R^-1)
+void launch_chol_unit_zero_diag(const CholOp* ops, int nops, cudaStream_t s);
+// S_j *= |R_jj| for the Cholesky factor R stored in C's upper triangle
+void launch_chol_scale_s(const CholOp* ops, int nops, cudaStream_t s);
 // Lanczos vector kernels; `part` is a scratch array of kRedBlocks doubles
 constexpr int kRedBlocks = 608;
 void launch_dot(const double* x, const double* y, int64_t n, double* part, double* out, cudaStream_t s);
@@ -172,5 +215,17 @@ void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, in
                      double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s);
 void launch_fill(double* x, int64_t n, double v, cudaStream_t s);
 int64_t kernel_launch_count();
+int64_t eig_launch_count();
+int sytrd_cluster_size(int n);
+int sytrd_max_n();
+size_t sytrd_smem_bytes(int n, int CL);
+void launch_sytrd(const SytrdOp* ops, int nops, int CL, int nmax, cudaStream_t s);
+void launch_tri_bounds(const TriOp* ops, int nops, cudaStream_t s);
+void launch_tri_bisect(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double floor_rel_unused,
+                       cudaStream_t s);
+void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double gap_rel,
+                      double* scratch, const int64_t* scratch_off, cudaStream_t s);
+void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s);
+void launch_eig_post(const EigPostOp* ops, int nops, cudaStream_t s);
 
 }  // namespace mpsg

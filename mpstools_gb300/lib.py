@@ -50,6 +50,9 @@ def load(build_if_missing: bool = False):
     L.mpsg_tensor_destroy.restype = None
     L.mpsg_contract_twosite.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, i32, P(vp)]
     L.mpsg_add_contraction_layer.argtypes = [vp, vp, vp, vp, vp, i32, i32, P(vp)]
+    L.mpsg_add_contraction_layer2.argtypes = [vp, vp, vp, vp, vp, vp, i32, i32, P(vp)]
+    L.mpsg_overlap.argtypes = [vp, i32, vp, vp, vp, P(f64)]
+    L.mpsg_mpo_measure.argtypes = [vp, i32, vp, vp, vp, P(f64)]
     L.mpsg_theta.argtypes = [vp, vp, vp, P(vp)]
     L.mpsg_split2.argtypes = [vp, vp, vp, vp, u32, i32, f64, i32, P(vp), P(vp), P(vp), P(f64), P(u32)]
     L.mpsg_lanczos2.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, i32, P(vp), P(f64), P(i32)]
@@ -64,6 +67,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_site.argtypes = [vp, i32, P(vp)]
     L.mpsg_dmrg_lambda.argtypes = [vp, i32, P(vp)]
     L.mpsg_dmrg_measure_energy.argtypes = [vp, P(f64)]
+    L.mpsg_dmrg_measure_mpo.argtypes = [vp, vp, P(f64)]
     L.mpsg_dmrg_destroy.argtypes = [vp]
     L.mpsg_dmrg_destroy.restype = None
     L.mpsg_dmrg_build_environments.argtypes = [vp, i32]
@@ -105,8 +109,9 @@ class Context:
         return int(self.L.mpsg_ctx_kernel_launches(self.h))
 
     def set_svd_method(self, method):
-        """'jacobi' (0, default) or 'density' (1): see mpsg_ctx_set_svd_method."""
-        m = {"jacobi": 0, "density": 1, "density_mt": 2}.get(method, method)
+        """'jacobi' (0, default), 'density' (1), 'density_mt' (2), 'density_eig' (3): see
+        mpsg_ctx_set_svd_method."""
+        m = {"jacobi": 0, "density": 1, "density_mt": 2, "density_eig": 3}.get(method, method)
         check(self.L.mpsg_ctx_set_svd_method(self.h, int(m)))
 
     def set_stream(self, stream_ptr: int | None):
@@ -307,3 +312,29 @@ class ItoKeyArg:
 
     def ref(self):
         return C.byref(self.s)
+
+
+class MPOArray:
+    """Contiguous mpsg_mpo[N] for entry points that take one MPO tensor per site."""
+
+    def __init__(self, mpos):
+        self.items = [MPOArg(w) for w in mpos]
+        self.arr = (_MPOStruct * len(self.items))(*[m.s for m in self.items])
+
+    def ptr(self):
+        return C.cast(self.arr, C.c_void_p)
+
+
+class ItoKeyArray:
+    """Contiguous mpsg_itokey[N]."""
+
+    def __init__(self, iks):
+        self.items = [ItoKeyArg(k) for k in iks]
+        self.arr = (_ItoKeyStruct * len(self.items))(*[k.s for k in self.items])
+
+    def ptr(self):
+        return C.cast(self.arr, C.c_void_p)
+
+
+def handle_array(tensors):
+    return (C.c_void_p * len(tensors))(*[t.h for t in tensors])

@@ -98,6 +98,22 @@ def spinless_fermions_mpo(V, t, mu):
     return W
 
 
+def local_operator_mpo(N, site, op):
+    """D = 1 MPO of the d x d operator `op` (op[out, in]) on `site`, identity elsewhere: MPO::measure
+    with it gives the local expectation value <op_site> (the role of SparseLocalOperator::measure,
+    src/MPOTypes.hpp:532-563, for states that are not in Vidal form)."""
+    op = np.asarray(op, dtype=np.float64)
+    d = op.shape[0]
+    W = []
+    for s in range(N):
+        if s == site:
+            terms = [(0, 0, o, i, float(op[o, i])) for i in range(d) for o in range(d) if op[o, i] != 0.0]
+        else:
+            terms = [(0, 0, i, i, 1.0) for i in range(d)]
+        W.append((terms, 1, 1))
+    return W
+
+
 def u1_itokeys(N, d=2):
     """itokey per site: local state n -> charge n (spin-1/2: down->0, up->1; fermions: empty->0, full->1)."""
     return [[k for k in range(d)] for _ in range(N)]

@@ -332,9 +332,11 @@ static void drop_dangling(BM& L, const Diag& lam, BM& R) {
 }
 
 // ---------------------------------------------------------------- env update
-// add_out_sub_2 (MPSfunctions.hpp:276-352)
+// add_out_sub_2 (MPSfunctions.hpp:276-352); with a separate upper tensor Ap it is add_out_sub
+// (MPSfunctions.hpp:360-434): lower blocks from A, upper blocks from Ap.
 static BM add_out_sub_2(const std::map<uint32_t, std::vector<BM::const_iterator>>& BLits, const BM& A,
-                        const MPOMat& mpo, Q p, const ItoKey& ik, int direction) {
+                        const MPOMat& mpo, Q p, const ItoKey& ik, int direction, const BM* Ap = nullptr) {
+  const BM& Aup = Ap ? *Ap : A;
   const int idir = direction > 0 ? 1 : 0;
   BM B;
   for (auto& a : A)
@@ -359,8 +361,8 @@ static BM add_out_sub_2(const std::map<uint32_t, std::vector<BM::const_iterator>
         if (direction <= 0 && kb.q1 != key_b.q1) continue;
         Q kyin = ik[oi.first.in];
         Key key_a = direction > 0 ? K1(kb.q0, kb.q0 + kyin, oi.first.in) : K1(kb.q0 - kyin, kb.q0, oi.first.in);
-        auto posa = A.find(key_a);
-        if (posa == A.end()) continue;
+        auto posa = Aup.find(key_a);
+        if (posa == Aup.end()) continue;
         Mat T2;
         if (direction > 0) {
           Mat T1 = gemm(1.0, itBL->second, 't', posa->second, 'n');
@@ -380,9 +382,10 @@ static BM add_out_sub_2(const std::map<uint32_t, std::vector<BM::const_iterator>
   return Bout;
 }
 
-// addContractionLayer (MPSfunctions.hpp:442-493)
+// addContractionLayer (MPSfunctions.hpp:442-493); the two-tensor overload (MPSfunctions.hpp:500-556)
+// when Ap is given (A lower, Ap upper)
 static BM add_contraction_layer(const BM& BL, const BM& A, const MPOMat& mpo, const ItoKey& ik,
-                                int direction, int maxthreads) {
+                                int direction, int maxthreads, const BM* Ap = nullptr) {
   const int idir = direction > 0 ? 1 : 0;
   std::set<Q> outs;
   for (auto& a : A) outs.insert(idir ? a.first.q1 : a.first.q0);
@@ -393,7 +396,7 @@ static BM add_contraction_layer(const BM& BL, const BM& A, const MPOMat& mpo, co
   const int n = (int)outgoing.size();
 #pragma omp parallel for num_threads(maxthreads) schedule(dynamic)
   for (int i = 0; i < n; ++i) {
-    BM Bi = add_out_sub_2(BLits, A, mpo, outgoing[i], ik, direction);
+    BM Bi = add_out_sub_2(BLits, A, mpo, outgoing[i], ik, direction, Ap);
     merge(bouts[omp_get_thread_num()], Bi);
   }
   BM out;
@@ -1036,6 +1039,43 @@ void* orc_contract_twosite(void* L, void* R, void* th, void* W1, void* W2, const
 void* orc_add_contraction_layer(void* BL, void* A, void* W, const uint64_t* ik, int d, int dir, int nthreads) {
   ItoKey a(ik, ik + d);
   return wrap_bm(add_contraction_layer(((orc_bm_t*)BL)->m, ((orc_bm_t*)A)->m, ((orc_mpo_t*)W)->w, a, dir, nthreads), 1);
+}
+// two-tensor addContractionLayer(BL, A, mpo, Ap, itokey, dir) (MPSfunctions.hpp:500-556): A lower, Ap upper
+void* orc_add_contraction_layer2(void* BL, void* A, void* Ap, void* W, const uint64_t* ik, int d, int dir,
+                                 int nthreads) {
+  ItoKey a(ik, ik + d);
+  return wrap_bm(add_contraction_layer(((orc_bm_t*)BL)->m, ((orc_bm_t*)A)->m, ((orc_mpo_t*)W)->w, a, dir, nthreads,
+                                       &((orc_bm_t*)Ap)->m),
+                 1);
+}
+// computeOverlap(a, b) (MPSfunctions.hpp:2066-2085): identity MPO (D = 1) layers, a lower, b upper.
+// ik holds the sites' i_to_key tables back to back, d[s] entries for site s.
+double orc_overlap(int N, void* const* a, void* const* b, const uint64_t* ik, const int* d, int nthreads) {
+  BM L = get_lmin();
+  size_t off = 0;
+  for (int s = 0; s < N; ++s) {
+    ItoKey k(ik + off, ik + off + d[s]);
+    off += d[s];
+    MPOMat id;
+    for (int i = 0; i < d[s]; ++i) id.m[{0u, 0u}][OpKey{(uint32_t)i, (uint32_t)i}] = 1.0;
+    id.Dl = id.Dr = 1;
+    L = add_contraction_layer(L, ((orc_bm_t*)a[s])->m, id, k, 1, nthreads, &((orc_bm_t*)b[s])->m);
+  }
+  return L.empty() ? 0.0 : L.begin()->second(0, 0);
+}
+// MPO::measure(mps) (MPOTypes.hpp:990-1020) on given site tensors and MPO tensors
+double orc_mpo_measure(int N, void* const* sites, void* const* W, const uint64_t* ik, const int* d, int nthreads) {
+  std::vector<BM> s;
+  std::vector<MPOMat> w;
+  std::vector<ItoKey> k;
+  size_t off = 0;
+  for (int i = 0; i < N; ++i) {
+    s.push_back(((orc_bm_t*)sites[i])->m);
+    w.push_back(((orc_mpo_t*)W[i])->w);
+    k.push_back(ItoKey(ik + off, ik + off + d[i]));
+    off += d[i];
+  }
+  return mpo_measure(s, w, k, nthreads);
 }
 int orc_split(void* th, const uint64_t* ik0, int d0, const uint64_t* ik1, int d1, int chimax,
               int doTrunc, double tr_weight, int normalize, int nthreads, void** U, void** Vt,

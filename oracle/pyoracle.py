@@ -75,6 +75,12 @@ def lib():
     L.orc_contract_twosite.argtypes = [vp, vp, vp, vp, vp, vp, i32, vp, i32, i32]
     L.orc_add_contraction_layer.restype = vp
     L.orc_add_contraction_layer.argtypes = [vp, vp, vp, vp, i32, i32, i32]
+    L.orc_add_contraction_layer2.restype = vp
+    L.orc_add_contraction_layer2.argtypes = [vp, vp, vp, vp, vp, i32, i32, i32]
+    L.orc_overlap.restype = f64
+    L.orc_overlap.argtypes = [i32, vp, vp, vp, vp, i32]
+    L.orc_mpo_measure.restype = f64
+    L.orc_mpo_measure.argtypes = [i32, vp, vp, vp, vp, i32]
     L.orc_split.argtypes = [vp, vp, i32, vp, i32, i32, i32, f64, i32, i32, P(vp), P(vp), P(vp),
                             P(f64), P(i32)]
     L.orc_lanczos.argtypes = [vp, vp, vp, vp, vp, vp, i32, vp, i32, i32, f64, i32, i32, P(f64),
@@ -242,6 +248,60 @@ def add_contraction_layer(BL, A, W, ik, direction, nthreads=8):
     L.orc_bm_free(hA)
     L.orc_mpo_free(w)
     return out
+
+
+def add_contraction_layer2(BL, A, Ap, W, ik, direction, nthreads=8):
+    """Two-tensor addContractionLayer(BL, A, mpo, Ap, itokey, direction): A lower, Ap upper."""
+    L = lib()
+    hB, hA, hP = bm_to_handle(BL, 1), bm_to_handle(A, 1), bm_to_handle(Ap, 1)
+    w = mpo_to_handle(*W)
+    a = np.asarray(ik, np.uint64)
+    out = handle_to_bm(L.orc_add_contraction_layer2(hB, hA, hP, w, _ptr(a), len(a), int(direction), nthreads))
+    for h in (hB, hA, hP):
+        L.orc_bm_free(h)
+    L.orc_mpo_free(w)
+    return out
+
+
+def _site_handles(sites):
+    hs = [bm_to_handle(s, 1) for s in sites]
+    arr = (C.c_void_p * len(hs))(*hs)
+    return hs, arr
+
+
+def _ik_tables(iks):
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(k, np.uint64) for k in iks]), np.uint64)
+    d = np.ascontiguousarray([len(k) for k in iks], np.int32)
+    return flat, d
+
+
+def overlap(a, b, iks, nthreads=8):
+    """computeOverlap(a, b): a lower (ket), b upper (bra)."""
+    L = lib()
+    ha, pa = _site_handles(a)
+    hb, pb = _site_handles(b)
+    flat, d = _ik_tables(iks)
+    try:
+        return L.orc_overlap(len(a), pa, pb, _ptr(flat), _ptr(d), nthreads)
+    finally:
+        for h in ha + hb:
+            L.orc_bm_free(h)
+
+
+def mpo_measure(sites, W, iks, nthreads=8):
+    """MPO::measure(mps) on the given site tensors and MPO (list of (terms, Dl, Dr))."""
+    L = lib()
+    hs, ps = _site_handles(sites)
+    ws = [mpo_to_handle(*w) for w in W]
+    pw = (C.c_void_p * len(ws))(*ws)
+    flat, d = _ik_tables(iks)
+    try:
+        return L.orc_mpo_measure(len(sites), ps, pw, _ptr(flat), _ptr(d), nthreads)
+    finally:
+        for h in hs:
+            L.orc_bm_free(h)
+        for w in ws:
+            L.orc_mpo_free(w)
 
 
 def split(th, ik0, ik1, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, nthreads=8):

@@ -25,6 +25,46 @@ def _basis(N, Nup):
 
 def xxz_ground_energy(Jz, Jxy, B, Nup):
     """H = sum_i Jxy_i/2 (S+S- + h.c.) + Jz_i Sz Sz - sum_i B_i Sz_i, fixed up-count Nup."""
+    H = xxz_hamiltonian(Jz, Jxy, B, Nup)
+    if H.shape[0] <= 64:
+        return float(np.linalg.eigvalsh(H.toarray())[0])
+    return float(spla.eigsh(H, k=1, which="SA", tol=1e-14)[0][0])
+
+
+def mps_sector_vector(sites, Nup):
+    """Amplitudes of a U(1) block MPS on the basis of _basis(N, Nup) (site i <-> bit i, index 1 = up).
+
+    Blocks (a, b, s) are placed at offsets of their charges on each bond; psi is contracted left to
+    right over all 2^N configurations (N <= 12)."""
+    N = len(sites)
+    lays = []
+    for i in range(N + 1):
+        dims = {}
+        if i > 0:
+            for (a, b, s), m in sites[i - 1].items():
+                dims[b] = m.shape[1]
+        if i < N:
+            for (a, b, s), m in sites[i].items():
+                dims.setdefault(a, m.shape[0])
+        lays.append(_bond_layout(dims))
+    psi = np.zeros((1, lays[0][1]))
+    psi[0, lays[0][0][0][0]] = 1.0
+    for i in range(N):
+        (lay_l, _), (lay_r, Dr) = lays[i], lays[i + 1]
+        new = np.zeros((psi.shape[0] * 2, Dr))
+        for (a, b, s), m in sites[i].items():
+            oa, da = lay_l[a]
+            ob, db = lay_r[b]
+            rows = np.arange(psi.shape[0]) + s * psi.shape[0]
+            new[rows, ob:ob + db] += psi[:, oa:oa + da] @ m
+        psi = new
+    full = psi[:, lays[N][0][Nup][0]] if Nup in lays[N][0] else np.zeros(psi.shape[0])
+    states, _ = _basis(N, Nup)
+    return full[np.asarray(states)]
+
+
+def xxz_hamiltonian(Jz, Jxy, B, Nup):
+    """Sparse H on the basis of _basis(N, Nup)."""
     N = len(B)
     states, idx = _basis(N, Nup)
     rows, cols, vals = [], [], []
@@ -40,10 +80,7 @@ def xxz_ground_energy(Jz, Jxy, B, Nup):
                 t = s ^ (1 << i) ^ (1 << (i + 1))
                 rows.append(idx[t]); cols.append(k); vals.append(Jxy[i] / 2.0)
         rows.append(k); cols.append(k); vals.append(diag)
-    H = sp.csr_matrix((vals, (rows, cols)), shape=(len(states), len(states)))
-    if H.shape[0] <= 64:
-        return float(np.linalg.eigvalsh(H.toarray())[0])
-    return float(spla.eigsh(H, k=1, which="SA", tol=1e-14)[0][0])
+    return sp.csr_matrix((vals, (rows, cols)), shape=(len(states), len(states)))
 
 
 def tv_ground_energy(V, t, mu, Nf):

@@ -117,3 +117,24 @@ def test_golden_fixtures_reproduce():
     assert set(out) == set(case["out"])
     for k in out:
         assert np.abs(out[k] - case["out"][k]).max() < 1e-13
+
+
+def test_oracle_overlap_and_measure_match_dense():
+    """computeOverlap and MPO::measure (energy, local Sz) against dense state vectors."""
+    N, Nup = 8, 4
+    ik = M.u1_itokeys(N)
+    a, b = M.random_u1_mps(N, Nup, 6, 1), M.random_u1_mps(N, Nup, 6, 2)
+    va, vb = ed.mps_sector_vector(a, Nup), ed.mps_sector_vector(b, Nup)
+    assert abs(O.overlap(a, b, ik) - va @ vb) <= 1e-12 * abs(va @ vb)
+    assert abs(O.overlap(b, a, ik) - va @ vb) <= 1e-12 * abs(va @ vb)
+    Jz = M.xxz_couplings(N, 1)
+    W = M.heisenberg_mpo(Jz, np.ones(N - 1), np.zeros(N))
+    H = ed.xxz_hamiltonian(Jz, np.ones(N - 1), np.zeros(N), Nup)
+    e_dense = va @ (H @ va)
+    assert abs(O.mpo_measure(a, W, ik) - e_dense) <= 1e-12 * abs(e_dense)
+    states, _ = ed._basis(N, Nup)
+    for site in (0, 3, N - 1):
+        sz = np.array([0.5 if (s >> site) & 1 else -0.5 for s in states])
+        ref = (va ** 2 * sz).sum()
+        got = O.mpo_measure(a, M.local_operator_mpo(N, site, np.diag([-0.5, 0.5])), ik)
+        assert abs(got - ref) <= 1e-12 * np.abs(va ** 2).sum()
