@@ -7,9 +7,8 @@
 //                    products through distributed shared memory, two cluster barriers per column.
 //   2. k_tri_bisect  eigenvalues of T above the resolution floor by bisection on Sturm counts
 //                    (one thread per eigenvalue).
-//   3. k_tri_invit   eigenvectors of T by inverse iteration with a partially pivoted tridiagonal LU;
-//                    eigenvalues closer than gap_rel * lambda_max are solved by one thread in
-//                    sequence and kept orthogonal to each other (modified Gram-Schmidt).
+//   3. k_tri_invit   eigenvectors of T by inverse iteration with a partially pivoted tridiagonal LU,
+//                    one thread per eigenvalue; the caller re-orthonormalises them (CholeskyQR).
 //   4. k_ormtr       eigenvectors of G = Q z: the reflectors applied to blocks of 8 eigenvector
 //                    columns held in shared memory, one warp per column.
 // The tridiagonalisation follows the Householder method (Golub & Van Loan, Matrix Computations,
@@ -212,50 +211,54 @@ void launch_sytrd(const SytrdOp* ops, int nops, int CL, int nmax, cudaStream_t s
 }
 
 // ----------------------------------------------------------------------------- 2. eigenvalues
-// Number of eigenvalues of T (diagonal d, off-diagonal e[0..n-2]) below x.
-__device__ int sturm_count(const double* d, const double* e, int n, double x, double pivmin) {
+// Number of eigenvalues of T below x from the sign changes of the characteristic-polynomial sequence
+// p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, rescaled by exact powers of two (no division: an FP64
+// division is a long instruction sequence on this GPU).  A zero p_i counts as a sign change.
+__device__ int sturm_count(const double* d, const double* e2, int n, double x) {
   int c = 0;
-  double q = d[0] - x;
-  if (fabs(q) < pivmin) q = -pivmin;
-  c += q < 0.0;
+  double p0 = 1.0, p1 = d[0] - x;
+  if (p1 == 0.0) p1 = -DBL_MIN;
+  c += p1 < 0.0;
   for (int i = 1; i < n; ++i) {
-    q = d[i] - x - e[i - 1] * e[i - 1] / q;
-    if (fabs(q) < pivmin) q = -pivmin;
-    c += q < 0.0;
+    double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+    if (p2 == 0.0) p2 = p1 > 0.0 ? -DBL_MIN : DBL_MIN;
+    c += (p2 < 0.0) != (p1 < 0.0);
+    p0 = p1;
+    p1 = p2;
+    const double m = fabs(p1);
+    if (m > 0x1p+400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
+    else if (m < 0x1p-400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
   }
   return c;
 }
 
-// Per sector (one warp): Gershgorin interval, pivmin, and the largest eigenvalue by bisection.
+// Per sector (one warp): e2 = e^2, Gershgorin interval, and the largest eigenvalue by multisection.
 __global__ void k_tri_bounds(const TriOp* __restrict__ ops) {
   const TriOp o = ops[blockIdx.x];
   const int lane = threadIdx.x;
   const int n = o.n;
-  double lo = DBL_MAX, hi = -DBL_MAX, e2max = 0.0;
+  double lo = DBL_MAX, hi = -DBL_MAX;
   for (int i = lane; i < n; i += 32) {
     const double r = (i > 0 ? fabs(o.e[i - 1]) : 0.0) + (i + 1 < n ? fabs(o.e[i]) : 0.0);
     lo = fmin(lo, o.d[i] - r);
     hi = fmax(hi, o.d[i] + r);
-    if (i + 1 < n) e2max = fmax(e2max, o.e[i] * o.e[i]);
+    if (i + 1 < n) o.e2[i] = o.e[i] * o.e[i];
   }
 #pragma unroll
   for (int off = 16; off; off >>= 1) {
     lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, off));
     hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, off));
-    e2max = fmax(e2max, __shfl_xor_sync(0xffffffffu, e2max, off));
   }
+  __syncwarp();
   const double tnorm = fmax(fabs(lo), fabs(hi));
-  const double pivmin = fmax(DBL_MIN, DBL_MIN * e2max);
-  lo -= 2.0 * DBL_EPSILON * tnorm + pivmin;
-  hi += 2.0 * DBL_EPSILON * tnorm + pivmin;
-  // largest eigenvalue: multisection with 32 points per round (count(x) = n - 1 means x is inside the
-  // last gap below lambda_max)
+  lo -= 2.0 * DBL_EPSILON * tnorm + DBL_MIN;
+  hi += 2.0 * DBL_EPSILON * tnorm + DBL_MIN;
+  // largest eigenvalue: count(x) <= n - 1 exactly when x <= lambda_max
   double a = lo, b = hi;
-  for (int round = 0; round < 40 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + pivmin; ++round) {
+  for (int round = 0; round < 40 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++round) {
     const double x = a + (b - a) * (double)(lane + 1) / 33.0;
-    const int c = sturm_count(o.d, o.e, n, x, pivmin);
-    const unsigned below = __ballot_sync(0xffffffffu, c <= n - 1);  // lambda_max >= x
-    // highest lane whose x is still <= lambda_max
+    const int c = sturm_count(o.d, o.e2, n, x);
+    const unsigned below = __ballot_sync(0xffffffffu, c <= n - 1);
     const int k = below ? 31 - __clz(below) : -1;
     const double xa = k >= 0 ? __shfl_sync(0xffffffffu, x, k) : a;
     const double xb = k < 31 ? __shfl_sync(0xffffffffu, x, (k + 1) & 31) : b;
@@ -264,7 +267,7 @@ __global__ void k_tri_bounds(const TriOp* __restrict__ ops) {
   }
   if (lane == 0) {
     o.meta[0] = 0.5 * (a + b);  // lambda_max
-    o.meta[1] = pivmin;
+    o.meta[1] = DBL_MIN;
     o.meta[2] = lo;
     o.meta[3] = hi;
   }
@@ -284,18 +287,17 @@ __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restric
   const TriOp o = ops[op_of[t]];
   const int k = k_of[t];  // 0 = largest
   const int n = o.n;
-  const double lmax = o.meta[0], pivmin = o.meta[1];
+  const double lmax = o.meta[0];
   const double floor_v = o.floor_rel * fmax(lmax, 0.0);
-  // index from the bottom: the eigenvalue with exactly m = n-1-k smaller ones
-  const int m = n - 1 - k;
-  if (sturm_count(o.d, o.e, n, floor_v, pivmin) > m) {  // this eigenvalue is below the floor
+  const int m = n - 1 - k;  // the eigenvalue with exactly m smaller ones
+  if (sturm_count(o.d, o.e2, n, floor_v) > m) {
     o.W[k] = -1.0;
     return;
   }
   double a = floor_v, b = o.meta[3];
-  for (int it = 0; it < 100 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + pivmin; ++it) {
+  for (int it = 0; it < 100 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++it) {
     const double x = 0.5 * (a + b);
-    if (sturm_count(o.d, o.e, n, x, pivmin) > m) b = x;
+    if (sturm_count(o.d, o.e2, n, x) > m) b = x;
     else a = x;
   }
   o.W[k] = 0.5 * (a + b);
@@ -303,7 +305,7 @@ __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restric
 void launch_tri_bisect(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double,
                        cudaStream_t s) {
   if (nthreads <= 0) return;
-  k_tri_bisect<<<(nthreads + 127) / 128, 128, 0, s>>>(ops, op_of, k_of, nthreads);
+  k_tri_bisect<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, nthreads);
   g_eig_launches.fetch_add(1);
 }
 
@@ -316,13 +318,12 @@ __device__ __forceinline__ double hash_unit(uint32_t a, uint32_t b) {  // determ
   return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
 
-// Solve (T - lam I) x = x in place with a partially pivoted LU of the tridiagonal (rows i, i+1 swapped
-// when the subdiagonal entry is larger than the pivot); zero pivots are replaced by eps * tnorm.
-// Scratch: u0 (pivots), u1, u2 (first and second superdiagonal of U), mul (multipliers), piv flags.
-__device__ void tri_shift_solve(const double* d, const double* e, int n, double lam, double tnorm, double* x,
-                                double* u0, double* u1, double* u2, double* mul, unsigned char* piv) {
+// Partially pivoted LU of T - lam I (rows i, i+1 swapped when the subdiagonal entry is larger than the
+// pivot); zero pivots are replaced by eps * tnorm.  u0 holds the reciprocal pivots, u1, u2 the first
+// and second superdiagonals of U, mul the multipliers, piv the interchange flags.
+__device__ void tri_shift_factor(const double* d, const double* e, int n, double lam, double tnorm, double* u0,
+                                 double* u1, double* u2, double* mul, unsigned char* piv) {
   const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
-  // factor
   double dd = d[0] - lam, du = n > 1 ? e[0] : 0.0;
   for (int i = 0; i + 1 < n; ++i) {
     const double sub = e[i];
@@ -330,20 +331,24 @@ __device__ void tri_shift_solve(const double* d, const double* e, int n, double 
     const double dunext = i + 2 < n ? e[i + 1] : 0.0;
     if (fabs(dd) >= fabs(sub)) {
       if (dd == 0.0) dd = tiny;
-      const double l = sub / dd;
-      u0[i] = dd; u1[i] = du; u2[i] = 0.0; mul[i] = l; piv[i] = 0;
+      const double inv = 1.0 / dd;
+      const double l = sub * inv;
+      u0[i] = inv; u1[i] = du; u2[i] = 0.0; mul[i] = l; piv[i] = 0;
       dd = dnext - l * du;
       du = dunext;
     } else {
       const double l = dd / sub;
-      u0[i] = sub; u1[i] = dnext; u2[i] = dunext; mul[i] = l; piv[i] = 1;
+      u0[i] = 1.0 / sub; u1[i] = dnext; u2[i] = dunext; mul[i] = l; piv[i] = 1;
       dd = du - l * dnext;
       du = -l * dunext;
     }
   }
   if (dd == 0.0) dd = tiny;
-  u0[n - 1] = dd;
-  // forward: apply the row interchanges and multipliers
+  u0[n - 1] = 1.0 / dd;
+}
+// x <- (T - lam I)^-1 x with the factors of tri_shift_factor.
+__device__ void tri_shift_solve(int n, double* x, const double* u0, const double* u1, const double* u2,
+                                const double* mul, const unsigned char* piv) {
   for (int i = 0; i + 1 < n; ++i) {
     if (piv[i]) {
       const double t = x[i];
@@ -353,61 +358,51 @@ __device__ void tri_shift_solve(const double* d, const double* e, int n, double 
       x[i + 1] -= mul[i] * x[i];
     }
   }
-  // back substitution with U (diagonal u0, superdiagonals u1, u2)
-  x[n - 1] /= u0[n - 1];
-  if (n >= 2) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) / u0[n - 2];
-  for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) / u0[i];
+  x[n - 1] *= u0[n - 1];
+  if (n >= 2) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0[n - 2];
+  for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0[i];
 }
 
-// One thread per group of consecutive eigenvalues (descending order) that lie closer than
-// gap_rel * lambda_max to each other: each vector is found by three inverse iterations, and inside a
-// group every iterate is orthogonalised against the group's earlier vectors.  Z column k receives the
-// eigenvector of W[k] (unit norm); columns of eigenvalues below the floor are zero.
+// One thread per eigenvalue: three inverse iterations from a deterministic pseudo-random start with
+// one LU of T - lambda I.  Vectors of eigenvalues closer than ~eps lambda_max are independent
+// combinations inside their cluster; the caller re-orthonormalises the eigenvector matrix
+// (CholeskyQR).  Z column k receives the vector of W[k]; columns below the floor are zero.
 __global__ void k_tri_invit(const TriOp* __restrict__ ops, const int* __restrict__ op_of,
-                            const int* __restrict__ k_of, int nthreads, double gap_rel, double* scratch,
+                            const int* __restrict__ k_of, int nthreads, double, double* scratch,
                             const int64_t* __restrict__ scratch_off) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nthreads) return;
   const TriOp o = ops[op_of[t]];
   const int n = o.n;
-  const int k0 = k_of[t];  // first eigenvalue of the candidate group
-  const double lmax = o.meta[0];
+  const int k = k_of[t];
   const double tnorm = fmax(fabs(o.meta[2]), fabs(o.meta[3]));
-  const double gap = gap_rel * fmax(lmax, DBL_MIN);
-  // a thread whose first eigenvalue continues the previous eigenvalue's group does nothing
-  if (k0 > 0 && o.W[k0] >= 0.0 && o.W[k0 - 1] - o.W[k0] < gap) return;
+  double* z = o.Z + (int64_t)k * o.ldz;
+  const double lam = o.W[k];
+  if (lam < 0.0) {  // below the floor
+    for (int i = 0; i < n; ++i) z[i] = 0.0;
+    return;
+  }
   double* base = scratch + scratch_off[t];
   double *u0 = base, *u1 = base + n, *u2 = base + 2 * n, *mul = base + 3 * n;
   unsigned char* piv = (unsigned char*)(base + 4 * n);
-  for (int k = k0; k < n; ++k) {
-    if (k > k0 && !(o.W[k] >= 0.0 && o.W[k - 1] - o.W[k] < gap)) break;  // end of this group
-    double* z = o.Z + (int64_t)k * o.ldz;
-    const double lam = o.W[k];
-    if (lam < 0.0) {  // below the floor
-      for (int i = 0; i < n; ++i) z[i] = 0.0;
-      continue;
-    }
-    for (int i = 0; i < n; ++i) z[i] = hash_unit(k, i);
-    for (int it = 0; it < 3; ++it) {
-      tri_shift_solve(o.d, o.e, n, lam, tnorm, z, u0, u1, u2, mul, piv);
-      for (int q = k0; q < k; ++q) {  // orthogonalise against the group's earlier vectors
-        const double* y = o.Z + (int64_t)q * o.ldz;
-        double s = 0.0;
-        for (int i = 0; i < n; ++i) s = fma(y[i], z[i], s);
-        for (int i = 0; i < n; ++i) z[i] -= s * y[i];
-      }
-      double nrm = 0.0;
-      for (int i = 0; i < n; ++i) nrm = fma(z[i], z[i], nrm);
-      nrm = sqrt(nrm);
-      const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
-      for (int i = 0; i < n; ++i) z[i] *= inv;
-    }
+  for (int i = 0; i < n; ++i) z[i] = hash_unit(k, i);
+  tri_shift_factor(o.d, o.e, n, lam, tnorm, u0, u1, u2, mul, piv);
+  for (int it = 0; it < 3; ++it) {
+    tri_shift_solve(n, z, u0, u1, u2, mul, piv);
+    double amax = 0.0;
+    for (int i = 0; i < n; ++i) amax = fmax(amax, fabs(z[i]));
+    const double inv = amax > 0.0 ? 1.0 / amax : 0.0;  // keep the iterate in range
+    for (int i = 0; i < n; ++i) z[i] *= inv;
   }
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) nrm = fma(z[i], z[i], nrm);
+  const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+  for (int i = 0; i < n; ++i) z[i] *= inv;
 }
 void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double gap_rel,
                       double* scratch, const int64_t* scratch_off, cudaStream_t s) {
   if (nthreads <= 0) return;
-  k_tri_invit<<<(nthreads + 63) / 64, 64, 0, s>>>(ops, op_of, k_of, nthreads, gap_rel, scratch, scratch_off);
+  k_tri_invit<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, nthreads, gap_rel, scratch, scratch_off);
   g_eig_launches.fetch_add(1);
 }
 
@@ -420,13 +415,14 @@ __global__ void __launch_bounds__(256) k_ormtr(const OrmtrOp* __restrict__ ops) 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   extern __shared__ double zs[];  // 8 columns x n
   const int c = o.c0 + warp;
-  const bool active = c < o.c1;
+  const bool active = c < o.c1 && o.W[c] >= 0.0;  // eigenvectors below the floor are zero
   double* z = zs + (size_t)warp * n;
   if (active)
     for (int i = lane; i < n; i += 32) z[i] = o.Z[i + (int64_t)c * o.ldz];
+  if (!active) return;  // no block-wide synchronisation below: each warp owns its column
   for (int j = n - 3; j >= 0; --j) {
     const double tau = o.tau[j];
-    if (tau == 0.0 || !active) continue;
+    if (tau == 0.0) continue;
     const double* v = o.A + (int64_t)j * o.lda;  // v[j+1] = 1 implicitly, v[i] for i >= j+2
     double s = lane == 0 ? z[j + 1] : 0.0;
     for (int i = j + 2 + lane; i < n; i += 32) s = fma(v[i], z[i], s);
@@ -435,8 +431,7 @@ __global__ void __launch_bounds__(256) k_ormtr(const OrmtrOp* __restrict__ ops) 
     for (int i = j + 2 + lane; i < n; i += 32) z[i] -= s * v[i];
     __syncwarp();
   }
-  if (active)
-    for (int i = lane; i < n; i += 32) o.Z[i + (int64_t)c * o.ldz] = z[i];
+  for (int i = lane; i < n; i += 32) o.Z[i + (int64_t)c * o.ldz] = z[i];
 }
 void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s) {
   if (nops <= 0) return;
@@ -446,19 +441,156 @@ void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s) {
   g_eig_launches.fetch_add(1);
 }
 
+// ----------------------------------------------------------------------------- 5. CholeskyQR
+// k_chol<CL>: C = L L^T for the k x k symmetric positive definite C (lower triangle read), one cluster
+// of CL CTAs per sector with the columns round-robin in shared memory; column j of L is computed by
+// its owner (right after that owner applied the previous column's update to it) and pushed to every
+// CTA, one cluster barrier per column.  Output: R = L^T in the upper triangle of C (column j of R =
+// row j of L), rdiag[j] = 1 / R_jj, S[j] *= R_jj when S is given; info[0] = j + 1 for the first
+// non-positive pivot (then treated as 1).
+static __host__ __device__ size_t chol_smem_doubles(int k, int CL) {
+  const int ncol = (k + CL - 1) / CL;
+  return (size_t)ncol * k + 2 * (size_t)k + 8;
+}
+size_t chol_smem_bytes(int k, int CL) { return sizeof(double) * chol_smem_doubles(k, CL); }
+
+__device__ void chol_column(cg::cluster_group& cluster, int CL, const CholQROp& o, const double* col, int j,
+                            double* lbuf_local, int slot, int lane) {
+  const int k = o.k;
+  double piv = col[j];
+  if (!(piv > 0.0)) {
+    if (lane == 0) atomicCAS(o.info, 0, j + 1);
+    piv = 1.0;
+  }
+  const double ljj = sqrt(piv), inv = 1.0 / ljj;
+  for (int q = 0; q < CL; ++q) {
+    double* lr = cluster.map_shared_rank(lbuf_local + (size_t)slot * k, q);
+    for (int i = j + lane; i < k; i += 32) lr[i] = (i == j) ? ljj : col[i] * inv;
+  }
+  for (int i = j + lane; i < k; i += 32) o.C[j + (int64_t)i * o.ld] = (i == j) ? ljj : col[i] * inv;  // R(j, i)
+  if (lane == 0) {
+    o.rdiag[j] = inv;
+    if (o.S) o.S[j] *= ljj;
+  }
+}
+
+template <int CL>
+__global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const CholQROp o = ops[blockIdx.x / CL];
+  const int k = o.k;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  extern __shared__ double sm[];
+  const int ncol = (k - r + CL - 1) / CL;
+  const int ncol_max = (k + CL - 1) / CL;
+  double* cols = sm;
+  double* lbuf = cols + (size_t)ncol_max * k;  // 2 x k
+  for (int lc = warp; lc < ncol; lc += nwarp) {
+    const int c = r + lc * CL;
+    for (int i = lane; i < k; i += 32) cols[(size_t)lc * k + i] = o.C[i + (int64_t)c * o.ld];
+  }
+  cluster.sync();
+  if (k >= 1 && r == 0 && warp == 0) chol_column(cluster, CL, o, cols, 0, lbuf, 0, lane);
+  cluster.sync();
+  for (int j = 0; j + 1 < k; ++j) {
+    const int slot = j & 1;
+    const double* l = lbuf + (size_t)slot * k;
+    const int owner = (j + 1) % CL, lnext = (j + 1) / CL;
+    const int lc0 = (j + 1 - r + CL - 1) / CL;
+    if (r == owner && warp == 0) {  // column j+1 first, then its L column (lookahead)
+      double* a = cols + (size_t)lnext * k;
+      const double lc = l[j + 1];
+      for (int i = j + 1 + lane; i < k; i += 32) a[i] -= l[i] * lc;
+      __syncwarp();
+      chol_column(cluster, CL, o, a, j + 1, lbuf, slot ^ 1, lane);
+    }
+    for (int lc = lc0 + warp; lc < ncol; lc += nwarp) {
+      if (r == owner && lc == lnext) continue;
+      const int c = r + lc * CL;
+      double* a = cols + (size_t)lc * k;
+      const double lcv = l[c];
+      for (int i = c + lane; i < k; i += 32) a[i] -= l[i] * lcv;
+    }
+    cluster.sync();
+  }
+  cluster.sync();
+}
+
+template <int CL>
+static void launch_chol_cl(const CholQROp* ops, int nops, int kmax, cudaStream_t s) {
+  const size_t smem = chol_smem_bytes(kmax, CL);
+  MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nops * CL);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_chol<CL>, ops));
+  g_eig_launches.fetch_add(1);
+}
+void launch_chol(const CholQROp* ops, int nops, int CL, int kmax, cudaStream_t s) {
+  if (nops <= 0) return;
+  MPSG_CHECK(kmax <= sytrd_max_n(), "Cholesky: sector too large for the cluster kernel");
+  switch (CL) {
+    case 1: launch_chol_cl<1>(ops, nops, kmax, s); break;
+    case 2: launch_chol_cl<2>(ops, nops, kmax, s); break;
+    case 4: launch_chol_cl<4>(ops, nops, kmax, s); break;
+    case 8: launch_chol_cl<8>(ops, nops, kmax, s); break;
+    case 16: launch_chol_cl<16>(ops, nops, kmax, s); break;
+    default: throw Err(1, "Cholesky: unsupported cluster size");
+  }
+}
+
+// X <- X R^-1 (R upper triangular from k_chol, rdiag its reciprocal diagonal) for rows [r0, r1) of
+// one sector: one thread per row, forward substitution x_j = (x_j - sum_{i<j} x_i R_ij) / R_jj over a
+// 32-row tile in shared memory (column-major tile: conflict-free).
+__global__ void __launch_bounds__(32) k_trsm_rows(const TrsmRowsOp* __restrict__ ops) {
+  const TrsmRowsOp o = ops[blockIdx.x];
+  const int k = o.k, lane = threadIdx.x;
+  extern __shared__ double xs[];  // k x 32
+  const int row = o.r0 + lane;
+  const bool act = row < o.r1;
+  for (int j = 0; j < k; ++j) xs[(size_t)j * 32 + lane] = act ? o.X[row + (int64_t)j * o.ldx] : 0.0;
+  __syncwarp();
+  for (int j = 0; j < k; ++j) {
+    const double* rc = o.R + (int64_t)j * o.ldr;  // column j of R: R(i, j), i <= j
+    double a0 = xs[(size_t)j * 32 + lane], a1 = 0.0;
+    int i = 0;
+    for (; i + 1 < j; i += 2) {
+      a0 = fma(-xs[(size_t)i * 32 + lane], rc[i], a0);
+      a1 = fma(-xs[(size_t)(i + 1) * 32 + lane], rc[i + 1], a1);
+    }
+    if (i < j) a0 = fma(-xs[(size_t)i * 32 + lane], rc[i], a0);
+    xs[(size_t)j * 32 + lane] = (a0 + a1) * o.rdiag[j];
+  }
+  __syncwarp();
+  if (act)
+    for (int j = 0; j < k; ++j) o.X[row + (int64_t)j * o.ldx] = xs[(size_t)j * 32 + lane];
+}
+void launch_trsm_rows(const TrsmRowsOp* ops, int nops, int kmax, cudaStream_t s) {
+  if (nops <= 0) return;
+  const size_t smem = sizeof(double) * 32 * (size_t)kmax;
+  MPSG_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_trsm_rows<<<nops, 32, smem, s>>>(ops);
+  g_eig_launches.fetch_add(1);
+}
+
 // ----------------------------------------------------------------------------- post-processing
-// S[k] = sqrt(W[k]) (0 below the floor); P = 1.5 I - 0.5 C for one Newton-Schulz orthonormalisation
-// step of the eigenvector matrix (C = Z^T Z over the first k columns, k x k, leading dimension ld).
+// S[k] = sqrt(W[k]) (0 below the floor).
 __global__ void k_eig_post(const EigPostOp* __restrict__ ops) {
   const EigPostOp o = ops[blockIdx.x];
   for (int k = threadIdx.x; k < o.n; k += blockDim.x) {
     const double w = o.W[k];
     o.S[k] = w > 0.0 ? sqrt(w) : 0.0;
-  }
-  for (int64_t idx = threadIdx.x; idx < (int64_t)o.n * o.n; idx += blockDim.x) {
-    const int i = (int)(idx % o.n), j = (int)(idx / o.n);
-    double* c = o.C + i + (int64_t)j * o.ldc;
-    *c = (i == j ? 1.5 : 0.0) - 0.5 * *c;
   }
 }
 void launch_eig_post(const EigPostOp* ops, int nops, cudaStream_t s) {

@@ -790,10 +790,10 @@ struct SvdBatch {
 
   // Density-matrix route on the library's own batched eigensolver (eig_f64.cu): Gram matrices by the
   // grouped FP64 GEMM, cluster-parallel Householder tridiagonalisation, bisection and inverse
-  // iteration for the eigenpairs above the resolution floor, reflector back-transformation, one
-  // Newton-Schulz step that re-orthonormalises the eigenvectors (inverse iteration leaves
-  // ~eps lambda_max / gap between eigenvalues that are not grouped), then the left vectors as in the
-  // other density routes.  Sectors wider than the cluster kernel's limit use run_gram.
+  // iteration for the eigenpairs above the resolution floor, reflector back-transformation,
+  // CholeskyQR of the eigenvector matrix (inverse iteration leaves ~eps lambda_max / gap between
+  // close eigenvalues), then the left vectors as in the other density routes.  Sectors wider than the
+  // cluster kernel's limit use run_gram.
   void run_gram_custom() {
     std::vector<int> idx;
     int nmax = 0;
@@ -813,9 +813,10 @@ struct SvdBatch {
       oG += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
     }
     double* dG = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oG, 2));
-    // per sector: d (n), e (n), tau (n), W (n), meta (4)
-    double* dT = (double*)ctx->dmalloc(sizeof(double) * (size_t)(4 * nS + 4 * (int64_t)idx.size() + 2));
-    double *dd = dT, *de = dT + nS, *dtau = dT + 2 * nS, *dW = dT + 3 * nS, *dmeta = dT + 4 * nS;
+    // per sector: d (n), e (n), e^2 (n), tau (n), W (n), meta (4)
+    double* dT = (double*)ctx->dmalloc(sizeof(double) * (size_t)(5 * nS + 4 * (int64_t)idx.size() + 2));
+    double *dd = dT, *de = dT + nS, *de2 = dT + 2 * nS, *dtau = dT + 3 * nS, *dW = dT + 4 * nS,
+           *dmeta = dT + 5 * nS;
     {
       GemmPlan g;
       for (int i : idx)
@@ -850,7 +851,7 @@ struct SvdBatch {
     int64_t scratch = 0;
     for (size_t t = 0; t < idx.size(); ++t) {
       const Sec& x = s[idx[t]];
-      tops.push_back(TriOp{dd + x.offS, de + x.offS, dW + x.offS, dV + x.offV, dmeta + 4 * t,
+      tops.push_back(TriOp{dd + x.offS, de + x.offS, de2 + x.offS, dW + x.offS, dV + x.offV, dmeta + 4 * t,
                            32.0 * x.ns * DBL_EPSILON, x.ns, x.ns});
       for (int k = 0; k < x.ns; ++k) {
         op_of.push_back((int)t);
@@ -876,43 +877,23 @@ struct SvdBatch {
       std::vector<OrmtrOp> oo;
       for (int i : idx)
         for (int c0 = 0; c0 < s[i].ns; c0 += 8)
-          oo.push_back(OrmtrOp{dG + offG[i], dtau + s[i].offS, dV + s[i].offV, s[i].ns, s[i].ns, s[i].ns, c0,
-                               std::min(c0 + 8, s[i].ns)});
+          oo.push_back(OrmtrOp{dG + offG[i], dtau + s[i].offS, dW + s[i].offS, dV + s[i].offV, s[i].ns, s[i].ns,
+                               s[i].ns, c0, std::min(c0 + 8, s[i].ns)});
       OrmtrOp* d = (OrmtrOp*)ctx->dmalloc(sizeof(OrmtrOp) * oo.size());
       MPSG_CUDA(cudaMemcpyAsync(d, oo.data(), sizeof(OrmtrOp) * oo.size(), cudaMemcpyHostToDevice, st));
       launch_ormtr(d, (int)oo.size(), nmax, st);
       ctx->dfree(d);
     }
-    // 5. S = sqrt(W); one Newton-Schulz step V <- V (1.5 I - 0.5 V^T V) (G's storage reused for C)
+    // 5. S = sqrt(W); the eigenvector matrix re-orthonormalised (CholeskyQR, two passes)
     {
-      GemmPlan gc;
-      for (int i : idx)
-        gc.add_problem(2, offG[i], s[i].ns, s[i].ns, s[i].ns, false,
-                       {GSegH{1, 1, s[i].offV, s[i].offV, s[i].ns, s[i].ns, s[i].ns, 1, 0, 1.0}});
-      gc.upload(ctx);
-      const double* bases[8] = {nullptr, dV, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
-      gc.run(bases);
       std::vector<EigPostOp> po;
-      for (size_t t = 0; t < idx.size(); ++t) {
-        const Sec& x = s[idx[t]];
-        po.push_back(EigPostOp{dW + x.offS, dS + x.offS, dG + offG[idx[t]], x.ns, x.ns});
-      }
+      for (int i : idx) po.push_back(EigPostOp{dW + s[i].offS, dS + s[i].offS, s[i].ns});
       EigPostOp* d = (EigPostOp*)ctx->dmalloc(sizeof(EigPostOp) * po.size());
       MPSG_CUDA(cudaMemcpyAsync(d, po.data(), sizeof(EigPostOp) * po.size(), cudaMemcpyHostToDevice, st));
       launch_eig_post(d, (int)po.size(), st);
       ctx->dfree(d);
-      GemmPlan gv;  // U's storage holds V P, copied back into V
-      std::vector<CopyOp> cp;
-      for (int i : idx) {
-        const Sec& x = s[i];
-        gv.add_problem(2, x.offU, x.ns, x.ns, x.ns, false, {GSegH{1, 0, x.offV, offG[i], x.ns, x.ns, x.ns, 0, 0, 1.0}});
-        cp.push_back(CopyOp{dU + x.offU, dV + x.offV, nullptr, nullptr, x.ns, x.ns, x.ns, x.ns, 0, 1.0});
-      }
-      gv.upload(ctx);
-      const double* bv[8] = {dG, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
-      gv.run(bv);
-      run_copyops(ctx, cp);
     }
+    cholqr(false, 2);
     ctx->dfree(dscr);
     ctx->dfree(dsoff);
     ctx->dfree(dmap);
@@ -1087,87 +1068,95 @@ struct SvdBatch {
     }
   }
 
-  // CholeskyQR of every sector's Ust (columns in descending s order): C = U^T U, C = R^T R (cuSOLVER
-  // potrf), U <- U R^-1 (cuBLAS trsm); s_j is multiplied by R_jj (the norm of y_j after removing its
-  // components along the larger pairs).  The resolution floor bounds |C - I| well below 1, so one
-  // pass leaves U orthonormal to rounding (error ~ eps cond(U)^2).  Sectors are spread over the
-  // worker streams, largest first; the context stream waits for all of them.
-  void orthonormalize_left() {
-    const int nw = ctx->nworkers();
+  // CholeskyQR of every sector's matrix X (columns in descending s order), in place: C = X^T X by the
+  // grouped FP64 GEMM (zero columns get C_jj = 1 and stay zero), C = R^T R by the cluster Cholesky
+  // kernel, X <- X R^-1 by row-parallel forward substitution.  left: X = Ust (ms x ns) and s_j is
+  // multiplied by R_jj of the first pass (the norm of y_j after removing its components along the
+  // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
+  void cholqr(bool left, int passes) {
     std::vector<int> idx;
+    int kmax = 0;
     for (size_t i = 0; i < s.size(); ++i)
-      if (s[i].k > 0) idx.push_back((int)i);
+      if (s[i].k > 0) {
+        idx.push_back((int)i);
+        kmax = std::max(kmax, s[i].ns);
+      }
     if (idx.empty()) return;
-    std::sort(idx.begin(), idx.end(), [&](int a, int b) { return s[a].ns > s[b].ns; });
+    MPSG_CHECK(kmax <= sytrd_max_n(), "CholeskyQR: sector wider than the cluster kernel's limit");
+    cudaStream_t st = ctx->stream;
+    double* X = left ? dU : dV;
+    auto rows = [&](int i) { return left ? s[i].ms : s[i].ns; };
+    auto offX = [&](int i) { return left ? s[i].offU : s[i].offV; };
     std::vector<int64_t> offC(s.size(), 0);
     int64_t oC = 0;
-    int lwork = 0;
     for (int i : idx) {
       offC[i] = oC;
       oC += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
     }
     double* dC = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
-    for (int i : idx) {
-      int lw = 0;
-      if (cusolverDnDpotrf_bufferSize(ctx->whandles[0], CUBLAS_FILL_MODE_UPPER, s[i].ns, dC + offC[i], s[i].ns, &lw) !=
-          CUSOLVER_STATUS_SUCCESS)
-        throw Err(3, "potrf_bufferSize failed");
-      lwork = std::max(lwork, lw);
-    }
-    lwork = std::max(lwork, 2);
-    double* work = (double*)ctx->dmalloc(sizeof(double) * (size_t)lwork * nw);
+    double* dR = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));  // 1 / R_jj
     int* dinf = (int*)ctx->dmalloc(sizeof(int) * idx.size());
-    std::vector<CholOp> ops;
-    for (int i : idx) ops.push_back(CholOp{dC + offC[i], dS + s[i].offS, s[i].ns, s[i].ns});
-    CholOp* dops = (CholOp*)ctx->dmalloc(sizeof(CholOp) * ops.size());
-    MPSG_CUDA(cudaMemcpyAsync(dops, ops.data(), sizeof(CholOp) * ops.size(), cudaMemcpyHostToDevice, ctx->stream));
+    MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * idx.size(), st));
     GemmPlan g;
     for (int i : idx)
       g.add_problem(2, offC[i], s[i].ns, s[i].ns, s[i].ns, false,
-                    {GSegH{0, 0, s[i].offU, s[i].offU, s[i].ms, s[i].ms, s[i].ms, 1, 0, 1.0}});
+                    {GSegH{0, 0, offX(i), offX(i), rows(i), rows(i), rows(i), 1, 0, 1.0}});
     g.upload(ctx);
-    cudaEvent_t fork;
-    std::vector<cudaEvent_t> join(nw);
-    MPSG_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-    for (auto& e : join) MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    const double one = 1.0;
-    std::string err;
-    for (int pass = 0; pass < 1 && err.empty(); ++pass) {
-      const double* bases[8] = {dU, nullptr, dC, nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::vector<CholOp> zd;
+    std::map<int, std::vector<CholQROp>> byCL[2];
+    std::map<int, int> kmaxCL;
+    std::vector<TrsmRowsOp> tr;
+    for (size_t t = 0; t < idx.size(); ++t) {
+      const int i = idx[t];
+      zd.push_back(CholOp{dC + offC[i], nullptr, s[i].ns, s[i].ns});
+      const int CL = sytrd_cluster_size(s[i].ns);
+      for (int pass = 0; pass < 2; ++pass)
+        byCL[pass][CL].push_back(CholQROp{dC + offC[i], dR + s[i].offS, (pass == 0 && left) ? dS + s[i].offS : nullptr,
+                                          dinf + t, s[i].ns, s[i].ns});
+      kmaxCL[CL] = std::max(kmaxCL[CL], s[i].ns);
+      for (int r0 = 0; r0 < rows(i); r0 += 32)
+        tr.push_back(TrsmRowsOp{X + offX(i), dC + offC[i], dR + s[i].offS, s[i].ns, rows(i), s[i].ns, r0,
+                                std::min(r0 + 32, rows(i))});
+    }
+    size_t bytes = sizeof(CholOp) * zd.size() + sizeof(TrsmRowsOp) * tr.size();
+    for (int pass = 0; pass < 2; ++pass)
+      for (auto& c : byCL[pass]) bytes += sizeof(CholQROp) * c.second.size() + 16;
+    char* dops = (char*)ctx->dmalloc(bytes + 64);
+    std::vector<char> hops(bytes + 64);
+    size_t off = 0;
+    auto put = [&](const void* p, size_t n) {
+      std::memcpy(hops.data() + off, p, n);
+      char* d = dops + off;
+      off += (n + 15) / 16 * 16;
+      return d;
+    };
+    CholOp* dzd = (CholOp*)put(zd.data(), sizeof(CholOp) * zd.size());
+    TrsmRowsOp* dtr = (TrsmRowsOp*)put(tr.data(), sizeof(TrsmRowsOp) * tr.size());
+    std::map<int, CholQROp*> dch[2];
+    for (int pass = 0; pass < 2; ++pass)
+      for (auto& c : byCL[pass]) dch[pass][c.first] = (CholQROp*)put(c.second.data(), sizeof(CholQROp) * c.second.size());
+    MPSG_CHECK(off <= bytes + 64, "CholeskyQR descriptor overflow");
+    MPSG_CUDA(cudaMemcpyAsync(dops, hops.data(), off, cudaMemcpyHostToDevice, st));
+    for (int pass = 0; pass < passes; ++pass) {
+      const double* bases[8] = {X, nullptr, dC, nullptr, nullptr, nullptr, nullptr, nullptr};
       g.run(bases);
-      launch_chol_unit_zero_diag(dops, (int)ops.size(), ctx->stream);
-      MPSG_CUDA(cudaEventRecord(fork, ctx->stream));
-      for (int w = 0; w < nw; ++w) MPSG_CUDA(cudaStreamWaitEvent(ctx->wstreams[w], fork, 0));
-      for (size_t t = 0; t < idx.size() && err.empty(); ++t) {
-        const int i = idx[t], w = (int)(t % nw);
-        const Sec& x = s[i];
-        if (cusolverDnDpotrf(ctx->whandles[w], CUBLAS_FILL_MODE_UPPER, x.ns, dC + offC[i], x.ns,
-                             work + (size_t)w * lwork, lwork, dinf + pass * idx.size() + t) != CUSOLVER_STATUS_SUCCESS)
-          err = "potrf failed";
-        else if (cublasDtrsm(ctx->wblas[w], CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N,
-                             CUBLAS_DIAG_NON_UNIT, x.ms, x.ns, &one, dC + offC[i], x.ns, dU + x.offU, x.ms) !=
-                 CUBLAS_STATUS_SUCCESS)
-          err = "trsm failed";
-      }
-      for (int w = 0; w < nw; ++w) {
-        MPSG_CUDA(cudaEventRecord(join[w], ctx->wstreams[w]));
-        MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, join[w], 0));
-      }
-      if (pass == 0) launch_chol_scale_s(dops, (int)ops.size(), ctx->stream);
+      launch_chol_unit_zero_diag(dzd, (int)zd.size(), st);
+      const int which = pass == 0 ? 0 : 1;
+      for (auto& c : byCL[which]) launch_chol(dch[which][c.first], (int)c.second.size(), c.first, kmaxCL[c.first], st);
+      launch_trsm_rows(dtr, (int)tr.size(), kmax, st);
     }
     std::vector<int> inf(idx.size(), 0);
-    MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * inf.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * inf.size(), cudaMemcpyDeviceToHost, st));
     ctx->sync();
-    cudaEventDestroy(fork);
-    for (auto& e : join) cudaEventDestroy(e);
     ctx->dfree(dops);
     ctx->dfree(dinf);
-    ctx->dfree(work);
+    ctx->dfree(dR);
     ctx->dfree(dC);
-    if (!err.empty()) throw Err(3, err);
     for (int v : inf)
-      if (v != 0) throw Err(3, "Cholesky of the left-vector overlap failed (info=" + std::to_string(v) + ")");
+      if (v != 0) throw Err(3, "CholeskyQR: the Gram matrix of the singular vectors is not positive definite (column " +
+                                   std::to_string(v - 1) + ")");
   }
+  void orthonormalize_left() { cholqr(true, 1); }
 
   void run(int method) {
     if (method == 1) run_gram();

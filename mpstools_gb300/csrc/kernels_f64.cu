@@ -405,23 +405,40 @@ void launch_fill(double* x, int64_t n, double v, cudaStream_t s) {
 // ============================================================================ tridiagonal eigensolver
 // Lowest eigenvalue of T (diag a[0..n), offdiag b[1..n)) by Sturm-count multisection in one warp,
 // eigenvector by inverse iteration with a pivoted tridiagonal LU (one thread).
-__device__ int sturm_below(const double* a, const double* b, int n, double x, double pivmin) {
+// Number of eigenvalues of the tridiagonal (diagonal a[0..n), off-diagonal squares b2[i] coupling
+// i-1 and i) below x: sign changes of the characteristic-polynomial sequence p_i = (a_i - x) p_{i-1}
+// - b2_i p_{i-2}, kept in range by exact power-of-two rescaling (no division: FP64 division is a
+// long instruction sequence on this GPU).  A zero p_i counts as a sign change (the ratio form's
+// -pivmin rule).
+__device__ int sturm_count_nodiv(const double* a, const double* b2, int n, double x) {
   int c = 0;
-  double d = a[0] - x;
-  if (fabs(d) < pivmin) d = -pivmin;
-  if (d < 0) ++c;
+  double p0 = 1.0, p1 = a[0] - x;
+  if (p1 == 0.0) p1 = -DBL_MIN;
+  c += p1 < 0.0;
   for (int i = 1; i < n; ++i) {
-    d = a[i] - x - b[i] * b[i] / d;
-    if (fabs(d) < pivmin) d = -pivmin;
-    if (d < 0) ++c;
+    double p2 = fma(a[i] - x, p1, -b2[i] * p0);
+    if (p2 == 0.0) p2 = p1 > 0.0 ? -DBL_MIN : DBL_MIN;
+    c += (p2 < 0.0) != (p1 < 0.0);
+    p0 = p1;
+    p1 = p2;
+    const double m = fabs(p1);
+    if (m > 0x1p+400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
+    else if (m < 0x1p-400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
   }
   return c;
 }
 
-__global__ void k_tri_lowest(const double* __restrict__ a, const double* __restrict__ b, int n, double* E0,
+__global__ void k_tri_lowest(const double* __restrict__ a_g, const double* __restrict__ b, int n, double* E0,
                              double* z) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x;
+  double* a = sm + 6 * n;   // diagonal and squared off-diagonal, staged for the Sturm counts
+  double* b2 = sm + 7 * n;
+  for (int i = lane; i < n; i += 32) {
+    a[i] = a_g[i];
+    b2[i] = i > 0 ? b[i] * b[i] : 0.0;
+  }
+  __syncwarp();
   // Gershgorin interval
   double lo = DBL_MAX, hi = -DBL_MAX, bmax = 0.0;
   for (int i = lane; i < n; i += 32) {
@@ -443,7 +460,7 @@ __global__ void k_tri_lowest(const double* __restrict__ a, const double* __restr
   for (int round = 0; round < 80; ++round) {
     if (hi - lo <= 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin) break;
     const double x = lo + (hi - lo) * (double)(lane + 1) / 33.0;
-    const int c = sturm_below(a, b, n, x, pivmin);
+    const int c = sturm_count_nodiv(a, b2, n, x);
     const unsigned ball = __ballot_sync(0xffffffffu, c >= 1);
     const double xprev = __shfl_up_sync(0xffffffffu, x, 1);
     if (ball == 0) {
@@ -497,6 +514,7 @@ __global__ void k_tri_lowest(const double* __restrict__ a, const double* __restr
     }
   }
   if (d[n - 1] == 0.0) d[n - 1] = tiny;
+  for (int i = 0; i < n; ++i) d[i] = 1.0 / d[i];  // reciprocal pivots: the solves only multiply
   for (int it = 0; it < 3; ++it) {
     // forward: apply L^{-1} P
     for (int i = 0; i < n - 1; ++i) {
@@ -509,9 +527,9 @@ __global__ void k_tri_lowest(const double* __restrict__ a, const double* __restr
       }
     }
     // backward: U x = y
-    x[n - 1] /= d[n - 1];
-    if (n > 1) x[n - 2] = (x[n - 2] - du[n - 2] * x[n - 1]) / d[n - 2];
-    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / d[i];
+    x[n - 1] *= d[n - 1];
+    if (n > 1) x[n - 2] = (x[n - 2] - du[n - 2] * x[n - 1]) * d[n - 2];
+    for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) * d[i];
     double nrm = 0.0, amax = 0.0;
     int imax = 0;
     for (int i = 0; i < n; ++i) {
@@ -525,7 +543,7 @@ __global__ void k_tri_lowest(const double* __restrict__ a, const double* __restr
 }
 void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s) {
   if (n <= 0) return;
-  const size_t sh = (size_t)n * (5 * sizeof(double) + sizeof(int)) + 16;
+  const size_t sh = (size_t)n * 8 * sizeof(double) + 16;
   k_tri_lowest<<<1, 32, sh, s>>>(alpha, beta, n, E0, z);
   LAUNCHED();
 }

@@ -154,23 +154,37 @@ struct SytrdOp {  // n x n symmetric matrix A (full storage); out: diagonal d, o
 struct TriOp {  // tridiagonal (d, e) of one sector -> W (eigenvalues, descending; -1 below the floor), Z
   const double* d;
   const double* e;
+  double* e2;    // e^2 (written by launch_tri_bounds)
   double* W;
   double* Z;
   double* meta;  // 4 doubles: lambda_max, pivmin, Gershgorin lo, hi
   double floor_rel;
   int32_t n, ldz;
 };
-struct OrmtrOp {  // columns [c0, c1) of Z <- Q Z with the reflectors of SytrdOp
+struct OrmtrOp {  // columns [c0, c1) of Z <- Q Z with the reflectors of SytrdOp (columns with W < 0 skipped)
   const double* A;
   const double* tau;
+  const double* W;
   double* Z;
   int32_t n, lda, ldz, c0, c1;
 };
-struct EigPostOp {  // S = sqrt(W) (0 below the floor); C <- 1.5 I - 0.5 C (n x n, leading dimension ldc)
+struct EigPostOp {  // S = sqrt(W) (0 below the floor)
   const double* W;
   double* S;
+  int32_t n;
+};
+struct CholQROp {  // Cholesky of the k x k Gram matrix C (ld) of one sector: R = L^T in C's upper triangle
   double* C;
-  int32_t n, ldc;
+  double* rdiag;  // 1 / R_jj
+  double* S;      // optional: S_j *= R_jj
+  int* info;      // first non-positive pivot + 1 (0: none)
+  int32_t k, ld;
+};
+struct TrsmRowsOp {  // rows [r0, r1) of X (ldx) <- X R^-1, R upper (ldr), k columns
+  double* X;
+  const double* R;
+  const double* rdiag;
+  int32_t k, ldx, ldr, r0, r1;
 };
 struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
   double* A;
@@ -227,5 +241,8 @@ void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int n
                       double* scratch, const int64_t* scratch_off, cudaStream_t s);
 void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s);
 void launch_eig_post(const EigPostOp* ops, int nops, cudaStream_t s);
+size_t chol_smem_bytes(int k, int CL);
+void launch_chol(const CholQROp* ops, int nops, int CL, int kmax, cudaStream_t s);
+void launch_trsm_rows(const TrsmRowsOp* ops, int nops, int kmax, cudaStream_t s);
 
 }  // namespace mpsg
