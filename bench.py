@@ -261,6 +261,30 @@ def gpu_arm(args):
     matvecs = st1["matvecs"] - st0["matvecs"]
     value = mv_flops * world / total / 1e12
     steps_rec = eng.steps()[n_steps0:]
+
+    # ------------------------------------------------- the plain FP64 GPU path on the same updates
+    fp64_leg = None
+    if prec != "fp64" and not args.no_fp64_leg:
+        eng64 = api.DMRGengine(sites, W, ik, prec="fp64", ctx=ctx)
+        eng64.build_environments(center)
+        for i in range(args.warmup):
+            eng64.do_step(center, 1 if i % 2 == 0 else -1, args.chi)
+        n64 = len(eng64.steps())
+        t64 = []
+        for i in range(args.steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            eng64.do_step(center, 1 if (args.warmup + i) % 2 == 0 else -1, args.chi)
+            e1.record(stream)
+            e1.synchronize()
+            t64.append(e0.elapsed_time(e1) * 1e-3)
+        e64 = [r["E"] for r in eng64.steps()[n64:]]
+        emix = [r["E"] for r in steps_rec]
+        fp64_leg = {"ms_per_step": float(np.sum(t64)) / args.steps * 1e3, "energies": e64,
+                    "speedup_of_this_line": float(np.sum(t64)) / (total / world),
+                    "max_rel_energy_diff": max(abs(a - b) / abs(b) for a, b in zip(emix, e64))}
+        eng64.close()
     lam_c = eng.lam(center)
     lam_all = np.sort(np.concatenate([np.asarray(v) for v in lam_c.values() if len(v)]))[::-1]
     spectrum = {"chi": int(lam_all.size), "s_max": float(lam_all[0]), "s_min_kept": float(lam_all[-1]),
@@ -358,7 +382,7 @@ def gpu_arm(args):
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
                 "env_seconds_per_step": (st1["env_seconds"] - st0["env_seconds"]) / args.steps,
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
-                "centre_bond_spectrum": spectrum,
+                "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg,
                 "matvec_flops_reference_schedule": info["flops_ref"]}
         print(json.dumps(line), flush=True)
     if dist:
@@ -442,6 +466,8 @@ def main():
     ap.add_argument("--svd", default="density", choices=["density", "density_mt", "density_eig", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
+    ap.add_argument("--no-fp64-leg", action="store_true",
+                    help="skip the plain FP64 GPU path timed on the same updates (mixed precisions only)")
     ap.add_argument("--steps-only", action="store_true",
                     help="time the DMRG steps only (no roofline / e2e / CPU legs); for profiler launch lists")
     args = ap.parse_args()

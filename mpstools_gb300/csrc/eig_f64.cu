@@ -2,9 +2,10 @@
 //
 // Stages, each one launch over all sectors:
 //   1. k_sytrd<CL>   Householder tridiagonalisation Q^T G Q = T.  One thread-block cluster of CL CTAs
-//                    per sector; the CTAs own the matrix columns round-robin in shared memory and
-//                    exchange the Householder vector, the product p = tau G v and the partial dot
-//                    products through distributed shared memory, two cluster barriers per column.
+//                    per sector; the CTAs own the matrix columns round-robin in shared memory; the
+//                    Householder vector is copied from its owner, the product p = tau G v and the
+//                    partial dot products are pushed through distributed shared memory; two
+//                    cluster barriers per column.
 //   2. k_tri_bisect  eigenvalues of T above the resolution floor by bisection on Sturm counts
 //                    (one thread per eigenvalue).
 //   3. k_tri_invit   eigenvectors of T by inverse iteration with a partially pivoted tridiagonal LU,
@@ -46,11 +47,11 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 // Householder vector of column j (held by the calling warp's CTA as local column `col`): alpha =
-// x[j+1], the rest x[j+2..n-1].  Writes v (v[j+1] = 1) into every CTA's v buffer `slot`, tau and beta
-// into every CTA's scal, the reflector (without the unit entry) into column j of the global matrix,
-// tau[j] and e[j].
-__device__ void sytrd_householder(cg::cluster_group& cluster, int CL, const SytrdOp& o, const double* col, int j,
-                                  double* vbuf_local, double* scal_local, int slot, int lane) {
+// x[j+1], the rest x[j+2..n-1].  Writes v (v[j+1] = 1) into this CTA's v buffer `slot`, tau and beta
+// into its scal (the other CTAs copy them after the next cluster barrier), the reflector (without the
+// unit entry) into column j of the global matrix, tau[j] and e[j].
+__device__ void sytrd_householder(const SytrdOp& o, const double* col, int j, double* vbuf_local,
+                                  double* scal_local, int slot, int lane) {
   const int n = o.n;
   double s2 = 0.0;
   for (int i = j + 2 + lane; i < n; i += 32) s2 = fma(col[i], col[i], s2);
@@ -62,20 +63,28 @@ __device__ void sytrd_householder(cg::cluster_group& cluster, int CL, const Sytr
     tau = (beta - alpha) / beta;
     scale = 1.0 / (alpha - beta);
   }
-  for (int q = 0; q < CL; ++q) {
-    double* vr = cluster.map_shared_rank(vbuf_local + (size_t)slot * n, q);
-    for (int i = j + 1 + lane; i < n; i += 32) vr[i] = (i == j + 1) ? 1.0 : col[i] * scale;
-    if (lane == 0) {
-      double* sr = cluster.map_shared_rank(scal_local, q);
-      sr[slot] = tau;
-      sr[2 + slot] = beta;
-    }
+  double* vr = vbuf_local + (size_t)slot * n;
+  for (int i = j + 1 + lane; i < n; i += 32) vr[i] = (i == j + 1) ? 1.0 : col[i] * scale;
+  if (lane == 0) {
+    scal_local[slot] = tau;
+    scal_local[2 + slot] = beta;
   }
   for (int i = j + 2 + lane; i < n; i += 32) o.A[i + (int64_t)j * o.lda] = col[i] * scale;
   if (lane == 0) {
     o.tau[j] = tau;
     o.e[j] = beta;
   }
+}
+
+// Copy the Householder vector of step j (and its tau) from the CTA that computed it.
+__device__ void sytrd_pull(cg::cluster_group& cluster, int CL, int r, int n, int j, double* vbuf, double* scal) {
+  const int src = j % CL;  // owner of column j computed its reflector
+  const int slot = j & 1;
+  if (src == r) return;
+  const double* rv = cluster.map_shared_rank(vbuf + (size_t)slot * n, src);
+  double* lv = vbuf + (size_t)slot * n;
+  for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) lv[i] = rv[i];
+  if (threadIdx.x == 0) scal[slot] = *cluster.map_shared_rank(scal + slot, src);
 }
 
 template <int CL>
@@ -98,12 +107,13 @@ __global__ void __launch_bounds__(256) k_sytrd(const SytrdOp* __restrict__ ops) 
     const int c = r + lc * CL;
     for (int i = lane; i < n; i += 32) cols[(size_t)lc * n + i] = o.A[i + (int64_t)c * o.lda];
   }
-  cluster.sync();  // every CTA of the cluster runs before distributed shared memory is written
-  if (n >= 3 && r == 0 && warp == 0) sytrd_householder(cluster, CL, o, cols, 0, vbuf, scal, 0, lane);
+  if (n >= 3 && r == 0 && warp == 0) sytrd_householder(o, cols, 0, vbuf, scal, 0, lane);
   if (n >= 1 && r == 0 && threadIdx.x == 0) o.d[0] = cols[0];
-  cluster.sync();
+  cluster.sync();  // every CTA runs (distributed shared memory is addressable) and reflector 0 exists
   for (int j = 0; j + 2 < n; ++j) {
     const int slot = j & 1;
+    sytrd_pull(cluster, CL, r, n, j, vbuf, scal);
+    __syncthreads();
     const double* v = vbuf + (size_t)slot * n;
     const double tau = scal[slot];
     // (b) p_c = tau * G(:, c) . v for own columns c >= j+1, pushed to every CTA; partial v . p
@@ -142,7 +152,7 @@ __global__ void __launch_bounds__(256) k_sytrd(const SytrdOp* __restrict__ ops) 
       for (int i = j + 1 + lane; i < n; i += 32) a[i] -= v[i] * wc + w[i] * vc;
       __syncwarp();
       if (lane == 0) o.d[j + 1] = a[j + 1];
-      if (j + 3 < n) sytrd_householder(cluster, CL, o, a, j + 1, vbuf, scal, slot ^ 1, lane);
+      if (j + 3 < n) sytrd_householder(o, a, j + 1, vbuf, scal, slot ^ 1, lane);
     }
     for (int lc = lc0 + warp; lc < ncol; lc += nwarp) {
       if (r == owner && lc == lnext) continue;
@@ -151,7 +161,7 @@ __global__ void __launch_bounds__(256) k_sytrd(const SytrdOp* __restrict__ ops) 
       const double wc = w[c], vc = v[c];
       for (int i = j + 1 + lane; i < n; i += 32) a[i] -= v[i] * wc + w[i] * vc;
     }
-    cluster.sync();  // #2: columns updated, next Householder vector everywhere
+    cluster.sync();  // #2: columns updated, next Householder vector ready on its owner
   }
   // trailing 2 x 2 block: d[n-2] was recorded by the last step (or above for n == 2), e[n-2], d[n-1]
   if (n >= 2 && threadIdx.x == 0) {
@@ -215,19 +225,25 @@ void launch_sytrd(const SytrdOp* ops, int nops, int CL, int nmax, cudaStream_t s
 // p_i = (d_i - x) p_{i-1} - e_{i-1}^2 p_{i-2}, rescaled by exact powers of two (no division: an FP64
 // division is a long instruction sequence on this GPU).  A zero p_i counts as a sign change.
 __device__ int sturm_count(const double* d, const double* e2, int n, double x) {
-  int c = 0;
+  // signs compared through the bit patterns (integer pipe); magnitudes checked every 4 steps (the
+  // recurrence cannot leave [2^-1000, 2^1000] from [2^-400, 2^400] in 4 steps for |T| <= 2^100)
+  auto neg = [](double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); };
   double p0 = 1.0, p1 = d[0] - x;
   if (p1 == 0.0) p1 = -DBL_MIN;
-  c += p1 < 0.0;
-  for (int i = 1; i < n; ++i) {
-    double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
-    if (p2 == 0.0) p2 = p1 > 0.0 ? -DBL_MIN : DBL_MIN;
-    c += (p2 < 0.0) != (p1 < 0.0);
-    p0 = p1;
-    p1 = p2;
-    const double m = fabs(p1);
-    if (m > 0x1p+400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
-    else if (m < 0x1p-400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
+  int c = neg(p1);
+  int i = 1;
+  while (i < n) {
+    const int iend = min(n, i + 4);
+    for (; i < iend; ++i) {
+      double p2 = fma(d[i] - x, p1, -e2[i - 1] * p0);
+      if ((__double_as_longlong(p2) << 1) == 0) p2 = neg(p1) ? DBL_MIN : -DBL_MIN;  // zero: a sign change
+      c += neg(p2) ^ neg(p1);
+      p0 = p1;
+      p1 = p2;
+    }
+    const int ex = (int)((__double_as_longlong(p1) >> 52) & 0x7ff) - 1023;  // binary exponent of p1
+    if (ex > 400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
+    else if (ex < -400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
   }
   return c;
 }
@@ -280,6 +296,8 @@ void launch_tri_bounds(const TriOp* ops, int nops, cudaStream_t s) {
 
 // One thread per (sector, eigenvalue index in descending order).  Eigenvalues at or below the sector's
 // floor (floor_rel * lambda_max) are not computed: W holds -1 there.  W[k] = k-th largest eigenvalue.
+// (Four interleaved bisections per thread were measured 4x slower: a quarter of the warps, on a
+// quarter of the SMs.)
 __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restrict__ op_of, const int* __restrict__ k_of,
                              int nthreads) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -443,36 +461,19 @@ void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s) {
 
 // ----------------------------------------------------------------------------- 5. CholeskyQR
 // k_chol<CL>: C = L L^T for the k x k symmetric positive definite C (lower triangle read), one cluster
-// of CL CTAs per sector with the columns round-robin in shared memory; column j of L is computed by
-// its owner (right after that owner applied the previous column's update to it) and pushed to every
-// CTA, one cluster barrier per column.  Output: R = L^T in the upper triangle of C (column j of R =
-// row j of L), rdiag[j] = 1 / R_jj, S[j] *= R_jj when S is given; info[0] = j + 1 for the first
-// non-positive pivot (then treated as 1).
+// of CL CTAs per sector.  Columns are distributed in panels of kPanel columns, panel b on CTA b % CL.
+// Per panel: its owner factorises the panel in shared memory (columns in sequence, CTA barriers only),
+// one cluster barrier, every CTA copies the panel from the owner's shared memory (distributed shared
+// memory loads by all its threads) and applies the rank-kPanel update to its own later columns.
+// Output: R = L^T in the upper triangle of C (column j of R = row j of L), rdiag[j] = 1 / R_jj,
+// S[j] *= R_jj when S is given; info[0] = j + 1 for the first non-positive pivot (then treated as 1).
+constexpr int kPanel = 16;
 static __host__ __device__ size_t chol_smem_doubles(int k, int CL) {
-  const int ncol = (k + CL - 1) / CL;
-  return (size_t)ncol * k + 2 * (size_t)k + 8;
+  const int nb = (k + kPanel - 1) / kPanel;
+  const int nbl = (nb + CL - 1) / CL;  // panels per CTA (at most)
+  return (size_t)nbl * kPanel * k + (size_t)kPanel * k + 8;
 }
 size_t chol_smem_bytes(int k, int CL) { return sizeof(double) * chol_smem_doubles(k, CL); }
-
-__device__ void chol_column(cg::cluster_group& cluster, int CL, const CholQROp& o, const double* col, int j,
-                            double* lbuf_local, int slot, int lane) {
-  const int k = o.k;
-  double piv = col[j];
-  if (!(piv > 0.0)) {
-    if (lane == 0) atomicCAS(o.info, 0, j + 1);
-    piv = 1.0;
-  }
-  const double ljj = sqrt(piv), inv = 1.0 / ljj;
-  for (int q = 0; q < CL; ++q) {
-    double* lr = cluster.map_shared_rank(lbuf_local + (size_t)slot * k, q);
-    for (int i = j + lane; i < k; i += 32) lr[i] = (i == j) ? ljj : col[i] * inv;
-  }
-  for (int i = j + lane; i < k; i += 32) o.C[j + (int64_t)i * o.ld] = (i == j) ? ljj : col[i] * inv;  // R(j, i)
-  if (lane == 0) {
-    o.rdiag[j] = inv;
-    if (o.S) o.S[j] *= ljj;
-  }
-}
 
 template <int CL>
 __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) {
@@ -480,41 +481,93 @@ __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) 
   const int r = (int)cluster.block_rank();
   const CholQROp o = ops[blockIdx.x / CL];
   const int k = o.k;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   extern __shared__ double sm[];
-  const int ncol = (k - r + CL - 1) / CL;
-  const int ncol_max = (k + CL - 1) / CL;
-  double* cols = sm;
-  double* lbuf = cols + (size_t)ncol_max * k;  // 2 x k
-  for (int lc = warp; lc < ncol; lc += nwarp) {
-    const int c = r + lc * CL;
-    for (int i = lane; i < k; i += 32) cols[(size_t)lc * k + i] = o.C[i + (int64_t)c * o.ld];
-  }
-  cluster.sync();
-  if (k >= 1 && r == 0 && warp == 0) chol_column(cluster, CL, o, cols, 0, lbuf, 0, lane);
-  cluster.sync();
-  for (int j = 0; j + 1 < k; ++j) {
-    const int slot = j & 1;
-    const double* l = lbuf + (size_t)slot * k;
-    const int owner = (j + 1) % CL, lnext = (j + 1) / CL;
-    const int lc0 = (j + 1 - r + CL - 1) / CL;
-    if (r == owner && warp == 0) {  // column j+1 first, then its L column (lookahead)
-      double* a = cols + (size_t)lnext * k;
-      const double lc = l[j + 1];
-      for (int i = j + 1 + lane; i < k; i += 32) a[i] -= l[i] * lc;
-      __syncwarp();
-      chol_column(cluster, CL, o, a, j + 1, lbuf, slot ^ 1, lane);
+  const int nb = (k + kPanel - 1) / kPanel;
+  const int nbl_max = (nb + CL - 1) / CL;
+  double* cols = sm;                                        // local panel p (global panel r + p*CL): kPanel x k
+  double* pbuf = cols + (size_t)nbl_max * kPanel * k;       // current panel, copied from its owner
+  auto colptr = [&](double* base, int lp, int jj) { return base + ((size_t)lp * kPanel + jj) * k; };
+  const int nbl = (nb - r + CL - 1) / CL;
+  for (int lp = 0; lp < nbl; ++lp)
+    for (int jj = warp; jj < kPanel; jj += nwarp) {
+      const int c = (r + lp * CL) * kPanel + jj;
+      double* dst = colptr(cols, lp, jj);
+      for (int i = lane; i < k; i += 32) dst[i] = c < k ? o.C[i + (int64_t)c * o.ld] : 0.0;
     }
-    for (int lc = lc0 + warp; lc < ncol; lc += nwarp) {
-      if (r == owner && lc == lnext) continue;
-      const int c = r + lc * CL;
-      double* a = cols + (size_t)lc * k;
-      const double lcv = l[c];
-      for (int i = c + lane; i < k; i += 32) a[i] -= l[i] * lcv;
-    }
-    cluster.sync();
-  }
   cluster.sync();
+  for (int b = 0; b < nb; ++b) {
+    const int j0 = b * kPanel, jn = min(kPanel, k - j0);
+    const int owner = b % CL;
+    if (r == owner) {  // factorise panel b (its columns already hold all earlier panels' updates)
+      const int lp = b / CL;
+      for (int jj = 0; jj < jn; ++jj) {
+        double* a = colptr(cols, lp, jj);
+        const int j = j0 + jj;
+        __shared__ double ljj_s;
+        if (tid == 0) {
+          double piv = a[j];
+          if (!(piv > 0.0)) {
+            atomicCAS(o.info, 0, j + 1);
+            piv = 1.0;
+          }
+          const double l = sqrt(piv);
+          ljj_s = l;
+          o.rdiag[j] = 1.0 / l;
+          if (o.S) o.S[j] *= l;
+        }
+        __syncthreads();
+        const double l = ljj_s, inv = 1.0 / l;
+        for (int i = j + tid; i < k; i += blockDim.x) a[i] = (i == j) ? l : a[i] * inv;
+        __syncthreads();
+        // update the rest of the panel: column j0+q -= L(:, j) L(j0+q, j), rows >= j0+q
+        for (int q = jj + 1 + warp; q < jn; q += nwarp) {
+          double* c = colptr(cols, lp, q);
+          const double f = a[j0 + q];
+          for (int i = j0 + q + lane; i < k; i += 32) c[i] -= a[i] * f;
+        }
+        __syncthreads();
+      }
+      // R = L^T rows of this panel
+      for (int jj = warp; jj < jn; jj += nwarp) {
+        const double* a = colptr(cols, lp, jj);
+        const int j = j0 + jj;
+        for (int i = j + lane; i < k; i += 32) o.C[j + (int64_t)i * o.ld] = a[i];
+      }
+    }
+    cluster.sync();  // panel b factorised
+    if (b + 1 == nb) break;
+    // copy panel b (rows >= j0 + jn) from the owner's shared memory
+    {
+      const double* src = cluster.map_shared_rank(colptr(cols, b / CL, 0), owner);
+      for (int idx = tid; idx < jn * k; idx += blockDim.x) {
+        const int i = idx % k;
+        if (i >= j0 + jn) pbuf[idx] = src[idx];
+      }
+    }
+    __syncthreads();
+    // rank-jn update of the own columns of later panels: C(i, c) -= sum_jj L(i, jj) L(c, jj), i >= c
+    for (int lp = 0; lp < nbl; ++lp) {
+      const int gb = r + lp * CL;
+      if (gb <= b) continue;
+      for (int jj = warp; jj < kPanel; jj += nwarp) {
+        const int c = gb * kPanel + jj;
+        if (c >= k) break;
+        double* a = colptr(cols, lp, jj);
+        double f[kPanel];
+#pragma unroll
+        for (int q = 0; q < kPanel; ++q) f[q] = q < jn ? pbuf[(size_t)q * k + c] : 0.0;
+        for (int i = c + lane; i < k; i += 32) {
+          double acc = a[i];
+#pragma unroll
+          for (int q = 0; q < kPanel; ++q) acc = fma(-pbuf[(size_t)q * k + i], f[q], acc);
+          a[i] = acc;
+        }
+      }
+    }
+    __syncthreads();  // own columns updated before this CTA factorises or copies the next panel
+  }
+  cluster.sync();  // no CTA leaves while another may still read its panels
 }
 
 template <int CL>
@@ -537,9 +590,16 @@ static void launch_chol_cl(const CholQROp* ops, int nops, int kmax, cudaStream_t
   MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_chol<CL>, ops));
   g_eig_launches.fetch_add(1);
 }
+int chol_max_k() { return 512; }
+int chol_cluster_size(int k) {
+  // smallest cluster whose shared memory holds the panels (<= 200 KB per CTA)
+  for (int CL : {1, 2, 4, 8, 16})
+    if (chol_smem_bytes(k, CL) <= 200 * 1024 && (CL >= 16 || k <= 48 * CL)) return CL;
+  return 16;
+}
 void launch_chol(const CholQROp* ops, int nops, int CL, int kmax, cudaStream_t s) {
   if (nops <= 0) return;
-  MPSG_CHECK(kmax <= sytrd_max_n(), "Cholesky: sector too large for the cluster kernel");
+  MPSG_CHECK(chol_smem_bytes(kmax, CL) <= 227 * 1024, "Cholesky: sector too large for the cluster kernel");
   switch (CL) {
     case 1: launch_chol_cl<1>(ops, nops, kmax, s); break;
     case 2: launch_chol_cl<2>(ops, nops, kmax, s); break;
@@ -581,6 +641,24 @@ void launch_trsm_rows(const TrsmRowsOp* ops, int nops, int kmax, cudaStream_t s)
   const size_t smem = sizeof(double) * 32 * (size_t)kmax;
   MPSG_CUDA(cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   k_trsm_rows<<<nops, 32, smem, s>>>(ops);
+  g_eig_launches.fetch_add(1);
+}
+
+// cnt[t] = number of eigenvalues of sector t above the floor (W >= 0; W is descending).
+__global__ void k_count_nonneg(const TriOp* __restrict__ ops, int* cnt) {
+  const TriOp o = ops[blockIdx.x];
+  __shared__ int c;
+  if (threadIdx.x == 0) c = 0;
+  __syncthreads();
+  int mine = 0;
+  for (int k = threadIdx.x; k < o.n; k += blockDim.x) mine += o.W[k] >= 0.0;
+  atomicAdd(&c, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) cnt[blockIdx.x] = c;
+}
+void launch_count_nonneg(const TriOp* ops, int nops, int* cnt, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_count_nonneg<<<nops, 128, 0, s>>>(ops, cnt);
   g_eig_launches.fetch_add(1);
 }
 

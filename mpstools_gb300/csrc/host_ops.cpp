@@ -614,6 +614,8 @@ struct SvdBatch {
     int64_t offM, offU, offV, offS;
   };
   std::vector<Sec> s;
+  std::vector<int> kr;  // resolved singular pairs per sector (density routes; empty: all k)
+  int kcols(size_t i) const { return kr.empty() ? s[i].k : kr[i]; }
   Ctx* ctx = nullptr;
   double *dM = nullptr, *dU = nullptr, *dV = nullptr, *dS = nullptr;
   int* dinfo = nullptr;
@@ -803,7 +805,7 @@ struct SvdBatch {
         nmax = std::max(nmax, s[i].ns);
       }
     if (idx.empty()) return;
-    if (nmax > sytrd_max_n()) { run_gram(); return; }
+    MPSG_CHECK(nmax <= sytrd_max_n() && nmax <= chol_max_k(), "density split: sector too wide");
     cudaStream_t st = ctx->stream;
     MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(s.size(), 1), st));  // no solver status
     std::vector<int64_t> offG(s.size(), 0);
@@ -872,13 +874,23 @@ struct SvdBatch {
     launch_tri_bounds(dtops, (int)tops.size(), st);
     launch_tri_bisect(dtops, dmap, dmap + nthreads, nthreads, 0.0, st);
     launch_tri_invit(dtops, dmap, dmap + nthreads, nthreads, 1e-12, dscr, dsoff, st);
+    {  // resolved eigenpairs per sector (W is descending, -1 below the floor)
+      int* dcnt = (int*)ctx->dmalloc(sizeof(int) * idx.size());
+      launch_count_nonneg(dtops, (int)tops.size(), dcnt, st);
+      std::vector<int> cnt(idx.size());
+      MPSG_CUDA(cudaMemcpyAsync(cnt.data(), dcnt, sizeof(int) * cnt.size(), cudaMemcpyDeviceToHost, st));
+      ctx->sync();
+      ctx->dfree(dcnt);
+      kr.assign(s.size(), 0);
+      for (size_t t = 0; t < idx.size(); ++t) kr[idx[t]] = cnt[t];
+    }
     // 4. back-transformation V = Q Z, blocks of 8 columns
     {
       std::vector<OrmtrOp> oo;
       for (int i : idx)
-        for (int c0 = 0; c0 < s[i].ns; c0 += 8)
+        for (int c0 = 0; c0 < kr[i]; c0 += 8)
           oo.push_back(OrmtrOp{dG + offG[i], dtau + s[i].offS, dW + s[i].offS, dV + s[i].offV, s[i].ns, s[i].ns,
-                               s[i].ns, c0, std::min(c0 + 8, s[i].ns)});
+                               s[i].ns, c0, std::min(c0 + 8, kr[i])});
       OrmtrOp* d = (OrmtrOp*)ctx->dmalloc(sizeof(OrmtrOp) * oo.size());
       MPSG_CUDA(cudaMemcpyAsync(d, oo.data(), sizeof(OrmtrOp) * oo.size(), cudaMemcpyHostToDevice, st));
       launch_ormtr(d, (int)oo.size(), nmax, st);
@@ -1054,8 +1066,10 @@ struct SvdBatch {
     for (size_t i = 0; i < s.size(); ++i) {
       const Sec& x = s[i];
       if (x.k == 0) continue;
-      g.add_problem(2, x.offU, x.ms, x.ms, x.k, false, {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
-      cn.push_back(ColNorm{dU + x.offU, dS + x.offS, x.ms, x.k, x.ms});
+      if (kcols(i) > 0)
+        g.add_problem(2, x.offU, x.ms, x.ms, kcols(i), false,
+                      {GSegH{0, 1, x.offM, x.offV, x.ms, x.ns, x.ns, 0, 0, 1.0}});
+      cn.push_back(ColNorm{dU + x.offU, dS + x.offS, x.ms, x.k, x.ms});  // clears the unresolved columns
     }
     g.upload(ctx);
     const double* bases[8] = {dM, dV, dU, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -1070,19 +1084,19 @@ struct SvdBatch {
 
   // CholeskyQR of every sector's matrix X (columns in descending s order), in place: C = X^T X by the
   // grouped FP64 GEMM (zero columns get C_jj = 1 and stay zero), C = R^T R by the cluster Cholesky
-  // kernel, X <- X R^-1 by row-parallel forward substitution.  left: X = Ust (ms x ns) and s_j is
+  // kernel, X <- X R^-1 by blocked forward substitution.  left: X = Ust (ms x ns) and s_j is
   // multiplied by R_jj of the first pass (the norm of y_j after removing its components along the
   // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
   void cholqr(bool left, int passes) {
     std::vector<int> idx;
     int kmax = 0;
     for (size_t i = 0; i < s.size(); ++i)
-      if (s[i].k > 0) {
+      if (kcols(i) > 0) {
         idx.push_back((int)i);
-        kmax = std::max(kmax, s[i].ns);
+        kmax = std::max(kmax, kcols(i));
       }
     if (idx.empty()) return;
-    MPSG_CHECK(kmax <= sytrd_max_n(), "CholeskyQR: sector wider than the cluster kernel's limit");
+    MPSG_CHECK(kmax <= chol_max_k(), "CholeskyQR: sector wider than the cluster kernel's limit (512)");
     cudaStream_t st = ctx->stream;
     double* X = left ? dU : dV;
     auto rows = [&](int i) { return left ? s[i].ms : s[i].ns; };
@@ -1091,7 +1105,7 @@ struct SvdBatch {
     int64_t oC = 0;
     for (int i : idx) {
       offC[i] = oC;
-      oC += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+      oC += ((int64_t)kcols(i) * kcols(i) + kAlign - 1) / kAlign * kAlign;
     }
     double* dC = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
     double* dR = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));  // 1 / R_jj
@@ -1099,26 +1113,45 @@ struct SvdBatch {
     MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * idx.size(), st));
     GemmPlan g;
     for (int i : idx)
-      g.add_problem(2, offC[i], s[i].ns, s[i].ns, s[i].ns, false,
+      g.add_problem(2, offC[i], kcols(i), kcols(i), kcols(i), false,
                     {GSegH{0, 0, offX(i), offX(i), rows(i), rows(i), rows(i), 1, 0, 1.0}});
     g.upload(ctx);
     std::vector<CholOp> zd;
     std::map<int, std::vector<CholQROp>> byCL[2];
     std::map<int, int> kmaxCL;
-    std::vector<TrsmRowsOp> tr;
     for (size_t t = 0; t < idx.size(); ++t) {
       const int i = idx[t];
-      zd.push_back(CholOp{dC + offC[i], nullptr, s[i].ns, s[i].ns});
-      const int CL = sytrd_cluster_size(s[i].ns);
+      const int kc = kcols(i);
+      zd.push_back(CholOp{dC + offC[i], nullptr, kc, kc});
+      const int CL = chol_cluster_size(kc);
       for (int pass = 0; pass < 2; ++pass)
         byCL[pass][CL].push_back(CholQROp{dC + offC[i], dR + s[i].offS, (pass == 0 && left) ? dS + s[i].offS : nullptr,
-                                          dinf + t, s[i].ns, s[i].ns});
-      kmaxCL[CL] = std::max(kmaxCL[CL], s[i].ns);
-      for (int r0 = 0; r0 < rows(i); r0 += 32)
-        tr.push_back(TrsmRowsOp{X + offX(i), dC + offC[i], dR + s[i].offS, s[i].ns, rows(i), s[i].ns, r0,
-                                std::min(r0 + 32, rows(i))});
+                                          dinf + t, kc, kc});
+      kmaxCL[CL] = std::max(kmaxCL[CL], kc);
     }
-    size_t bytes = sizeof(CholOp) * zd.size() + sizeof(TrsmRowsOp) * tr.size();
+    // X <- X R^-1 by 64-column blocks: X_b -= X_<b R_<b,b (grouped GEMM), then X_b <- X_b R_bb^-1
+    // (row-parallel substitution over 64 columns)
+    constexpr int kTB = 64;
+    const int nblk = (kmax + kTB - 1) / kTB;
+    std::vector<std::unique_ptr<GemmPlan>> upd(nblk);
+    std::vector<std::vector<TrsmRowsOp>> tr(nblk);
+    for (int b = 0; b < nblk; ++b) {
+      upd[b].reset(new GemmPlan());
+      for (int i : idx) {
+        const int c0 = b * kTB, kc = kcols(i);
+        if (c0 >= kc) continue;
+        const int bw = std::min(kTB, kc - c0);
+        if (b > 0)
+          upd[b]->add_problem(2, offX(i) + (int64_t)c0 * rows(i), rows(i), rows(i), bw, true,
+                              {GSegH{0, 1, offX(i), offC[i] + (int64_t)c0 * kc, rows(i), kc, c0, 0, 0, -1.0}});
+        for (int r0 = 0; r0 < rows(i); r0 += 32)
+          tr[b].push_back(TrsmRowsOp{X + offX(i) + (int64_t)c0 * rows(i), dC + offC[i] + c0 + (int64_t)c0 * kc,
+                                     dR + s[i].offS + c0, bw, rows(i), kc, r0, std::min(r0 + 32, rows(i))});
+      }
+      upd[b]->upload(ctx);
+    }
+    size_t bytes = sizeof(CholOp) * zd.size() + 16;
+    for (int b = 0; b < nblk; ++b) bytes += sizeof(TrsmRowsOp) * tr[b].size() + 16;
     for (int pass = 0; pass < 2; ++pass)
       for (auto& c : byCL[pass]) bytes += sizeof(CholQROp) * c.second.size() + 16;
     char* dops = (char*)ctx->dmalloc(bytes + 64);
@@ -1131,7 +1164,8 @@ struct SvdBatch {
       return d;
     };
     CholOp* dzd = (CholOp*)put(zd.data(), sizeof(CholOp) * zd.size());
-    TrsmRowsOp* dtr = (TrsmRowsOp*)put(tr.data(), sizeof(TrsmRowsOp) * tr.size());
+    std::vector<TrsmRowsOp*> dtr(nblk);
+    for (int b = 0; b < nblk; ++b) dtr[b] = (TrsmRowsOp*)put(tr[b].data(), sizeof(TrsmRowsOp) * tr[b].size());
     std::map<int, CholQROp*> dch[2];
     for (int pass = 0; pass < 2; ++pass)
       for (auto& c : byCL[pass]) dch[pass][c.first] = (CholQROp*)put(c.second.data(), sizeof(CholQROp) * c.second.size());
@@ -1143,7 +1177,11 @@ struct SvdBatch {
       launch_chol_unit_zero_diag(dzd, (int)zd.size(), st);
       const int which = pass == 0 ? 0 : 1;
       for (auto& c : byCL[which]) launch_chol(dch[which][c.first], (int)c.second.size(), c.first, kmaxCL[c.first], st);
-      launch_trsm_rows(dtr, (int)tr.size(), kmax, st);
+      const double* tb[8] = {X, dC, X, nullptr, nullptr, nullptr, nullptr, nullptr};
+      for (int b = 0; b < nblk; ++b) {
+        if (b > 0) upd[b]->run(tb);
+        launch_trsm_rows(dtr[b], (int)tr[b].size(), kTB, st);
+      }
     }
     std::vector<int> inf(idx.size(), 0);
     MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * inf.size(), cudaMemcpyDeviceToHost, st));
@@ -1159,6 +1197,9 @@ struct SvdBatch {
   void orthonormalize_left() { cholqr(true, 1); }
 
   void run(int method) {
+    int nmax = 0;
+    for (auto& x : s) nmax = std::max(nmax, x.k > 0 ? x.ns : 0);
+    if (method != 0 && nmax > chol_max_k()) method = 0;  // the density routes' CholeskyQR covers widths <= 512
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
     else if (method == 3) run_gram_custom();

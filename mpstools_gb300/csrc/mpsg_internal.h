@@ -241,7 +241,10 @@ void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int n
                       double* scratch, const int64_t* scratch_off, cudaStream_t s);
 void launch_ormtr(const OrmtrOp* ops, int nops, int nmax, cudaStream_t s);
 void launch_eig_post(const EigPostOp* ops, int nops, cudaStream_t s);
+void launch_count_nonneg(const TriOp* ops, int nops, int* cnt, cudaStream_t s);
 size_t chol_smem_bytes(int k, int CL);
+int chol_cluster_size(int k);
+int chol_max_k();
 void launch_chol(const CholQROp* ops, int nops, int CL, int kmax, cudaStream_t s);
 void launch_trsm_rows(const TrsmRowsOp* ops, int nops, int kmax, cudaStream_t s);
 
