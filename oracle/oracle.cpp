@@ -23,6 +23,11 @@
 //   TSLanzcosEngine::simulate / getState .......... src/lanzcos.hpp:81-92,165-278
 //   DMRGengine::doStep / simulate ................. src/container.hpp:292-337,381-438
 //   MPO::measure .................................. src/MPOTypes.hpp:990-1020
+//   MPO::getNNGate (two-site gate exp(-i dt h_b)) . src/MPOTypes.hpp:1090-1209
+//   applyGate ..................................... src/MPSfunctions.hpp:1492-1548
+//   TEBDengine doTimeSlice / second-order simulate  src/container.hpp:1195-1233,1325-1395
+//   SparseLocalOperator::measure (on lambda Gamma lambda) src/MPOTypes.hpp:532-563
+//   complex FixPhase .............................. blas/helperfunctions.hpp:52-67
 //   HeisenbergMPO / SpinlessFermionsMPO ........... src/Hamiltonians.hpp:84-131,527-566
 //   SparseOperator product ........................ src/MPOTypes.hpp:200-230
 //   BoostSVD -> rsvd (dgesvd 'S','S') + FixPhase .. blas/lapack_routines.cpp:334-366,614-634,
@@ -47,6 +52,7 @@
 #include <string>
 #include <vector>
 #include <algorithm>
+#include <complex>
 
 namespace orc {
 
@@ -909,6 +915,390 @@ static std::vector<MPOMat> spinless(int N, const double* V, const double* t, con
 // ============================================================================ C ABI for ctypes
 using namespace orc;
 
+
+// ================================================================ complex FP64 (TEBD)
+typedef std::complex<double> cplx;
+typedef void (*zgemm_t)(const char*, const char*, const int*, const int*, const int*, const cplx*, const cplx*,
+                        const int*, const cplx*, const int*, const cplx*, cplx*, const int*, size_t, size_t);
+typedef void (*zgesvd_t)(const char*, const char*, const int*, const int*, cplx*, const int*, double*, cplx*,
+                         const int*, cplx*, const int*, cplx*, const int*, double*, int*, size_t, size_t);
+static zgemm_t p_zgemm = nullptr;
+static zgesvd_t p_zgesvd = nullptr;
+
+struct CMat {
+  int r = 0, c = 0;
+  std::vector<cplx> d;  // column-major
+  CMat() {}
+  CMat(int r_, int c_) : r(r_), c(c_), d((size_t)r_ * c_, cplx(0.0, 0.0)) {}
+  cplx& operator()(int i, int j) { return d[(size_t)i + (size_t)j * r]; }
+  cplx operator()(int i, int j) const { return d[(size_t)i + (size_t)j * r]; }
+};
+typedef std::map<Key, CMat> CBM;
+
+// out = op(A) op(B), op in 'n', 't', 'c' (MatMatProd for Complex)
+static CMat cgemm(const CMat& A, char ta, const CMat& B, char tb) {
+  int m = (ta == 'n') ? A.r : A.c;
+  int k = (ta == 'n') ? A.c : A.r;
+  int n = (tb == 'n') ? B.c : B.r;
+  CMat C(m, n);
+  if (m == 0 || n == 0 || k == 0) return C;
+  int lda = std::max(1, A.r), ldb = std::max(1, B.r), ldc = std::max(1, m);
+  cplx one(1.0, 0.0), zero(0.0, 0.0);
+  char TA = ta == 'n' ? 'N' : (ta == 't' ? 'T' : 'C'), TB = tb == 'n' ? 'N' : (tb == 't' ? 'T' : 'C');
+  p_zgemm(&TA, &TB, &m, &n, &k, &one, A.d.data(), &lda, B.d.data(), &ldb, &zero, C.d.data(), &ldc, 1, 1);
+  return C;
+}
+
+// BoostSVD for Complex: zgesvd 'S','S', then the complex FixPhase (the phase of the first abs-max
+// entry of each row of Vt removed from that row and given to the column of U).
+static int csvd(const CMat& M, CMat& U, std::vector<double>& D, CMat& Vt) {
+  int m = M.r, n = M.c, k = std::min(m, n);
+  U = CMat(m, k);
+  Vt = CMat(k, n);
+  D.assign(k, 0.0);
+  if (k == 0) return 0;
+  CMat A = M;
+  char J = 'S';
+  int lda = m, ldu = m, ldvt = k, info = 0, lwork = -1;
+  cplx wq;
+  std::vector<double> rwork(5 * (size_t)k + 8);
+  p_zgesvd(&J, &J, &m, &n, A.d.data(), &lda, D.data(), U.d.data(), &ldu, Vt.d.data(), &ldvt, &wq, &lwork,
+           rwork.data(), &info, 1, 1);
+  lwork = std::max((int)wq.real(), 2 * k + std::max(m, n));
+  std::vector<cplx> work(lwork);
+  p_zgesvd(&J, &J, &m, &n, A.d.data(), &lda, D.data(), U.d.data(), &ldu, Vt.d.data(), &ldvt, work.data(), &lwork,
+           rwork.data(), &info, 1, 1);
+  for (int i = 0; i < k; ++i) {
+    int ind = 0;
+    double val = 0;
+    for (int j = 0; j < n; ++j)
+      if (std::abs(Vt(i, j)) > val) { val = std::abs(Vt(i, j)); ind = j; }
+    const double phi = std::arg(Vt(i, ind));
+    const cplx e = std::exp(cplx(0.0, -phi)), ec = std::exp(cplx(0.0, phi));
+    for (int j = 0; j < n; ++j) Vt(i, j) *= e;
+    for (int j = 0; j < m; ++j) U(j, i) *= ec;
+  }
+  return info;
+}
+
+// BlockMatrix::squeeze(thresh): erase blocks whose entries are all <= thresh in magnitude
+static void csqueeze(CBM& B, double thresh) {
+  for (auto it = B.begin(); it != B.end();) {
+    bool keep = false;
+    for (auto& v : it->second.d)
+      if (std::abs(v) > thresh) { keep = true; break; }
+    if (!keep) it = B.erase(it);
+    else ++it;
+  }
+}
+
+// lambda * B (rows by the left charge), B * lambda (columns by the right charge), and the divisions;
+// blocks whose charge has no lambda are dropped (src/BlockTensor.hpp:653-733)
+static CBM lam_scale(const Diag& lam, const CBM& B, bool left, bool divide) {
+  CBM out;
+  for (auto& b : B) {
+    auto l = lam.find(left ? b.first.q0 : b.first.q1);
+    if (l == lam.end()) continue;
+    CMat t = b.second;
+    for (int j = 0; j < t.c; ++j)
+      for (int i = 0; i < t.r; ++i) {
+        const double f = left ? l->second[i] : l->second[j];
+        t(i, j) = divide ? t(i, j) * (1.0 / f) : t(i, j) * f;
+      }
+    out[b.first] = t;
+  }
+  return out;
+}
+
+// BlockMatrix<2>(A1, A2)
+static CBM ctheta(const CBM& B1, const CBM& B2) {
+  CBM out;
+  for (auto& a : B1)
+    for (auto& b : B2)
+      if (a.first.q1 == b.first.q0) {
+        Key k = K2(a.first.q0, b.first.q1, a.first.p0, b.first.p0);
+        CMat t = cgemm(a.second, 'n', b.second, 'n');
+        auto y = out.find(k);
+        if (y != out.end())
+          for (size_t i = 0; i < t.d.size(); ++i) t.d[i] += y->second.d[i];
+        out[k] = t;
+      }
+  return out;
+}
+
+template <class M>
+static void drop_dangling_t(std::map<Key, M>& L, const Diag& lam, std::map<Key, M>& R) {
+  for (auto it = L.begin(); it != L.end();) {
+    auto l = lam.find(it->first.q1);
+    if (l == lam.end()) { it = L.erase(it); continue; }
+    const int k = (int)l->second.size();
+    if (it->second.c > k) {
+      M t(it->second.r, k);
+      for (int j = 0; j < k; ++j)
+        for (int i = 0; i < t.r; ++i) t(i, j) = it->second(i, j);
+      it->second = t;
+    }
+    ++it;
+  }
+  for (auto it = R.begin(); it != R.end();) {
+    auto l = lam.find(it->first.q0);
+    if (l == lam.end()) { it = R.erase(it); continue; }
+    const int k = (int)l->second.size();
+    if (it->second.r > k) {
+      M t(k, it->second.c);
+      for (int j = 0; j < t.c; ++j)
+        for (int i = 0; i < k; ++i) t(i, j) = it->second(i, j);
+      it->second = t;
+    }
+    ++it;
+  }
+}
+
+struct CSplitOut {
+  CBM U, Vt;
+  Diag lam;
+  double tw = 0;
+  int chi = 0;
+};
+// split (two-site) for Complex (MPSfunctions.hpp:1142-1278): sectors by centre charge, zgesvd,
+// global truncation, dropDangling
+static CSplitOut csplit2(const CBM& A, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
+                         double tr_weight, bool normalize) {
+  std::map<Q, std::vector<CBM::const_iterator>> blocks;
+  std::map<Q, std::map<uint32_t, std::pair<int, int>>> RX, RY;
+  for (auto a = A.begin(); a != A.end(); ++a) {
+    Q qc = a->first.q0 + ik0[a->first.p0];
+    blocks[qc].push_back(a);
+    RX[qc][a->first.p0] = std::make_pair(0, a->second.r);
+    RY[qc][a->first.p1] = std::make_pair(0, a->second.c);
+  }
+  std::map<Q, int> sx, sy;
+  for (auto& r : RX) { int s = 0; for (auto& x : r.second) { x.second.first = s; s += x.second.second; } sx[r.first] = s; }
+  for (auto& r : RY) { int s = 0; for (auto& x : r.second) { x.second.first = s; s += x.second.second; } sy[r.first] = s; }
+  CSplitOut o;
+  for (auto& bq : blocks) {
+    const Q qc = bq.first;
+    CMat tmp(sx.at(qc), sy.at(qc)), U, Vt;
+    std::vector<double> D;
+    for (auto b : bq.second) {
+      auto rx = RX.at(qc).at(b->first.p0);
+      auto ry = RY.at(qc).at(b->first.p1);
+      for (int j = 0; j < b->second.c; ++j)
+        for (int i = 0; i < b->second.r; ++i) tmp(rx.first + i, ry.first + j) = b->second(i, j);
+    }
+    csvd(tmp, U, D, Vt);
+    const int chi = (int)D.size();
+    for (auto& x : RX.at(qc)) {
+      CMat u(x.second.second, chi);
+      for (int j = 0; j < chi; ++j)
+        for (int i = 0; i < u.r; ++i) u(i, j) = U(x.second.first + i, j);
+      o.U[K1(qc - ik0[x.first], qc, x.first)] = u;
+    }
+    o.lam[qc] = D;
+    for (auto& y : RY.at(qc)) {
+      CMat v(chi, y.second.second);
+      for (int j = 0; j < v.c; ++j)
+        for (int i = 0; i < chi; ++i) v(i, j) = Vt(i, y.second.first + j);
+      o.Vt[K1(qc, qc + ik1[y.first], y.first)] = v;
+    }
+  }
+  if (!chimax && doTrunc) chimax = 100;
+  if (!chimax && !doTrunc) chimax = 200;
+  std::pair<double, int> t = doTrunc ? truncate_tw(o.lam, tr_weight, chimax, normalize)
+                                     : truncate_chi(o.lam, chimax, normalize);
+  o.tw = t.first;
+  o.chi = t.second;
+  drop_dangling_t(o.U, o.lam, o.Vt);
+  return o;
+}
+
+// Two-site gate G[(o1,o2),(i1,i2)] = exp(-(dt_im + i dt_re) h_b), h_b = sum_i W1[row, i] (x) W2[i, 0]
+// with the boundary-aware halves of the on-site channels (MPO::getNNGate).  Dense d1*d2 square,
+// index o1 + d1*o2.
+struct Gate {
+  int d1 = 0, d2 = 0;
+  std::vector<cplx> g;  // (d1 d2) x (d1 d2), column-major
+  cplx at(int o1, int o2, int i1, int i2) const { return g[(size_t)(o1 + d1 * o2) + (size_t)(i1 + d1 * i2) * d1 * d2]; }
+};
+static void jacobi_eig_sym(int n, std::vector<double>& A, std::vector<double>& V, std::vector<double>& E) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[i + (size_t)i * n] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) off += A[p + (size_t)q * n] * A[p + (size_t)q * n];
+    if (off < 1e-32) break;
+    for (int p = 0; p < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[p + (size_t)q * n];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double app = A[p + (size_t)p * n], aqq = A[q + (size_t)q * n];
+        const double th = 0.5 * (aqq - app) / apq;
+        const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+        for (int k = 0; k < n; ++k) {  // A <- J^T A J
+          const double akp = A[k + (size_t)p * n], akq = A[k + (size_t)q * n];
+          A[k + (size_t)p * n] = c * akp - s * akq;
+          A[k + (size_t)q * n] = s * akp + c * akq;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double apk = A[p + (size_t)k * n], aqk = A[q + (size_t)k * n];
+          A[p + (size_t)k * n] = c * apk - s * aqk;
+          A[q + (size_t)k * n] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          const double vkp = V[k + (size_t)p * n], vkq = V[k + (size_t)q * n];
+          V[k + (size_t)p * n] = c * vkp - s * vkq;
+          V[k + (size_t)q * n] = s * vkp + c * vkq;
+        }
+      }
+  }
+  E.resize(n);
+  for (int i = 0; i < n; ++i) E[i] = A[i + (size_t)i * n];
+}
+static Gate nn_gate(const MPOMat& m1, const MPOMat& m2, int site1, int N, double dt_re, double dt_im, int d1, int d2) {
+  const int site2 = site1 + 1;
+  const int D = d1 * d2;
+  std::vector<double> H((size_t)D * D, 0.0);
+  auto add = [&](uint32_t r1, uint32_t c1, uint32_t r2, uint32_t c2, double w1, double w2) {
+    auto a = m1.m.find(WKey{r1, c1});
+    auto b = m2.m.find(WKey{r2, c2});
+    if (a == m1.m.end() || b == m2.m.end()) return;
+    for (auto& x : a->second)
+      for (auto& y : b->second) {
+        const int o = (int)x.first.out + d1 * (int)y.first.out, in = (int)x.first.in + d1 * (int)y.first.in;
+        H[o + (size_t)in * D] += x.second * w1 * y.second * w2;
+      }
+  };
+  const uint32_t lend = (uint32_t)m1.Dl - 1, last = (uint32_t)m1.Dr - 1;
+  for (uint32_t i = 0; i <= last; ++i) {
+    if (site1 == 0 && site2 != N - 1) {
+      if (i == 0) add(0, i, i, 0, 1.0, 1.0);
+      else if (i == last) add(0, i, i, 0, 1.0, 0.5);
+      else add(0, i, i, 0, 1.0, 1.0);
+    }
+    if (site2 == N - 1 && site1 != 0) {
+      if (i == 0) add(lend, i, i, 0, 0.5, 1.0);
+      else if (i == last) add(lend, i, i, 0, 1.0, 1.0);
+      else add(lend, i, i, 0, 1.0, 1.0);
+    }
+    if (site2 != N - 1 && site1 != 0) {
+      if (i == 0) add(lend, i, i, 0, 0.5, 1.0);
+      else if (i == last) add(lend, i, i, 0, 1.0, 0.5);
+      else add(lend, i, i, 0, 1.0, 1.0);
+    }
+  }
+  for (auto& h : H)
+    if (std::fabs(h) < 1e-14) h = 0.0;  // gate.squeeze(1e-14) before the exponential
+  std::vector<double> V, E;
+  std::vector<double> A = H;
+  jacobi_eig_sym(D, A, V, E);
+  Gate G;
+  G.d1 = d1;
+  G.d2 = d2;
+  G.g.assign((size_t)D * D, cplx(0, 0));
+  for (int x = 0; x < D; ++x)
+    for (int y = 0; y < D; ++y) {
+      cplx s(0, 0);
+      for (int k = 0; k < D; ++k) s += V[x + (size_t)k * D] * std::exp(-cplx(dt_im, dt_re) * E[k]) * V[y + (size_t)k * D];
+      G.g[x + (size_t)y * D] = std::abs(s) < 1e-15 ? cplx(0, 0) : s;  // gateC.squeeze(1e-15)
+    }
+  return G;
+}
+
+// Vidal-form state: Gamma[s] (s = 0..N-1), lambda[b] for b = -1..N-1 (stored at b+1)
+struct TEBDState {
+  int N = 0;
+  std::vector<CBM> G;
+  std::vector<Diag> lam;
+  std::vector<ItoKey> ik;
+};
+// product state: Gamma[s] = (q_s, q_s + q(sigma_s); sigma_s) = [[1]], all lambdas [1]
+static TEBDState tebd_product(const std::vector<int>& local, const std::vector<ItoKey>& ik) {
+  TEBDState st;
+  st.N = (int)local.size();
+  st.ik = ik;
+  st.G.resize(st.N);
+  st.lam.resize(st.N + 1);
+  Q q = 0;
+  st.lam[0][q] = {1.0};
+  for (int s = 0; s < st.N; ++s) {
+    const Q q1 = q + ik[s][local[s]];
+    CMat one(1, 1);
+    one(0, 0) = cplx(1.0, 0.0);
+    st.G[s][K1(q, q1, (uint32_t)local[s])] = one;
+    st.lam[s + 1][q1] = {1.0};
+    q = q1;
+  }
+  return st;
+}
+// applyGate (MPSfunctions.hpp:1492-1548) on bond (site, site+1)
+static std::pair<double, int> apply_gate(TEBDState& st, int site, const Gate& gate, int chimax, bool doTrunc,
+                                         double tr_weight, bool normalize) {
+  const Diag &ll = st.lam[site], &lc = st.lam[site + 1], &lr = st.lam[site + 2];
+  CBM Ml = lam_scale(lc, lam_scale(ll, st.G[site], true, false), false, false);
+  CBM Mr = lam_scale(lr, st.G[site + 1], false, false);
+  CBM Ain = ctheta(Ml, Mr), th;
+  for (auto& a : Ain) {
+    const uint32_t i1 = a.first.p0, i2 = a.first.p1;
+    for (int o2 = 0; o2 < gate.d2; ++o2)
+      for (int o1 = 0; o1 < gate.d1; ++o1) {
+        const cplx g = gate.at(o1, o2, (int)i1, (int)i2);
+        if (g == cplx(0, 0)) continue;
+        Key k = K2(a.first.q0, a.first.q1, (uint32_t)o1, (uint32_t)o2);
+        CMat t = a.second;
+        for (auto& v : t.d) v *= g;
+        auto y = th.find(k);
+        if (y != th.end())
+          for (size_t i = 0; i < t.d.size(); ++i) t.d[i] += y->second.d[i];
+        th[k] = t;
+      }
+  }
+  csqueeze(th, 1e-15);
+  CSplitOut o = csplit2(th, st.ik[site], st.ik[site + 1], chimax, doTrunc, tr_weight, normalize);
+  csqueeze(o.U, 1e-15);
+  csqueeze(o.Vt, 1e-15);
+  st.G[site] = lam_scale(ll, o.U, true, true);
+  st.G[site + 1] = lam_scale(lr, o.Vt, false, true);
+  st.lam[site + 1] = o.lam;
+  return std::make_pair(o.tw, o.chi);
+}
+// doTimeSlice: bonds start, start+2, ... (container.hpp:1195-1233)
+static void tebd_slice(TEBDState& st, const std::vector<Gate>& gates, int start, int chimax, bool doTrunc,
+                       double tr_weight, bool normalize, std::vector<double>* tw) {
+  for (int site = start; site < st.N - 1; site += 2) {
+    auto r = apply_gate(st, site, gates[site], chimax, doTrunc, tr_weight, normalize);
+    if (tw) (*tw)[site] = r.first;
+  }
+}
+// second-order Trotter (TEBDengine::simulate "second", without intermediate measurements):
+// odd/2, then steps x (even, odd) with the last odd step halved
+static void tebd_second_order(TEBDState& st, const std::vector<MPOMat>& mpo, int steps, double dt, int chimax,
+                              bool doTrunc, double tr_weight, bool normalize) {
+  std::vector<Gate> full, half;
+  for (int s = 0; s + 1 < st.N; ++s) {
+    const int d1 = (int)st.ik[s].size(), d2 = (int)st.ik[s + 1].size();
+    full.push_back(nn_gate(mpo[s], mpo[s + 1], s, st.N, dt, 0.0, d1, d2));
+    half.push_back(nn_gate(mpo[s], mpo[s + 1], s, st.N, dt / 2, 0.0, d1, d2));
+  }
+  tebd_slice(st, half, 1, chimax, doTrunc, tr_weight, normalize, nullptr);
+  for (int step = 1; step <= steps; ++step) {
+    tebd_slice(st, full, 0, chimax, doTrunc, tr_weight, normalize, nullptr);
+    tebd_slice(st, step < steps ? full : half, 1, chimax, doTrunc, tr_weight, normalize, nullptr);
+  }
+}
+// SparseLocalOperator::measure for a diagonal operator diag(op) on lambda Gamma lambda
+static double tebd_measure_diag(const TEBDState& st, int site, const std::vector<double>& op) {
+  CBM M = lam_scale(st.lam[site + 1], lam_scale(st.lam[site], st.G[site], true, false), false, false);
+  double mean = 0;
+  for (auto& b : M) {
+    double nrm = 0;
+    for (auto& v : b.second.d) nrm += std::norm(v);
+    mean += op[b.first.p0] * nrm;
+  }
+  return mean;
+}
+
 struct orc_bm_t { BM m; int nphys; };
 struct orc_mpo_t { MPOMat w; };
 struct orc_dmrg_t { DMRG g; };
@@ -922,9 +1312,11 @@ int orc_init(const char* path) {
   p_ddot = (ddot_t)sym(h, "scipy_ddot_", "ddot_");
   p_dgesvd = (dgesvd_t)sym(h, "scipy_dgesvd_", "dgesvd_");
   p_dstev = (dstev_t)sym(h, "scipy_dstev_", "dstev_");
+  p_zgemm = (zgemm_t)sym(h, "scipy_zgemm_", "zgemm_");
+  p_zgesvd = (zgesvd_t)sym(h, "scipy_zgesvd_", "zgesvd_");
   setthreads_t st = (setthreads_t)sym(h, "scipy_openblas_set_num_threads", "openblas_set_num_threads");
   if (st) st(1);  // OpenMP parallelism is over charge sectors, as in the reference
-  if (!p_dgemm || !p_ddot || !p_dgesvd || !p_dstev) return 2;
+  if (!p_dgemm || !p_ddot || !p_dgesvd || !p_dstev || !p_zgemm || !p_zgesvd) return 2;
   return 0;
 }
 
@@ -1187,5 +1579,53 @@ double orc_dmrg_measure(void* ee, int nthreads) {
   return mpo_measure(g.mps.s, g.mpo, g.mps.ik, nthreads);
 }
 void orc_dmrg_free(void* e) { delete (orc_dmrg_t*)e; }
+
+
+// ---- TEBD: product state, second-order evolution, diagonal local measurement, export
+struct orc_tebd_t { TEBDState st; std::vector<MPOMat> mpo; };
+void* orc_tebd_new(int N, const int* local, void* const* W, const uint64_t* ik, const int* d) {
+  orc_tebd_t* t = new orc_tebd_t;
+  std::vector<ItoKey> iks;
+  size_t off = 0;
+  for (int s = 0; s < N; ++s) {
+    iks.push_back(ItoKey(ik + off, ik + off + d[s]));
+    off += d[s];
+    t->mpo.push_back(((orc_mpo_t*)W[s])->w);
+  }
+  t->st = tebd_product(std::vector<int>(local, local + N), iks);
+  return t;
+}
+void orc_tebd_second_order(void* tt, int steps, double dt, int chimax, int doTrunc, double tr_weight, int normalize) {
+  orc_tebd_t* t = (orc_tebd_t*)tt;
+  tebd_second_order(t->st, t->mpo, steps, dt, chimax, doTrunc != 0, tr_weight, normalize != 0);
+}
+double orc_tebd_measure_diag(void* tt, int site, const double* op, int d) {
+  return tebd_measure_diag(((orc_tebd_t*)tt)->st, site, std::vector<double>(op, op + d));
+}
+// complex block export of Gamma[site]: sizes via orc_tebd_gamma_info, data interleaved (re, im)
+int orc_tebd_gamma_info(void* tt, int site, long* nelem) {
+  const CBM& g = ((orc_tebd_t*)tt)->st.G[site];
+  long n = 0;
+  for (auto& b : g) n += (long)b.second.d.size();
+  *nelem = n;
+  return (int)g.size();
+}
+void orc_tebd_gamma_export(void* tt, int site, uint64_t* q, uint32_t* p, int32_t* rows, int32_t* cols, double* data) {
+  const CBM& g = ((orc_tebd_t*)tt)->st.G[site];
+  size_t i = 0, off = 0;
+  for (auto& b : g) {
+    q[2 * i] = b.first.q0; q[2 * i + 1] = b.first.q1; p[i] = b.first.p0;
+    rows[i] = b.second.r; cols[i] = b.second.c;
+    for (auto& v : b.second.d) { data[off++] = v.real(); data[off++] = v.imag(); }
+    ++i;
+  }
+}
+void* orc_tebd_lambda(void* tt, int bond) { return wrap_diag(((orc_tebd_t*)tt)->st.lam[bond + 1]); }
+// the dense two-site gate (d1 d2 x d1 d2, column-major, index o1 + d1 o2), interleaved complex
+void orc_nn_gate(void* W1, void* W2, int site1, int N, double dt_re, double dt_im, int d1, int d2, double* out) {
+  Gate G = nn_gate(((orc_mpo_t*)W1)->w, ((orc_mpo_t*)W2)->w, site1, N, dt_re, dt_im, d1, d2);
+  for (size_t i = 0; i < G.g.size(); ++i) { out[2 * i] = G.g[i].real(); out[2 * i + 1] = G.g[i].imag(); }
+}
+void orc_tebd_free(void* t) { delete (orc_tebd_t*)t; }
 
 }  // extern "C"

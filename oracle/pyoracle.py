@@ -107,6 +107,18 @@ def lib():
     L.orc_dmrg_measure.restype = f64
     L.orc_dmrg_measure.argtypes = [vp, i32]
     L.orc_dmrg_free.argtypes = [vp]
+    L.orc_tebd_new.restype = vp
+    L.orc_tebd_new.argtypes = [i32, vp, vp, vp, vp]
+    L.orc_tebd_second_order.argtypes = [vp, i32, f64, i32, i32, f64, i32]
+    L.orc_tebd_measure_diag.restype = f64
+    L.orc_tebd_measure_diag.argtypes = [vp, i32, vp, i32]
+    L.orc_tebd_gamma_info.restype = i32
+    L.orc_tebd_gamma_info.argtypes = [vp, i32, P(C.c_long)]
+    L.orc_tebd_gamma_export.argtypes = [vp, i32, vp, vp, vp, vp, vp]
+    L.orc_tebd_lambda.restype = vp
+    L.orc_tebd_lambda.argtypes = [vp, i32]
+    L.orc_nn_gate.argtypes = [vp, vp, i32, i32, f64, f64, i32, i32, vp]
+    L.orc_tebd_free.argtypes = [vp]
     rc = L.orc_init(openblas_path().encode())
     if rc != 0:
         raise RuntimeError(f"oracle: orc_init failed ({rc})")
@@ -399,5 +411,69 @@ class DMRG:
     def __del__(self):
         try:
             lib().orc_dmrg_free(self.h)
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ TEBD (complex FP64)
+def nn_gate(W1, W2, site1, N, dt, d1=2, d2=2):
+    """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
+    L = lib()
+    w1, w2 = mpo_to_handle(*W1), mpo_to_handle(*W2)
+    out = np.zeros(2 * (d1 * d2) ** 2)
+    dt_c = complex(dt)
+    L.orc_nn_gate(w1, w2, int(site1), int(N), dt_c.real, dt_c.imag, d1, d2, _ptr(out))
+    L.orc_mpo_free(w1)
+    L.orc_mpo_free(w2)
+    g = out[0::2] + 1j * out[1::2]
+    return g.reshape((d1 * d2, d1 * d2), order="F")
+
+
+class TEBD:
+    """TEBDengine from a product state (Vidal form), second-order Trotter evolution."""
+
+    def __init__(self, local_state, W, itokeys):
+        L = lib()
+        self.N = len(local_state)
+        loc = np.ascontiguousarray(local_state, np.int32)
+        ws = [mpo_to_handle(*w) for w in W]
+        pw = (C.c_void_p * len(ws))(*ws)
+        flat, d = _ik_tables(itokeys)
+        self.h = L.orc_tebd_new(self.N, _ptr(loc), pw, _ptr(flat), _ptr(d))
+        for w in ws:
+            L.orc_mpo_free(w)
+
+    def second_order(self, steps, dt, chimax, doTrunc=False, tr_weight=1e-10, normalize=True):
+        lib().orc_tebd_second_order(self.h, int(steps), float(dt), int(chimax), int(doTrunc), float(tr_weight),
+                                    int(normalize))
+
+    def measure_diag(self, site, op_diag):
+        op = np.ascontiguousarray(op_diag, np.float64)
+        return lib().orc_tebd_measure_diag(self.h, int(site), _ptr(op), len(op))
+
+    def gamma(self, site):
+        L = lib()
+        ne = C.c_long()
+        n = L.orc_tebd_gamma_info(self.h, int(site), C.byref(ne))
+        q = np.zeros(2 * max(n, 1), np.uint64)
+        p = np.zeros(max(n, 1), np.uint32)
+        r = np.zeros(max(n, 1), np.int32)
+        c = np.zeros(max(n, 1), np.int32)
+        data = np.zeros(2 * max(ne.value, 1))
+        L.orc_tebd_gamma_export(self.h, int(site), _ptr(q), _ptr(p), _ptr(r), _ptr(c), _ptr(data))
+        z = data[0::2] + 1j * data[1::2]
+        out, off = {}, 0
+        for i in range(n):
+            rr, cc = int(r[i]), int(c[i])
+            out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[i]))] = z[off:off + rr * cc].reshape((rr, cc), order="F")
+            off += rr * cc
+        return out
+
+    def lam(self, bond):
+        return handle_to_bm(lib().orc_tebd_lambda(self.h, int(bond)))
+
+    def __del__(self):
+        try:
+            lib().orc_tebd_free(self.h)
         except Exception:
             pass

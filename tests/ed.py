@@ -168,3 +168,51 @@ def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
                     blk = out[oa:oa + na, s1, s2, ob:ob + nb]
                     res[(a, b, s1, s2)] = blk.copy()
     return res
+
+
+# --------------------------------------------------------------------------- dense TEBD reference
+def spin_ops():
+    sz = np.diag([-0.5, 0.5])
+    sp = np.array([[0.0, 0.0], [1.0, 0.0]])  # |up><down| with index 1 = up
+    return sz, sp, sp.T
+
+
+def bond_hamiltonian(Jz, Jxy, B1, B2, w1, w2):
+    """h_b = Jz SzSz + Jxy/2 (S+S- + S-S+) - w1 B1 Sz (x) 1 - w2 B2 1 (x) Sz, dense index o1 + 2*o2
+    (site 1 is the fast index, numpy kron(op_site2, op_site1))."""
+    sz, sp, sm = spin_ops()
+    one = np.eye(2)
+    h = Jz * np.kron(sz, sz) + 0.5 * Jxy * (np.kron(sm, sp) + np.kron(sp, sm))
+    h -= w1 * B1 * np.kron(one, sz) + w2 * B2 * np.kron(sz, one)
+    return h
+
+
+def apply_two_site(psi, gate, s, N):
+    """psi: full 2^N vector (site i <-> bit i, 1 = up); gate on sites (s, s+1), index o1 + 2*o2."""
+    t = psi.reshape((2,) * N, order="F")  # axis i = site i
+    g = gate.reshape((2, 2, 2, 2), order="F")  # (o1, o2, i1, i2)
+    t = np.moveaxis(t, (s, s + 1), (0, 1))
+    t = np.tensordot(g, t, axes=([2, 3], [0, 1]))
+    t = np.moveaxis(t, (0, 1), (s, s + 1))
+    return t.reshape(-1, order="F")
+
+
+def dense_tebd_second_order(local, gates_full, gates_half, steps):
+    N = len(local)
+    psi = np.zeros(2 ** N, complex)
+    psi[sum(int(v) << i for i, v in enumerate(local))] = 1.0
+    def slice_(gates, start):
+        nonlocal psi
+        for s in range(start, N - 1, 2):
+            psi = apply_two_site(psi, gates[s], s, N)
+    slice_(gates_half, 1)
+    for step in range(1, steps + 1):
+        slice_(gates_full, 0)
+        slice_(gates_full if step < steps else gates_half, 1)
+    return psi
+
+
+def sz_expect(psi, site, N):
+    idx = np.arange(2 ** N)
+    sz = np.where((idx >> site) & 1, 0.5, -0.5)
+    return float(np.real(np.vdot(psi, sz * psi)))
