@@ -217,6 +217,37 @@ mpsg_status mpsg_dmrg_measure_energy(mpsg_dmrg e, double* E);
 /* MPO::measure of the engine's state with another MPO (N tensors), e.g. a local operator
  * -- src/MPOTypes.hpp:990-1020. */
 mpsg_status mpsg_dmrg_measure_mpo(mpsg_dmrg e, const mpsg_mpo* W, double* out);
+
+/* ---------------------------------------------------------------- TEBD (complex FP64, Vidal form)
+ * TEBDengine (src/container.hpp:1195-1406) from a product state: Gamma tensors complex (planar on
+ * the device), lambdas real.  The two-site gate of bond b is exp(-i dt h_b) built from the MPO like
+ * MPO::getNNGate (src/MPOTypes.hpp:1090-1209); each bond update is applyGate
+ * (src/MPSfunctions.hpp:1492-1548) with the complex split (per-sector Jacobi SVD, complex FixPhase,
+ * the reference's truncation, dropDangling, squeeze(1e-15)). */
+typedef struct mpsg_tebd_s* mpsg_tebd;
+/* local_state[s]: index into ik[s] of site s (e.g. the Neel state s % 2). */
+mpsg_status mpsg_tebd_create(mpsg_ctx ctx, int32_t N, const int32_t* local_state, const mpsg_mpo* W,
+                             const mpsg_itokey* ik, mpsg_tebd* out);
+/* Second-order Trotter evolution (TEBDengine::simulate "second" without intermediate measurements):
+ * odd bonds dt/2, then steps x (even dt, odd dt) with the last odd step dt/2. */
+mpsg_status mpsg_tebd_second_order(mpsg_tebd e, int32_t steps, double dt, uint32_t chimax, int32_t doTrunc,
+                                   double tr_weight, int32_t normalize);
+/* SparseLocalOperator::measure (src/MPOTypes.hpp:532-563) of a diagonal operator on
+ * lambda(site-1) Gamma(site) lambda(site). */
+mpsg_status mpsg_tebd_measure_diag(mpsg_tebd e, int32_t site, const double* op_diag, int32_t d, double* out);
+/* lambda of bond b (b = -1 .. N-1) as an nphys = 0 tensor (n x 1 blocks keyed (q, q)). */
+mpsg_status mpsg_tebd_lambda(mpsg_tebd e, int32_t bond, mpsg_tensor* out);
+/* Gamma(site): block table and interleaved (re, im) column-major data in key order. */
+mpsg_status mpsg_tebd_gamma_shape(mpsg_tebd e, int32_t site, int32_t* nblocks, int64_t* nelem);
+mpsg_status mpsg_tebd_gamma_export(mpsg_tebd e, int32_t site, uint64_t* q, uint32_t* p, int32_t* rows,
+                                   int32_t* cols, double* data_interleaved);
+/* wall seconds of the evolution, of the split part, and bond updates applied. */
+mpsg_status mpsg_tebd_stats(mpsg_tebd e, double* seconds, double* split_seconds, int64_t* gates);
+void mpsg_tebd_destroy(mpsg_tebd e);
+/* MPO::getNNGate: dense (d1 d2) x (d1 d2) gate exp(-(dt_im + i dt_re) h_b), index o1 + d1*o2,
+ * column-major, interleaved complex -- src/MPOTypes.hpp:1090-1209. */
+mpsg_status mpsg_nn_gate(const mpsg_mpo* W1, const mpsg_mpo* W2, int32_t site1, int32_t N, double dt_re, double dt_im,
+                         int32_t d1, int32_t d2, double* out_interleaved);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
 
 #ifdef __cplusplus

@@ -7,6 +7,7 @@ Names and argument meaning follow MPSTools:
   TSLanzcosEngine      src/lanzcos.hpp:96-278
   DMRGengine           src/container.hpp:236-438
   computeOverlap       src/MPSfunctions.hpp:2066-2085
+  TEBDengine           src/container.hpp:1195-1406 (applyGate src/MPSfunctions.hpp:1492-1548)
   MPO::measure         src/MPOTypes.hpp:990-1020
 Block matrices are dicts keyed like TensorKeyType ((q0, q1, p0) or (q0, q1, p0, p1));
 lambdas are dicts {q: 1-D array}; MPO matrices are (terms, Dl, Dr) with
@@ -233,6 +234,82 @@ class DMRGengine:
     def close(self):
         if getattr(self, "h", None):
             self.ctx.L.mpsg_dmrg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def getNNGate(W1, W2, site1, N, dt, d1=2, d2=2):
+    """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
+    L = lib.load()
+    w1, w2 = MPOArg(W1), MPOArg(W2)
+    out = np.zeros(2 * (d1 * d2) ** 2)
+    dt = complex(dt)
+    check(L.mpsg_nn_gate(w1.ref(), w2.ref(), int(site1), int(N), dt.real, dt.imag, d1, d2,
+                         out.ctypes.data_as(C.c_void_p)))
+    return (out[0::2] + 1j * out[1::2]).reshape((d1 * d2, d1 * d2), order="F")
+
+
+class TEBDengine:
+    """TEBDengine from a product state on the GPU: complex Gamma tensors, real lambdas."""
+
+    def __init__(self, local_state, mpo, itokeys, ctx=None):
+        self.ctx = ctx or default_context()
+        self.N = len(local_state)
+        loc = np.ascontiguousarray(local_state, np.int32)
+        self._w, self._k = MPOArray(mpo), ItoKeyArray(itokeys)
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_tebd_create(self.ctx.h, self.N, loc.ctypes.data_as(C.c_void_p), self._w.ptr(),
+                                           self._k.ptr(), C.byref(h)))
+        self.h = h
+
+    def second_order(self, steps, dt, chimax, doTrunc=False, tr_weight=1e-10, normalize=True):
+        check(self.ctx.L.mpsg_tebd_second_order(self.h, int(steps), float(dt), int(chimax), int(doTrunc),
+                                                 float(tr_weight), int(normalize)))
+
+    def measure_diag(self, site, op_diag):
+        op = np.ascontiguousarray(op_diag, np.float64)
+        out = C.c_double()
+        check(self.ctx.L.mpsg_tebd_measure_diag(self.h, int(site), op.ctypes.data_as(C.c_void_p), len(op),
+                                                 C.byref(out)))
+        return out.value
+
+    def lam(self, bond):
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_tebd_lambda(self.h, int(bond), C.byref(h)))
+        return Tensor(self.ctx, h).to_dict()
+
+    def gamma(self, site):
+        n, ne = C.c_int32(), C.c_int64()
+        check(self.ctx.L.mpsg_tebd_gamma_shape(self.h, int(site), C.byref(n), C.byref(ne)))
+        nb = max(n.value, 1)
+        q = np.zeros(2 * nb, np.uint64)
+        p = np.zeros(nb, np.uint32)
+        r = np.zeros(nb, np.int32)
+        c = np.zeros(nb, np.int32)
+        data = np.zeros(2 * max(ne.value, 1))
+        ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+        check(self.ctx.L.mpsg_tebd_gamma_export(self.h, int(site), ptr(q), ptr(p), ptr(r), ptr(c), ptr(data)))
+        z = data[0::2] + 1j * data[1::2]
+        out, off = {}, 0
+        for i in range(n.value):
+            rr, cc = int(r[i]), int(c[i])
+            out[(int(q[2 * i]), int(q[2 * i + 1]), int(p[i]))] = z[off:off + rr * cc].reshape((rr, cc), order="F")
+            off += rr * cc
+        return out
+
+    def stats(self):
+        s, sp, g = C.c_double(), C.c_double(), C.c_int64()
+        check(self.ctx.L.mpsg_tebd_stats(self.h, C.byref(s), C.byref(sp), C.byref(g)))
+        return {"seconds": s.value, "split_seconds": sp.value, "gates": g.value}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.mpsg_tebd_destroy(self.h)
             self.h = None
 
     def __del__(self):

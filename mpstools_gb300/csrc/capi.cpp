@@ -3,16 +3,9 @@
 #include <cmath>
 #include <cstring>
 
-#include "host_ops.h"
+#include "capi_types.h"
 
 using namespace mpsg;
-
-struct mpsg_ctx_s {
-  std::shared_ptr<Ctx> c;  // tensors, plans and engines hold further references
-};
-struct mpsg_tensor_s {
-  TensorP t;
-};
 
 namespace mpsg {
 
@@ -241,32 +234,6 @@ struct mpsg_matvec_plan_s {
 };
 
 // ============================================================================ error plumbing
-#define API_BEGIN try {
-#define API_END                                  \
-  }                                              \
-  catch (const Err& ex) {                        \
-    g_last_error = ex.what();                    \
-    return (mpsg_status)ex.code;                 \
-  }                                              \
-  catch (const std::exception& ex) {             \
-    g_last_error = ex.what();                    \
-    return MPSG_ERR_ARG;                         \
-  }                                              \
-  return MPSG_OK;
-
-static Ctx* C(mpsg_ctx c) {
-  MPSG_CHECK(c && c->c, "null context");
-  return c->c.get();
-}
-static const Tensor& T(mpsg_tensor t) {
-  MPSG_CHECK(t && t->t, "null tensor");
-  return *t->t;
-}
-static mpsg_tensor wrap(TensorP t) {
-  mpsg_tensor w = new mpsg_tensor_s;
-  w->t = t;
-  return w;
-}
 
 extern "C" {
 
@@ -305,7 +272,7 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   C(ctx)->sync();
   API_END
 }
-int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count() + eig_launch_count(); }
+int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count(); }
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
   API_BEGIN
   MPSG_CHECK(method >= 0 && method <= 3,

@@ -186,6 +186,39 @@ struct TrsmRowsOp {  // rows [r0, r1) of X (ldx) <- X R^-1, R upper (ldr), k col
   const double* rdiag;
   int32_t k, ldx, ldr, r0, r1;
 };
+// ---- complex (TEBD) path (tebd_kernels.cu); planar blocks: re at p, im at p + plane offset
+struct CGatherOp {  // interleaved dst(i, j) = re(i, j) + i im(i, j); conj_trans: dst(j, i) = conj(...)
+  const double* re;
+  const double* im;
+  double2* dst;
+  int32_t rows, cols, lds, ldd, conj_trans;
+};
+struct CScatterOp {  // planar dst(i, j) = rs[i] cs[j] (conj_trans ? conj(src(j, i)) : src(i, j))
+  const double2* src;
+  double* re;
+  double* im;
+  const double* rs;
+  const double* cs;
+  int32_t rows, cols, lds, ldd, conj_trans;
+};
+struct CPhaseOp {  // complex FixPhase of one sector: U (m x k), V (n x k) with Vt = V^H
+  double2* U;
+  double2* V;
+  int32_t m, n, k, ldu, ldv;
+};
+struct CBlockOp {  // one planar block of n elements
+  const double* re;
+  const double* im;
+  int64_t n;
+};
+struct CMeasureOp {  // w * sum |x_ij|^2 ll_i^2 lr_j^2
+  const double* re;
+  const double* im;
+  const double* ll;
+  const double* lr;
+  int32_t rows, cols;
+  double w;
+};
 struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
   double* A;
   int32_t nc, n;
@@ -229,6 +262,13 @@ void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, in
                      double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s);
 void launch_fill(double* x, int64_t n, double v, cudaStream_t s);
 int64_t kernel_launch_count();
+int64_t tebd_launch_count();
+void launch_cgather(const CGatherOp* ops, int nops, cudaStream_t s);
+void launch_cscatter(const CScatterOp* ops, int nops, cudaStream_t s);
+void launch_cfixphase(const CPhaseOp* ops, int nops, cudaStream_t s);
+void launch_cblock_max2(const CBlockOp* ops, int nops, double* out, cudaStream_t s);
+void launch_cmeasure(const CMeasureOp* ops, int nops, double* out, cudaStream_t s);
+void launch_recip(double* dst, const double* src, int64_t n, cudaStream_t s);
 int64_t eig_launch_count();
 int sytrd_cluster_size(int n);
 int sytrd_max_n();

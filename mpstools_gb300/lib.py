@@ -68,6 +68,16 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_lambda.argtypes = [vp, i32, P(vp)]
     L.mpsg_dmrg_measure_energy.argtypes = [vp, P(f64)]
     L.mpsg_dmrg_measure_mpo.argtypes = [vp, vp, P(f64)]
+    L.mpsg_tebd_create.argtypes = [vp, i32, vp, vp, vp, P(vp)]
+    L.mpsg_tebd_second_order.argtypes = [vp, i32, f64, u32, i32, f64, i32]
+    L.mpsg_tebd_measure_diag.argtypes = [vp, i32, vp, i32, P(f64)]
+    L.mpsg_tebd_lambda.argtypes = [vp, i32, P(vp)]
+    L.mpsg_tebd_gamma_shape.argtypes = [vp, i32, P(i32), P(C.c_int64)]
+    L.mpsg_tebd_gamma_export.argtypes = [vp, i32, vp, vp, vp, vp, vp]
+    L.mpsg_tebd_stats.argtypes = [vp, P(f64), P(f64), P(C.c_int64)]
+    L.mpsg_tebd_destroy.argtypes = [vp]
+    L.mpsg_tebd_destroy.restype = None
+    L.mpsg_nn_gate.argtypes = [vp, vp, i32, i32, f64, f64, i32, i32, vp]
     L.mpsg_dmrg_destroy.argtypes = [vp]
     L.mpsg_dmrg_destroy.restype = None
     L.mpsg_dmrg_build_environments.argtypes = [vp, i32]
