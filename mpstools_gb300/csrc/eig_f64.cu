@@ -6,8 +6,8 @@
 //                    Householder vector is copied from its owner, the product p = tau G v and the
 //                    partial dot products are pushed through distributed shared memory; two
 //                    cluster barriers per column.
-//   2. k_tri_bisect  eigenvalues of T above the resolution floor by bisection on Sturm counts
-//                    (one thread per eigenvalue).
+//   2. k_tri_bisect  eigenvalues of T above the resolution floor by multisection on Sturm counts
+//                    (a group of 4 lanes per eigenvalue, 4 points per round).
 //   3. k_tri_invit   eigenvectors of T by inverse iteration with a partially pivoted tridiagonal LU,
 //                    one thread per eigenvalue; the caller re-orthonormalises them (CholeskyQR).
 //   4. k_ormtr       eigenvectors of G = Q z: the reflectors applied to blocks of 8 eigenvector
@@ -294,36 +294,53 @@ void launch_tri_bounds(const TriOp* ops, int nops, cudaStream_t s) {
   g_eig_launches.fetch_add(1);
 }
 
-// One thread per (sector, eigenvalue index in descending order).  Eigenvalues at or below the sector's
-// floor (floor_rel * lambda_max) are not computed: W holds -1 there.  W[k] = k-th largest eigenvalue.
-// (Four interleaved bisections per thread were measured 4x slower: a quarter of the warps, on a
-// quarter of the SMs.)
+// Multisection: LN lanes per (sector, eigenvalue index in descending order).  Each round the LN lanes
+// count at the LN interior points of an equal division of [a, b] into LN + 1 parts, and the interval
+// shrinks to the part that holds the eigenvalue (log2(LN + 1) bits per round, LN times the warps of
+// one-thread bisection, whose single dependent chain per thread left the SMs with one warp each).
+// Eigenvalues at or below the sector's floor (floor_rel * lambda_max) are not computed: W holds -1
+// there.  W[k] = k-th largest eigenvalue.  LN divides 32, so a lane group never spans two warps.
+constexpr int kBisectLanes = 4;
+
+template <int LN>
 __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restrict__ op_of, const int* __restrict__ k_of,
                              int nthreads) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nthreads) return;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / LN, g = gt % LN;
+  if (t >= nthreads) return;  // whole lane groups leave together (blockDim.x is a multiple of LN)
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << LN) - 1u) << (lane & ~(LN - 1));
   const TriOp o = ops[op_of[t]];
   const int k = k_of[t];  // 0 = largest
   const int n = o.n;
   const double lmax = o.meta[0];
   const double floor_v = o.floor_rel * fmax(lmax, 0.0);
   const int m = n - 1 - k;  // the eigenvalue with exactly m smaller ones
-  if (sturm_count(o.d, o.e2, n, floor_v) > m) {
-    o.W[k] = -1.0;
+  if (sturm_count(o.d, o.e2, n, floor_v) > m) {  // same answer in every lane of the group
+    if (g == 0) o.W[k] = -1.0;
     return;
   }
+  const double frac = (double)(g + 1) / (double)(LN + 1);
   double a = floor_v, b = o.meta[3];
   for (int it = 0; it < 100 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++it) {
-    const double x = 0.5 * (a + b);
-    if (sturm_count(o.d, o.e2, n, x) > m) b = x;
-    else a = x;
+    const double x = fma(b - a, frac, a);
+    const unsigned above = (__ballot_sync(gmask, sturm_count(o.d, o.e2, n, x) > m) >> (lane & ~(LN - 1))) &
+                           ((1u << LN) - 1u);
+    // the counts grow with x: the first point above the eigenvalue bounds it from above, the one
+    // before it from below
+    const int first = above ? __ffs(above) - 1 : LN;
+    const double xb = __shfl_sync(gmask, x, first < LN ? first : LN - 1, LN);
+    const double xa = __shfl_sync(gmask, x, first > 0 ? first - 1 : 0, LN);
+    if (first < LN) b = xb;
+    if (first > 0) a = xa;
   }
-  o.W[k] = 0.5 * (a + b);
+  if (g == 0) o.W[k] = 0.5 * (a + b);
 }
 void launch_tri_bisect(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double,
                        cudaStream_t s) {
   if (nthreads <= 0) return;
-  k_tri_bisect<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, nthreads);
+  const int64_t lanes = (int64_t)kBisectLanes * nthreads;
+  k_tri_bisect<kBisectLanes><<<(unsigned)((lanes + 127) / 128), 128, 0, s>>>(ops, op_of, k_of, nthreads);
   g_eig_launches.fetch_add(1);
 }
 

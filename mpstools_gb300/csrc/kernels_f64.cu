@@ -92,8 +92,9 @@ __global__ void __launch_bounds__(256) k_gemm_f64(const GProb* __restrict__ prob
 void launch_gemm_f64(const GProb* prob, const GSeg* seg, const GTile* tile, int ntiles, const Bases& bases,
                      cudaStream_t s) {
   if (ntiles <= 0) return;
-  // (an FP64 tensor-core variant with mma.sync m8n8k4 on the same 64 x 64 tiling measured 7.05 ms
-  // per chi=2048 matvec against 6.0 ms for this FMA kernel, and was dropped)
+  // (FP64 tensor-core variants with mma.sync m8n8k4 measured slower on this GPU: 7.05 ms per chi=2048
+  // matvec with 64 x 64 tiles on 8 warps, 6.97 ms with 32 x 32 warp tiles and double-buffered slices,
+  // against 6.0 ms for this FMA kernel)
   k_gemm_f64<<<ntiles, 256, 0, s>>>(prob, seg, tile, bases);
   LAUNCHED();
 }
