@@ -248,6 +248,32 @@ void mpsg_tebd_destroy(mpsg_tebd e);
  * column-major, interleaved complex -- src/MPOTypes.hpp:1090-1209. */
 mpsg_status mpsg_nn_gate(const mpsg_mpo* W1, const mpsg_mpo* W2, int32_t site1, int32_t N, double dt_re, double dt_im,
                          int32_t d1, int32_t d2, double* out_interleaved);
+/* The bond Hamiltonian h_b that MPO::getNNGate exponentiates (boundary-aware one-half weights of
+ * the on-site terms), real (d1 d2) x (d1 d2), index o1 + d1*o2, column-major
+ * -- src/MPOTypes.hpp:1090-1209. */
+mpsg_status mpsg_bond_hamiltonian(const mpsg_mpo* W1, const mpsg_mpo* W2, int32_t site1, int32_t N, int32_t d1,
+                                  int32_t d2, double* out);
+/* Tangent of the gate G = exp(-i dt h_b) along a real symmetric direction dh (d1 d2 square, same
+ * index): (dG/dtheta) G^H for h_b(theta) with dh_b/dtheta = dh, interleaved complex.  Used by the
+ * TEBD adjoint; no counterpart in the reference (MPO::getNNGate, src/MPOTypes.hpp:1090-1209, is the
+ * gate it differentiates). */
+mpsg_status mpsg_nn_gate_tangent(const mpsg_mpo* W1, const mpsg_mpo* W2, int32_t site1, int32_t N, double dt,
+                                 const double* dh, int32_t d1, int32_t d2, double* out_interleaved);
+/* TEBD adjoint (no counterpart in the reference, which has no gradients; the forward map is
+ * TEBDengine::simulate "second", src/container.hpp:1272-1406): runs the schedule of
+ * mpsg_tebd_second_order (normalised, same truncation) from the engine's current state, returns
+ * value = <O> of the diagonal operator obs_diag (d entries) on site obs_site at the end, and
+ * grad[b] = d value / d theta_b for one parameter per bond entering h_b with derivative dh_b:
+ * dh holds N-1 real matrices, bond b's of size (d_b d_{b+1})^2 (index o1 + d_b o2, column-major),
+ * one after another.  Truncation and renormalisation are not differentiated (exact when nothing is
+ * truncated).  The forward states are kept every checkpoint_every layers (<= 0: about the square
+ * root of the layer count) and recomputed segment by segment in the backward pass.  The engine ends
+ * at the evolved state, as after mpsg_tebd_second_order. */
+mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt, uint32_t chimax, int32_t doTrunc,
+                                           double tr_weight, int32_t obs_site, const double* obs_diag, int32_t d,
+                                           const double* dh, int32_t checkpoint_every, double* value, double* grad);
+/* wall seconds spent in mpsg_tebd_adjoint_second_order (forward, recomputation and backward). */
+mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
 
 #ifdef __cplusplus

@@ -254,6 +254,43 @@ def getNNGate(W1, W2, site1, N, dt, d1=2, d2=2):
     return (out[0::2] + 1j * out[1::2]).reshape((d1 * d2, d1 * d2), order="F")
 
 
+def bondHamiltonian(W1, W2, site1, N, d1=2, d2=2):
+    """The bond Hamiltonian h_b that MPO::getNNGate exponentiates: real (d1 d2 x d1 d2), index o1 + d1*o2."""
+    L = lib.load()
+    w1, w2 = MPOArg(W1), MPOArg(W2)
+    out = np.zeros((d1 * d2) ** 2)
+    check(L.mpsg_bond_hamiltonian(w1.ref(), w2.ref(), int(site1), int(N), d1, d2, out.ctypes.data_as(C.c_void_p)))
+    return out.reshape((d1 * d2, d1 * d2), order="F")
+
+
+def gateTangent(W1, W2, site1, N, dt, dh, d1=2, d2=2):
+    """(dG/dtheta) G^H for the gate G = exp(-i dt h_b) of getNNGate when dh_b/dtheta = dh (real symmetric)."""
+    L = lib.load()
+    w1, w2 = MPOArg(W1), MPOArg(W2)
+    dhf = np.asfortranarray(dh, np.float64)
+    out = np.zeros(2 * (d1 * d2) ** 2)
+    check(L.mpsg_nn_gate_tangent(w1.ref(), w2.ref(), int(site1), int(N), float(dt), dhf.ctypes.data_as(C.c_void_p),
+                                 d1, d2, out.ctypes.data_as(C.c_void_p)))
+    return (out[0::2] + 1j * out[1::2]).reshape((d1 * d2, d1 * d2), order="F")
+
+
+def couplingDerivatives(make_mpo, theta, itokeys):
+    """dh_b / dtheta_b for every bond from an MPO builder that is affine in its per-bond parameters:
+    make_mpo(theta) -> list of MPO tensors; the bond Hamiltonians are differenced at theta + e_b and
+    theta (exact for affine dependence up to rounding)."""
+    theta = np.asarray(theta, np.float64)
+    N = len(itokeys)
+    W0 = make_mpo(theta)
+    out = []
+    for b in range(N - 1):
+        d1, d2 = len(itokeys[b]), len(itokeys[b + 1])
+        tp = theta.copy()
+        tp[b] += 1.0
+        W1 = make_mpo(tp)
+        out.append(bondHamiltonian(W1[b], W1[b + 1], b, N, d1, d2) - bondHamiltonian(W0[b], W0[b + 1], b, N, d1, d2))
+    return out
+
+
 class TEBDengine:
     """TEBDengine from a product state on the GPU: complex Gamma tensors, real lambdas."""
 
@@ -270,6 +307,25 @@ class TEBDengine:
     def second_order(self, steps, dt, chimax, doTrunc=False, tr_weight=1e-10, normalize=True):
         check(self.ctx.L.mpsg_tebd_second_order(self.h, int(steps), float(dt), int(chimax), int(doTrunc),
                                                  float(tr_weight), int(normalize)))
+
+    def adjoint_second_order(self, steps, dt, chimax, obs_site, obs_diag, dh, doTrunc=True, tr_weight=1e-10,
+                             checkpoint_every=0):
+        """Second-order evolution (as second_order, normalised) and the gradient of <O_obs_site> at the end
+        with respect to one parameter per bond (dh[b] = d h_b / d theta_b).  Returns (value, grad)."""
+        op = np.ascontiguousarray(obs_diag, np.float64)
+        flat = np.concatenate([np.asarray(m, np.float64).reshape(-1, order="F") for m in dh])
+        grad = np.zeros(self.N - 1)
+        val = C.c_double()
+        check(self.ctx.L.mpsg_tebd_adjoint_second_order(
+            self.h, int(steps), float(dt), int(chimax), int(doTrunc), float(tr_weight), int(obs_site),
+            op.ctypes.data_as(C.c_void_p), len(op), flat.ctypes.data_as(C.c_void_p), int(checkpoint_every),
+            C.byref(val), grad.ctypes.data_as(C.c_void_p)))
+        return val.value, grad
+
+    def adjoint_seconds(self):
+        s = C.c_double()
+        check(self.ctx.L.mpsg_tebd_adjoint_seconds(self.h, C.byref(s)))
+        return s.value
 
     def measure_diag(self, site, op_diag):
         op = np.ascontiguousarray(op_diag, np.float64)

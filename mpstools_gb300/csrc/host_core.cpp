@@ -208,10 +208,14 @@ void GemmPlan::upload(Ctx* ctx) {
   this->ctx = ctx;
   keep = ctx->shared_from_this();
   std::vector<GTile> tiles;
-  for (size_t i = 0; i < hprob.size(); ++i)
+  prob_tile0.assign(hprob.size() + 1, 0);
+  for (size_t i = 0; i < hprob.size(); ++i) {
+    prob_tile0[i] = (int)tiles.size();
     for (int m0 = 0; m0 < hprob[i].M; m0 += 64)
       for (int n0 = 0; n0 < hprob[i].N; n0 += 64) tiles.push_back(GTile{(int32_t)i, m0, n0});
+  }
   ntiles = (int)tiles.size();
+  prob_tile0[hprob.size()] = ntiles;
   std::vector<GProb> p(hprob.size());
   std::vector<GSeg> s(hseg.size());
   for (size_t i = 0; i < hprob.size(); ++i) {
@@ -251,6 +255,14 @@ void GemmPlan::run(const double* const* bases) {
   Bases b;
   for (int i = 0; i < 8; ++i) b.p[i] = bases[i];
   launch_gemm_f64(dprob, dseg, dtile, ntiles, b, ctx->stream);
+}
+void GemmPlan::run_range(const double* const* bases, int p0, int p1) {
+  MPSG_CHECK(p0 >= 0 && p0 <= p1 && p1 <= (int)hprob.size(), "GEMM problem range outside the plan");
+  const int t0 = prob_tile0[p0], t1 = prob_tile0[p1];
+  if (t1 <= t0) return;
+  Bases b;
+  for (int i = 0; i < 8; ++i) b.p[i] = bases[i];
+  launch_gemm_f64(dprob, dseg, dtile + t0, t1 - t0, b, ctx->stream);
 }
 GemmPlan::~GemmPlan() {
   if (ctx) {

@@ -81,10 +81,13 @@ struct GemmPlan {
   GSeg* dseg = nullptr;
   GTile* dtile = nullptr;
   int ntiles = 0;
+  std::vector<int> prob_tile0;  // first tile of each problem (set by upload), then the tile count
   double flops = 0;
   void add_problem(int baseC, int64_t offC, int ldc, int M, int N, bool accumulate, const std::vector<GSegH>& segs);
+  int nprob() const { return (int)hprob.size(); }
   void upload(Ctx* ctx);
   void run(const double* const* bases);
+  void run_range(const double* const* bases, int p0, int p1);  // problems [p0, p1) only
   GemmPlan() {}
   GemmPlan(const GemmPlan&) = delete;
   ~GemmPlan();

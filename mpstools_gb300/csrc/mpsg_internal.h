@@ -219,6 +219,13 @@ struct CMeasureOp {  // w * sum |x_ij|^2 ll_i^2 lr_j^2
   int32_t rows, cols;
   double w;
 };
+struct CDotOp {  // Re sum conj(a) b = sum a_re b_re + a_im b_im over n elements
+  const double* ar;
+  const double* ai;
+  const double* br;
+  const double* bi;
+  int64_t n;
+};
 struct GramPad {  // diagonal entries [n, nc) of an nc x nc slot set to -1
   double* A;
   int32_t nc, n;
@@ -268,6 +275,7 @@ void launch_cscatter(const CScatterOp* ops, int nops, cudaStream_t s);
 void launch_cfixphase(const CPhaseOp* ops, int nops, cudaStream_t s);
 void launch_cblock_max2(const CBlockOp* ops, int nops, double* out, cudaStream_t s);
 void launch_cmeasure(const CMeasureOp* ops, int nops, double* out, cudaStream_t s);
+void launch_cdot_re(const CDotOp* ops, int nops, double* out, cudaStream_t s);
 void launch_recip(double* dst, const double* src, int64_t n, cudaStream_t s);
 int64_t eig_launch_count();
 int sytrd_cluster_size(int n);

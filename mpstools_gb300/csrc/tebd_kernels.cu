@@ -140,6 +140,27 @@ void launch_cmeasure(const CMeasureOp* ops, int nops, double* out, cudaStream_t 
   g_tebd_launches.fetch_add(1);
 }
 
+// out[b] = Re <a, b> = sum a_re b_re + a_im b_im over one block pair (mixed two-site expectation values
+// of the adjoint)
+__global__ void k_cdot_re(const CDotOp* __restrict__ ops, double* out) {
+  const CDotOp o = ops[blockIdx.x];
+  double acc = 0.0;
+  for (int64_t e = threadIdx.x; e < o.n; e += blockDim.x) acc = fma(o.ar[e], o.br[e], fma(o.ai[e], o.bi[e], acc));
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+void launch_cdot_re(const CDotOp* ops, int nops, double* out, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_cdot_re<<<nops, 256, 0, s>>>(ops, out);
+  g_tebd_launches.fetch_add(1);
+}
+
 // dst = 1 / src (0 where src is 0: padding)
 __global__ void k_recip(double* dst, const double* src, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

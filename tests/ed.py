@@ -216,3 +216,40 @@ def sz_expect(psi, site, N):
     idx = np.arange(2 ** N)
     sz = np.where((idx >> site) & 1, 0.5, -0.5)
     return float(np.real(np.vdot(psi, sz * psi)))
+
+
+def tebd_schedule(steps):
+    """Layers of the second-order schedule: (first bond, half step?)."""
+    out = [(1, True)]
+    for step in range(1, steps + 1):
+        out += [(0, False), (1, step == steps)]
+    return out
+
+
+def dense_tebd_adjoint(local, gates_full, gates_half, tang_full, tang_half, steps, obs_site):
+    """<Sz_obs_site> after the dense second-order evolution and its gradient by the adjoint formula
+    d<O>/dtheta_b = sum over layers holding b of 2 Re <chi_l| B_b |psi_l>, B_b = (dG_b/dtheta) G_b^H,
+    psi_l the state after layer l, chi_l = (later layers)^H O psi_T."""
+    N = len(local)
+    psi = np.zeros(2 ** N, complex)
+    psi[sum(int(v) << i for i, v in enumerate(local))] = 1.0
+    states = []
+    for start, half in tebd_schedule(steps):
+        gates = gates_half if half else gates_full
+        for s in range(start, N - 1, 2):
+            psi = apply_two_site(psi, gates[s], s, N)
+        states.append(psi)
+    idx = np.arange(2 ** N)
+    sz = np.where((idx >> obs_site) & 1, 0.5, -0.5)
+    value = float(np.real(np.vdot(psi, sz * psi)))
+    chi = sz * psi
+    grad = np.zeros(N - 1)
+    for li in range(len(states) - 1, -1, -1):
+        start, half = tebd_schedule(steps)[li]
+        tang = tang_half if half else tang_full
+        gates = gates_half if half else gates_full
+        for s in range(start, N - 1, 2):
+            grad[s] += 2.0 * np.real(np.vdot(chi, apply_two_site(states[li], tang[s], s, N)))
+        for s in range(start, N - 1, 2):
+            chi = apply_two_site(chi, gates[s].conj().T, s, N)
+    return value, grad
