@@ -28,6 +28,8 @@ Ctx::~Ctx() {
   for (auto h : whandles) cusolverDnDestroy(h);
   for (auto h : wblas) cublasDestroy(h);
   for (auto s : wstreams) cudaStreamDestroy(s);
+  for (auto e : wevents) cudaEventDestroy(e);
+  if (fork_event) cudaEventDestroy(fork_event);
   if (part) cudaFreeAsync(part, stream);
   cudaStreamSynchronize(stream);
   if (hscal) cudaFreeHost(hscal);
@@ -73,6 +75,23 @@ int Ctx::nworkers() {
     wblas.push_back(b);
   }
   return kWorkers;
+}
+void Ctx::fork(int n) {
+  MPSG_CHECK(n >= 0 && n <= nworkers(), "fork: more streams than workers");
+  if (!fork_event) MPSG_CUDA(cudaEventCreateWithFlags(&fork_event, cudaEventDisableTiming));
+  MPSG_CUDA(cudaEventRecord(fork_event, stream));
+  for (int i = 0; i < n; ++i) MPSG_CUDA(cudaStreamWaitEvent(wstreams[i], fork_event, 0));
+}
+void Ctx::join(int n) {
+  while ((int)wevents.size() < n) {
+    cudaEvent_t e;
+    MPSG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    wevents.push_back(e);
+  }
+  for (int i = 0; i < n; ++i) {
+    MPSG_CUDA(cudaEventRecord(wevents[i], wstreams[i]));
+    MPSG_CUDA(cudaStreamWaitEvent(stream, wevents[i], 0));
+  }
 }
 void Ctx::sync() { MPSG_CUDA(cudaStreamSynchronize(stream)); }
 

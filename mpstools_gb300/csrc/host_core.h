@@ -31,6 +31,12 @@ struct Ctx : std::enable_shared_from_this<Ctx> {
   std::vector<cusolverDnHandle_t> whandles;
   std::vector<cublasHandle_t> wblas;
   int nworkers();
+  // fork(n): worker streams 0..n-1 wait for the work queued on `stream` so far; join(n): `stream`
+  // waits for the work queued on them.  Independent launches between the two run concurrently.
+  std::vector<cudaEvent_t> wevents;
+  cudaEvent_t fork_event = nullptr;
+  void fork(int n);
+  void join(int n);
   void sync();
 };
 

@@ -837,14 +837,20 @@ struct SvdBatch {
         byCL[CL].push_back(SytrdOp{dG + offG[i], dd + s[i].offS, de + s[i].offS, dtau + s[i].offS, s[i].ns, s[i].ns});
         nmaxCL[CL] = std::max(nmaxCL[CL], s[i].ns);
       }
-      std::vector<void*> bufs;
-      for (auto& g : byCL) {
-        SytrdOp* d = (SytrdOp*)ctx->dmalloc(sizeof(SytrdOp) * g.second.size());
-        MPSG_CUDA(cudaMemcpyAsync(d, g.second.data(), sizeof(SytrdOp) * g.second.size(), cudaMemcpyHostToDevice, st));
-        launch_sytrd(d, (int)g.second.size(), g.first, nmaxCL[g.first], st);
-        bufs.push_back(d);
+      // the cluster sizes are independent launches: one worker stream each, largest clusters first
+      std::vector<std::pair<int, SytrdOp*>> bufs;
+      for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) {
+        SytrdOp* d = (SytrdOp*)ctx->dmalloc(sizeof(SytrdOp) * it->second.size());
+        MPSG_CUDA(cudaMemcpyAsync(d, it->second.data(), sizeof(SytrdOp) * it->second.size(), cudaMemcpyHostToDevice, st));
+        bufs.push_back({it->first, d});
       }
-      for (void* b : bufs) ctx->dfree(b);
+      const int nw = std::min<int>((int)bufs.size(), ctx->nworkers());
+      ctx->fork(nw);
+      for (size_t j = 0; j < bufs.size(); ++j)
+        launch_sytrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, nmaxCL[bufs[j].first],
+                     ctx->wstreams[j % nw]);
+      ctx->join(nw);
+      for (auto& b : bufs) ctx->dfree(b.second);
     }
     // 2./3. eigenvalues and eigenvectors of T, written in descending order into V's columns
     std::vector<TriOp> tops;
@@ -1176,7 +1182,15 @@ struct SvdBatch {
       g.run(bases);
       launch_chol_unit_zero_diag(dzd, (int)zd.size(), st);
       const int which = pass == 0 ? 0 : 1;
-      for (auto& c : byCL[which]) launch_chol(dch[which][c.first], (int)c.second.size(), c.first, kmaxCL[c.first], st);
+      {  // cluster sizes concurrently on worker streams, largest first
+        const int nw = std::min<int>((int)byCL[which].size(), ctx->nworkers());
+        ctx->fork(nw);
+        int j = 0;
+        for (auto it = byCL[which].rbegin(); it != byCL[which].rend(); ++it, ++j)
+          launch_chol(dch[which][it->first], (int)it->second.size(), it->first, kmaxCL[it->first],
+                      ctx->wstreams[j % nw]);
+        ctx->join(nw);
+      }
       const double* tb[8] = {X, dC, X, nullptr, nullptr, nullptr, nullptr, nullptr};
       for (int b = 0; b < nblk; ++b) {
         if (b > 0) upd[b]->run(tb);
