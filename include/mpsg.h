@@ -276,6 +276,30 @@ mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt
 mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
 
+/* ---------------------------------------------------------------- batched chains
+ * Many independent DMRGengine runs (src/container.hpp:292-438) in lockstep: every global step each
+ * chain performs its own next doStep, and the work of all chains goes through one launch per matvec
+ * stage, one batched split and one environment update per sweep direction (the chains form a
+ * block-diagonal direct sum: charges of chain i shifted by i << 32, MPO channels concatenated).
+ * Lanczos reductions, convergence, truncation and normalisation stay per chain.  No counterpart in
+ * the reference, which runs one chain per process; the per-chain results follow DMRGengine. */
+typedef struct mpsg_batch_s* mpsg_batch;
+/* chains: engines created with mpsg_dmrg_create on ctx (charges below 2^32, the same i_to_key at the
+ * sites that update together); they must outlive the batch and are updated in place. */
+mpsg_status mpsg_batch_create(mpsg_ctx ctx, int32_t nchains, const mpsg_dmrg* chains, mpsg_batch* out);
+/* matvec precision (FP64, a mixed mode or AUTO) and the Lanczos iteration cap of every chain. */
+mpsg_status mpsg_batch_set_options(mpsg_batch b, mpsg_prec prec, int32_t lanmax);
+/* DMRGengine::simulate of every chain with exactly `sweeps` sweeps (orthonormalize("rl"), then the
+ * sweeps, then the final doStep(0, -1)); energies[c] = the last step's energy of chain c.  Each
+ * chain's step records are available through mpsg_dmrg_steps. */
+mpsg_status mpsg_batch_simulate(mpsg_batch b, uint32_t sweeps, uint32_t chimax, int32_t doTrunc, double tr_weight,
+                                double delta, int32_t testenergy, double* energies);
+/* st[10]: global steps, chain steps, matvecs (one per lockstep iteration), matvec FLOPs (all chains),
+ * matvec kernel launches, Lanczos seconds, split seconds, environment seconds, wall seconds, device
+ * seconds of the sweeps. */
+mpsg_status mpsg_batch_stats(mpsg_batch b, double* st);
+void mpsg_batch_destroy(mpsg_batch b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -243,6 +243,44 @@ class DMRGengine:
             pass
 
 
+class DMRGbatch:
+    """Independent DMRGengine chains swept in lockstep, every step's work batched over the chains
+    (one launch per matvec stage for all chains).  The engines are updated in place."""
+
+    def __init__(self, engines, prec="fp64", lanmax=500, ctx=None):
+        self.ctx = ctx or engines[0].ctx
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e.h.value for e in self.engines])
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_batch_create(self.ctx.h, len(self.engines), arr, C.byref(h)))
+        self.h = h
+        check(self.ctx.L.mpsg_batch_set_options(self.h, _prec(prec), int(lanmax)))
+
+    def simulate(self, sweeps, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
+        out = np.zeros(len(self.engines))
+        check(self.ctx.L.mpsg_batch_simulate(self.h, int(sweeps), int(chimax), int(doTrunc), float(tr_weight),
+                                              float(delta), int(testenergy), out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def stats(self):
+        st = np.zeros(10)
+        check(self.ctx.L.mpsg_batch_stats(self.h, st.ctypes.data_as(C.c_void_p)))
+        keys = ["global_steps", "chain_steps", "matvecs", "matvec_flops", "matvec_launches", "lanczos_seconds",
+                "split_seconds", "env_seconds", "wall_seconds", "device_seconds"]
+        return dict(zip(keys, st.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.mpsg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def getNNGate(W1, W2, site1, N, dt, d1=2, d2=2):
     """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
     L = lib.load()

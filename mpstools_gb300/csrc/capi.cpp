@@ -4,231 +4,10 @@
 #include <cstring>
 
 #include "capi_types.h"
+#include "engine.h"
 
 using namespace mpsg;
 
-namespace mpsg {
-
-struct StepRec {
-  int site, dir, iters, chi;
-  double E, tw;
-};
-
-// DMRGengine (src/container.hpp:236-438) with all tensors resident on the device.
-struct Engine {
-  Ctx* ctx;
-  std::shared_ptr<Ctx> keep;
-  int N;
-  std::vector<TensorP> mps;
-  std::vector<MPO> mpo;
-  std::vector<ItoKey> ik;
-  std::map<int, TensorP> L, R, lam;
-  mpsg_prec prec = MPSG_PREC_FP64;
-  bool reorth = false;
-  int lanmax = 500;
-  std::vector<StepRec> steps;
-  LanczosStats lst;
-  double env_seconds = 0, split_seconds = 0, env_flops = 0, wall = 0;
-
-  static TensorP lmin(Ctx* ctx) {  // getLMin: (0,0;0) = [[1]]
-    uint64_t q[2] = {0, 0};
-    uint32_t p[1] = {0};
-    int32_t r[1] = {1}, c[1] = {1};
-    double d[1] = {1.0};
-    return tensor_from_host(ctx, 1, 1, q, p, r, c, d);
-  }
-  static TensorP rmax(Ctx* ctx, const Tensor& last) {  // getRMax: identity per right charge
-    std::map<Q, int> dims;
-    for (auto& b : last.b)
-      if (!dims.count(b.k.q1)) dims[b.k.q1] = b.c;
-    std::vector<uint64_t> q;
-    std::vector<uint32_t> p;
-    std::vector<int32_t> r, c;
-    std::vector<double> d;
-    for (auto& x : dims) {
-      q.push_back(x.first);
-      q.push_back(x.first);
-      p.push_back(0);
-      r.push_back(x.second);
-      c.push_back(x.second);
-      for (int j = 0; j < x.second; ++j)
-        for (int i = 0; i < x.second; ++i) d.push_back(i == j ? 1.0 : 0.0);
-    }
-    return tensor_from_host(ctx, 1, (int)dims.size(), q.data(), p.data(), r.data(), c.data(), d.data());
-  }
-
-  void prepare() {
-    // orthonormalize(mps, "rl") (src/MPSfunctions.hpp:1776-1784) with truncation of values <= 1e-16
-    for (int site = N - 1; site >= 0; --site) {
-      TensorP lamt;
-      if (site > 0) prepare_matrix_r(ctx, &mps[site - 1], mps[site], &lamt, 1e-16);
-      else prepare_matrix_r(ctx, nullptr, mps[0], &lamt, 1e-16);
-      lam[site - 1] = lamt;
-    }
-    auto t0 = std::chrono::steady_clock::now();
-    R.clear();
-    R[N] = rmax(ctx, *mps[N - 1]);
-    for (int s = N - 1; s >= 2; --s) R[s] = env_update(ctx, *R[s + 1], *mps[s], mpo[s], ik[s], 0, &env_flops);
-    ctx->sync();
-    env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    L.clear();
-    L[-1] = lmin(ctx);
-  }
-
-  void build_environments(int c) {
-    MPSG_CHECK(c >= 0 && c + 1 < N, "center out of range");
-    auto t0 = std::chrono::steady_clock::now();
-    L.clear();
-    L[-1] = lmin(ctx);
-    for (int s = 0; s < c; ++s) L[s] = env_update(ctx, *L[s - 1], *mps[s], mpo[s], ik[s], 1, &env_flops);
-    R.clear();
-    R[N] = rmax(ctx, *mps[N - 1]);
-    for (int s = N - 1; s >= c + 2; --s) R[s] = env_update(ctx, *R[s + 1], *mps[s], mpo[s], ik[s], 0, &env_flops);
-    ctx->sync();
-    env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
-
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  double step_device_seconds = 0;
-  int64_t nstep_calls = 0;
-
-  StepRec do_step(int site, int dir, int chimax, bool doTrunc, double tr_weight, double delta, bool testenergy) {
-    if (!ev0) {
-      MPSG_CUDA(cudaEventCreate(&ev0));
-      MPSG_CUDA(cudaEventCreate(&ev1));
-    }
-    MPSG_CUDA(cudaEventRecord(ev0, ctx->stream));
-    StepRec r = do_step_impl(site, dir, chimax, doTrunc, tr_weight, delta, testenergy);
-    MPSG_CUDA(cudaEventRecord(ev1, ctx->stream));
-    MPSG_CUDA(cudaEventSynchronize(ev1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, ev0, ev1);
-    step_device_seconds += ms * 1e-3;
-    ++nstep_calls;
-    return r;
-  }
-  ~Engine() {
-    if (ev0) cudaEventDestroy(ev0);
-    if (ev1) cudaEventDestroy(ev1);
-  }
-
-  StepRec do_step_impl(int site, int dir, int chimax, bool doTrunc, double tr_weight, double delta,
-                       bool testenergy) {
-    MPSG_CHECK(site >= 0 && site + 1 < N, "site out of range");
-    MPSG_CHECK(L.count(site - 1) && R.count(site + 2), "environments missing (call prepare first)");
-    const Tensor& Le = *L[site - 1];
-    const Tensor& Re = *R[site + 2];
-    // theta structure: blocks of BlockMatrix<2>(mps[site], mps[site+1]) and everything the matvec reaches
-    Layout s0;
-    {
-      std::map<Q, std::vector<int>> by_left;
-      for (int j = 0; j < (int)mps[site + 1]->b.size(); ++j) by_left[mps[site + 1]->b[j].k.q0].push_back(j);
-      for (auto& a : mps[site]->b) {
-        auto it = by_left.find(a.k.q1);
-        if (it == by_left.end()) continue;
-        for (int j : it->second) {
-          const Block& b = mps[site + 1]->b[j];
-          s0.add(K2(a.k.q0, b.k.q1, a.k.p0, b.k.p0), a.r, b.c);
-        }
-      }
-      s0.finalize();
-    }
-    Layout sx = theta_closure(Le, Re, s0, mpo[site], mpo[site + 1], ik[site], ik[site + 1]);
-    TensorP th = theta_form(ctx, *mps[site], *mps[site + 1], &sx);
-    TensorP psi = make_tensor(ctx, 2, sx, true);
-    LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], *th, *psi,
-                                    lanmax, delta, testenergy, reorth, (int)prec, &lst);
-    th.reset();
-    auto t0 = std::chrono::steady_clock::now();
-    SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
-    ctx->sync();
-    auto t1 = std::chrono::steady_clock::now();
-    split_seconds += std::chrono::duration<double>(t1 - t0).count();
-    psi.reset();
-    mps[site] = sp.U;
-    mps[site + 1] = sp.Vt;
-    lam[site] = sp.lam;
-    if (dir > 0) L[site] = env_update(ctx, *L[site - 1], *mps[site], mpo[site], ik[site], 1, &env_flops);
-    else R[site + 1] = env_update(ctx, *R[site + 2], *mps[site + 1], mpo[site + 1], ik[site + 1], -1, &env_flops);
-    ctx->sync();
-    env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
-    StepRec r{site, dir, lr.iterations, sp.chi, lr.E0, sp.tw};
-    steps.push_back(r);
-    return r;
-  }
-
-  double simulate(int maxsteps, double EnConv, int chimax, bool doTrunc, double tr_weight, double delta,
-                  bool testenergy) {
-    auto t0 = std::chrono::steady_clock::now();
-    prepare();
-    double globalE = 1e100;
-    StepRec out{};
-    int step = 0;
-    while (true) {
-      for (int site = 0; site < N - 2; ++site) out = do_step(site, 1, chimax, doTrunc, tr_weight, delta, testenergy);
-      for (int site = N - 2; site > 0; --site) out = do_step(site, -1, chimax, doTrunc, tr_weight, delta, testenergy);
-      ++step;
-      bool conv = std::fabs(globalE - out.E) < EnConv;
-      if (step >= maxsteps) conv = true;
-      globalE = out.E;
-      if (conv) break;
-    }
-    out = do_step(0, -1, chimax, doTrunc, tr_weight, delta, testenergy);
-    wall += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    return out.E;
-  }
-
-  double measure_energy() { return measure(mpo); }
-
-  // MPO::measure (src/MPOTypes.hpp:990-1020): left environments through the chain, then the sum of
-  // the diagonals of the charge-diagonal blocks.
-  double measure(const std::vector<MPO>& W) {
-    std::vector<const Tensor*> s;
-    for (auto& t : mps) s.push_back(t.get());
-    return mpo_expectation(ctx, s, W, ik);
-  }
-  static double mpo_expectation(Ctx* ctx, const std::vector<const Tensor*>& sites, const std::vector<MPO>& W,
-                                const std::vector<ItoKey>& ik) {
-    TensorP l = lmin(ctx);
-    for (size_t s = 0; s < sites.size(); ++s) l = env_update(ctx, *l, *sites[s], W[s], ik[s], 1, nullptr);
-    std::vector<double> h;
-    tensor_to_host(*l, h);
-    double e = 0;
-    int64_t off = 0;
-    for (auto& b : l->b) {
-      if (b.k.q0 == b.k.q1)
-        for (int i = 0; i < std::min(b.r, b.c); ++i) e += h[off + i + (int64_t)i * b.r];
-      off += (int64_t)b.r * b.c;
-    }
-    return e;
-  }
-  // computeOverlap(a, b) (src/MPSfunctions.hpp:2066-2085): identity MPO layers with a lower and b upper;
-  // the value is entry (0,0) of the first block of the last environment (0 if there is none).
-  static double overlap(Ctx* ctx, const std::vector<const Tensor*>& a, const std::vector<const Tensor*>& b,
-                        const std::vector<ItoKey>& ik) {
-    TensorP l = lmin(ctx);
-    for (size_t s = 0; s < a.size(); ++s) {
-      MPO id;
-      id.Dl = id.Dr = 1;
-      MPOEntry en;
-      en.wl = en.wr = 0;
-      for (uint32_t i = 0; i < (uint32_t)ik[s].size(); ++i) en.ops.push_back(OpEl{i, i, 1.0});
-      id.e.push_back(en);
-      l = env_update(ctx, *l, *a[s], id, ik[s], 1, nullptr, b[s]);
-    }
-    if (l->b.empty()) return 0.0;
-    double v = 0;
-    MPSG_CUDA(cudaMemcpyAsync(&v, l->d + l->b[0].off, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->sync();
-    return v;
-  }
-};
-
-}  // namespace mpsg
-
-struct mpsg_dmrg_s {
-  Engine* e = nullptr;
-};
 struct mpsg_matvec_plan_s {
   std::unique_ptr<MatvecPlan> p;
 };

@@ -1281,7 +1281,8 @@ struct SvdBatch {
 
 // ============================================================================ split
 SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
-                   double tr_weight, bool normalize, int absorb) {
+                   double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
+                   const std::vector<int>* seg_absorb) {
   struct SecInfo {
     std::map<uint32_t, std::pair<int, int>> rx, ry;  // index -> (start, size)
     std::vector<int> blocks;
@@ -1320,24 +1321,54 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   }
   run_copyops(ctx, gops);
   sv.run(ctx->svd_method);
-  // global truncation
+  // global truncation; with segments (a direct sum of independent chains, chain c holding the
+  // centre charges in [seg_q0[c], seg_q0[c + 1])) one truncation per chain over its own sectors
+  const int nseg = seg_q0 ? (int)seg_q0->size() : 1;
+  std::vector<int> seg_of_sec(qcs.size(), 0), s0(nseg + 1, (int)qcs.size());
+  if (seg_q0) {
+    for (size_t si = 0; si < qcs.size(); ++si) {
+      const int c = (int)(std::upper_bound(seg_q0->begin(), seg_q0->end(), qcs[si]) - seg_q0->begin()) - 1;
+      MPSG_CHECK(c >= 0, "centre charge below the first segment");
+      MPSG_CHECK(si == 0 || c >= seg_of_sec[si - 1], "segments out of charge order");
+      seg_of_sec[si] = c;
+    }
+  }
+  for (int si = (int)qcs.size() - 1; si >= 0; --si) s0[seg_of_sec[si]] = si;
+  for (int c = nseg - 1; c >= 0; --c) s0[c] = std::min(s0[c], s0[c + 1]);
   std::vector<int32_t> sec_of(sv.nS);
   for (size_t si = 0; si < qcs.size(); ++si)
-    for (int j = 0; j < sv.s[si].k; ++j) sec_of[sv.s[si].offS + j] = (int32_t)si;
+    for (int j = 0; j < sv.s[si].k; ++j) sec_of[sv.s[si].offS + j] = (int32_t)si - s0[seg_of_sec[si]];
   const int nS = (int)sv.nS;
-  int32_t* dsec = (int32_t*)ctx->dmalloc(sizeof(int32_t) * std::max(nS, 1) * 3 + sizeof(int32_t) * (qcs.size() + 1));
+  int32_t* dsec = (int32_t*)ctx->dmalloc(sizeof(int32_t) * std::max(nS, 1) * 3 + sizeof(int32_t) * (qcs.size() + 1) +
+                                         sizeof(double) * 3 * (nseg + 1));
   int32_t* drank = dsec + std::max(nS, 1);
   int32_t* dcnt = drank + 2 * std::max(nS, 1);
-  double* dout3 = ctx->part + kRedBlocks;
+  double* dout3 = (double*)(((uintptr_t)(dcnt + qcs.size() + 1) + 7) & ~(uintptr_t)7);
   if (nS) MPSG_CUDA(cudaMemcpyAsync(dsec, sec_of.data(), sizeof(int32_t) * nS, cudaMemcpyHostToDevice, ctx->stream));
-  launch_truncate(sv.dS, nS, dsec, (int)qcs.size(), chimax, doTrunc ? 1 : 0, tr_weight, drank, dcnt, dout3, ctx->stream);
+  MPSG_CUDA(cudaMemsetAsync(dout3, 0, sizeof(double) * 3 * nseg, ctx->stream));
+  for (int c = 0; c < nseg; ++c) {
+    const int a = s0[c], b = s0[c + 1];
+    if (a >= b) continue;
+    const int v0 = (int)sv.s[a].offS, v1 = (int)(sv.s[b - 1].offS + sv.s[b - 1].k);
+    launch_truncate(sv.dS + v0, v1 - v0, dsec + v0, b - a, chimax, doTrunc ? 1 : 0, tr_weight, drank + 2 * v0,
+                    dcnt + a, dout3 + 3 * c, ctx->stream);
+  }
   std::vector<int32_t> counts(qcs.size() + 1);
+  std::vector<double> out3(3 * nseg);
   MPSG_CUDA(cudaMemcpyAsync(counts.data(), dcnt, sizeof(int32_t) * qcs.size(), cudaMemcpyDeviceToHost, ctx->stream));
-  MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dout3, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+  MPSG_CUDA(cudaMemcpyAsync(out3.data(), dout3, sizeof(double) * 3 * nseg, cudaMemcpyDeviceToHost, ctx->stream));
   sv.check_info();  // syncs
-  const double tw = ctx->hscal[0];
-  const int chi = (int)ctx->hscal[1];
-  const double inv_norm = normalize ? ctx->hscal[2] : 1.0;
+  std::vector<double> inv_norm_seg(nseg, 1.0);
+  SplitResult R;
+  R.tw_seg.resize(nseg);
+  R.chi_seg.resize(nseg);
+  for (int c = 0; c < nseg; ++c) {
+    R.tw_seg[c] = out3[3 * c];
+    R.chi_seg[c] = (int)out3[3 * c + 1];
+    if (normalize) inv_norm_seg[c] = out3[3 * c + 2];
+  }
+  const double tw = R.tw_seg[0];
+  const int chi = R.chi_seg[0];
   ctx->dfree(dsec);
   // result layouts (dropDangling: sectors without kept values vanish, blocks cut to the kept count)
   Layout lu, lv, ll;
@@ -1353,7 +1384,6 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   lu.finalize();
   lv.finalize();
   ll.finalize();
-  SplitResult R;
   R.U = make_tensor(ctx, 1, lu, false);
   R.Vt = make_tensor(ctx, 1, lv, false);
   R.lam = make_tensor(ctx, 0, ll, true);
@@ -1365,6 +1395,8 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
     if (c <= 0) continue;
     const Q qc = qcs[si];
     SecInfo& s = secs[qc];
+    const double inv_norm = inv_norm_seg[seg_of_sec[si]];
+    const int ab = seg_absorb ? seg_absorb->at(seg_of_sec[si]) : absorb;
     int ldq, ldp;
     double* Qm = sv.Qp((int)si, &ldq);
     double* Pm = sv.Pp((int)si, &ldp);
@@ -1375,13 +1407,13 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
       o.src = Qm + r.second.first;
       o.dst = R.U->d + R.U->b[ob].off;
       o.rs = nullptr;
-      o.cs = absorb < 0 ? Sv : nullptr;
+      o.cs = ab < 0 ? Sv : nullptr;
       o.rows = r.second.second;
       o.cols = c;
       o.lds = ldq;
       o.ldd = r.second.second;
       o.trans = 0;
-      o.scale = absorb < 0 ? inv_norm : 1.0;
+      o.scale = ab < 0 ? inv_norm : 1.0;
       ops.push_back(o);
     }
     for (auto& r : s.ry) {
@@ -1389,14 +1421,14 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
       CopyOp o;
       o.src = Pm + r.second.first;
       o.dst = R.Vt->d + R.Vt->b[ob].off;
-      o.rs = absorb > 0 ? Sv : nullptr;
+      o.rs = ab > 0 ? Sv : nullptr;
       o.cs = nullptr;
       o.rows = c;
       o.cols = r.second.second;
       o.lds = ldp;
       o.ldd = c;
       o.trans = 1;
-      o.scale = absorb > 0 ? inv_norm : 1.0;
+      o.scale = ab > 0 ? inv_norm : 1.0;
       ops.push_back(o);
     }
     const int ol = R.lam->find(K1(qc, qc, 0));
@@ -1653,7 +1685,7 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
 
 // Relative energy-change floor of the Lanczos energy test per matvec precision (FP32 accumulation
 // bounds the hi/lo modes; single-product modes are limited by the 10 / 7 bit operands).
-static double prec_tol(int prec) {
+double prec_tol(int prec) {
   switch (prec) {
     case MPSG_PREC_TF32X3: return 1e-11;
     case MPSG_PREC_BF16X3: return 1e-9;
@@ -1662,7 +1694,7 @@ static double prec_tol(int prec) {
     default: return 0.0;
   }
 }
-static double prec_stall(int prec) {
+double prec_stall(int prec) {
   switch (prec) {
     case MPSG_PREC_TF32X3: return 1e-9;
     case MPSG_PREC_BF16X3: return 1e-7;

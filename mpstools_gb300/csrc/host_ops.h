@@ -116,10 +116,15 @@ struct SplitResult {
   TensorP U, Vt, lam;
   double tw = 0;
   int chi = 0;
+  std::vector<double> tw_seg;  // per segment (one entry without segments)
+  std::vector<int> chi_seg;
 };
-// absorb: 0 none, +1 lambda into Vt (rows), -1 lambda into U (columns)
+// absorb: 0 none, +1 lambda into Vt (rows), -1 lambda into U (columns).  seg_q0 (optional, ascending):
+// th is a direct sum of independent chains, chain c holding the centre charges from seg_q0[c] up to
+// the next entry; truncation, truncated weight, kept count and normalisation are then per chain.
 SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
-                   double tr_weight, bool normalize, int absorb);
+                   double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0 = nullptr,
+                   const std::vector<int>* seg_absorb = nullptr);  // per-segment absorb
 
 // prepareMatrix(BL1, lambda, BL2, "r", multiply=true, truncate=true, delta): right-orthonormalise BL2,
 // multiply U*D into BL1 (BL1 may be null at the left edge).
@@ -140,6 +145,9 @@ struct LanczosResult {
 // The energy test runs every ndiag iterations (reference: 5) and passes when
 // |E - E_prev| < max(delta, tol_rel*|E|); stall_rel > 0 also stops once |E - E_prev| is below
 // stall_rel*|E| and stopped shrinking (the noise floor of a low-precision matvec).
+// energy-test tolerance and stall level of the Lanczos for a matvec precision (0 for FP64)
+double prec_tol(int prec);
+double prec_stall(int prec);
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
                       double stall_rel = 0.0);

@@ -431,8 +431,8 @@ __device__ int sturm_count_nodiv(const double* a, const double* b2, int n, doubl
   return c;
 }
 
-__global__ void k_tri_lowest(const double* __restrict__ a_g, const double* __restrict__ b, int n, double* E0,
-                             double* z) {
+__device__ void tri_lowest_dev(const double* __restrict__ a_g, const double* __restrict__ b, int n, double* E0,
+                               double* z) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x;
   double* a = sm + 6 * n;   // diagonal and squared off-diagonal, staged for the Sturm counts
@@ -544,10 +544,31 @@ __global__ void k_tri_lowest(const double* __restrict__ a_g, const double* __res
   }
   for (int i = 0; i < n; ++i) z[i] = x[i];
 }
+__global__ void k_tri_lowest(const double* __restrict__ a_g, const double* __restrict__ b, int n, double* E0,
+                             double* z) {
+  tri_lowest_dev(a_g, b, n, E0, z);
+}
 void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s) {
   if (n <= 0) return;
   const size_t sh = (size_t)n * 8 * sizeof(double) + 16;
   k_tri_lowest<<<1, 32, sh, s>>>(alpha, beta, n, E0, z);
+  LAUNCHED();
+}
+// One block per chain c: the lowest eigenpair of chain c's tridiagonal (alpha / beta at c * stride,
+// n_of[c] rows; chains with n_of[c] <= 0 are skipped); E0 at c * estride, z at c * stride.
+__global__ void k_tri_lowest_seg(const double* __restrict__ alpha, const double* __restrict__ beta,
+                                 const int* __restrict__ n_of, int stride, double* E0, int estride, double* z) {
+  const int c = blockIdx.x;
+  const int n = n_of[c];
+  if (n <= 0) return;
+  tri_lowest_dev(alpha + (int64_t)c * stride, beta + (int64_t)c * stride, n, E0 + (int64_t)c * estride,
+                 z ? z + (int64_t)c * stride : nullptr);
+}
+void launch_tri_lowest_seg(const double* alpha, const double* beta, const int* n_of, int nchains, int nmax, int stride,
+                           double* E0, int estride, double* z, cudaStream_t s) {
+  if (nchains <= 0 || nmax <= 0) return;
+  const size_t sh = (size_t)nmax * 8 * sizeof(double) + 16;
+  k_tri_lowest_seg<<<nchains, 32, sh, s>>>(alpha, beta, n_of, stride, E0, estride, z);
   LAUNCHED();
 }
 

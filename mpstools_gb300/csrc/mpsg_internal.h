@@ -264,6 +264,21 @@ void launch_project(const double* const* V, int nv, const double* x, int64_t n, 
                     cudaStream_t s);
 // lowest eigenpair of the symmetric tridiagonal (alpha[0..n), offdiag beta[1..n)); z may be null
 void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s);
+void launch_tri_lowest_seg(const double* alpha, const double* beta, const int* n_of, int nchains, int nmax, int stride,
+                           double* E0, int estride, double* z, cudaStream_t s);
+// segmented Lanczos vector operations (batch_kernels.cu): chain c owns [segoff[c], segoff[c + 1]),
+// its scalars sit at c * stride; `part` holds seg_chunks() doubles per chain
+int seg_chunks();
+int64_t batch_launch_count();
+void launch_sdot(const double* x, const double* y, const int64_t* segoff, int nseg, double* part, double* out,
+                 int ostride, cudaStream_t s);
+void launch_sscale_by_norm(double* x, const int64_t* segoff, int nseg, const double* norm2, int stride, double delta,
+                           double* beta_out, cudaStream_t s);
+void launch_saxpy3(double* out, const double* w, const double* v, const double* vprev, const double* alpha,
+                   const double* beta, int stride, const int64_t* segoff, int nseg, double* part, double* norm2_out,
+                   cudaStream_t s);
+void launch_scombine(double* y, const double* const* V, const int* nv_of, const double* z, int zstride,
+                     const int64_t* segoff, int nseg, cudaStream_t s);
 // global truncation over concatenated singular values (see kernels.cu)
 void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, int chimax, int doTrunc,
                      double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s);
