@@ -73,6 +73,9 @@ mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
 mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
+/* Number of splits on the library's own density-matrix eigensolver (svd method 3) that were redone
+ * on the exact Jacobi route because their singular vectors were too dependent for CholeskyQR. */
+int64_t mpsg_split_fallbacks(void);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
  * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default, exact),
  * 1, 2, 3 = eigen-decomposition of each sector's reduced density matrix G = M^T M (FP64) with the

@@ -51,7 +51,10 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   C(ctx)->sync();
   API_END
 }
-int64_t mpsg_ctx_kernel_launches(mpsg_ctx) { return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count(); }
+int64_t mpsg_ctx_kernel_launches(mpsg_ctx) {
+  return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count() + batch_launch_count();
+}
+int64_t mpsg_split_fallbacks(void) { return split_fallback_count(); }
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
   API_BEGIN
   MPSG_CHECK(method >= 0 && method <= 3,

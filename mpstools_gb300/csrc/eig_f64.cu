@@ -398,10 +398,43 @@ __device__ void tri_shift_solve(int n, double* x, const double* u0, const double
   for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0[i];
 }
 
-// One thread per eigenvalue: three inverse iterations from a deterministic pseudo-random start with
-// one LU of T - lambda I.  Vectors of eigenvalues closer than ~eps lambda_max are independent
-// combinations inside their cluster; the caller re-orthonormalises the eigenvector matrix
-// (CholeskyQR).  Z column k receives the vector of W[k]; columns below the floor are zero.
+// Eigenvectors of T by inverse iteration: three iterations from a deterministic pseudo-random start
+// with one LU of T - lambda I.  Eigenvalues closer than kClusterGap * tnorm to their predecessor
+// (descending order) form a cluster: the thread of the cluster's first eigenvalue computes all its
+// vectors one after another and orthogonalises each iterate against the cluster's earlier vectors
+// (modified Gram-Schmidt), as LAPACK's dstein does, so that (near-)degenerate eigenvalues do not
+// yield the same vector twice; the other threads of the cluster return.  The caller still
+// re-orthonormalises the eigenvector matrix (CholeskyQR).  Z column k receives the vector of W[k];
+// columns below the floor are zero.
+constexpr double kClusterGap = 1e-11;
+
+__device__ void invit_one(const TriOp& o, int k, double tnorm, double* z, double* base) {
+  const int n = o.n;
+  double *u0 = base, *u1 = base + n, *u2 = base + 2 * n, *mul = base + 3 * n;
+  unsigned char* piv = (unsigned char*)(base + 4 * n);
+  for (int i = 0; i < n; ++i) z[i] = hash_unit(k, i);
+  tri_shift_factor(o.d, o.e, n, o.W[k], tnorm, u0, u1, u2, mul, piv);
+  for (int it = 0; it < 3; ++it) {
+    tri_shift_solve(n, z, u0, u1, u2, mul, piv);
+    // orthogonalise against the earlier vectors of the cluster (columns k0 .. k-1, already final)
+    for (int j = k - 1; j >= 0; --j) {
+      if (!(o.W[j] >= 0.0) || o.W[j] - o.W[j + 1] > kClusterGap * tnorm) break;
+      const double* y = o.Z + (int64_t)j * o.ldz;
+      double dot = 0.0;
+      for (int i = 0; i < n; ++i) dot = fma(y[i], z[i], dot);
+      for (int i = 0; i < n; ++i) z[i] = fma(-dot, y[i], z[i]);
+    }
+    double amax = 0.0;
+    for (int i = 0; i < n; ++i) amax = fmax(amax, fabs(z[i]));
+    const double inv = amax > 0.0 ? 1.0 / amax : 0.0;  // keep the iterate in range
+    for (int i = 0; i < n; ++i) z[i] *= inv;
+  }
+  double nrm = 0.0;
+  for (int i = 0; i < n; ++i) nrm = fma(z[i], z[i], nrm);
+  const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+  for (int i = 0; i < n; ++i) z[i] *= inv;
+}
+
 __global__ void k_tri_invit(const TriOp* __restrict__ ops, const int* __restrict__ op_of,
                             const int* __restrict__ k_of, int nthreads, double, double* scratch,
                             const int64_t* __restrict__ scratch_off) {
@@ -412,27 +445,18 @@ __global__ void k_tri_invit(const TriOp* __restrict__ ops, const int* __restrict
   const int k = k_of[t];
   const double tnorm = fmax(fabs(o.meta[2]), fabs(o.meta[3]));
   double* z = o.Z + (int64_t)k * o.ldz;
-  const double lam = o.W[k];
-  if (lam < 0.0) {  // below the floor
+  if (o.W[k] < 0.0) {  // below the floor
     for (int i = 0; i < n; ++i) z[i] = 0.0;
     return;
   }
+  // a member of a cluster that started earlier is computed by the cluster's first thread
+  if (k > 0 && o.W[k - 1] >= 0.0 && o.W[k - 1] - o.W[k] <= kClusterGap * tnorm) return;
   double* base = scratch + scratch_off[t];
-  double *u0 = base, *u1 = base + n, *u2 = base + 2 * n, *mul = base + 3 * n;
-  unsigned char* piv = (unsigned char*)(base + 4 * n);
-  for (int i = 0; i < n; ++i) z[i] = hash_unit(k, i);
-  tri_shift_factor(o.d, o.e, n, lam, tnorm, u0, u1, u2, mul, piv);
-  for (int it = 0; it < 3; ++it) {
-    tri_shift_solve(n, z, u0, u1, u2, mul, piv);
-    double amax = 0.0;
-    for (int i = 0; i < n; ++i) amax = fmax(amax, fabs(z[i]));
-    const double inv = amax > 0.0 ? 1.0 / amax : 0.0;  // keep the iterate in range
-    for (int i = 0; i < n; ++i) z[i] *= inv;
-  }
-  double nrm = 0.0;
-  for (int i = 0; i < n; ++i) nrm = fma(z[i], z[i], nrm);
-  const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
-  for (int i = 0; i < n; ++i) z[i] *= inv;
+  int m = k;
+  do {
+    invit_one(o, m, tnorm, o.Z + (int64_t)m * o.ldz, base);
+    ++m;
+  } while (m < n && o.W[m] >= 0.0 && o.W[m - 1] - o.W[m] <= kClusterGap * tnorm);
 }
 void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double gap_rel,
                       double* scratch, const int64_t* scratch_off, cudaStream_t s) {

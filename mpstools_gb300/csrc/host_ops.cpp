@@ -3,6 +3,7 @@
 #include "host_ops.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cfloat>
 #include <cmath>
@@ -12,6 +13,9 @@
 #include <tuple>
 
 namespace mpsg {
+
+static std::atomic<int64_t> g_split_fallbacks{0};
+int64_t split_fallback_count() { return g_split_fallbacks.load(); }
 
 static inline Q qat(const ItoKey& ik, uint32_t s) {
   MPSG_CHECK(s < ik.size(), "physical index outside itokey");
@@ -911,13 +915,13 @@ struct SvdBatch {
       launch_eig_post(d, (int)po.size(), st);
       ctx->dfree(d);
     }
-    cholqr(false, 2);
-    ctx->dfree(dscr);
+    ctx->dfree(dscr);  // stream-ordered: released after the kernels above
     ctx->dfree(dsoff);
     ctx->dfree(dmap);
     ctx->dfree(dtops);
     ctx->dfree(dT);
     ctx->dfree(dG);
+    cholqr(false, 2);
     left_vectors();
     orthonormalize_left();
     fixphase();
@@ -1216,8 +1220,19 @@ struct SvdBatch {
     if (method != 0 && nmax > chol_max_k()) method = 0;  // the density routes' CholeskyQR covers widths <= 512
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
-    else if (method == 3) run_gram_custom();
-    else run_jacobi();
+    else if (method == 3) {
+      try {
+        run_gram_custom();
+      } catch (const Err& e) {
+        // eigenvectors too dependent for CholeskyQR (a failed Cholesky pivot): redo this split exactly
+        if (e.code != 3 || std::string(e.what()).find("CholeskyQR") == std::string::npos) throw;
+        g_split_fallbacks.fetch_add(1);
+        kr.clear();
+        run_jacobi();
+      }
+    } else {
+      run_jacobi();
+    }
   }
 
   void run_jacobi() {
