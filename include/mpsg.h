@@ -73,8 +73,9 @@ mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
 mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
-/* Number of splits on the library's own density-matrix eigensolver (svd method 3) that were redone
- * on the exact Jacobi route because their singular vectors were too dependent for CholeskyQR. */
+/* Number of charge sectors of splits on the library's own density-matrix eigensolver (svd method 3)
+ * that were redone on the exact Jacobi route because their singular vectors were too dependent for
+ * CholeskyQR. */
 int64_t mpsg_split_fallbacks(void);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
  * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default, exact),
@@ -297,9 +298,9 @@ mpsg_status mpsg_batch_set_options(mpsg_batch b, mpsg_prec prec, int32_t lanmax)
  * chain's step records are available through mpsg_dmrg_steps. */
 mpsg_status mpsg_batch_simulate(mpsg_batch b, uint32_t sweeps, uint32_t chimax, int32_t doTrunc, double tr_weight,
                                 double delta, int32_t testenergy, double* energies);
-/* st[10]: global steps, chain steps, matvecs (one per lockstep iteration), matvec FLOPs (all chains),
+/* st[11]: global steps, chain steps, matvecs (one per lockstep iteration), matvec FLOPs (all chains),
  * matvec kernel launches, Lanczos seconds, split seconds, environment seconds, wall seconds, device
- * seconds of the sweeps. */
+ * seconds of the sweeps, seconds of the preparation (orthonormalisation and right environments). */
 mpsg_status mpsg_batch_stats(mpsg_batch b, double* st);
 void mpsg_batch_destroy(mpsg_batch b);
 

@@ -263,10 +263,10 @@ class DMRGbatch:
         return out
 
     def stats(self):
-        st = np.zeros(10)
+        st = np.zeros(11)
         check(self.ctx.L.mpsg_batch_stats(self.h, st.ctypes.data_as(C.c_void_p)))
         keys = ["global_steps", "chain_steps", "matvecs", "matvec_flops", "matvec_launches", "lanczos_seconds",
-                "split_seconds", "env_seconds", "wall_seconds", "device_seconds"]
+                "split_seconds", "env_seconds", "wall_seconds", "device_seconds", "prepare_seconds"]
         return dict(zip(keys, st.tolist()))
 
     def close(self):

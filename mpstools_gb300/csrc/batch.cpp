@@ -22,14 +22,18 @@ inline Q chain_shift(int i) { return (Q)i << kChainShiftBits; }
 // Direct sum of per-chain tensors (chain i: charges + i << 32, p0 + pshift[i]).  Shifting keeps every
 // chain's key order and puts chain i after chain i - 1, so the arena is the concatenation of the
 // chains' arenas (one device copy per chain).
-TensorP direct_sum(Ctx* ctx, const std::vector<const Tensor*>& parts, const std::vector<uint32_t>& pshift, int nphys) {
+// `slot` (optional, ascending) puts part i at slot[i] instead of i.
+TensorP direct_sum(Ctx* ctx, const std::vector<const Tensor*>& parts, const std::vector<uint32_t>& pshift, int nphys,
+                   const std::vector<int>* slot = nullptr) {
   Layout lay;
   for (size_t i = 0; i < parts.size(); ++i)
     for (const Block& b : parts[i]->b) {
       MPSG_CHECK(b.k.q0 < chain_shift(1) && b.k.q1 < chain_shift(1), "charge too large for the chain direct sum");
+      const int si = slot ? (*slot)[i] : (int)i;
+      MPSG_CHECK(i == 0 || !slot || (*slot)[i] > (*slot)[i - 1], "direct-sum slots must ascend");
       BKey k = b.k;
-      k.q0 += chain_shift((int)i);
-      k.q1 += chain_shift((int)i);
+      k.q0 += chain_shift(si);
+      k.q1 += chain_shift(si);
       k.p0 += pshift.empty() ? 0u : pshift[i];
       lay.add(k, b.r, b.c);
     }
@@ -225,7 +229,7 @@ struct BatchEngine {
   int lanmax = 500;
   LanczosStats lst;
   int64_t global_steps = 0, chain_steps = 0, matvec_launches = 0;
-  double split_seconds = 0, env_seconds = 0, wall = 0, device_seconds = 0;
+  double split_seconds = 0, env_seconds = 0, wall = 0, device_seconds = 0, prepare_seconds = 0;
 
   // the (site, direction) sequence of DMRGengine::simulate with a fixed sweep count
   static std::vector<std::pair<int, int>> schedule(int N, int sweeps) {
@@ -356,30 +360,19 @@ struct BatchEngine {
       if (grp.empty()) continue;
       std::vector<const Tensor *> envs, As;
       std::vector<const MPO*> Ws;
-      std::vector<uint32_t> oin(grp.size()), oout(grp.size());
-      uint32_t a = 0, b = 0;
-      for (size_t g = 0; g < grp.size(); ++g) {
-        Engine& e = *ch[act[grp[g]]];
-        const int s = site[grp[g]];
-        const MPO& W = d > 0 ? e.mpo[s] : e.mpo[s + 1];
+      for (int i : grp) {
+        Engine& e = *ch[act[i]];
+        const int s = site[i];
         envs.push_back(d > 0 ? e.L[s - 1].get() : e.R[s + 2].get());
         As.push_back(d > 0 ? e.mps[s].get() : e.mps[s + 1].get());
-        Ws.push_back(&W);
-        oin[g] = a;   // channel of the incoming environment: left channel (d > 0) or right channel
-        oout[g] = b;  // channel of the new environment
-        a += d > 0 ? W.Dl : W.Dr;
-        b += d > 0 ? W.Dr : W.Dl;
+        Ws.push_back(d > 0 ? &e.mpo[s] : &e.mpo[s + 1]);
       }
-      std::vector<uint32_t> zg(grp.size(), 0u);
-      TensorP Et = direct_sum(ctx, envs, oin, 1), At = direct_sum(ctx, As, zg, 1);
-      const MPO Wt = d > 0 ? mpo_direct_sum(Ws, oin, oout) : mpo_direct_sum(Ws, oout, oin);
-      TensorP out = env_update(ctx, *Et, *At, Wt, d > 0 ? ik0 : ik1, d > 0 ? 1 : -1, nullptr);
+      auto out = env_batch(d, envs, As, Ws, d > 0 ? ik0 : ik1);
       for (size_t g = 0; g < grp.size(); ++g) {
         Engine& e = *ch[act[grp[g]]];
         const int s = site[grp[g]];
-        TensorP part = unsum(ctx, *out, (int)g, oout[g]);
-        if (d > 0) e.L[s] = part;
-        else e.R[s + 1] = part;
+        if (d > 0) e.L[s] = out[g];
+        else e.R[s + 1] = out[g];
       }
     }
     ctx->sync();
@@ -392,6 +385,88 @@ struct BatchEngine {
     chain_steps += n;
   }
 
+  // Environment updates of several chains at once: item g = (environment, site tensor, MPO tensor),
+  // all in direction d (> 0: L, else R); returns the new environments in item order.
+  std::vector<TensorP> env_batch(int d, const std::vector<const Tensor*>& envs, const std::vector<const Tensor*>& As,
+                                 const std::vector<const MPO*>& Ws, const ItoKey& ik) {
+    const size_t n = envs.size();
+    std::vector<uint32_t> oin(n), oout(n), zg(n, 0u);
+    uint32_t a = 0, b = 0;
+    for (size_t g = 0; g < n; ++g) {
+      oin[g] = a;  // channel of the incoming environment (left channel for d > 0, right otherwise)
+      oout[g] = b;
+      a += d > 0 ? Ws[g]->Dl : Ws[g]->Dr;
+      b += d > 0 ? Ws[g]->Dr : Ws[g]->Dl;
+    }
+    TensorP Et = direct_sum(ctx, envs, oin, 1), At = direct_sum(ctx, As, zg, 1);
+    const MPO Wt = d > 0 ? mpo_direct_sum(Ws, oin, oout) : mpo_direct_sum(Ws, oout, oin);
+    TensorP out = env_update(ctx, *Et, *At, Wt, ik, d > 0 ? 1 : -1, nullptr);
+    std::vector<TensorP> res;
+    for (size_t g = 0; g < n; ++g) res.push_back(unsum(ctx, *out, (int)g, oout[g]));
+    return res;
+  }
+
+  // Engine::prepare of every chain, batched: orthonormalize("rl") site by site counted from each
+  // chain's right end (prepareMatrix per left-charge group, so the direct sum separates the chains),
+  // then the right environments the same way.
+  void prepare_all() {
+    int K = 0;
+    for (Engine* e : ch) K = std::max(K, e->N);
+    for (int k = 0; k < K; ++k) {
+      std::vector<int> act;
+      for (size_t c = 0; c < ch.size(); ++c)
+        if (ch[c]->N - 1 - k >= 0) act.push_back((int)c);
+      std::vector<const Tensor *> b2, b1;
+      std::vector<int> slot1;
+      for (size_t i = 0; i < act.size(); ++i) {
+        Engine& e = *ch[act[i]];
+        const int s = e.N - 1 - k;
+        b2.push_back(e.mps[s].get());
+        if (s > 0) {
+          b1.push_back(e.mps[s - 1].get());
+          slot1.push_back((int)i);
+        }
+      }
+      TensorP B2 = direct_sum(ctx, b2, {}, 1);
+      TensorP B1 = b1.empty() ? nullptr : direct_sum(ctx, b1, {}, 1, &slot1);
+      TensorP lamt;
+      prepare_matrix_r(ctx, B1 ? &B1 : nullptr, B2, &lamt, 1e-16);
+      for (size_t i = 0; i < act.size(); ++i) {
+        Engine& e = *ch[act[i]];
+        const int s = e.N - 1 - k;
+        e.mps[s] = unsum(ctx, *B2, (int)i, 0);
+        if (s > 0) e.mps[s - 1] = unsum(ctx, *B1, (int)i, 0);
+        e.lam[s - 1] = unsum(ctx, *lamt, (int)i, 0);
+      }
+    }
+    for (Engine* e : ch) {
+      e->R.clear();
+      e->R[e->N] = Engine::rmax(ctx, *e->mps[e->N - 1]);
+      e->L.clear();
+      e->L[-1] = Engine::lmin(ctx);
+    }
+    for (int k = 0;; ++k) {  // R[s] for s = N-1 .. 2, aligned at the right ends
+      std::vector<int> act;
+      for (size_t c = 0; c < ch.size(); ++c)
+        if (ch[c]->N - 1 - k >= 2) act.push_back((int)c);
+      if (act.empty()) break;
+      std::vector<const Tensor *> envs, As;
+      std::vector<const MPO*> Ws;
+      for (int c : act) {
+        Engine& e = *ch[c];
+        const int s = e.N - 1 - k;
+        envs.push_back(e.R[s + 1].get());
+        As.push_back(e.mps[s].get());
+        Ws.push_back(&e.mpo[s]);
+        MPSG_CHECK(e.ik[s] == ch[act[0]]->ik[ch[act[0]]->N - 1 - k], "batched chains need the same local charge map");
+      }
+      const ItoKey& ik = ch[act[0]]->ik[ch[act[0]]->N - 1 - k];
+      auto out = env_batch(-1, envs, As, Ws, ik);
+      for (size_t i = 0; i < act.size(); ++i) ch[act[i]]->R[ch[act[i]]->N - 1 - k] = out[i];
+    }
+    ctx->sync();
+  }
+
   // DMRGengine::simulate for every chain with `sweeps` sweeps (no early stop on EnConv), the final
   // doStep(0, -1) included; energies[c] = the last step's energy of chain c
   void simulate(int sweeps, int chimax, bool doTrunc, double tr_weight, double delta, bool testenergy,
@@ -400,7 +475,9 @@ struct BatchEngine {
     cudaEvent_t e0, e1;
     MPSG_CUDA(cudaEventCreate(&e0));
     MPSG_CUDA(cudaEventCreate(&e1));
-    for (Engine* e : ch) e->prepare();
+    auto tp = std::chrono::steady_clock::now();
+    prepare_all();
+    prepare_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count();
     std::vector<std::vector<std::pair<int, int>>> sch;
     size_t longest = 0;
     for (Engine* e : ch) {
@@ -491,6 +568,7 @@ mpsg_status mpsg_batch_stats(mpsg_batch b, double* st) {
   st[7] = x.env_seconds;
   st[8] = x.wall;
   st[9] = x.device_seconds;
+  st[10] = x.prepare_seconds;
   API_END
 }
 

@@ -301,6 +301,10 @@ void launch_tri_bounds(const TriOp* ops, int nops, cudaStream_t s) {
 // Eigenvalues at or below the sector's floor (floor_rel * lambda_max) are not computed: W holds -1
 // there.  W[k] = k-th largest eigenvalue.  LN divides 32, so a lane group never spans two warps.
 constexpr int kBisectLanes = 4;
+// Eigenvalues at or below 1e-30 (singular values at or below 1e-15) are never computed: the split's
+// truncation drops every singular value <= 1e-15, and a zero or denormal-scale sector would otherwise
+// give inverse iteration reciprocal pivots that overflow.
+constexpr double kAbsFloor = 1e-30;
 
 template <int LN>
 __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restrict__ op_of, const int* __restrict__ k_of,
@@ -314,7 +318,7 @@ __global__ void k_tri_bisect(const TriOp* __restrict__ ops, const int* __restric
   const int k = k_of[t];  // 0 = largest
   const int n = o.n;
   const double lmax = o.meta[0];
-  const double floor_v = o.floor_rel * fmax(lmax, 0.0);
+  const double floor_v = fmax(o.floor_rel * fmax(lmax, 0.0), kAbsFloor);
   const int m = n - 1 - k;  // the eigenvalue with exactly m smaller ones
   if (sturm_count(o.d, o.e2, n, floor_v) > m) {  // same answer in every lane of the group
     if (g == 0) o.W[k] = -1.0;
@@ -381,7 +385,13 @@ __device__ void tri_shift_factor(const double* d, const double* e, int n, double
   if (dd == 0.0) dd = tiny;
   u0[n - 1] = 1.0 / dd;
 }
-// x <- (T - lam I)^-1 x with the factors of tri_shift_factor.
+// x <- c (T - lam I)^-1 x with the factors of tri_shift_factor, for some c > 0: whenever an entry
+// passes 2^166 (~1e50) the whole vector is scaled by 2^-166, so that products of reciprocal tiny
+// pivots (near-singular shifts, clusters) cannot overflow (the caller normalises the result).
+__device__ __forceinline__ void tri_rescale(int n, double* x, double v) {
+  if (fabs(v) > 0x1p+166)
+    for (int k = 0; k < n; ++k) x[k] *= 0x1p-166;
+}
 __device__ void tri_shift_solve(int n, double* x, const double* u0, const double* u1, const double* u2,
                                 const double* mul, const unsigned char* piv) {
   for (int i = 0; i + 1 < n; ++i) {
@@ -392,10 +402,18 @@ __device__ void tri_shift_solve(int n, double* x, const double* u0, const double
     } else {
       x[i + 1] -= mul[i] * x[i];
     }
+    tri_rescale(n, x, x[i + 1]);
   }
   x[n - 1] *= u0[n - 1];
-  if (n >= 2) x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0[n - 2];
-  for (int i = n - 3; i >= 0; --i) x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0[i];
+  tri_rescale(n, x, x[n - 1]);
+  if (n >= 2) {
+    x[n - 2] = (x[n - 2] - u1[n - 2] * x[n - 1]) * u0[n - 2];
+    tri_rescale(n, x, x[n - 2]);
+  }
+  for (int i = n - 3; i >= 0; --i) {
+    x[i] = (x[i] - u1[i] * x[i + 1] - u2[i] * x[i + 2]) * u0[i];
+    tri_rescale(n, x, x[i]);
+  }
 }
 
 // Eigenvectors of T by inverse iteration: three iterations from a deterministic pseudo-random start

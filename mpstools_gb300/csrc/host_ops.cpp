@@ -3,6 +3,8 @@
 #include "host_ops.h"
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <cfloat>
@@ -921,10 +923,23 @@ struct SvdBatch {
     ctx->dfree(dtops);
     ctx->dfree(dT);
     ctx->dfree(dG);
-    cholqr(false, 2);
+    std::vector<int> failed;
+    cholqr(false, 2, &failed);
     left_vectors();
-    orthonormalize_left();
+    orthonormalize_left(&failed);
     fixphase();
+    if (!failed.empty()) {
+      // singular vectors too dependent for CholeskyQR: these sectors are redone exactly
+      std::sort(failed.begin(), failed.end());
+      failed.erase(std::unique(failed.begin(), failed.end()), failed.end());
+      g_split_fallbacks.fetch_add((int64_t)failed.size());
+      if (std::getenv("MPSG_VERBOSE"))
+        for (int i : failed)
+          std::fprintf(stderr, "libmpsg: CholeskyQR failed in sector %d (%d x %d); redone on the Jacobi route\n", i,
+                       s[i].ms, s[i].ns);
+      for (int i : failed) kr[i] = s[i].k;
+      run_jacobi(&failed);
+    }
   }
 
   // Density-matrix route with one cuSOLVER syevd per sector, sectors spread over worker threads
@@ -1097,7 +1112,8 @@ struct SvdBatch {
   // kernel, X <- X R^-1 by blocked forward substitution.  left: X = Ust (ms x ns) and s_j is
   // multiplied by R_jj of the first pass (the norm of y_j after removing its components along the
   // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
-  void cholqr(bool left, int passes) {
+  // failed (optional): sectors whose Cholesky met a non-positive pivot are appended instead of throwing
+  void cholqr(bool left, int passes, std::vector<int>* failed = nullptr) {
     std::vector<int> idx;
     int kmax = 0;
     for (size_t i = 0; i < s.size(); ++i)
@@ -1208,11 +1224,21 @@ struct SvdBatch {
     ctx->dfree(dinf);
     ctx->dfree(dR);
     ctx->dfree(dC);
-    for (int v : inf)
-      if (v != 0) throw Err(3, "CholeskyQR: the Gram matrix of the singular vectors is not positive definite (column " +
-                                   std::to_string(v - 1) + ")");
+    for (size_t t = 0; t < idx.size(); ++t)
+      if (inf[t] != 0) {
+        if (failed) {
+          failed->push_back(idx[t]);
+          continue;
+        }
+        const Sec& x = s[idx[t]];
+        throw Err(3, std::string("CholeskyQR of ") + (left ? "U" : "V") +
+                         ": the Gram matrix of the singular vectors is not positive definite (sector " +
+                         std::to_string(idx[t]) + " of " + std::to_string(s.size()) + ", " + std::to_string(x.ms) +
+                         " x " + std::to_string(x.ns) + ", " + std::to_string(kcols(idx[t])) +
+                         " resolved columns, column " + std::to_string(inf[t] - 1) + ")");
+      }
   }
-  void orthonormalize_left() { cholqr(true, 1); }
+  void orthonormalize_left(std::vector<int>* failed = nullptr) { cholqr(true, 1, failed); }
 
   void run(int method) {
     int nmax = 0;
@@ -1220,26 +1246,20 @@ struct SvdBatch {
     if (method != 0 && nmax > chol_max_k()) method = 0;  // the density routes' CholeskyQR covers widths <= 512
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
-    else if (method == 3) {
-      try {
-        run_gram_custom();
-      } catch (const Err& e) {
-        // eigenvectors too dependent for CholeskyQR (a failed Cholesky pivot): redo this split exactly
-        if (e.code != 3 || std::string(e.what()).find("CholeskyQR") == std::string::npos) throw;
-        g_split_fallbacks.fetch_add(1);
-        kr.clear();
-        run_jacobi();
-      }
-    } else {
-      run_jacobi();
-    }
+    else if (method == 3) run_gram_custom();
+    else run_jacobi();
   }
 
-  void run_jacobi() {
+  // only (optional): the sectors to decompose (the others keep their factors)
+  void run_jacobi(const std::vector<int>* only = nullptr) {
     cusolverDnHandle_t h = ctx->svd_handle();
+    std::vector<char> sel(s.size(), only ? 0 : 1);
+    if (only)
+      for (int i : *only) sel[i] = 1;
     int lwork = 0;
-    for (auto& x : s) {
-      if (x.k == 0) continue;
+    for (size_t i = 0; i < s.size(); ++i) {
+      const Sec& x = s[i];
+      if (x.k == 0 || !sel[i]) continue;
       int lw = 0;
       cusolverStatus_t st = cusolverDnDgesvdj_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, 1, x.ms, x.ns, dM + x.offM, x.ms,
                                                          dS + x.offS, dU + x.offU, x.ms, dV + x.offV, x.ns, &lw,
@@ -1250,7 +1270,7 @@ struct SvdBatch {
     double* work = (double*)ctx->dmalloc(sizeof(double) * std::max(lwork, 2));
     for (size_t i = 0; i < s.size(); ++i) {
       const Sec& x = s[i];
-      if (x.k == 0) continue;
+      if (x.k == 0 || !sel[i]) continue;
       cusolverStatus_t st = cusolverDnDgesvdj(h, CUSOLVER_EIG_MODE_VECTOR, 1, x.ms, x.ns, dM + x.offM, x.ms,
                                               dS + x.offS, dU + x.offU, x.ms, dV + x.offV, x.ns, work, lwork,
                                               dinfo + i, ctx->svdp);

@@ -122,8 +122,8 @@ struct SplitResult {
 // absorb: 0 none, +1 lambda into Vt (rows), -1 lambda into U (columns).  seg_q0 (optional, ascending):
 // th is a direct sum of independent chains, chain c holding the centre charges from seg_q0[c] up to
 // the next entry; truncation, truncated weight, kept count and normalisation are then per chain.
-// number of density-matrix splits (own eigensolver) redone on the exact Jacobi route because the
-// CholeskyQR of their singular vectors failed
+// number of charge sectors of density-matrix splits (own eigensolver) redone on the exact Jacobi
+// route because the CholeskyQR of their singular vectors failed
 int64_t split_fallback_count();
 SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
                    double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0 = nullptr,
