@@ -45,6 +45,11 @@ __device__ __forceinline__ double warp_sum(double v) {
   for (int off = 16; off; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
 }
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int off = 16; off; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
 
 // Householder vector of column j (held by the calling warp's CTA as local column `col`): alpha =
 // x[j+1], the rest x[j+2..n-1].  Writes v (v[j+1] = 1) into this CTA's v buffer `slot`, tau and beta
@@ -218,6 +223,32 @@ void launch_sytrd(const SytrdOp* ops, int nops, int CL, int nmax, cudaStream_t s
     case 16: launch_sytrd_cl<16>(ops, nops, nmax, s); break;
     default: throw Err(1, "sytrd: unsupported cluster size");
   }
+}
+
+// ----------------------------------------------------------------------------- 0. scaling
+// G <- 2^-p G with 2^p <= max |G| < 2^(p+1), per sector (exact): the eigenvalue stages below work on
+// matrices of norm ~1 whatever the scale of the input (the division-free Sturm counts assume
+// |T| <= 2^100; unnormalised tensors, e.g. a random MPS being orthonormalised, reach 2^400).  The
+// eigenvalues only rank and select the vectors; the singular values are recomputed from |M v|.
+__global__ void __launch_bounds__(256) k_gram_scale(const GramScaleOp* __restrict__ ops) {
+  const GramScaleOp o = ops[blockIdx.x];
+  double m = 0.0;
+  for (int64_t e = threadIdx.x; e < (int64_t)o.n * o.n; e += blockDim.x)
+    m = fmax(m, fabs(o.G[e % o.n + (e / o.n) * (int64_t)o.ld]));
+  m = warp_max(m);
+  __shared__ double red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  m = 0.0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+  if (!(m > 0.0) || !isfinite(m)) return;
+  const double sc = ldexp(1.0, -ilogb(m));
+  for (int64_t e = threadIdx.x; e < (int64_t)o.n * o.n; e += blockDim.x) o.G[e % o.n + (e / o.n) * (int64_t)o.ld] *= sc;
+}
+void launch_gram_scale(const GramScaleOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_gram_scale<<<nops, 256, 0, s>>>(ops);
+  g_eig_launches.fetch_add(1);
 }
 
 // ----------------------------------------------------------------------------- 2. eigenvalues

@@ -833,6 +833,12 @@ struct SvdBatch {
       g.upload(ctx);
       const double* bases[8] = {dM, nullptr, dG, nullptr, nullptr, nullptr, nullptr, nullptr};
       g.run(bases);
+      std::vector<GramScaleOp> so;
+      for (int i : idx) so.push_back(GramScaleOp{dG + offG[i], s[i].ns, s[i].ns});
+      GramScaleOp* d = (GramScaleOp*)ctx->dmalloc(sizeof(GramScaleOp) * so.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, so.data(), sizeof(GramScaleOp) * so.size(), cudaMemcpyHostToDevice, st));
+      launch_gram_scale(d, (int)so.size(), st);
+      ctx->dfree(d);
     }
     // 1. tridiagonalisation, one launch per cluster size
     {

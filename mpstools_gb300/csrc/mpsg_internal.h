@@ -219,6 +219,10 @@ struct CMeasureOp {  // w * sum |x_ij|^2 ll_i^2 lr_j^2
   int32_t rows, cols;
   double w;
 };
+struct GramScaleOp {  // n x n matrix G (leading dimension ld), scaled in place by a power of two
+  double* G;
+  int32_t n, ld;
+};
 struct CDotOp {  // Re sum conj(a) b = sum a_re b_re + a_im b_im over n elements
   const double* ar;
   const double* ai;
@@ -291,6 +295,7 @@ void launch_cfixphase(const CPhaseOp* ops, int nops, cudaStream_t s);
 void launch_cblock_max2(const CBlockOp* ops, int nops, double* out, cudaStream_t s);
 void launch_cmeasure(const CMeasureOp* ops, int nops, double* out, cudaStream_t s);
 void launch_cdot_re(const CDotOp* ops, int nops, double* out, cudaStream_t s);
+void launch_gram_scale(const GramScaleOp* ops, int nops, cudaStream_t s);
 void launch_recip(double* dst, const double* src, int64_t n, cudaStream_t s);
 int64_t eig_launch_count();
 int sytrd_cluster_size(int n);

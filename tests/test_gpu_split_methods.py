@@ -102,3 +102,30 @@ def test_orthonormalize_methods(ctx, method):
         ctx.set_svd_method("jacobi")
     print(f"{method}: max right-canonical error {max(errs):.2e}")
     assert max(errs) < 1e-10
+
+
+@pytest.mark.parametrize("log2_scale", [140, 300, -40])
+def test_density_eig_badly_scaled_sectors(ctx, log2_scale):
+    """Sectors far from unit norm (an unnormalised state being orthonormalised reaches norms of 2^200
+    and more): the own eigensolver scales each Gram matrix by a power of two, so its singular values
+    match the exact route relative to the largest one, with no sector falling back to the Jacobi route."""
+    rng = np.random.default_rng(5)
+    scale = 2.0 ** log2_scale
+    th = {(0, 0, 0, 0): scale * rng.standard_normal((15, 56)), (1, 1, 0, 0): scale * rng.standard_normal((40, 33)),
+          (2, 2, 0, 0): scale * rng.standard_normal((7, 9))}
+    ik = [0, 0]
+    out = {}
+    L = ctx.L
+    for method in ("jacobi", "density_eig"):
+        ctx.set_svd_method(method)
+        f0 = L.mpsg_split_fallbacks()
+        U, Vt, lam, tw, chi = api.split(th, (ik, ik), 1000, doTrunc=False, normalize=False, ctx=ctx)
+        out[method] = (lam, L.mpsg_split_fallbacks() - f0)
+    ctx.set_svd_method("jacobi")
+    assert out["density_eig"][1] == 0
+    lj, ld = out["jacobi"][0], out["density_eig"][0]
+    assert set(lj) == set(ld)
+    for q in lj:
+        a, b = np.sort(np.asarray(lj[q]))[::-1], np.sort(np.asarray(ld[q]))[::-1]
+        assert len(a) == len(b)
+        assert np.abs(a - b).max() <= 1e-10 * a[0], (q, np.abs(a - b).max() / a[0])
