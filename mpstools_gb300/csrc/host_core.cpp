@@ -27,6 +27,7 @@ Ctx::~Ctx() {
   if (params) cusolverDnDestroyParams(params);
   for (auto h : whandles) cusolverDnDestroy(h);
   for (auto h : wblas) cublasDestroy(h);
+  if (blas) cublasDestroy(blas);
   for (auto s : wstreams) cudaStreamDestroy(s);
   for (auto e : wevents) cudaEventDestroy(e);
   if (fork_event) cudaEventDestroy(fork_event);
@@ -54,6 +55,11 @@ cusolverDnHandle_t Ctx::svd_handle() {
   }
   cusolverDnSetStream(solver, stream);
   return solver;
+}
+cublasHandle_t Ctx::blas_handle() {
+  if (!blas && cublasCreate(&blas) != CUBLAS_STATUS_SUCCESS) throw Err(3, "cublasCreate failed");
+  cublasSetStream(blas, stream);
+  return blas;
 }
 cusolverDnParams_t Ctx::solver_params() {
   if (!params && cusolverDnCreateParams(&params) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreateParams failed");

@@ -26,6 +26,8 @@ struct Ctx : std::enable_shared_from_this<Ctx> {
   cusolverDnHandle_t svd_handle();
   cusolverDnParams_t params = nullptr;
   cusolverDnParams_t solver_params();
+  cublasHandle_t blas = nullptr;
+  cublasHandle_t blas_handle();  // bound to `stream`
   // worker streams / solver handles for concurrent per-sector eigen-solves (created on first use)
   std::vector<cudaStream_t> wstreams;
   std::vector<cusolverDnHandle_t> whandles;

@@ -219,6 +219,22 @@ struct CMeasureOp {  // w * sum |x_ij|^2 ll_i^2 lr_j^2
   int32_t rows, cols;
   double w;
 };
+struct CGramPad {  // complex nc x nc slot: diagonal entries [n, nc) set to -1 (ranked below the spectrum)
+  double2* A;
+  int32_t nc, n;
+};
+struct CGramPost {  // eigenpairs of a padded complex Gram slot -> V (n x n, descending), S (sqrt, floored)
+  const double2* W;
+  const double* lam;
+  double2* V;
+  double* S;
+  int32_t n, nc;
+};
+struct CColNorm {  // complex U (m x k, ldu): S_j = |U_j|, U_j /= S_j; columns with S_j == 0 cleared
+  double2* U;
+  double* S;
+  int32_t m, k, ldu;
+};
 struct GramScaleOp {  // n x n matrix G (leading dimension ld), scaled in place by a power of two
   double* G;
   int32_t n, ld;
@@ -296,6 +312,9 @@ void launch_cblock_max2(const CBlockOp* ops, int nops, double* out, cudaStream_t
 void launch_cmeasure(const CMeasureOp* ops, int nops, double* out, cudaStream_t s);
 void launch_cdot_re(const CDotOp* ops, int nops, double* out, cudaStream_t s);
 void launch_gram_scale(const GramScaleOp* ops, int nops, cudaStream_t s);
+void launch_cgram_pad(const CGramPad* ops, int nops, cudaStream_t s);
+void launch_cgram_post(const CGramPost* ops, int nops, cudaStream_t s);
+void launch_ccolnorm(const CColNorm* ops, int nops, cudaStream_t s);
 void launch_recip(double* dst, const double* src, int64_t n, cudaStream_t s);
 int64_t eig_launch_count();
 int sytrd_cluster_size(int n);

@@ -156,6 +156,144 @@ struct TebdEngine {
     }
   }
 
+  // one centre-charge sector of the split: rows (s1 ranges) x columns (s2 ranges); M stored tall
+  // (M^H for a wide sector) in the interleaved complex arena
+  struct Sec {
+    std::map<uint32_t, std::pair<int, int>> rx, ry;
+    std::vector<int> blocks;
+    int m = 0, n = 0, k = 0;
+    int64_t offM = 0, offU = 0, offV = 0, offS = 0;
+  };
+
+  // Density-matrix SVD of every sector (the exact route is cuSOLVER zgesvdj): G = A^H A of the stored
+  // tall matrix A (ms x ns) by cuBLAS zgemm into slots of power-of-two size classes (padding diagonal
+  // -1), cuSOLVER's batched Hermitian eigensolver per class, the eigenvectors ranked descending
+  // (eigenvalues below 32 ns eps lambda_max unresolved: zero), then y_j = A v_j, s_j = |y_j|, u_j =
+  // y_j / s_j.  A singular value s carries an absolute error ~ eps s_max^2 / s (the Gram matrix's
+  // resolution); the u_j are orthonormal to ~eps s_max / s.
+  void density_svd(std::map<Q, Sec>& secs, double2* dM, double2* dU, double2* dV, double* dS) {
+    cusolverDnHandle_t h = ctx->svd_handle();
+    cublasHandle_t bh = ctx->blas_handle();
+    std::map<int, std::vector<Sec*>> cls;
+    for (auto& x : secs) {
+      Sec& s = x.second;
+      if (s.k == 0) continue;
+      int c = 32;
+      while (c < std::min(s.m, s.n)) c <<= 1;
+      cls[c].push_back(&s);
+    }
+    int64_t oB = 0, oW = 0, nsec = 0;
+    for (auto& c : cls) {
+      oB += (int64_t)c.first * c.first * (int64_t)c.second.size();
+      oW += (int64_t)c.first * (int64_t)c.second.size();
+      nsec += (int64_t)c.second.size();
+    }
+    double2* dB = (double2*)ctx->dmalloc(sizeof(double2) * std::max<int64_t>(oB, 2));
+    double* dWv = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oW, 2));
+    int* dinf = (int*)ctx->dmalloc(sizeof(int) * (size_t)(nsec + 1));
+    MPSG_CUDA(cudaMemsetAsync(dB, 0, sizeof(double2) * std::max<int64_t>(oB, 2), ctx->stream));
+    MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * (size_t)(nsec + 1), ctx->stream));
+    const cuDoubleComplex one = make_cuDoubleComplex(1.0, 0.0), zero = make_cuDoubleComplex(0.0, 0.0);
+    struct Slot {
+      Sec* s;
+      double2* B;
+      double* W;
+      int nc;
+    };
+    std::vector<Slot> slots;
+    std::vector<CGramPad> pads;
+    {
+      int64_t b = 0, w = 0;
+      for (auto& c : cls)
+        for (Sec* s : c.second) {
+          slots.push_back(Slot{s, dB + b, dWv + w, c.first});
+          b += (int64_t)c.first * c.first;
+          w += c.first;
+        }
+    }
+    for (Slot& sl : slots) {
+      Sec& s = *sl.s;
+      const bool tall = s.m >= s.n;
+      const int ms = tall ? s.m : s.n, ns = tall ? s.n : s.m;
+      if (cublasZgemm(bh, CUBLAS_OP_C, CUBLAS_OP_N, ns, ns, ms, &one, (const cuDoubleComplex*)(dM + s.offM), ms,
+                      (const cuDoubleComplex*)(dM + s.offM), ms, &zero, (cuDoubleComplex*)sl.B, sl.nc) !=
+          CUBLAS_STATUS_SUCCESS)
+        throw Err(3, "zgemm (Gram matrix) failed");
+      pads.push_back(CGramPad{sl.B, sl.nc, ns});
+    }
+    {
+      CGramPad* d = (CGramPad*)ctx->dmalloc(sizeof(CGramPad) * pads.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, pads.data(), sizeof(CGramPad) * pads.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_cgram_pad(d, (int)pads.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    int ib = 0;
+    size_t first = 0;
+    for (auto& c : cls) {
+      const int64_t n = c.first, batch = (int64_t)c.second.size();
+      double2* A = slots[first].B;
+      double* W = slots[first].W;
+      size_t wd = 0, wh = 0;
+      if (cusolverDnXsyevBatched_bufferSize(h, ctx->solver_params(), CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                            CUDA_C_64F, A, n, CUDA_R_64F, W, CUDA_C_64F, &wd, &wh, batch) !=
+          CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "complex syevBatched_bufferSize failed");
+      void* dwork = ctx->dmalloc(wd + 16);
+      std::vector<char> hwork(wh + 16);
+      if (cusolverDnXsyevBatched(h, ctx->solver_params(), CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n,
+                                 CUDA_C_64F, A, n, CUDA_R_64F, W, CUDA_C_64F, dwork, wd, hwork.data(), wh, dinf + ib,
+                                 batch) != CUSOLVER_STATUS_SUCCESS)
+        throw Err(3, "complex syevBatched failed");
+      ctx->sync();  // the host workspace must outlive the call
+      ctx->dfree(dwork);
+      ib += (int)batch;
+      first += (size_t)batch;
+    }
+    {
+      std::vector<int> inf(ib + 1, 0);
+      MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * (ib + 1), cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->sync();
+      for (int i = 0; i < ib; ++i)
+        if (inf[i] != 0) throw Err(3, "batched Hermitian eigensolver failed (info=" + std::to_string(inf[i]) + ")");
+    }
+    std::vector<CGramPost> post;
+    std::vector<CColNorm> cn;
+    for (Slot& sl : slots) {
+      Sec& s = *sl.s;
+      const bool tall = s.m >= s.n;
+      const int ms = tall ? s.m : s.n, ns = tall ? s.n : s.m;
+      double2* uo = tall ? dU + s.offU : dV + s.offV;  // left vectors of the stored matrix
+      double2* vo = tall ? dV + s.offV : dU + s.offU;  // right vectors of the stored matrix
+      post.push_back(CGramPost{sl.B, sl.W, vo, dS + s.offS, ns, sl.nc});
+      cn.push_back(CColNorm{uo, dS + s.offS, ms, s.k, ms});
+    }
+    {
+      CGramPost* d = (CGramPost*)ctx->dmalloc(sizeof(CGramPost) * post.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, post.data(), sizeof(CGramPost) * post.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_cgram_post(d, (int)post.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    for (Slot& sl : slots) {  // y = A V
+      Sec& s = *sl.s;
+      const bool tall = s.m >= s.n;
+      const int ms = tall ? s.m : s.n, ns = tall ? s.n : s.m;
+      double2* uo = tall ? dU + s.offU : dV + s.offV;
+      const double2* vo = tall ? dV + s.offV : dU + s.offU;
+      if (cublasZgemm(bh, CUBLAS_OP_N, CUBLAS_OP_N, ms, s.k, ns, &one, (const cuDoubleComplex*)(dM + s.offM), ms,
+                      (const cuDoubleComplex*)vo, ns, &zero, (cuDoubleComplex*)uo, ms) != CUBLAS_STATUS_SUCCESS)
+        throw Err(3, "zgemm (left vectors) failed");
+    }
+    {
+      CColNorm* d = (CColNorm*)ctx->dmalloc(sizeof(CColNorm) * cn.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, cn.data(), sizeof(CColNorm) * cn.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_ccolnorm(d, (int)cn.size(), ctx->stream);
+      ctx->dfree(d);
+    }
+    ctx->dfree(dinf);
+    ctx->dfree(dWv);
+    ctx->dfree(dB);
+  }
+
   // applyGate on bond (site, site+1); returns (truncated weight, kept count)
   std::pair<double, int> apply_gate(int site, const CGate& gate, int chimax, bool doTrunc, double tr_weight,
                                     bool normalize) {
@@ -252,12 +390,6 @@ struct TebdEngine {
     }
     auto t0 = std::chrono::steady_clock::now();
     // split by centre charge
-    struct Sec {
-      std::map<uint32_t, std::pair<int, int>> rx, ry;
-      std::vector<int> blocks;
-      int m = 0, n = 0, k = 0;
-      int64_t offM = 0, offU = 0, offV = 0, offS = 0;
-    };
     const ItoKey &ik0 = ik[site], &ik1 = ik[site + 1];
     std::map<Q, Sec> secs;
     for (int i : kt) {
@@ -306,7 +438,9 @@ struct TebdEngine {
         ctx->dfree(d);
       }
     }
-    {
+    if (ctx->svd_method != 0) {
+      density_svd(secs, dM, dU, dV, dS);
+    } else {
       cusolverDnHandle_t h = ctx->svd_handle();
       int lwork = 0;
       for (auto& x : secs) {
@@ -337,6 +471,8 @@ struct TebdEngine {
         ++si;
       }
       ctx->dfree(work);
+    }
+    {
       std::vector<CPhaseOp> ph;
       for (auto& x : secs) {
         Sec& s = x.second;

@@ -161,6 +161,75 @@ void launch_cdot_re(const CDotOp* ops, int nops, double* out, cudaStream_t s) {
   g_tebd_launches.fetch_add(1);
 }
 
+// ---- complex density-matrix split (G = M^H M, batched Hermitian eigensolver, U = M V / s)
+__global__ void k_cgram_pad(const CGramPad* __restrict__ ops) {
+  const CGramPad o = ops[blockIdx.x];
+  for (int i = o.n + threadIdx.x; i < o.nc; i += blockDim.x) o.A[i + (int64_t)i * o.nc] = make_double2(-1.0, 0.0);
+}
+void launch_cgram_pad(const CGramPad* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_cgram_pad<<<nops, 128, 0, s>>>(ops);
+  g_tebd_launches.fetch_add(1);
+}
+// The n non-padding eigenvalues of the slot (any order) ranked descending (ties by index); V column
+// rank = the eigenvector, S[rank] = sqrt(lambda) or 0 below the resolution floor 32 n eps lambda_max.
+__global__ void k_cgram_post(const CGramPost* __restrict__ ops) {
+  const CGramPost o = ops[blockIdx.x];
+  const int n = o.n, nc = o.nc;
+  __shared__ double lmax_s;
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int j = 0; j < nc; ++j) m = fmax(m, o.lam[j]);
+    lmax_s = m;
+  }
+  __syncthreads();
+  const double floor_l = 32.0 * n * DBL_EPSILON * lmax_s;
+  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+    const double lj = o.lam[j];
+    if (!(lj > -0.5)) continue;  // padding
+    int rank = 0;
+    for (int l = 0; l < nc; ++l) {
+      const double ll = o.lam[l];
+      rank += (ll > -0.5) && (ll > lj || (ll == lj && l < j));
+    }
+    if (rank >= n) continue;
+    o.S[rank] = lj > floor_l ? sqrt(lj) : 0.0;
+    const double2* w = o.W + (int64_t)j * nc;
+    double2* v = o.V + (int64_t)rank * n;
+    for (int r = 0; r < n; ++r) v[r] = w[r];
+  }
+}
+void launch_cgram_post(const CGramPost* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_cgram_post<<<nops, 128, 0, s>>>(ops);
+  g_tebd_launches.fetch_add(1);
+}
+// S_j = |M v_j| (the value the pair carries), u_j = M v_j / S_j; unresolved columns (S_j == 0) cleared.
+__global__ void k_ccolnorm(const CColNorm* __restrict__ ops) {
+  const CColNorm o = ops[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int j = warp; j < o.k; j += nwarp) {
+    double2* u = o.U + (int64_t)j * o.ldu;
+    if (o.S[j] == 0.0) {
+      for (int r = lane; r < o.m; r += 32) u[r] = make_double2(0.0, 0.0);
+      continue;
+    }
+    double acc = 0.0;
+    for (int r = lane; r < o.m; r += 32) acc = fma(u[r].x, u[r].x, fma(u[r].y, u[r].y, acc));
+    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    const double nrm = sqrt(acc);
+    const double inv = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    for (int r = lane; r < o.m; r += 32) u[r] = make_double2(u[r].x * inv, u[r].y * inv);
+    __syncwarp();
+    if (lane == 0) o.S[j] = nrm;
+  }
+}
+void launch_ccolnorm(const CColNorm* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_ccolnorm<<<nops, 256, 0, s>>>(ops);
+  g_tebd_launches.fetch_add(1);
+}
+
 // dst = 1 / src (0 where src is 0: padding)
 __global__ void k_recip(double* dst, const double* src, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

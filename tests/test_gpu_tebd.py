@@ -53,3 +53,33 @@ def test_tebd_matches_oracle(ctx, N, steps, chimax, doTrunc):
     assert err_sz < 1e-10 and err_lam < 1e-10
     assert abs(got.measure_diag(N // 2, SZ)) < 0.5 - 1e-3  # the state evolved
     got.close()
+
+
+@pytest.mark.parametrize("N,steps,chimax", [(10, 12, 64), (14, 20, 12), (14, 20, 64)])
+def test_tebd_density_split_matches_oracle(ctx, N, steps, chimax):
+    """The density-matrix split (complex Gram matrix, batched Hermitian eigensolver, U = M V / s):
+    a singular value s carries an absolute error ~ eps s_max^2 / s, so the comparison is at 1e-8."""
+    dt = 0.05
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 4, 0.8, 1.2), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    local = M.neel_state(N)
+    ref = O.TEBD(local, W, ik)
+    ref.second_order(steps, dt, chimax, doTrunc=True, tr_weight=1e-10)
+    ctx.set_svd_method("density")
+    try:
+        got = api.TEBDengine(local, W, ik, ctx=ctx)
+        got.second_order(steps, dt, chimax, doTrunc=True, tr_weight=1e-10)
+        err_sz = max(abs(got.measure_diag(s, SZ) - ref.measure_diag(s, SZ)) for s in range(N))
+        err_lam = 0.0
+        for b in range(N - 1):
+            lg, lo = got.lam(b), ref.lam(b)
+            common = set(lg) & set(lo)
+            for q in common:
+                a, c = np.sort(np.asarray(lg[q]))[::-1], np.sort(np.asarray(lo[q]))[::-1]
+                k = min(len(a), len(c))
+                err_lam = max(err_lam, np.abs(a[:k] - c[:k]).max())
+        print(f"density split N={N} chimax={chimax}: <Sz> err {err_sz:.2e}, lambda err {err_lam:.2e}, {got.stats()}")
+        assert err_sz < 1e-8 and err_lam < 1e-8
+        got.close()
+    finally:
+        ctx.set_svd_method("jacobi")
