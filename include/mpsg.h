@@ -247,6 +247,10 @@ mpsg_status mpsg_tebd_gamma_export(mpsg_tebd e, int32_t site, uint64_t* q, uint3
                                    int32_t* cols, double* data_interleaved);
 /* wall seconds of the evolution, of the split part, and bond updates applied. */
 mpsg_status mpsg_tebd_stats(mpsg_tebd e, double* seconds, double* split_seconds, int64_t* gates);
+/* 1 (default): the disjoint bonds of a time slice are updated together (one theta formation, split
+ * and scatter for the slice, gates / truncation / normalisation per bond); 0: one bond at a time
+ * (doTimeSlice order).  The results are the same. */
+mpsg_status mpsg_tebd_set_batch_layers(mpsg_tebd e, int32_t batch_layers);
 void mpsg_tebd_destroy(mpsg_tebd e);
 /* MPO::getNNGate: dense (d1 d2) x (d1 d2) gate exp(-(dt_im + i dt_re) h_b), index o1 + d1*o2,
  * column-major, interleaved complex -- src/MPOTypes.hpp:1090-1209. */

@@ -360,6 +360,9 @@ class TEBDengine:
             C.byref(val), grad.ctypes.data_as(C.c_void_p)))
         return val.value, grad
 
+    def set_batch_layers(self, on=True):
+        check(self.ctx.L.mpsg_tebd_set_batch_layers(self.h, int(bool(on))))
+
     def adjoint_seconds(self):
         s = C.c_double()
         check(self.ctx.L.mpsg_tebd_adjoint_seconds(self.h, C.byref(s)))

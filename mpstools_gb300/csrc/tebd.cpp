@@ -255,6 +255,13 @@ mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt
   API_END
 }
 
+mpsg_status mpsg_tebd_set_batch_layers(mpsg_tebd e, int32_t batch_layers) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e, "null engine");
+  e->e->batch_layers = batch_layers != 0;
+  API_END
+}
+
 mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds) {
   API_BEGIN
   MPSG_CHECK(e && e->e && seconds, "null argument");

@@ -47,6 +47,76 @@ inline TensorP make_ctensor(Ctx* ctx, int nphys, Layout lay, bool zero) {
 inline double* re(const Tensor& t, int i) { return t.d + t.b[i].off; }
 inline double* im(const Tensor& t, int i) { return t.d + t.nelem + t.b[i].off; }
 
+// ---------------------------------------------------------------- direct sums of independent bonds
+// Part i's charges are shifted by i << 32; shifting keeps each part's key order and puts part i
+// after part i - 1, so a direct sum is the concatenation of the parts' planes.
+inline Layout shifted_layout(const std::vector<const Tensor*>& parts) {
+  Layout lay;
+  for (size_t i = 0; i < parts.size(); ++i)
+    for (const Block& b : parts[i]->b) {
+      MPSG_CHECK(b.k.q0 < ((Q)1 << 32) && b.k.q1 < ((Q)1 << 32), "charge too large for a bond direct sum");
+      BKey k = b.k;
+      k.q0 += (Q)i << 32;
+      k.q1 += (Q)i << 32;
+      lay.add(k, b.r, b.c);
+    }
+  return lay;
+}
+// planes = 2 for planar complex tensors, 1 for real ones
+inline TensorP bond_sum(Ctx* ctx, const std::vector<const Tensor*>& parts, int nphys, int planes) {
+  Layout lay = shifted_layout(parts);
+  TensorP t;
+  if (planes == 2) {
+    t = make_ctensor(ctx, nphys, lay, false);
+  } else {
+    lay.finalize();
+    t = make_tensor(ctx, nphys, lay, false);
+  }
+  int64_t pre = 0;
+  size_t j = 0;
+  for (const Tensor* p : parts) {
+    for (const Block& b : p->b) MPSG_CHECK(t->b[j++].off == pre + b.off, "bond direct sum is not a concatenation");
+    MPSG_CHECK(pre + p->nelem <= t->nelem, "bond direct sum smaller than its parts");
+    for (int pl = 0; pl < planes; ++pl)
+      if (p->nelem > 0)
+        MPSG_CUDA(cudaMemcpyAsync(t->d + pl * t->nelem + pre, p->d + pl * p->nelem, sizeof(double) * p->nelem,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+    pre += p->nelem;
+  }
+  return t;
+}
+inline TensorP bond_part(Ctx* ctx, const Tensor& t, int i, int planes) {
+  Layout lay;
+  int j0 = -1, j1 = -1;
+  for (int j = 0; j < (int)t.b.size(); ++j) {
+    const Block& b = t.b[j];
+    if ((b.k.q0 >> 32) != (Q)i) continue;
+    if (j0 < 0) j0 = j;
+    j1 = j + 1;
+    BKey k = b.k;
+    k.q0 -= (Q)i << 32;
+    k.q1 -= (Q)i << 32;
+    lay.add(k, b.r, b.c);
+  }
+  TensorP o;
+  if (planes == 2) {
+    o = make_ctensor(ctx, t.nphys, lay, false);
+  } else {
+    lay.finalize();
+    o = make_tensor(ctx, t.nphys, lay, false);
+  }
+  if (j0 >= 0) {
+    const int64_t off0 = t.b[j0].off;
+    for (int j = j0; j < j1; ++j) MPSG_CHECK(o->b[j - j0].off == t.b[j].off - off0, "bond part is not contiguous");
+    MPSG_CHECK(off0 + o->nelem <= t.nelem, "bond part outside the direct sum");
+    for (int pl = 0; pl < planes; ++pl)
+      if (o->nelem > 0)
+        MPSG_CUDA(cudaMemcpyAsync(o->d + pl * o->nelem, t.d + pl * t.nelem + off0, sizeof(double) * o->nelem,
+                                  cudaMemcpyDeviceToDevice, ctx->stream));
+  }
+  return o;
+}
+
 // ---------------------------------------------------------------- gate (host)
 // Dense (d1 d2) x (d1 d2) gate, index o1 + d1*o2, column-major.
 struct CGate {
@@ -80,6 +150,13 @@ struct TebdEngine {
   std::vector<TensorP> lam;  // lam[b + 1] = lambda of bond b (b = -1 .. N-1), real, blocks (q, q) n x 1
   double seconds = 0, split_seconds = 0, adjoint_seconds = 0;
   int64_t gates = 0;
+  // Layer batching: when seg_gates is set, the engine holds a direct sum of independent bonds (bond i's
+  // charges shifted by i << 32), block (q0, ...) uses the gate seg_gates[q0 >> 32], and truncation and
+  // normalisation run per bond; seg_tw / seg_chi receive the per-bond results.
+  std::vector<const CGate*> seg_gates;
+  std::vector<double> seg_tw;
+  std::vector<int> seg_chi;
+  bool batch_layers = true;  // slice(): one split per layer (direct sum over its bonds)
 
   const double* lam_ptr(const Tensor& l, Q q, int* n) const {
     const int i = l.find(K1(q, q, 0));
@@ -351,9 +428,10 @@ struct TebdEngine {
     std::map<BKey, std::vector<std::pair<int, cplx>>> gt;
     for (int i = 0; i < (int)th->b.size(); ++i) {
       const Block& b = th->b[i];
-      for (int o2 = 0; o2 < gate.d2; ++o2)
-        for (int o1 = 0; o1 < gate.d1; ++o1) {
-          const cplx gv = gate.at(o1, o2, (int)b.k.p0, (int)b.k.p1);
+      const CGate& gb = seg_gates.empty() ? gate : *seg_gates.at((size_t)(b.k.q0 >> 32));
+      for (int o2 = 0; o2 < gb.d2; ++o2)
+        for (int o1 = 0; o1 < gb.d1; ++o1) {
+          const cplx gv = gb.at(o1, o2, (int)b.k.p0, (int)b.k.p1);
           if (gv == cplx(0, 0)) continue;
           gt[K2(b.k.q0, b.k.q1, (uint32_t)o1, (uint32_t)o2)].push_back({i, gv});
         }
@@ -488,34 +566,62 @@ struct TebdEngine {
     // global truncation (DiagBlockMatrix::truncate, same rank rule as the real split)
     if (!chimax && doTrunc) chimax = 100;
     if (!chimax && !doTrunc) chimax = 200;
+    // sectors of one bond are contiguous (centre charges ascend, bond i in [i << 32, (i + 1) << 32))
+    const int nseg = seg_gates.empty() ? 1 : (int)seg_gates.size();
+    std::vector<int> seg_of_sec(qcs.size(), 0), s0(nseg + 1, (int)qcs.size());
+    if (!seg_gates.empty())
+      for (size_t si = 0; si < qcs.size(); ++si) {
+        seg_of_sec[si] = (int)(qcs[si] >> 32);
+        MPSG_CHECK(seg_of_sec[si] < nseg, "centre charge outside the bonds of the layer");
+      }
+    for (int si = (int)qcs.size() - 1; si >= 0; --si) s0[seg_of_sec[si]] = si;
+    for (int c = nseg - 1; c >= 0; --c) s0[c] = std::min(s0[c], s0[c + 1]);
+    std::vector<int64_t> offS_of(qcs.size() + 1, oS);
     std::vector<int32_t> sec_of(oS);
     {
       int si = 0;
       for (auto& x : secs) {
-        for (int j = 0; j < x.second.k; ++j) sec_of[x.second.offS + j] = si;
+        offS_of[si] = x.second.offS;
+        for (int j = 0; j < x.second.k; ++j) sec_of[x.second.offS + j] = si - s0[seg_of_sec[si]];
         ++si;
       }
     }
     const int nS = (int)oS;
-    int32_t* dsec = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (std::max(nS, 1) * 3 + qcs.size() + 1));
+    int32_t* dsec = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (std::max(nS, 1) * 3 + qcs.size() + 1) +
+                                           sizeof(double) * 3 * (nseg + 1));
     int32_t* drank = dsec + std::max(nS, 1);
     int32_t* dcnt = drank + 2 * std::max(nS, 1);
-    double* dout3 = ctx->part + kRedBlocks;
+    double* dout3 = (double*)(((uintptr_t)(dcnt + qcs.size() + 1) + 7) & ~(uintptr_t)7);
     if (nS) MPSG_CUDA(cudaMemcpyAsync(dsec, sec_of.data(), sizeof(int32_t) * nS, cudaMemcpyHostToDevice, ctx->stream));
-    launch_truncate(dS, nS, dsec, (int)qcs.size(), chimax, doTrunc ? 1 : 0, tr_weight, drank, dcnt, dout3, ctx->stream);
+    MPSG_CUDA(cudaMemsetAsync(dout3, 0, sizeof(double) * 3 * nseg, ctx->stream));
+    for (int c = 0; c < nseg; ++c) {
+      const int a = s0[c], b = s0[c + 1];
+      if (a >= b) continue;
+      const int64_t v0 = offS_of[a], v1 = offS_of[b];
+      launch_truncate(dS + v0, (int)(v1 - v0), dsec + v0, b - a, chimax, doTrunc ? 1 : 0, tr_weight, drank + 2 * v0,
+                      dcnt + a, dout3 + 3 * c, ctx->stream);
+    }
     std::vector<int32_t> counts(qcs.size() + 1, 0);
     std::vector<int> info(qcs.size() + 1, 0);
+    std::vector<double> out3(3 * nseg, 0.0);
     if (!qcs.empty()) {
       MPSG_CUDA(cudaMemcpyAsync(counts.data(), dcnt, sizeof(int32_t) * qcs.size(), cudaMemcpyDeviceToHost, ctx->stream));
       MPSG_CUDA(cudaMemcpyAsync(info.data(), dinfo, sizeof(int) * qcs.size(), cudaMemcpyDeviceToHost, ctx->stream));
     }
-    MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dout3, sizeof(double) * 3, cudaMemcpyDeviceToHost, ctx->stream));
+    MPSG_CUDA(cudaMemcpyAsync(out3.data(), dout3, sizeof(double) * 3 * nseg, cudaMemcpyDeviceToHost, ctx->stream));
     ctx->sync();
     for (size_t i = 0; i < qcs.size(); ++i)
       if (info[i] < 0) throw Err(3, "zgesvdj: invalid argument (info=" + std::to_string(info[i]) + ")");
-    const double tw = ctx->hscal[0];
-    const int chi = (int)ctx->hscal[1];
-    const double inv_norm = normalize ? ctx->hscal[2] : 1.0;
+    seg_tw.assign(nseg, 0.0);
+    seg_chi.assign(nseg, 0);
+    std::vector<double> inv_norm_seg(nseg, 1.0);
+    for (int c = 0; c < nseg; ++c) {
+      seg_tw[c] = out3[3 * c];
+      seg_chi[c] = (int)out3[3 * c + 1];
+      if (normalize) inv_norm_seg[c] = out3[3 * c + 2];
+    }
+    const double tw = seg_tw[0];
+    const int chi = seg_chi[0];
     ctx->dfree(dsec);
     // U, Vt and lambda (dropDangling: sectors without kept values vanish)
     Layout lu, lv, ll2;
@@ -553,7 +659,8 @@ struct TebdEngine {
                                   r.second.second, s.n, c, 1});
         }
         const int ol = lnew->find(K1(qc, qc, 0));
-        lo.push_back(CopyOp{dS + s.offS, lnew->d + lnew->b[ol].off, nullptr, nullptr, c, 1, c, c, 0, inv_norm});
+        lo.push_back(CopyOp{dS + s.offS, lnew->d + lnew->b[ol].off, nullptr, nullptr, c, 1, c, c, 0,
+                            inv_norm_seg[seg_of_sec[si - 1]]});
       }
       if (!so.empty()) {
         CScatterOp* d = (CScatterOp*)ctx->dmalloc(sizeof(CScatterOp) * so.size());
@@ -590,8 +697,43 @@ struct TebdEngine {
     return {tw, chi};
   }
 
+  // doTimeSlice: the gates of one parity.  The bonds of a slice are disjoint, so with batch_layers
+  // they are applied at once to the direct sum of the bonds (one theta formation, one split, one
+  // scatter for the whole slice; gate, truncation and normalisation per bond).
   void slice(const std::vector<CGate>& gates_, int start, int chimax, bool doTrunc, double tr_weight, bool normalize) {
-    for (int site = start; site < N - 1; site += 2) apply_gate(site, gates_[site], chimax, doTrunc, tr_weight, normalize);
+    std::vector<int> sites;
+    for (int site = start; site < N - 1; site += 2) sites.push_back(site);
+    bool uniform = true;
+    for (int s : sites) uniform = uniform && ik[s] == ik[sites[0]] && ik[s + 1] == ik[sites[0] + 1];
+    if (!batch_layers || sites.size() < 2 || !uniform) {
+      for (int site : sites) apply_gate(site, gates_[site], chimax, doTrunc, tr_weight, normalize);
+      return;
+    }
+    std::vector<const Tensor *> gl, gr, ll, lc, lr;
+    for (int s : sites) {
+      gl.push_back(G[s].get());
+      gr.push_back(G[s + 1].get());
+      ll.push_back(lam[s].get());
+      lc.push_back(lam[s + 1].get());
+      lr.push_back(lam[s + 2].get());
+    }
+    TebdEngine t;
+    t.ctx = ctx;
+    t.keep = keep;
+    t.N = 2;
+    t.ik = {ik[sites[0]], ik[sites[0] + 1]};
+    t.G = {bond_sum(ctx, gl, 1, 2), bond_sum(ctx, gr, 1, 2)};
+    t.lam = {bond_sum(ctx, ll, 0, 1), bond_sum(ctx, lc, 0, 1), bond_sum(ctx, lr, 0, 1)};
+    for (int s : sites) t.seg_gates.push_back(&gates_[s]);
+    t.apply_gate(0, gates_[sites[0]], chimax, doTrunc, tr_weight, normalize);
+    for (size_t i = 0; i < sites.size(); ++i) {
+      const int s = sites[i];
+      G[s] = bond_part(ctx, *t.G[0], (int)i, 2);
+      G[s + 1] = bond_part(ctx, *t.G[1], (int)i, 2);
+      lam[s + 1] = bond_part(ctx, *t.lam[1], (int)i, 1);
+    }
+    split_seconds += t.split_seconds;
+    gates += (int64_t)sites.size();
   }
   std::vector<CGate> make_gates(double dt) const {
     std::vector<CGate> g;

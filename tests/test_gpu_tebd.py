@@ -83,3 +83,30 @@ def test_tebd_density_split_matches_oracle(ctx, N, steps, chimax):
         got.close()
     finally:
         ctx.set_svd_method("jacobi")
+
+
+@pytest.mark.parametrize("svd", ["jacobi", "density"])
+def test_tebd_layer_batching_matches_bond_by_bond(ctx, svd):
+    """A time slice updated as one direct sum of its bonds gives the bond-by-bond results."""
+    N, steps, dt, chimax = 14, 20, 0.05, 24
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 4, 0.8, 1.2), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    ctx.set_svd_method(svd)
+    try:
+        out = []
+        for batched in (False, True):
+            e = api.TEBDengine(M.neel_state(N), W, ik, ctx=ctx)
+            e.set_batch_layers(batched)
+            e.second_order(steps, dt, chimax, doTrunc=True, tr_weight=1e-10)
+            out.append(([e.measure_diag(s, SZ) for s in range(N)], [e.lam(b) for b in range(N - 1)], e.stats()))
+            e.close()
+        (sz0, l0, st0), (sz1, l1, st1) = out
+        print(f"{svd}: bond by bond {st0['seconds']:.3f} s, batched slices {st1['seconds']:.3f} s")
+        assert max(abs(a - b) for a, b in zip(sz0, sz1)) < 1e-12
+        for a, b in zip(l0, l1):
+            assert set(a) == set(b)
+            for q in a:
+                assert len(a[q]) == len(b[q])
+                assert np.abs(np.sort(a[q]) - np.sort(b[q])).max() < 1e-12
+    finally:
+        ctx.set_svd_method("jacobi")
