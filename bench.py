@@ -520,6 +520,59 @@ def chains_arm(args):
     print(json.dumps(out))
 
 
+def tebd_arm(args):
+    """TEBD of the XXZ chain L=64 from the Neel state, second order, dt=0.05, chi <= 512, truncation
+    1e-10 (density-matrix split, slices batched): forward time, the gradient of <Sz_32(T)> w.r.t. the
+    63 per-bond anisotropies (Delta_i ~ U[0.8,1.2], seed 4) by the adjoint, and central differences
+    (h = 1e-5) of the same evolution on `--fd-bonds` bonds."""
+    from mpstools_gb300 import api, lib, models as M
+    N, dt, chimax, trw, obs = 64, 0.05, 512, 1e-10, 32
+    steps = args.tebd_steps
+    sz = [-0.5, 0.5]
+    ctx = lib.Context(0)
+    ctx.set_svd_method("density")
+    theta = 0.8 + 0.4 * M.uniform01(4, N - 1)
+    ik = M.u1_itokeys(N)
+    mk = lambda t: M.heisenberg_mpo(t, np.ones(N - 1), np.zeros(N))
+
+    def forward(t):
+        e = api.TEBDengine(M.neel_state(N), mk(t), ik, ctx=ctx)
+        t0 = time.perf_counter()
+        e.second_order(steps, dt, chimax, doTrunc=True, tr_weight=trw)
+        sec = time.perf_counter() - t0
+        v = e.measure_diag(obs, sz)
+        chis = [sum(len(x) for x in e.lam(b).values()) for b in range(N - 1)]
+        st = e.stats()
+        e.close()
+        return v, sec, max(chis), st
+
+    v0, t_fwd, chi_max, st = forward(theta)
+    dh = api.couplingDerivatives(mk, theta, ik)
+    e = api.TEBDengine(M.neel_state(N), mk(theta), ik, ctx=ctx)
+    t0 = time.perf_counter()
+    v_adj, grad = e.adjoint_second_order(steps, dt, chimax, obs, sz, dh, doTrunc=True, tr_weight=trw)
+    t_adj = time.perf_counter() - t0
+    e.close()
+    h, fd = 1e-5, {}
+    for b in args.fd_bonds:
+        tp, tm = theta.copy(), theta.copy()
+        tp[b] += h
+        tm[b] -= h
+        fd[b] = (forward(tp)[0] - forward(tm)[0]) / (2 * h)
+    out = {"metric": "TEBD second-order steps per second (XXZ L=64, chi<=512)", "impl": "ours",
+           "value": steps / t_fwd, "unit": "steps/s", "higher_is_better": True, "n_gpus": 1, "dtype": "c128",
+           "data": "synthetic",
+           "config": {"workload": "tebd_xxz_L64_neel_dt0.05_chi512", "steps": steps, "dt": dt, "chimax": chimax,
+                      "tr_weight": trw, "observable": "Sz_32", "couplings": "Delta_i ~ U[0.8,1.2] seed 4",
+                      "svd": "density (complex Gram, batched Hermitian eigensolver), slices batched"},
+           "forward_seconds": t_fwd, "max_chi": chi_max, "value_Sz32": v0, "gates": st["gates"],
+           "split_seconds": st["split_seconds"],
+           "adjoint": {"seconds_forward_plus_gradient": t_adj, "value": v_adj, "grad_max_abs": float(np.abs(grad).max()),
+                       "grad_bonds_fd": {str(b): {"adjoint": float(grad[b]), "central_difference": float(fd[b])}
+                                         for b in fd}}}
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,14 +589,19 @@ def main():
                     help="skip the plain FP64 GPU path timed on the same updates (mixed precisions only)")
     ap.add_argument("--steps-only", action="store_true",
                     help="time the DMRG steps only (no roofline / e2e / CPU legs); for profiler launch lists")
-    ap.add_argument("--workload", default="centre_update", choices=["centre_update", "chains"],
-                    help="chains: batched independent chains (--nchains, --sweeps, --seq-chains; --chi 256)")
+    ap.add_argument("--workload", default="centre_update", choices=["centre_update", "chains", "tebd"],
+                    help="chains: batched independent chains (--nchains, --sweeps, --seq-chains; --chi 256); "
+                         "tebd: L=64 TEBD forward + adjoint gradient (--tebd-steps, --fd-bonds)")
+    ap.add_argument("--tebd-steps", type=int, default=200)
+    ap.add_argument("--fd-bonds", type=int, nargs="*", default=[31])
     ap.add_argument("--nchains", type=int, default=64)
     ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--seq-chains", type=int, default=8)
     args = ap.parse_args()
     if args.workload == "chains":
         chains_arm(args)
+    elif args.workload == "tebd":
+        tebd_arm(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:
