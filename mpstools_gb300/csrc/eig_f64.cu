@@ -448,16 +448,22 @@ __device__ void tri_shift_solve(int n, double* x, const double* u0, const double
 }
 
 // Eigenvectors of T by inverse iteration: three iterations from a deterministic pseudo-random start
-// with one LU of T - lambda I.  Eigenvalues closer than kClusterGap * tnorm to their predecessor
-// (descending order) form a cluster: the thread of the cluster's first eigenvalue computes all its
-// vectors one after another and orthogonalises each iterate against the cluster's earlier vectors
-// (modified Gram-Schmidt), as LAPACK's dstein does, so that (near-)degenerate eigenvalues do not
-// yield the same vector twice; the other threads of the cluster return.  The caller still
-// re-orthonormalises the eigenvector matrix (CholeskyQR).  Z column k receives the vector of W[k];
-// columns below the floor are zero.
-constexpr double kClusterGap = 1e-11;
+// with one LU of T - lambda I.  Eigenvalues that bisection cannot tell apart (within kClusterGap *
+// ||T|| of their predecessor in descending order, a few eps) form a cluster, handled in groups of at
+// most kMaxGroup consecutive members: the thread of a group's first member computes the group's
+// vectors one after another and orthogonalises each iterate against the group's earlier vectors
+// (modified Gram-Schmidt, as LAPACK's dstein does), so that degenerate eigenvalues do not yield the
+// same vector twice; the group's other threads return.  The caller still re-orthonormalises the
+// eigenvector matrix (CholeskyQR).  Z column k receives the vector of W[k]; columns below the floor
+// are zero.
+constexpr double kClusterGap = 16.0 * DBL_EPSILON;
+constexpr int kMaxGroup = 32;
 
-__device__ void invit_one(const TriOp& o, int k, double tnorm, double* z, double* base) {
+__device__ __forceinline__ bool same_cluster(const TriOp& o, int j, double tnorm) {  // W[j - 1] ~ W[j]
+  return j > 0 && o.W[j - 1] >= 0.0 && o.W[j] >= 0.0 && o.W[j - 1] - o.W[j] <= kClusterGap * tnorm;
+}
+
+__device__ void invit_one(const TriOp& o, int k, int k_first, double tnorm, double* z, double* base) {
   const int n = o.n;
   double *u0 = base, *u1 = base + n, *u2 = base + 2 * n, *mul = base + 3 * n;
   unsigned char* piv = (unsigned char*)(base + 4 * n);
@@ -465,9 +471,7 @@ __device__ void invit_one(const TriOp& o, int k, double tnorm, double* z, double
   tri_shift_factor(o.d, o.e, n, o.W[k], tnorm, u0, u1, u2, mul, piv);
   for (int it = 0; it < 3; ++it) {
     tri_shift_solve(n, z, u0, u1, u2, mul, piv);
-    // orthogonalise against the earlier vectors of the cluster (columns k0 .. k-1, already final)
-    for (int j = k - 1; j >= 0; --j) {
-      if (!(o.W[j] >= 0.0) || o.W[j] - o.W[j + 1] > kClusterGap * tnorm) break;
+    for (int j = k - 1; j >= k_first; --j) {  // the group's earlier vectors (already final)
       const double* y = o.Z + (int64_t)j * o.ldz;
       double dot = 0.0;
       for (int i = 0; i < n; ++i) dot = fma(y[i], z[i], dot);
@@ -498,14 +502,12 @@ __global__ void k_tri_invit(const TriOp* __restrict__ ops, const int* __restrict
     for (int i = 0; i < n; ++i) z[i] = 0.0;
     return;
   }
-  // a member of a cluster that started earlier is computed by the cluster's first thread
-  if (k > 0 && o.W[k - 1] >= 0.0 && o.W[k - 1] - o.W[k] <= kClusterGap * tnorm) return;
+  int c0 = k;  // first member of the cluster
+  while (same_cluster(o, c0, tnorm)) --c0;
+  if ((k - c0) % kMaxGroup != 0) return;  // computed by the first thread of its group
   double* base = scratch + scratch_off[t];
-  int m = k;
-  do {
-    invit_one(o, m, tnorm, o.Z + (int64_t)m * o.ldz, base);
-    ++m;
-  } while (m < n && o.W[m] >= 0.0 && o.W[m - 1] - o.W[m] <= kClusterGap * tnorm);
+  for (int m = k; m < n && m < k + kMaxGroup && (m == k || same_cluster(o, m, tnorm)); ++m)
+    invit_one(o, m, k, tnorm, o.Z + (int64_t)m * o.ldz, base);
 }
 void launch_tri_invit(const TriOp* ops, const int* op_of, const int* k_of, int nthreads, double gap_rel,
                       double* scratch, const int64_t* scratch_off, cudaStream_t s) {
