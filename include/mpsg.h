@@ -283,6 +283,14 @@ mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt
 /* wall seconds spent in mpsg_tebd_adjoint_second_order (forward, recomputation and backward). */
 mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
+/* Portable checkpoint of the engine's state (what MPSBase::save keeps, src/MPSTypes.hpp:377-426, in a
+ * documented little-endian format instead of a Boost binary archive): per site the charge map, the
+ * MPO tensor and the site tensor, then the lambdas.  Format "MPSGCKP1": see checkpoint.cpp; the
+ * Python module mpstools_gb300.checkpoint reads and writes the same files (e.g. for states made by
+ * the CPU oracle).  mpsg_dmrg_load creates an engine on ctx; simulate() or build_environments()
+ * continues from the loaded state. */
+mpsg_status mpsg_dmrg_save(mpsg_dmrg e, const char* path);
+mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out);
 
 /* ---------------------------------------------------------------- batched chains
  * Many independent DMRGengine runs (src/container.hpp:292-438) in lockstep: every global step each

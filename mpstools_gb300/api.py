@@ -16,6 +16,7 @@ terms (wl, wr, out, in, value).  All arithmetic runs on the GPU.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -164,6 +165,26 @@ class DMRGengine:
         check(ctx.L.mpsg_dmrg_create(ctx.h, self.N, harr, marr, karr, C.byref(h)))
         self.h = h
         check(ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
+
+    def save(self, path):
+        """Write the state (site tensors, lambdas, charge maps, MPO) as an MPSGCKP1 checkpoint."""
+        check(self.ctx.L.mpsg_dmrg_save(self.h, os.fsencode(path)))
+
+    @classmethod
+    def load(cls, path, prec="fp64", reorth=False, lanmax=500, ctx=None):
+        """An engine holding the state of an MPSGCKP1 checkpoint (written by save() or by
+        mpstools_gb300.checkpoint.save)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        check(self.ctx.L.mpsg_dmrg_load(self.ctx.h, os.fsencode(path), C.byref(h)))
+        self.h = h
+        from . import checkpoint
+        hdr = checkpoint.read_header(path)
+        self.N = hdr["N"]
+        self._tensors, self._mpos, self._iks = [], [], []
+        check(self.ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
+        return self
 
     def simulate(self, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12, delta=1e-13,
                  testenergy=True):
