@@ -283,6 +283,13 @@ mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt
 /* wall seconds spent in mpsg_tebd_adjoint_second_order (forward, recomputation and backward). */
 mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
+/* SSDMRGengine::simulate (src/container.hpp:827-925): single-site DMRG (no bond growth) from the
+ * engine's state: orthonormalize("rl"), sweeps until |dE| < EnConv or more than maxsteps sweeps, then
+ * doStep(0, -1); E = the last step's energy.  Each update is SSLanzcosEngine on one site
+ * (contractSingle, src/MPSfunctions.hpp:857-885) and prepareSite without truncation; the matvec
+ * precision of mpsg_dmrg_set_options applies. */
+mpsg_status mpsg_dmrg_ss_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, double delta, int32_t testenergy,
+                                  double* E);
 /* Portable checkpoint of the engine's state (what MPSBase::save keeps, src/MPSTypes.hpp:377-426, in a
  * documented little-endian format instead of a Boost binary archive): per site the charge map, the
  * MPO tensor and the site tensor, then the lambdas.  Format "MPSGCKP1": see checkpoint.cpp; the

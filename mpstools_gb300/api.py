@@ -166,6 +166,13 @@ class DMRGengine:
         self.h = h
         check(ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
 
+    def ss_simulate(self, maxsteps=5, EnConv=1e-10, delta=1e-12, testenergy=True):
+        """SSDMRGengine::simulate: single-site sweeps (no bond growth) from the engine's state."""
+        E = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_ss_simulate(self.h, int(maxsteps), float(EnConv), float(delta), int(testenergy),
+                                                C.byref(E)))
+        return E.value
+
     def save(self, path):
         """Write the state (site tensors, lambdas, charge maps, MPO) as an MPSGCKP1 checkpoint."""
         check(self.ctx.L.mpsg_dmrg_save(self.h, os.fsencode(path)))

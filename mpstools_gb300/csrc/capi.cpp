@@ -287,6 +287,14 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
   *out = d;
   API_END
 }
+mpsg_status mpsg_dmrg_ss_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, double delta, int32_t testenergy,
+                                  double* E) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e && E, "null argument");
+  MPSG_CHECK(EnConv > 0, "EnConv must be > 0");
+  *E = e->e->ss_simulate((int)maxsteps, EnConv, delta, testenergy != 0);
+  API_END
+}
 mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax) {
   API_BEGIN
   MPSG_CHECK(e && e->e, "null engine");

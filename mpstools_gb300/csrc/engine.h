@@ -178,6 +178,104 @@ struct Engine {
     return out.E;
   }
 
+  // ---------------------------------------------------------------- single-site DMRG
+  // SSDMRGengine::doStep (src/container.hpp:865-883): SSLanzcosEngine on site with L[site-1] and
+  // R[site+1] (contractSingle, src/MPSfunctions.hpp:857-885), prepareSite "l" (dir > 0, D Vd into the
+  // right neighbour) or "r" (dir <= 0, U D into the left neighbour) without truncation, then the
+  // environment update.  contractSingle is the two-site matvec with a dummy second site: an identity
+  // MPO tensor carrying the right MPO channel and a one-state local space of charge 0, so the
+  // grouped matvec, its closure and every Lanczos precision serve the single-site update unchanged.
+  StepRec ss_do_step(int site, int dir, double delta, bool testenergy) {
+    MPSG_CHECK(site >= 0 && site < N, "site out of range");
+    MPSG_CHECK(L.count(site - 1) && R.count(site + 1), "environments missing (single-site)");
+    const Tensor& Le = *L[site - 1];
+    const Tensor& Re = *R[site + 1];
+    const MPO& W1 = mpo[site];
+    MPO W2;  // identity on the right channels, one-state local space
+    W2.Dl = W2.Dr = W1.Dr;
+    for (int w = 0; w < W1.Dr; ++w) {
+      MPOEntry en;
+      en.wl = en.wr = (uint32_t)w;
+      en.ops.push_back(OpEl{0, 0, 1.0});
+      W2.e.push_back(en);
+    }
+    const ItoKey ikd(1, (Q)0);
+    const Tensor& A = *mps[site];
+    Layout s0;
+    for (auto& b : A.b) s0.add(K2(b.k.q0, b.k.q1, b.k.p0, 0), b.r, b.c);
+    s0.finalize();
+    Layout sx = theta_closure(Le, Re, s0, W1, W2, ik[site], ikd);
+    TensorP th = make_tensor(ctx, 2, sx, true);
+    {
+      std::vector<CopyOp> ops;
+      for (auto& b : A.b) {
+        const int j = th->find(K2(b.k.q0, b.k.q1, b.k.p0, 0));
+        ops.push_back(CopyOp{A.d + b.off, th->d + th->b[j].off, nullptr, nullptr, b.r, b.c, b.r, b.r, 0, 1.0});
+      }
+      run_copyops(ctx, ops);
+    }
+    TensorP psi = make_tensor(ctx, 2, sx, true);
+    LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, W1, W2, ik[site], ikd, *th, *psi, lanmax, delta, testenergy,
+                                    reorth, (int)prec, &lst);
+    th.reset();
+    // the ground state as a single-site tensor (every block of the closure)
+    Layout l1;
+    for (auto& b : psi->b) l1.add(K1(b.k.q0, b.k.q1, b.k.p0), b.r, b.c);
+    l1.finalize();
+    TensorP a = make_tensor(ctx, 1, l1, false);
+    MPSG_CHECK(a->nelem == psi->nelem, "single-site state layout mismatch");
+    MPSG_CUDA(cudaMemcpyAsync(a->d, psi->d, sizeof(double) * std::max<int64_t>(psi->nelem, 1), cudaMemcpyDeviceToDevice,
+                              ctx->stream));
+    psi.reset();
+    auto t0 = std::chrono::steady_clock::now();
+    mps[site] = a;
+    TensorP lamt;
+    if (dir > 0) {
+      prepare_matrix_l(ctx, mps[site], site + 1 < N ? &mps[site + 1] : nullptr, &lamt, 0.0);
+      lam[site] = lamt;
+    } else {
+      prepare_matrix_r(ctx, site > 0 ? &mps[site - 1] : nullptr, mps[site], &lamt, 0.0);
+      lam[site - 1] = lamt;
+    }
+    ctx->sync();
+    auto t1 = std::chrono::steady_clock::now();
+    split_seconds += std::chrono::duration<double>(t1 - t0).count();
+    if (dir > 0) L[site] = env_update(ctx, *L[site - 1], *mps[site], mpo[site], ik[site], 1, &env_flops);
+    else R[site] = env_update(ctx, *R[site + 1], *mps[site], mpo[site], ik[site], -1, &env_flops);
+    ctx->sync();
+    env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+    int chi = 0;
+    if (lamt)
+      for (auto& b : lamt->b) chi += b.r;
+    StepRec r{site, dir, lr.iterations, chi, lr.E0, 0.0};
+    steps.push_back(r);
+    return r;
+  }
+
+  // SSDMRGengine::simulate (src/container.hpp:886-925): orthonormalize("rl"), computeR(mps, mpo, 1),
+  // sweeps 0 .. N-2 right and N-1 .. 1 left until the energy changes by less than EnConv or more than
+  // maxsteps sweeps were made (the reference's step > maxsteps test), then doStep(0, -1).
+  double ss_simulate(int maxsteps, double EnConv, double delta, bool testenergy) {
+    auto t0 = std::chrono::steady_clock::now();
+    prepare();
+    R[1] = env_update(ctx, *R[2], *mps[1], mpo[1], ik[1], 0, &env_flops);
+    double globalE = 1e100;
+    StepRec out{};
+    int step = 0;
+    while (true) {
+      for (int site = 0; site < N - 1; ++site) out = ss_do_step(site, 1, delta, testenergy);
+      for (int site = N - 1; site > 0; --site) out = ss_do_step(site, -1, delta, testenergy);
+      ++step;
+      bool conv = std::fabs(globalE - out.E) < EnConv;
+      if (step > maxsteps) conv = true;
+      globalE = out.E;
+      if (conv) break;
+    }
+    out = ss_do_step(0, -1, delta, testenergy);
+    wall += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return out.E;
+  }
+
   double measure_energy() { return measure(mpo); }
 
   // MPO::measure (src/MPOTypes.hpp:990-1020): left environments through the chain, then the sum of

@@ -1609,6 +1609,129 @@ void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, do
   if (lam_out) *lam_out = lam;
 }
 
+// ============================================================================ left canonicalisation
+// prepareMatrix(BL1, lambda, BL2, "l", multiply=true, truncate, delta) (src/MPSfunctions.hpp:21-142,
+// dir "l"): per right charge q the blocks (a, q; s) of BL1 stacked by rows form M_q = U D Vd; BL1
+// becomes U (left-orthonormal), lambda(q) = D, and D Vd multiplies the blocks (q, b; s) of BL2 from
+// the left (BL2 may be null at the right edge).  Singular values <= delta are dropped (delta = 0
+// keeps every nonzero one).
+void prepare_matrix_l(Ctx* ctx, TensorP& BL1, TensorP* BL2, TensorP* lam_out, double delta) {
+  std::map<Q, std::vector<int>> groups;  // right charge -> blocks (key order)
+  for (int i = 0; i < (int)BL1->b.size(); ++i) groups[BL1->b[i].k.q1].push_back(i);
+  std::vector<Q> keys;
+  std::vector<std::pair<int, int>> mn;
+  std::vector<std::vector<int>> rowoff;
+  for (auto& g : groups) {
+    int rows = 0;
+    const int cols = BL1->b[g.second[0]].c;
+    std::vector<int> ro;
+    for (int i : g.second) {
+      MPSG_CHECK(BL1->b[i].c == cols, "column mismatch inside a charge group");
+      ro.push_back(rows);
+      rows += BL1->b[i].r;
+    }
+    keys.push_back(g.first);
+    mn.push_back({rows, cols});
+    rowoff.push_back(ro);
+  }
+  SvdBatch sv(ctx);
+  sv.plan(mn);
+  std::vector<CopyOp> gops;
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    const auto& bl = groups[keys[gi]];
+    for (size_t t = 0; t < bl.size(); ++t) {
+      const Block& b = BL1->b[bl[t]];
+      gops.push_back(sv.gather_op((int)gi, BL1->d + b.off, b.r, b.c, rowoff[gi][t], 0));
+    }
+  }
+  run_copyops(ctx, gops);
+  sv.run(ctx->svd_method);
+  sv.check_info();
+  std::vector<double> S(std::max<int64_t>(sv.nS, 1));
+  if (sv.nS) MPSG_CUDA(cudaMemcpyAsync(S.data(), sv.dS, sizeof(double) * sv.nS, cudaMemcpyDeviceToHost, ctx->stream));
+  ctx->sync();
+  std::vector<int> keep(keys.size());
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    int l = 0;
+    while (l < sv.s[gi].k && std::fabs(S[sv.s[gi].offS + l]) > delta) ++l;
+    keep[gi] = l;
+  }
+  Layout l1, ll;
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    if (!keep[gi]) continue;
+    for (int i : groups[keys[gi]]) l1.add(BL1->b[i].k, BL1->b[i].r, keep[gi]);
+    ll.add(K1(keys[gi], keys[gi], 0), keep[gi], 1);
+  }
+  l1.finalize();
+  ll.finalize();
+  TensorP nb1 = make_tensor(ctx, 1, l1, false);
+  TensorP lam = make_tensor(ctx, 0, ll, false);
+  std::vector<CopyOp> ops;
+  KeyedArena<Q> dv;  // D Vd per group (keep x cols)
+  for (size_t gi = 0; gi < keys.size(); ++gi)
+    if (keep[gi]) dv.add(keys[gi], keep[gi], sv.s[gi].n);
+  double* dDV = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(dv.nelem, 2));
+  for (size_t gi = 0; gi < keys.size(); ++gi) {
+    const int l = keep[gi];
+    if (!l) continue;
+    int ldq, ldp;
+    double* Qm = sv.Qp((int)gi, &ldq);
+    double* Pm = sv.Pp((int)gi, &ldp);
+    const double* Sv = sv.dS + sv.s[gi].offS;
+    const auto& bl = groups[keys[gi]];
+    for (size_t t = 0; t < bl.size(); ++t) {
+      const Block& ob = nb1->b[nb1->find(BL1->b[bl[t]].k)];
+      ops.push_back(CopyOp{Qm + rowoff[gi][t], nb1->d + ob.off, nullptr, nullptr, ob.r, l, ldq, ob.r, 0, 1.0});
+    }
+    const Block& lb = lam->b[lam->find(K1(keys[gi], keys[gi], 0))];
+    ops.push_back(CopyOp{Sv, lam->d + lb.off, nullptr, nullptr, l, 1, l, l, 0, 1.0});
+    const auto& Bq = dv.at(keys[gi]);
+    ops.push_back(CopyOp{Pm, dDV + Bq.off, Sv, nullptr, l, sv.s[gi].n, ldp, l, 1, 1.0});  // D Vd = D P^T
+  }
+  run_copyops(ctx, ops);
+  if (BL2 && *BL2) {
+    Tensor& b2 = **BL2;
+    Layout l2;
+    std::vector<std::pair<int, int>> src;  // (old block, group); group -1 = copy unchanged
+    std::map<Q, int> gidx;
+    for (size_t gi = 0; gi < keys.size(); ++gi) gidx[keys[gi]] = (int)gi;
+    for (int i = 0; i < (int)b2.b.size(); ++i) {
+      auto it = gidx.find(b2.b[i].k.q0);
+      if (it == gidx.end()) {
+        l2.add(b2.b[i].k, b2.b[i].r, b2.b[i].c);
+        src.push_back({i, -1});
+      } else if (keep[it->second]) {
+        l2.add(b2.b[i].k, keep[it->second], b2.b[i].c);
+        src.push_back({i, it->second});
+      }
+    }
+    l2.finalize();
+    TensorP nb2 = make_tensor(ctx, 1, l2, true);
+    GemmPlan g;
+    std::vector<CopyOp> cps;
+    for (auto& p : src) {
+      const Block& ob = b2.b[p.first];
+      const Block& nb = nb2->b[nb2->find(ob.k)];
+      if (p.second < 0) {
+        cps.push_back(CopyOp{b2.d + ob.off, nb2->d + nb.off, nullptr, nullptr, ob.r, ob.c, ob.r, ob.r, 0, 1.0});
+      } else {
+        const auto& Bq = dv.at(keys[p.second]);
+        MPSG_CHECK(ob.r == Bq.c, "bond dimension mismatch in prepareMatrix");
+        g.add_problem(2, nb.off, nb.r, nb.r, nb.c, false, {GSegH{1, 0, Bq.off, ob.off, Bq.r, ob.r, ob.r, 0, 0, 1.0}});
+      }
+    }
+    g.upload(ctx);
+    const double* bases[8] = {b2.d, dDV, nb2->d, nullptr, nullptr, nullptr, nullptr, nullptr};
+    g.run(bases);
+    run_copyops(ctx, cps);
+    ctx->sync();
+    *BL2 = nb2;
+  }
+  ctx->dfree(dDV);
+  BL1 = nb1;
+  if (lam_out) *lam_out = lam;
+}
+
 // ============================================================================ Lanczos
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel, int ndiag, double stall_rel) {

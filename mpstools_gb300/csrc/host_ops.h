@@ -132,6 +132,9 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
 // prepareMatrix(BL1, lambda, BL2, "r", multiply=true, truncate=true, delta): right-orthonormalise BL2,
 // multiply U*D into BL1 (BL1 may be null at the left edge).
 void prepare_matrix_r(Ctx* ctx, TensorP* BL1, TensorP& BL2, TensorP* lam_out, double delta);
+// prepareMatrix(BL1, lambda, BL2, "l", multiply=true): left-orthonormalise BL1, multiply D*Vd into BL2
+// from the left (BL2 may be null at the right edge); singular values <= delta dropped.
+void prepare_matrix_l(Ctx* ctx, TensorP& BL1, TensorP* BL2, TensorP* lam_out, double delta);
 
 struct LanczosStats {
   int64_t matvecs = 0;

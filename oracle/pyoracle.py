@@ -415,6 +415,116 @@ class DMRG:
             pass
 
 
+# ------------------------------------------------------------------ single-site DMRG (CPU restatement)
+def _svd_groups(mats):
+    """Economy SVD (LAPACK through numpy) of each group matrix, no truncation (prepareBlock with
+    truncate=false, src/MPSfunctions.hpp:21-142)."""
+    return {q: np.linalg.svd(m, full_matrices=False) for q, m in mats.items()}
+
+
+def prepare_left(A, B=None):
+    """prepareMatrix(A, lambda, B, "l", multiply=true): per right charge the blocks of A stacked by rows
+    = U D Vd; A <- U, lambda = D, B <- D Vd B for B's blocks with that left charge."""
+    groups = {}
+    for k in sorted(A):
+        groups.setdefault(k[1], []).append(k)
+    mats = {q: np.vstack([A[k] for k in ks]) for q, ks in groups.items()}
+    out, lam, dv = {}, {}, {}
+    for q, (U, D, Vd) in _svd_groups(mats).items():
+        r0 = 0
+        for k in groups[q]:
+            out[k] = U[r0:r0 + A[k].shape[0], :].copy()
+            r0 += A[k].shape[0]
+        lam[q] = D.copy()
+        dv[q] = D[:, None] * Vd
+    if B is not None:
+        B = {k: (dv[k[0]] @ v if k[0] in dv else v) for k, v in B.items()}
+    return out, B, lam
+
+
+def prepare_right(A, B):
+    """prepareMatrix(A, lambda, B, "r", multiply=true): per left charge the blocks of B side by side =
+    U D Vd; B <- Vd, lambda = D, A <- A U D for A's blocks with that right charge (A may be None)."""
+    groups = {}
+    for k in sorted(B):
+        groups.setdefault(k[0], []).append(k)
+    mats = {q: np.hstack([B[k] for k in ks]) for q, ks in groups.items()}
+    out, lam, ud = {}, {}, {}
+    for q, (U, D, Vd) in _svd_groups(mats).items():
+        c0 = 0
+        for k in groups[q]:
+            out[k] = Vd[:, c0:c0 + B[k].shape[1]].copy()
+            c0 += B[k].shape[1]
+        lam[q] = D.copy()
+        ud[q] = U * D[None, :]
+    if A is not None:
+        A = {k: (v @ ud[k[1]] if k[1] in ud else v) for k, v in A.items()}
+    return A, out, lam
+
+
+class SSDMRG:
+    """SSDMRGengine (src/container.hpp:827-925) restated on the oracle's kernels: the single-site
+    Lanczos (SSLanzcosEngine, src/lanzcos.hpp:503-600) is the oracle's Lanczos on contractSingle,
+    written as the two-site contraction with a dummy second site (identity MPO tensor on the right
+    channels, one local state of charge 0); prepareSite without truncation; addContractionLayer for
+    the environments."""
+
+    def __init__(self, sites, mpo, itokeys):
+        self.N = len(sites)
+        self.W, self.ik = mpo, itokeys
+        g = DMRG(sites, mpo, itokeys, maxthreads=2)
+        g.prepare()  # orthonormalize("rl")
+        self.sites = [g.site(s) for s in range(self.N)]
+        last = self.sites[-1]
+        dims = {}
+        for (q0, q1, p), v in last.items():
+            dims.setdefault(q1, v.shape[1])
+        self.R = {self.N: {(q, q, 0): np.eye(n) for q, n in dims.items()}}  # getRMax
+        for s in range(self.N - 1, 0, -1):  # computeR(mps, mpo, 1)
+            self.R[s] = add_contraction_layer(self.R[s + 1], self.sites[s], mpo[s], itokeys[s], 0)
+        self.L = {-1: {(0, 0, 0): np.ones((1, 1))}}  # getLMin
+        self.steps = []
+
+    def do_step(self, site, direction, delta=1e-12, testenergy=True, itmax=500):
+        W1 = self.W[site]
+        D = W1[2]
+        W2 = ([(w, w, 0, 0, 1.0) for w in range(D)], D, D)
+        th = {(a, b, p, 0): v for (a, b, p), v in self.sites[site].items()}
+        E, it, psi = lanczos(self.L[site - 1], self.R[site + 1], th, W1, W2, self.ik[site], [0], itmax, delta,
+                             testenergy)
+        A = {(a, b, p): v for (a, b, p, _), v in psi.items()}
+        if direction > 0:
+            nxt = self.sites[site + 1] if site + 1 < self.N else None
+            A, nxt, lam = prepare_left(A, nxt)
+            if nxt is not None:
+                self.sites[site + 1] = nxt
+            self.sites[site] = A
+            self.L[site] = add_contraction_layer(self.L[site - 1], A, W1, self.ik[site], 1)
+        else:
+            prv = self.sites[site - 1] if site > 0 else None
+            prv, A, lam = prepare_right(prv, A)
+            if prv is not None:
+                self.sites[site - 1] = prv
+            self.sites[site] = A
+            self.R[site] = add_contraction_layer(self.R[site + 1], A, W1, self.ik[site], -1)
+        self.steps.append(dict(site=site, dir=direction, iters=it, E=E))
+        return E
+
+    def simulate(self, maxsteps=5, EnConv=1e-10, delta=1e-12, testenergy=True):
+        globalE, step = 1e100, 0
+        while True:
+            for site in range(self.N - 1):
+                out = self.do_step(site, 1, delta, testenergy)
+            for site in range(self.N - 1, 0, -1):
+                out = self.do_step(site, -1, delta, testenergy)
+            step += 1
+            conv = abs(globalE - out) < EnConv or step > maxsteps
+            globalE = out
+            if conv:
+                break
+        return self.do_step(0, -1, delta, testenergy)
+
+
 # ------------------------------------------------------------------ TEBD (complex FP64)
 def nn_gate(W1, W2, site1, N, dt, d1=2, d2=2):
     """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
