@@ -283,6 +283,15 @@ mpsg_status mpsg_tebd_adjoint_second_order(mpsg_tebd e, int32_t steps, double dt
 /* wall seconds spent in mpsg_tebd_adjoint_second_order (forward, recomputation and backward). */
 mpsg_status mpsg_tebd_adjoint_seconds(mpsg_tebd e, double* seconds);
 void mpsg_dmrg_destroy(mpsg_dmrg e);
+/* DMRGengine::simulate(mps, delta_ortho, ...) (src/container.hpp:441-570): two-site DMRG whose Lanczos
+ * keeps every Krylov vector orthogonal to the target state (N site tensors, e.g. a converged ground
+ * state), in the current basis through overlap environments; E = the last step's energy (the lowest
+ * state orthogonal to the target in the engine's sector).  delta_ortho is accepted and unused, as in
+ * the reference.  Deviation: the reference's last update forms the target's two-site state from its
+ * site 0 twice; here from sites 0 and 1. */
+mpsg_status mpsg_dmrg_excited_simulate(mpsg_dmrg e, const mpsg_tensor* target, double delta_ortho, uint32_t maxsteps,
+                                       double EnConv, uint32_t chimax, int32_t doTrunc, double tr_weight, double delta,
+                                       int32_t testenergy, int32_t leaveoutlast, double* E);
 /* SSDMRGengine::simulate (src/container.hpp:827-925): single-site DMRG (no bond growth) from the
  * engine's state: orthonormalize("rl"), sweeps until |dE| < EnConv or more than maxsteps sweeps, then
  * doStep(0, -1); E = the last step's energy.  Each update is SSLanzcosEngine on one site

@@ -166,6 +166,16 @@ class DMRGengine:
         self.h = h
         check(ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
 
+    def excited_simulate(self, target_sites, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12,
+                         delta=1e-12, testenergy=True, leaveoutlast=False, delta_ortho=1e-10):
+        """DMRGengine::simulate(mps, ...): two-site DMRG orthogonal to the target MPS (site dicts)."""
+        ts = [Tensor.from_dict(self.ctx, x, 1) for x in target_sites]
+        E = C.c_double()
+        check(self.ctx.L.mpsg_dmrg_excited_simulate(self.h, handle_array(ts), float(delta_ortho), int(maxsteps),
+                                                     float(EnConv), int(chimax), int(doTrunc), float(tr_weight),
+                                                     float(delta), int(testenergy), int(leaveoutlast), C.byref(E)))
+        return E.value
+
     def ss_simulate(self, maxsteps=5, EnConv=1e-10, delta=1e-12, testenergy=True):
         """SSDMRGengine::simulate: single-site sweeps (no bond growth) from the engine's state."""
         E = C.c_double()

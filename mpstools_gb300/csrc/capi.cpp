@@ -287,6 +287,23 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
   *out = d;
   API_END
 }
+mpsg_status mpsg_dmrg_excited_simulate(mpsg_dmrg e, const mpsg_tensor* target, double delta_ortho, uint32_t maxsteps,
+                                       double EnConv, uint32_t chimax, int32_t doTrunc, double tr_weight, double delta,
+                                       int32_t testenergy, int32_t leaveoutlast, double* E) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e && target && E, "null argument");
+  MPSG_CHECK(EnConv > 0, "EnConv must be > 0");
+  (void)delta_ortho;  // the reference's only use of it is commented out (src/lanzcos.hpp:349)
+  std::vector<TensorP> tgt;
+  for (int i = 0; i < e->e->N; ++i) {
+    MPSG_CHECK(target[i], "null target tensor");
+    MPSG_CHECK(T(target[i]).nphys == 1, "target site tensors must have one physical index");
+    tgt.push_back(tensor_copy(T(target[i])));
+  }
+  *E = e->e->excited_simulate(tgt, (int)maxsteps, EnConv, (int)chimax, doTrunc != 0, tr_weight, delta,
+                              testenergy != 0, leaveoutlast != 0);
+  API_END
+}
 mpsg_status mpsg_dmrg_ss_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, double delta, int32_t testenergy,
                                   double* E) {
   API_BEGIN

@@ -112,6 +112,21 @@ struct Engine {
     if (ev1) cudaEventDestroy(ev1);
   }
 
+  // Identity MPO tensor of a site (IdentityMPO, Dl = Dr = 1): overlap environments and basis changes.
+  static MPO identity_mpo(int d) {
+    MPO m;
+    m.Dl = m.Dr = 1;
+    MPOEntry en;
+    en.wl = en.wr = 0;
+    for (uint32_t i = 0; i < (uint32_t)d; ++i) en.ops.push_back(OpEl{i, i, 1.0});
+    m.e.push_back(en);
+    return m;
+  }
+
+  // excited-state targeting: the target MPS and its overlap environments with the engine's state
+  const std::vector<TensorP>* target = nullptr;
+  std::map<int, TensorP> ovL, ovR;
+
   StepRec do_step_impl(int site, int dir, int chimax, bool doTrunc, double tr_weight, double delta,
                        bool testenergy) {
     MPSG_CHECK(site >= 0 && site + 1 < N, "site out of range");
@@ -133,11 +148,32 @@ struct Engine {
       }
       s0.finalize();
     }
+    // doStepExcited: the target's two-site state in the current basis (contractTwosite with the
+    // overlap environments and identity MPOs, src/container.hpp:488-498), projected out of the Lanczos
+    TensorP tstate;
+    const MPO id0 = identity_mpo((int)ik[site].size()), id1 = identity_mpo((int)ik[site + 1].size());
+    if (target) {
+      TensorP told = theta_form(ctx, *(*target)[site], *(*target)[site + 1], nullptr);
+      auto nat = build_matvec(ctx, *ovL.at(site - 1), *ovR.at(site + 2), layout_of(*told), id0, id1, ik[site],
+                              ik[site + 1], nullptr, MPSG_PREC_FP64);
+      for (auto& b : nat->out.b)
+        if (!s0.idx.count(b.k)) s0.add(b.k, b.r, b.c);
+      s0.finalize();
+      told.reset();
+    }
     Layout sx = theta_closure(Le, Re, s0, mpo[site], mpo[site + 1], ik[site], ik[site + 1]);
+    if (target) {
+      TensorP told = theta_form(ctx, *(*target)[site], *(*target)[site + 1], nullptr);
+      auto mvs = build_matvec(ctx, *ovL.at(site - 1), *ovR.at(site + 2), layout_of(*told), id0, id1, ik[site],
+                              ik[site + 1], &sx, MPSG_PREC_FP64);
+      tstate = make_tensor(ctx, 2, sx, true);
+      mvs->run(told->d, tstate->d);
+    }
     TensorP th = theta_form(ctx, *mps[site], *mps[site + 1], &sx);
     TensorP psi = make_tensor(ctx, 2, sx, true);
     LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], *th, *psi,
-                                    lanmax, delta, testenergy, reorth, (int)prec, &lst);
+                                    lanmax, delta, testenergy, reorth, (int)prec, &lst, tstate ? tstate->d : nullptr);
+    tstate.reset();
     th.reset();
     auto t0 = std::chrono::steady_clock::now();
     SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
@@ -274,6 +310,58 @@ struct Engine {
     out = ss_do_step(0, -1, delta, testenergy);
     wall += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return out.E;
+  }
+
+  // DMRGengine::simulate(mps, delta_ortho, ...) (src/container.hpp:441-570): two-site sweeps whose
+  // Lanczos stays orthogonal to the target state `tgt` (e.g. a ground state), giving the lowest state
+  // orthogonal to it.  Overlap environments <tgt|engine> are kept left and right of the updated bond.
+  // Sweeps 0 .. N-3 right and N-2 .. 1 left (skipping N-2 when leaveoutlast) until |dE| < EnConv or
+  // maxsteps sweeps, then the update of bond (0, 1) leftwards.  The reference forms the target's
+  // two-site state of that last update from tgt[0] twice (state_oldbasis(mps[site], mps[site])); here
+  // it is tgt[0] tgt[1] as in every other update.
+  double excited_simulate(const std::vector<TensorP>& tgt, int maxsteps, double EnConv, int chimax, bool doTrunc,
+                          double tr_weight, double delta, bool testenergy, bool leaveoutlast) {
+    MPSG_CHECK((int)tgt.size() == N, "target state has a different length");
+    auto t0 = std::chrono::steady_clock::now();
+    prepare();
+    target = &tgt;
+    ovR.clear();
+    ovL.clear();
+    try {
+      ovR[N] = rmax(ctx, *tgt[N - 1]);
+      for (int s = N - 1; s >= 0; --s)
+        ovR[s] = env_update(ctx, *ovR[s + 1], *tgt[s], identity_mpo((int)ik[s].size()), ik[s], 0, nullptr,
+                            mps[s].get());
+      ovL[-1] = lmin(ctx);
+      double globalE = 1e100;
+      StepRec out{};
+      int step = 0;
+      while (true) {
+        for (int site = 0; site < N - 2; ++site) {
+          out = do_step(site, 1, chimax, doTrunc, tr_weight, delta, testenergy);
+          ovL[site] = env_update(ctx, *ovL[site - 1], *tgt[site], identity_mpo((int)ik[site].size()), ik[site], 1,
+                                 nullptr, mps[site].get());
+        }
+        for (int site = N - 2; site > 0; --site) {
+          if (leaveoutlast && site == N - 2) continue;
+          out = do_step(site, -1, chimax, doTrunc, tr_weight, delta, testenergy);
+          ovR[site + 1] = env_update(ctx, *ovR[site + 2], *tgt[site + 1], identity_mpo((int)ik[site + 1].size()),
+                                     ik[site + 1], -1, nullptr, mps[site + 1].get());
+        }
+        ++step;
+        bool conv = std::fabs(globalE - out.E) < EnConv;
+        if (step >= maxsteps) conv = true;
+        globalE = out.E;
+        if (conv) break;
+      }
+      out = do_step(0, -1, chimax, doTrunc, tr_weight, delta, testenergy);
+      target = nullptr;
+      wall += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return out.E;
+    } catch (...) {
+      target = nullptr;
+      throw;
+    }
   }
 
   double measure_energy() { return measure(mpo); }

@@ -1734,7 +1734,8 @@ void prepare_matrix_l(Ctx* ctx, TensorP& BL1, TensorP* BL2, TensorP* lam_out, do
 
 // ============================================================================ Lanczos
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
-                      bool testenergy, bool reorth, LanczosStats* st, double tol_rel, int ndiag, double stall_rel) {
+                      bool testenergy, bool reorth, LanczosStats* st, double tol_rel, int ndiag, double stall_rel,
+                      const double* proj) {
   MPSG_CHECK(ndiag >= 1, "ndiag must be >= 1");
   auto t_start = std::chrono::steady_clock::now();
   const int64_t n = th_init.nelem;
@@ -1762,6 +1763,28 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   double* w = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(n, 2));
   MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * std::max<int64_t>(n, 2), s));
   MPSG_CUDA(cudaMemcpyAsync(slot(0), th_init.d, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+  // projected Lanczos (TSLanzcosEngine::simulate with a state, src/lanzcos.hpp:282-400): the start
+  // vector and every new Krylov vector lose their component along `proj`
+  double* d_ph = nullptr;
+  double** d_pp = nullptr;
+  if (proj) {
+    d_ph = (double*)ctx->dmalloc(sizeof(double) * (std::max<int64_t>(n, 2) + 2 + 64));
+    d_pp = (double**)ctx->dmalloc(sizeof(double*));
+    MPSG_CUDA(cudaMemcpyAsync(d_ph, proj, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    double* d_pn = d_ph + std::max<int64_t>(n, 2);
+    launch_dot(d_ph, d_ph, n, ctx->part, d_pn, s);
+    launch_scale_by_norm(d_ph, n, d_pn, 0.0, nullptr, s);  // unit vector (a zero state projects nothing)
+    MPSG_CUDA(cudaMemcpyAsync(d_pp, &d_ph, sizeof(double*), cudaMemcpyHostToDevice, s));
+    ctx->sync();
+  }
+  auto project_out = [&](double* x) {
+    if (!proj) return;
+    double* d_pc = d_ph + std::max<int64_t>(n, 2) + 1;
+    double* d_pparts = d_pc + 1;
+    launch_project((const double* const*)d_pp, 1, x, n, d_pparts, d_pc, s);
+    launch_combine(x, (const double* const*)d_pp, 1, d_pc, n, 1, s);
+  };
+  project_out(V[0]);
   launch_dot(V[0], V[0], n, ctx->part, d_norm2, s);
   cudaEvent_t e0, e1;
   MPSG_CUDA(cudaEventCreate(&e0));
@@ -1785,6 +1808,10 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
         launch_tri_lowest(d_alpha, d_beta, j + 1, d_E + j / ndiag, nullptr, s);
       launch_axpy3(V[j + 1], w, V[j], j > 0 ? V[j - 1] : nullptr, d_alpha + j, d_beta + j, n, ctx->part,
                    d_norm2 + j + 1, s);
+      if (proj) {
+        project_out(V[j + 1]);
+        launch_dot(V[j + 1], V[j + 1], n, ctx->part, d_norm2 + j + 1, s);
+      }
       if (reorth) {
         for (int pass = 0; pass < 2; ++pass) {
           launch_project((const double* const*)dV, j + 1, V[j + 1], n, d_proj, d_coef, s);
@@ -1842,6 +1869,8 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   ctx->dfree(dV);
   ctx->dfree(dsc);
   if (d_proj) ctx->dfree(d_proj);
+  if (d_ph) ctx->dfree(d_ph);
+  if (d_pp) ctx->dfree(d_pp);
   ctx->sync();
   if (st) st->seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   return res;
@@ -1870,23 +1899,23 @@ double prec_stall(int prec) {
 
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
-                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st) {
+                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj) {
   if (prec == MPSG_PREC_FP64) {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
-    return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st);
+    return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, 0.0, 5, 0.0, proj);
   }
   const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_TF32X3 : prec;
   LanczosResult r;
   {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
-    r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo));
+    r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo), proj);
   }
   if (prec != MPSG_PREC_AUTO) return r;
   // FP64 finish: the reference's Lanczos restarted from the mixed-precision ground state, energy test
   // every iteration, so the final energy carries the same convergence criterion as the FP64 path
   auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
   TensorP start = tensor_copy(psi);
-  LanczosResult r2 = lanczos(ctx, *mv64, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0);
+  LanczosResult r2 = lanczos(ctx, *mv64, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0, proj);
   r2.iterations += r.iterations;
   return r2;
 }

@@ -525,6 +525,134 @@ class SSDMRG:
         return self.do_step(0, -1, delta, testenergy)
 
 
+# ------------------------------------------------------------------ excited states (CPU restatement)
+def _dot(a, b):
+    return float(sum(np.vdot(a[k], b[k]) for k in a.keys() & b.keys()))
+
+
+def _axpy(y, a, x):
+    """y + a x over the union of the blocks (BlockMatrix arithmetic)."""
+    out = {k: v.copy() for k, v in y.items()}
+    for k, v in x.items():
+        out[k] = out[k] + a * v if k in out else a * v
+    return out
+
+
+def identity_mpo(d):
+    return ([(0, 0, i, i, 1.0) for i in range(d)], 1, 1)
+
+
+def lanczos_projected(Lenv, Renv, th, W1, W2, ik0, ik1, state, itmax=500, delta=1e-12, testenergy=True):
+    """TSLanzcosEngine::simulate(itmax, delta, testenergy, state, delta_ortho) (src/lanzcos.hpp:282-400):
+    the Lanczos of the oracle with the start vector and every new Krylov vector projected orthogonal
+    to `state` (squeezed at 1e-15).  Returns (E0, iterations, lowest Ritz vector)."""
+    from scipy.linalg import eigh_tridiagonal
+    state = {k: v for k, v in state.items() if np.abs(v).max() > 1e-15}
+    sn = _dot(state, state)
+    A1 = _axpy(th, -_dot(state, th) / sn, state) if sn > 0 else dict(th)
+    As, es, ks = [], [], []
+    eold, it, first, A0 = 1e100, 0, True, None
+    while True:
+        k = np.sqrt(_dot(A1, A1))
+        if abs(k) < delta:
+            break
+        if not first:
+            ks.append(k)
+        A1 = {key: v / k for key, v in A1.items()}
+        A2 = contract_twosite(Lenv, Renv, A1, W1, W2, ik0, ik1)
+        As.append(A1)
+        e = _dot(A2, A1)
+        es.append(e)
+        if it % 5 == 0 and it != 0 and testenergy:
+            E0 = eigh_tridiagonal(np.array(es), np.array(ks), eigvals_only=True)[0]
+            if abs(E0 - eold) < delta:
+                break
+            eold = E0
+        A3 = _axpy(A2, -e, A1)
+        if not first:
+            A3 = _axpy(A3, -k, A0)
+        if sn > 0:
+            A3 = _axpy(A3, -_dot(state, A3) / sn, state)
+        A0, A1, first = A1, A3, False
+        it += 1
+        if it >= itmax:
+            break
+    w, z = eigh_tridiagonal(np.array(es), np.array(ks))
+    psi = {}
+    for zi, Ai in zip(z[:, 0], As):
+        psi = _axpy(psi, zi, Ai)
+    return float(w[0]), len(es), psi
+
+
+class ExcitedDMRG:
+    """DMRGengine::simulate(mps, delta_ortho, ...) (src/container.hpp:441-570) restated on the oracle's
+    kernels: two-site sweeps with the projected Lanczos; the target state enters each update through
+    the overlap environments <target|state> and contractTwosite with identity MPOs.  The last update
+    uses the target's sites 0 and 1 (the reference pairs site 0 with itself there)."""
+
+    def __init__(self, sites, mpo, itokeys, target):
+        self.N = len(sites)
+        self.W, self.ik, self.tgt = mpo, itokeys, target
+        g = DMRG(sites, mpo, itokeys, maxthreads=2)
+        g.prepare()
+        self.sites = [g.site(s) for s in range(self.N)]
+        self.R = {s: g.env("R", s) for s in range(2, self.N + 1)}
+        self.L = {-1: {(0, 0, 0): np.ones((1, 1))}}
+        ids = [identity_mpo(len(k)) for k in itokeys]
+        self.ids = ids
+        last = target[-1]
+        dims = {}
+        for (q0, q1, p), v in last.items():
+            dims.setdefault(q1, v.shape[1])
+        self.oR = {self.N: {(q, q, 0): np.eye(n) for q, n in dims.items()}}
+        for s in range(self.N - 1, -1, -1):
+            self.oR[s] = add_contraction_layer2(self.oR[s + 1], target[s], self.sites[s], ids[s], itokeys[s], 0)
+        self.oL = {-1: {(0, 0, 0): np.ones((1, 1))}}
+        self.steps = []
+
+    def do_step(self, site, direction, chimax, doTrunc=False, tr_weight=1e-12, delta=1e-12, testenergy=True):
+        ik0, ik1 = self.ik[site], self.ik[site + 1]
+        old = theta(self.tgt[site], self.tgt[site + 1])
+        state = contract_twosite(self.oL[site - 1], self.oR[site + 2], old, self.ids[site], self.ids[site + 1], ik0,
+                                 ik1)
+        th = theta(self.sites[site], self.sites[site + 1])
+        E, it, psi = lanczos_projected(self.L[site - 1], self.R[site + 2], th, self.W[site], self.W[site + 1], ik0,
+                                       ik1, state, 500, delta, testenergy)
+        U, Vt, lam, tw, chi = split(psi, ik0, ik1, chimax, doTrunc, tr_weight)
+        if direction > 0:
+            self.sites[site] = U
+            self.sites[site + 1] = {k: lam[k[0]][:, None] * v for k, v in Vt.items()}
+            self.L[site] = add_contraction_layer(self.L[site - 1], self.sites[site], self.W[site], ik0, 1)
+        else:
+            self.sites[site] = {k: v * lam[k[1]][None, :] for k, v in U.items()}
+            self.sites[site + 1] = Vt
+            self.R[site + 1] = add_contraction_layer(self.R[site + 2], Vt, self.W[site + 1], ik1, -1)
+        self.steps.append(dict(site=site, dir=direction, iters=it, chi=chi, E=E))
+        return E
+
+    def simulate(self, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12, delta=1e-12,
+                 testenergy=True, leaveoutlast=False):
+        N = self.N
+        globalE, step = 1e100, 0
+        while True:
+            for site in range(N - 2):
+                out = self.do_step(site, 1, chimax, doTrunc, tr_weight, delta, testenergy)
+                self.oL[site] = add_contraction_layer2(self.oL[site - 1], self.tgt[site], self.sites[site],
+                                                       self.ids[site], self.ik[site], 1)
+            for site in range(N - 2, 0, -1):
+                if leaveoutlast and site == N - 2:
+                    continue
+                out = self.do_step(site, -1, chimax, doTrunc, tr_weight, delta, testenergy)
+                self.oR[site + 1] = add_contraction_layer2(self.oR[site + 2], self.tgt[site + 1], self.sites[site + 1],
+                                                           self.ids[site + 1], self.ik[site + 1], -1)
+            step += 1
+            conv = abs(globalE - out) < EnConv or step >= maxsteps
+            globalE = out
+            if conv:
+                break
+        return self.do_step(0, -1, chimax, doTrunc, tr_weight, delta, testenergy)
+
+
 # ------------------------------------------------------------------ TEBD (complex FP64)
 def nn_gate(W1, W2, site1, N, dt, d1=2, d2=2):
     """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
