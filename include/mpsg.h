@@ -292,6 +292,20 @@ void mpsg_dmrg_destroy(mpsg_dmrg e);
 mpsg_status mpsg_dmrg_excited_simulate(mpsg_dmrg e, const mpsg_tensor* target, double delta_ortho, uint32_t maxsteps,
                                        double EnConv, uint32_t chimax, int32_t doTrunc, double tr_weight, double delta,
                                        int32_t testenergy, int32_t leaveoutlast, double* E);
+/* applyMPO (src/MPSfunctions.hpp:2088-2346): the exact product W|psi> of an MPO (N tensors) and an MPS
+ * (N site tensors); out receives N new site tensors.  New bond charges are propagated from the left
+ * ((b, w) takes charge(a, w') + q(s_out) when first seen); a new charge sector is the direct sum over
+ * the MPO channels of the old sectors that reach it (largest size per channel, zero padding). */
+mpsg_status mpsg_apply_mpo(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W, const mpsg_itokey* ik,
+                           mpsg_tensor* out);
+/* compressTwoSite (src/MPSfunctions.hpp:2797-2940): variational two-site fit of W|psi> at bond
+ * dimension <= chimax (initial guess: W applied to psi truncated to chimax / D, D the MPO dimension
+ * at site 1; sweeps until the convergence measure grows, maxstep sweeps or |conv| < delta).  out
+ * receives the fitted site tensors, conv the reference's measure (n1^2 + n2^2 - 2 |<fit|psi>|) / n1^2
+ * (its overlap term is with psi, as the reference computes it). */
+mpsg_status mpsg_compress_two_site(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
+                                   const mpsg_itokey* ik, uint32_t chimax, uint32_t maxstep, double delta,
+                                   int32_t doTrunc, double tr_weight, mpsg_tensor* out, double* conv);
 /* SSDMRGengine::simulate (src/container.hpp:827-925): single-site DMRG (no bond growth) from the
  * engine's state: orthonormalize("rl"), sweeps until |dE| < EnConv or more than maxsteps sweeps, then
  * doStep(0, -1); E = the last step's energy.  Each update is SSLanzcosEngine on one site

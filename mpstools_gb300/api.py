@@ -100,6 +100,29 @@ def measureMPO(sites, mpo, itokeys, ctx=None):
     return out.value
 
 
+def applyMPO(mpo, sites, itokeys, ctx=None):
+    """applyMPO(mpo, mps): the exact MPS of W|psi> (site dicts)."""
+    ctx = ctx or default_context()
+    ts = [Tensor.from_dict(ctx, x, 1) for x in sites]
+    ws, ks = MPOArray(mpo), ItoKeyArray(itokeys)
+    out = (C.c_void_p * len(ts))()
+    check(ctx.L.mpsg_apply_mpo(ctx.h, len(ts), handle_array(ts), ws.ptr(), ks.ptr(), out))
+    return [Tensor(ctx, C.c_void_p(h)).to_dict() for h in out]
+
+
+def compressTwoSite(sites, mpo, itokeys, chimax=100, maxstep=5, delta=1e-10, doTrunc=True, tr_weight=1e-10,
+                    ctx=None):
+    """compressTwoSite(mps, mpo, ...): returns (conv, fitted site dicts)."""
+    ctx = ctx or default_context()
+    ts = [Tensor.from_dict(ctx, x, 1) for x in sites]
+    ws, ks = MPOArray(mpo), ItoKeyArray(itokeys)
+    out = (C.c_void_p * len(ts))()
+    conv = C.c_double()
+    check(ctx.L.mpsg_compress_two_site(ctx.h, len(ts), handle_array(ts), ws.ptr(), ks.ptr(), int(chimax), int(maxstep),
+                                       float(delta), int(doTrunc), float(tr_weight), out, C.byref(conv)))
+    return conv.value, [Tensor(ctx, C.c_void_p(h)).to_dict() for h in out]
+
+
 def split(A, itokey, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, ctx=None):
     """Returns (U, Vt, lambda, truncated_weight, chi) -- direction 0 of the reference."""
     ctx = ctx or default_context()

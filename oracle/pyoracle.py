@@ -653,6 +653,130 @@ class ExcitedDMRG:
         return self.do_step(0, -1, chimax, doTrunc, tr_weight, delta, testenergy)
 
 
+# ------------------------------------------------------------------ applyMPO / compressTwoSite (CPU)
+def apply_mpo(sites, W, itokeys):
+    """applyMPO (src/MPSfunctions.hpp:2088-2346) restated: five-leg pieces v*A((a, wl), (b, wr); s_out)
+    for every MPS block and MPO element; new charges propagated from the left ((b, wr) takes
+    charge(a, wl) + q(s_out) when first seen, in key order); per new charge a coarse grid over the MPO
+    channels with the largest piece size per channel (zero padding)."""
+    N = len(sites)
+    q0 = min(k[0] for k in sites[0])
+    qleft = {(q0, w): q0 for w in range(W[0][1])}
+    size_left = {q0: [1] * W[0][1]}
+    out = []
+    for s in range(N):
+        terms, Dl, Dr = W[s]
+        five = {}
+        for (wl, wr, o, i, v) in terms:
+            for (a, b, p), blk in sites[s].items():
+                if p != i:
+                    continue
+                key = ((a, wl), (b, wr), o)
+                five[key] = five[key] + v * blk if key in five else v * blk
+        qright, size_right, kept = {}, {}, []
+        for key in sorted(five):
+            if key[0] not in qleft:
+                continue
+            qr = qleft[key[0]] + int(itokeys[s][key[2]])
+            qright.setdefault(key[1], qr)
+            kept.append(key)
+        for key in kept:
+            qr = qright[key[1]]
+            v = size_right.setdefault(qr, [0] * Dr)
+            v[key[1][1]] = max(v[key[1][1]], five[key].shape[1])
+        site = {}
+        for key in kept:
+            ql, qr = qleft[key[0]], qright[key[1]]
+            sl, sr = size_left[ql], size_right[qr]
+            nk = (ql, qr, key[2])
+            if nk not in site:
+                site[nk] = np.zeros((sum(sl), sum(sr)))
+            r0, c0 = sum(sl[:key[0][1]]), sum(sr[:key[1][1]])
+            m = five[key]
+            site[nk][r0:r0 + m.shape[0], c0:c0 + m.shape[1]] = m
+        out.append(site)
+        qleft, size_left = qright, size_right
+    return out
+
+
+def truncate_lambda(lam, chimax, tr_weight):
+    """DiagBlockMatrix::truncate(tr_weight, chimax, false) (src/BlockTensor.hpp:26-136): values in the
+    order (value descending, later insertion first), kept while the truncated weight exceeds
+    norm * tr_weight and fewer than chimax are kept; returns the kept count per charge."""
+    qs = sorted(lam)
+    vals = [(float(v), q) for q in qs for v in lam[q]]
+    order = sorted(range(len(vals)), key=lambda i: (-vals[i][0], -i))
+    norm = np.sqrt(sum(v * v for v, _ in vals))
+    tw, cnt, keep = norm, 0, {q: 0 for q in qs}
+    for i in order:
+        if not (abs(tw) > norm * tr_weight and cnt < chimax):
+            break
+        tw -= vals[i][0] ** 2 / norm
+        keep[vals[i][1]] += 1
+        cnt += 1
+    return keep
+
+
+def compress_two_site(sites, W, itokeys, chimax=100, maxstep=5, delta=1e-10, doTrunc=True, tr_weight=1e-10):
+    """compressTwoSite (src/MPSfunctions.hpp:2797-2940) restated on the oracle's kernels; returns
+    (conv, fitted sites).  conv = (n1^2 + n2^2 - 2 |<fit|psi>|) / n1^2 as the reference computes it."""
+    N = len(sites)
+    full = apply_mpo(sites, W, itokeys)
+    n1 = np.sqrt(overlap(full, full, itokeys))
+    t = [dict(x) for x in sites]
+    lam = {}
+    for s in range(N - 1):
+        t[s], t[s + 1], lam[s] = prepare_left(t[s], t[s + 1])
+    for s in range(N - 1, 0, -1):
+        t[s - 1], t[s], lam[s - 1] = prepare_right(t[s - 1], t[s])
+    chi = int(np.floor(chimax / W[1][2]))
+    for s in range(N - 1):  # truncate(mps, chi, delta): dropDangling of the cut columns / rows
+        keep = truncate_lambda(lam[s], chi, delta)
+        t[s] = {k: v[:, :keep.get(k[1], 0)] for k, v in t[s].items() if keep.get(k[1], 0) > 0}
+        t[s + 1] = {k: v[:keep.get(k[0], 0), :] for k, v in t[s + 1].items() if keep.get(k[0], 0) > 0}
+    comp = apply_mpo(t, W, itokeys)
+    for s in range(N - 1):
+        comp[s], comp[s + 1], _ = prepare_left(comp[s], comp[s + 1])
+    for s in range(N - 1, 0, -1):
+        comp[s - 1], comp[s], _ = prepare_right(comp[s - 1], comp[s])
+    last = sites[-1]
+    dims = {}
+    for (a, b, p), v in last.items():
+        dims.setdefault(b, v.shape[1])
+    BL = {-1: {(0, 0, 0): np.ones((1, 1))}}
+    BR = {N: {(q, q, 0): np.eye(n) for q, n in dims.items()}}
+    for s in range(N - 1, 1, -1):
+        BR[s] = add_contraction_layer2(BR[s + 1], sites[s], comp[s], W[s], itokeys[s], -1)
+
+    def fit(s):
+        return contract_twosite(BL[s - 1], BR[s + 2], theta(sites[s], sites[s + 1]), W[s], W[s + 1], itokeys[s],
+                                itokeys[s + 1])
+
+    conv, conv_old, step, converged = 0.0, 1.0, 1, maxstep == 0
+    while not converged:
+        for s in range(N - 2):
+            U, Vt, lm, tw, ch = split(fit(s), itokeys[s], itokeys[s + 1], chimax, doTrunc, tr_weight, False)
+            comp[s] = U
+            comp[s + 1] = {k: lm[k[0]][:, None] * v for k, v in Vt.items()}
+            BL[s] = add_contraction_layer2(BL[s - 1], sites[s], comp[s], W[s], itokeys[s], 1)
+        for s in range(N - 2, 0, -1):
+            U, Vt, lm, tw, ch = split(fit(s), itokeys[s], itokeys[s + 1], chimax, doTrunc, tr_weight, False)
+            comp[s] = {k: v * lm[k[1]][None, :] for k, v in U.items()}
+            comp[s + 1] = Vt
+            BR[s + 1] = add_contraction_layer2(BR[s + 2], sites[s + 1], comp[s + 1], W[s + 1], itokeys[s + 1], -1)
+        n2 = np.sqrt(overlap(comp, comp, itokeys))
+        conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, sites, itokeys))) / (n1 * n1)
+        if conv_old < conv:
+            break
+        conv_old = conv
+        if step >= maxstep or abs(conv) < delta:
+            converged = True
+        step += 1
+    n2 = np.sqrt(overlap(comp, comp, itokeys))
+    conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, sites, itokeys))) / (n1 * n1)
+    return conv, comp
+
+
 # ------------------------------------------------------------------ TEBD (complex FP64)
 def nn_gate(W1, W2, site1, N, dt, d1=2, d2=2):
     """MPO::getNNGate: dense (d1 d2 x d1 d2) complex gate exp(-i dt h_b), index o1 + d1*o2."""
