@@ -306,6 +306,21 @@ mpsg_status mpsg_apply_mpo(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, co
 mpsg_status mpsg_compress_two_site(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
                                    const mpsg_itokey* ik, uint32_t chimax, uint32_t maxstep, double delta,
                                    int32_t doTrunc, double tr_weight, mpsg_tensor* out, double* conv);
+/* compress (src/MPSfunctions.hpp:2349-2510): variational single-site compression of psi to bond
+ * dimension <= chimax.  psi is first swept with prepareSite (left over sites 0 .. N-2, right over
+ * N-2 .. 1; with normalize over all sites, which normalises it); the initial guess is psi truncated to
+ * chimax with those lambdas; single-site sweeps (contractSingle with the identity MPO) until the
+ * measure grows, maxstep sweeps or |conv| < delta; site 0 fitted once more; the fit left and right
+ * canonicalised.  out receives the fit, conv = |fit - psi|^2 / |psi|^2.  maxstep must be >= 1 (with 0 the
+ * reference reads an environment it never built). */
+mpsg_status mpsg_compress(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_itokey* ik, uint32_t chimax,
+                          uint32_t maxstep, double delta, int32_t normalize, mpsg_tensor* out, double* conv);
+/* compressSingleSite (src/MPSfunctions.hpp:2667-2792): variational single-site fit of W|psi> (the
+ * initial guess and the measure as mpsg_compress_two_site; the bond dimensions stay those of the
+ * initial guess). */
+mpsg_status mpsg_compress_single_site(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
+                                      const mpsg_itokey* ik, uint32_t chimax, uint32_t maxstep, double delta,
+                                      mpsg_tensor* out, double* conv);
 /* SSDMRGengine::simulate (src/container.hpp:827-925): single-site DMRG (no bond growth) from the
  * engine's state: orthonormalize("rl"), sweeps until |dE| < EnConv or more than maxsteps sweeps, then
  * doStep(0, -1); E = the last step's energy.  Each update is SSLanzcosEngine on one site

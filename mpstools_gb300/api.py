@@ -123,6 +123,31 @@ def compressTwoSite(sites, mpo, itokeys, chimax=100, maxstep=5, delta=1e-10, doT
     return conv.value, [Tensor(ctx, C.c_void_p(h)).to_dict() for h in out]
 
 
+def compress(sites, itokeys, chimax=100, maxstep=5, delta=1e-10, normalize=False, ctx=None):
+    """compress(mps, chimax, maxstep, delta, verbose, normalize): variational single-site compression;
+    returns (conv, fitted site dicts)."""
+    ctx = ctx or default_context()
+    ts = [Tensor.from_dict(ctx, x, 1) for x in sites]
+    ks = ItoKeyArray(itokeys)
+    out = (C.c_void_p * len(ts))()
+    conv = C.c_double()
+    check(ctx.L.mpsg_compress(ctx.h, len(ts), handle_array(ts), ks.ptr(), int(chimax), int(maxstep), float(delta),
+                              int(normalize), out, C.byref(conv)))
+    return conv.value, [Tensor(ctx, C.c_void_p(h)).to_dict() for h in out]
+
+
+def compressSingleSite(sites, mpo, itokeys, chimax=100, maxstep=5, delta=1e-10, ctx=None):
+    """compressSingleSite(mps, mpo, chimax, maxstep, delta): returns (conv, fitted site dicts)."""
+    ctx = ctx or default_context()
+    ts = [Tensor.from_dict(ctx, x, 1) for x in sites]
+    ws, ks = MPOArray(mpo), ItoKeyArray(itokeys)
+    out = (C.c_void_p * len(ts))()
+    conv = C.c_double()
+    check(ctx.L.mpsg_compress_single_site(ctx.h, len(ts), handle_array(ts), ws.ptr(), ks.ptr(), int(chimax),
+                                          int(maxstep), float(delta), out, C.byref(conv)))
+    return conv.value, [Tensor(ctx, C.c_void_p(h)).to_dict() for h in out]
+
+
 def split(A, itokey, chimax, doTrunc=False, tr_weight=1e-12, normalize=True, ctx=None):
     """Returns (U, Vt, lambda, truncated_weight, chi) -- direction 0 of the reference."""
     ctx = ctx or default_context()

@@ -123,6 +123,20 @@ struct Engine {
     return m;
   }
 
+  // The dummy second site of a single-site contraction: identity on D MPO channels, one local state
+  // (of charge 0, ItoKey(1, 0)).
+  static MPO dummy_site_mpo(int D) {
+    MPO m;
+    m.Dl = m.Dr = D;
+    for (int w = 0; w < D; ++w) {
+      MPOEntry en;
+      en.wl = en.wr = (uint32_t)w;
+      en.ops.push_back(OpEl{0, 0, 1.0});
+      m.e.push_back(en);
+    }
+    return m;
+  }
+
   // excited-state targeting: the target MPS and its overlap environments with the engine's state
   const std::vector<TensorP>* target = nullptr;
   std::map<int, TensorP> ovL, ovR;
@@ -227,14 +241,7 @@ struct Engine {
     const Tensor& Le = *L[site - 1];
     const Tensor& Re = *R[site + 1];
     const MPO& W1 = mpo[site];
-    MPO W2;  // identity on the right channels, one-state local space
-    W2.Dl = W2.Dr = W1.Dr;
-    for (int w = 0; w < W1.Dr; ++w) {
-      MPOEntry en;
-      en.wl = en.wr = (uint32_t)w;
-      en.ops.push_back(OpEl{0, 0, 1.0});
-      W2.e.push_back(en);
-    }
+    const MPO W2 = dummy_site_mpo(W1.Dr);
     const ItoKey ikd(1, (Q)0);
     const Tensor& A = *mps[site];
     Layout s0;

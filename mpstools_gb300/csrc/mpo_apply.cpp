@@ -1,4 +1,5 @@
-// applyMPO (src/MPSfunctions.hpp:2088-2346) and compressTwoSite (src/MPSfunctions.hpp:2797-2940).
+// applyMPO (src/MPSfunctions.hpp:2088-2346), compressTwoSite (src/MPSfunctions.hpp:2797-2940), compress
+// (src/MPSfunctions.hpp:2349-2510) and compressSingleSite (src/MPSfunctions.hpp:2667-2792).
 //
 // applyMPO: the exact product W|psi>.  Each MPS block A(a, b; s_in) and each MPO element
 // W[wl, wr](s_out <- s_in) = v give a piece v A of the "five-leg" block ((a, wl), (b, wr); s_out).
@@ -10,7 +11,9 @@
 // piece of channels (wl, wr) at the channels' offsets.  Host planning, device copies (pieces with one
 // term copied with their factor, several terms summed by a block linear combination first).
 //
-// compressTwoSite: variational two-site fit of W|psi> at bond dimension <= chimax (see the function).
+// compressTwoSite, compress, compressSingleSite: variational fits of W|psi> (of psi for compress) at
+// bond dimension <= chimax; see the functions.  The single-site update is contractSingle, the two-site
+// matvec plan with a dummy second site.
 #include <algorithm>
 #include <cmath>
 
@@ -167,6 +170,7 @@ std::vector<const Tensor*> cptrs(const std::vector<TensorP>& v) {
 // then dropDangling: columns of site s and rows of site s+1 beyond the kept count of their sector go.
 void truncate_mps(Ctx* ctx, std::vector<TensorP>& mps, std::map<int, TensorP>& lam, int chimax, double delta) {
   const int N = (int)mps.size();
+  if (chimax <= 0) return;  // truncate() with chimax 0 leaves the state as it is
   for (int site = 0; site + 1 < N; ++site) {
     const Tensor& l = *lam.at(site);
     std::vector<double> vals;  // the sectors' values back to back (the arena has padding between them)
@@ -221,18 +225,101 @@ void truncate_mps(Ctx* ctx, std::vector<TensorP>& mps, std::map<int, TensorP>& l
   ctx->sync();
 }
 
+// prepareSite(mps, site, "l" / "r", true) (src/MPSTypes.hpp:586-621) without truncation; the last site
+// ("l") and site 0 ("r") multiply into the boundary dummies, i.e. the norm is dropped.
+TensorP prep_l(Ctx* ctx, std::vector<TensorP>& m, int site) {
+  TensorP l;
+  prepare_matrix_l(ctx, m[site], site + 1 < (int)m.size() ? &m[site + 1] : nullptr, &l, 0.0);
+  return l;
+}
+
+TensorP prep_r(Ctx* ctx, std::vector<TensorP>& m, int site) {
+  TensorP l;
+  prepare_matrix_r(ctx, site > 0 ? &m[site - 1] : nullptr, m[site], &l, 0.0);
+  return l;
+}
+
 void sweep_lr(Ctx* ctx, std::vector<TensorP>& m, std::map<int, TensorP>& lam) {
   const int N = (int)m.size();
-  for (int site = 0; site + 1 < N; ++site) {  // prepareSite(site, "l", true)
-    TensorP l;
-    prepare_matrix_l(ctx, m[site], &m[site + 1], &l, 0.0);
-    lam[site] = l;
+  for (int site = 0; site + 1 < N; ++site) lam[site] = prep_l(ctx, m, site);
+  for (int site = N - 1; site > 0; --site) lam[site - 1] = prep_r(ctx, m, site);
+}
+
+// contractSingle(out, BL, A, W, BR, itokey) (src/MPSfunctions.hpp:857-885): the two-site matvec plan
+// with a dummy second site (identity on W's right channels, one local state of charge 0); the output
+// holds every block the contraction reaches.
+TensorP contract_single(Ctx* ctx, const Tensor& BL, const Tensor& BR, const Tensor& A, const MPO& W, const ItoKey& ik) {
+  const MPO W2 = Engine::dummy_site_mpo(W.Dr);
+  const ItoKey ikd(1, (Q)0);
+  Layout s0;
+  for (auto& b : A.b) s0.add(K2(b.k.q0, b.k.q1, b.k.p0, 0), b.r, b.c);
+  s0.finalize();
+  TensorP th = make_tensor(ctx, 2, s0, true);
+  std::vector<CopyOp> ops;
+  for (auto& b : A.b) {
+    const Block& t = th->b[th->find(K2(b.k.q0, b.k.q1, b.k.p0, 0))];
+    ops.push_back(CopyOp{A.d + b.off, th->d + t.off, nullptr, nullptr, b.r, b.c, b.r, t.r, 0, 1.0});
   }
-  for (int site = N - 1; site > 0; --site) {  // prepareSite(site, "r", true)
-    TensorP l;
-    prepare_matrix_r(ctx, &m[site - 1], m[site], &l, 0.0);
-    lam[site - 1] = l;
+  run_copyops(ctx, ops);
+  auto mv = build_matvec(ctx, BL, BR, s0, W, W2, ik, ikd, nullptr, MPSG_PREC_FP64);
+  TensorP o2 = make_tensor(ctx, 2, mv->out, true);
+  mv->run(th->d, o2->d);
+  Layout l1;
+  for (auto& b : o2->b) l1.add(K1(b.k.q0, b.k.q1, b.k.p0), b.r, b.c);
+  l1.finalize();
+  TensorP o = make_tensor(ctx, 1, l1, false);
+  ops.clear();
+  for (auto& b : o2->b) {
+    const Block& t = o->b[o->find(K1(b.k.q0, b.k.q1, b.k.p0))];
+    ops.push_back(CopyOp{o2->d + b.off, o->d + t.off, nullptr, nullptr, b.r, b.c, b.r, t.r, 0, 1.0});
   }
+  run_copyops(ctx, ops);
+  ctx->sync();
+  return o;
+}
+
+// The sweeps shared by compress and compressSingleSite (src/MPSfunctions.hpp:2397-2468, 2715-2777):
+// environments <mps| W |comp> (mps lower, the fit upper), sites 0 .. N-2 right (contractSingle,
+// prepareSite "l") and N-1 .. 1 left (contractSingle, prepareSite "r"); after each sweep
+// conv = (n1^2 + n2^2 - 2 |<comp|mps>|) / n1^2; stop when conv grows, after maxstep sweeps or when
+// |conv| < delta.  Leaves the environments in BL / BR.
+void single_site_fit(Ctx* ctx, const std::vector<TensorP>& mps, std::vector<TensorP>& comp, const std::vector<MPO>& W,
+                     const std::vector<ItoKey>& ik, double n1, int maxstep, double delta, std::map<int, TensorP>& BL,
+                     std::map<int, TensorP>& BR) {
+  const int N = (int)mps.size();
+  BL[-1] = Engine::lmin(ctx);
+  BR[N] = Engine::rmax(ctx, *mps[N - 1]);
+  bool converged = maxstep == 0;
+  if (!converged)
+    for (int site = N - 1; site > 0; --site)
+      BR[site] = env_update(ctx, *BR[site + 1], *mps[site], W[site], ik[site], -1, nullptr, comp[site].get());
+  double conv_old = 1.0;
+  int step = 1;
+  while (!converged) {
+    for (int site = 0; site < N - 1; ++site) {
+      comp[site] = contract_single(ctx, *BL[site - 1], *BR[site + 1], *mps[site], W[site], ik[site]);
+      prep_l(ctx, comp, site);
+      BL[site] = env_update(ctx, *BL[site - 1], *mps[site], W[site], ik[site], 1, nullptr, comp[site].get());
+    }
+    for (int site = N - 1; site > 0; --site) {
+      comp[site] = contract_single(ctx, *BL[site - 1], *BR[site + 1], *mps[site], W[site], ik[site]);
+      prep_r(ctx, comp, site);
+      BR[site] = env_update(ctx, *BR[site + 1], *mps[site], W[site], ik[site], -1, nullptr, comp[site].get());
+    }
+    const double n2 = std::sqrt(Engine::overlap(ctx, cptrs(comp), cptrs(comp), ik));
+    const double conv =
+        (n1 * n1 + n2 * n2 - 2 * std::fabs(Engine::overlap(ctx, cptrs(comp), cptrs(mps), ik))) / (n1 * n1);
+    if (conv_old < conv) break;
+    conv_old = conv;
+    if (step >= maxstep || std::fabs(conv) < delta) converged = true;
+    ++step;
+  }
+}
+
+double conv_measure(Ctx* ctx, const std::vector<TensorP>& comp, const std::vector<TensorP>& mps,
+                    const std::vector<ItoKey>& ik, double n1) {
+  const double n2 = std::sqrt(Engine::overlap(ctx, cptrs(comp), cptrs(comp), ik));
+  return (n1 * n1 + n2 * n2 - 2 * std::fabs(Engine::overlap(ctx, cptrs(comp), cptrs(mps), ik))) / (n1 * n1);
 }
 
 }  // namespace
@@ -306,8 +393,70 @@ double compress_two_site(Ctx* ctx, std::vector<TensorP>& mps, const std::vector<
     if (step >= maxstep || std::fabs(conv) < delta) converged = true;
     ++step;
   }
-  const double n2 = std::sqrt(Engine::overlap(ctx, cptrs(comp), cptrs(comp), ik));
-  conv = (n1 * n1 + n2 * n2 - 2 * std::fabs(Engine::overlap(ctx, cptrs(comp), cptrs(mps), ik))) / (n1 * n1);
+  conv = conv_measure(ctx, comp, mps, ik, n1);
+  mps = comp;
+  return conv;
+}
+
+// compress(mps, chimax, maxstep, delta, verbose, normalize) (src/MPSfunctions.hpp:2349-2510): variational
+// single-site compression of psi to bond dimension <= chimax.  psi is swept with prepareSite "l" over
+// 0 .. Nmax-1 and "r" over Nmax-1 .. Nmin (Nmax = N-1, Nmin = 1; with normalize N and 0, which drops the
+// norm into the boundary dummies); the initial guess is psi truncated to chimax with the lambdas of
+// those sweeps, itself swept l and r; the fit sweeps with the identity MPO; then site 0 is fitted once
+// more and the fit swept l and r.  conv = |fit - psi|^2 / |psi|^2.  Replaces mps by the fit.
+// maxstep = 0 is rejected: the reference's last-site update then reads an environment it never built.
+double compress(Ctx* ctx, std::vector<TensorP>& mps, const std::vector<ItoKey>& ik, int chimax, int maxstep,
+                double delta, bool normalize) {
+  const int N = (int)mps.size();
+  MPSG_CHECK(N >= 3 && (int)ik.size() == N, "compress: sizes differ");
+  MPSG_CHECK(maxstep >= 1, "compress: maxstep must be at least 1");
+  const int nmin = normalize ? 0 : 1, nmax = normalize ? N : N - 1;
+  std::map<int, TensorP> lam;
+  for (int site = 0; site < nmax; ++site) lam[site] = prep_l(ctx, mps, site);
+  for (int site = nmax - 1; site >= nmin; --site) lam[site - 1] = prep_r(ctx, mps, site);
+  std::vector<TensorP> comp;
+  for (auto& t : mps) comp.push_back(tensor_copy(*t));
+  truncate_mps(ctx, comp, lam, chimax, delta);
+  std::map<int, TensorP> lamc;
+  sweep_lr(ctx, comp, lamc);
+  const double n1 = std::sqrt(Engine::overlap(ctx, cptrs(mps), cptrs(mps), ik));
+  std::vector<MPO> id;
+  for (int s = 0; s < N; ++s) id.push_back(Engine::identity_mpo((int)ik[s].size()));
+  std::map<int, TensorP> BL, BR;
+  single_site_fit(ctx, mps, comp, id, ik, n1, maxstep, delta, BL, BR);
+  comp[0] = contract_single(ctx, *BL[-1], *BR[1], *mps[0], id[0], ik[0]);
+  sweep_lr(ctx, comp, lamc);
+  const double conv = conv_measure(ctx, comp, mps, ik, n1);
+  mps = comp;
+  return conv;
+}
+
+// compressSingleSite(mps, mpo, chimax, maxstep, delta) (src/MPSfunctions.hpp:2667-2792): variational
+// single-site fit of W|psi>.  n1 = |W psi| from the exact product; the initial guess is W applied to psi
+// truncated to chimax / D (D = the MPO's right bond dimension at site 1) after an l and an r sweep,
+// itself swept l and r; conv as compressTwoSite computes it (the overlap term with psi).  Replaces mps by
+// the fit.
+double compress_single_site(Ctx* ctx, std::vector<TensorP>& mps, const std::vector<MPO>& W,
+                            const std::vector<ItoKey>& ik, int chimax, int maxstep, double delta) {
+  const int N = (int)mps.size();
+  MPSG_CHECK(N >= 3 && (int)W.size() == N && (int)ik.size() == N, "compress: sizes differ");
+  double n1;
+  {
+    auto full = apply_mpo(ctx, cptrs(mps), W, ik);
+    n1 = std::sqrt(Engine::overlap(ctx, cptrs(full), cptrs(full), ik));
+  }
+  std::vector<TensorP> tmps;
+  for (auto& t : mps) tmps.push_back(tensor_copy(*t));
+  std::map<int, TensorP> lam;
+  sweep_lr(ctx, tmps, lam);
+  truncate_mps(ctx, tmps, lam, (int)std::floor((double)chimax / (double)W[1].Dr), delta);
+  std::vector<TensorP> comp = apply_mpo(ctx, cptrs(tmps), W, ik);
+  tmps.clear();
+  std::map<int, TensorP> lamc;
+  sweep_lr(ctx, comp, lamc);
+  std::map<int, TensorP> BL, BR;
+  single_site_fit(ctx, mps, comp, W, ik, n1, maxstep, delta, BL, BR);
+  const double conv = conv_measure(ctx, comp, mps, ik, n1);
   mps = comp;
   return conv;
 }
@@ -353,6 +502,36 @@ mpsg_status mpsg_compress_two_site(mpsg_ctx ctx, int32_t N, const mpsg_tensor* s
   std::vector<ItoKey> k;
   sites_in(N, sites, W, ik, m, w, k);
   *conv = compress_two_site(C(ctx), m, w, k, (int)chimax, (int)maxstep, delta, doTrunc != 0, tr_weight);
+  for (int i = 0; i < N; ++i) out[i] = wrap(m[i]);
+  API_END
+}
+
+mpsg_status mpsg_compress(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_itokey* ik, uint32_t chimax,
+                          uint32_t maxstep, double delta, int32_t normalize, mpsg_tensor* out, double* conv) {
+  API_BEGIN
+  MPSG_CHECK(ctx && sites && ik && out && conv && N >= 1, "null argument");
+  std::vector<TensorP> m;
+  std::vector<ItoKey> k;
+  for (int i = 0; i < N; ++i) {
+    MPSG_CHECK(sites[i] && T(sites[i]).nphys == 1, "MPS site tensors must have one physical index");
+    m.push_back(tensor_copy(T(sites[i])));
+    k.push_back(itokey_from_c(&ik[i]));
+  }
+  *conv = compress(C(ctx), m, k, (int)chimax, (int)maxstep, delta, normalize != 0);
+  for (int i = 0; i < N; ++i) out[i] = wrap(m[i]);
+  API_END
+}
+
+mpsg_status mpsg_compress_single_site(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* W,
+                                      const mpsg_itokey* ik, uint32_t chimax, uint32_t maxstep, double delta,
+                                      mpsg_tensor* out, double* conv) {
+  API_BEGIN
+  MPSG_CHECK(ctx && sites && W && ik && out && conv && N >= 1, "null argument");
+  std::vector<TensorP> m;
+  std::vector<MPO> w;
+  std::vector<ItoKey> k;
+  sites_in(N, sites, W, ik, m, w, k);
+  *conv = compress_single_site(C(ctx), m, w, k, (int)chimax, (int)maxstep, delta);
   for (int i = 0; i < N; ++i) out[i] = wrap(m[i]);
   API_END
 }

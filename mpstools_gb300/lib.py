@@ -87,6 +87,8 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_excited_simulate.argtypes = [vp, vp, f64, u32, f64, u32, i32, f64, f64, i32, i32, P(f64)]
     L.mpsg_apply_mpo.argtypes = [vp, i32, vp, vp, vp, vp]
     L.mpsg_compress_two_site.argtypes = [vp, i32, vp, vp, vp, u32, u32, f64, i32, f64, vp, P(f64)]
+    L.mpsg_compress.argtypes = [vp, i32, vp, vp, u32, u32, f64, i32, vp, P(f64)]
+    L.mpsg_compress_single_site.argtypes = [vp, i32, vp, vp, vp, u32, u32, f64, vp, P(f64)]
     L.mpsg_dmrg_save.argtypes = [vp, C.c_char_p]
     L.mpsg_dmrg_load.argtypes = [vp, C.c_char_p, P(vp)]
     L.mpsg_split_fallbacks.argtypes = []

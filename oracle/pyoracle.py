@@ -729,11 +729,7 @@ def compress_two_site(sites, W, itokeys, chimax=100, maxstep=5, delta=1e-10, doT
         t[s], t[s + 1], lam[s] = prepare_left(t[s], t[s + 1])
     for s in range(N - 1, 0, -1):
         t[s - 1], t[s], lam[s - 1] = prepare_right(t[s - 1], t[s])
-    chi = int(np.floor(chimax / W[1][2]))
-    for s in range(N - 1):  # truncate(mps, chi, delta): dropDangling of the cut columns / rows
-        keep = truncate_lambda(lam[s], chi, delta)
-        t[s] = {k: v[:, :keep.get(k[1], 0)] for k, v in t[s].items() if keep.get(k[1], 0) > 0}
-        t[s + 1] = {k: v[:keep.get(k[0], 0), :] for k, v in t[s + 1].items() if keep.get(k[0], 0) > 0}
+    _truncate_sites(t, lam, int(np.floor(chimax / W[1][2])), delta)
     comp = apply_mpo(t, W, itokeys)
     for s in range(N - 1):
         comp[s], comp[s + 1], _ = prepare_left(comp[s], comp[s + 1])
@@ -776,6 +772,146 @@ def compress_two_site(sites, W, itokeys, chimax=100, maxstep=5, delta=1e-10, doT
     conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, sites, itokeys))) / (n1 * n1)
     return conv, comp
 
+
+
+def contract_single(BL, BR, A, W, ik):
+    """contractSingle(out, BL, A, W, BR, itokey) (src/MPSfunctions.hpp:857-885) as the two-site
+    contraction with a dummy second site (identity MPO tensor on W's right channels, one local state of
+    charge 0)."""
+    D = W[2]
+    W2 = ([(w, w, 0, 0, 1.0) for w in range(D)], D, D)
+    th = {(a, b, p, 0): v for (a, b, p), v in A.items()}
+    out = contract_twosite(BL, BR, th, W, W2, ik, [0])
+    return {(a, b, p): v for (a, b, p, _), v in out.items()}
+
+
+def _prep_l(m, s):
+    """prepareSite(mps, s, "l", true) in place (the last site multiplies into the right dummy)."""
+    nxt = m[s + 1] if s + 1 < len(m) else None
+    m[s], nxt, lam = prepare_left(m[s], nxt)
+    if nxt is not None:
+        m[s + 1] = nxt
+    return lam
+
+
+def _prep_r(m, s):
+    """prepareSite(mps, s, "r", true) in place (site 0 multiplies into the left dummy)."""
+    prv = m[s - 1] if s > 0 else None
+    prv, m[s], lam = prepare_right(prv, m[s])
+    if prv is not None:
+        m[s - 1] = prv
+    return lam
+
+
+def _truncate_sites(t, lam, chimax, delta):
+    """truncate(mps, chimax, delta) (src/MPSfunctions.hpp:1705-1728): per bond the kept count of
+    DiagBlockMatrix::truncate, then dropDangling; chimax = 0 returns without truncating."""
+    if chimax == 0:
+        return
+    for s in range(len(t) - 1):
+        keep = truncate_lambda(lam[s], chimax, delta)
+        t[s] = {k: v[:, :keep.get(k[1], 0)] for k, v in t[s].items() if keep.get(k[1], 0) > 0}
+        t[s + 1] = {k: v[:keep.get(k[0], 0), :] for k, v in t[s + 1].items() if keep.get(k[0], 0) > 0}
+
+
+def _rmax(sites):
+    dims = {}
+    for (a, b, p), v in sites[-1].items():
+        dims.setdefault(b, v.shape[1])
+    return {(q, q, 0): np.eye(n) for q, n in dims.items()}
+
+
+def _single_site_fit(mps, comp, W, itokeys, n1, maxstep, delta):
+    """The sweeps shared by compress and compressSingleSite: environments <mps| W |comp> (mps lower,
+    the fit upper), sites 0 .. N-2 right (contractSingle, prepareSite "l") and N-1 .. 1 left
+    (contractSingle, prepareSite "r"); after each sweep conv = (n1^2 + n2^2 - 2 |<comp|mps>|) / n1^2; stop
+    when conv grows, after maxstep sweeps or when |conv| < delta.  Returns the left environments."""
+    N = len(mps)
+    BL = {-1: {(0, 0, 0): np.ones((1, 1))}}
+    BR = {N: _rmax(mps)}
+    converged = maxstep == 0
+    if not converged:
+        for s in range(N - 1, 0, -1):
+            BR[s] = add_contraction_layer2(BR[s + 1], mps[s], comp[s], W[s], itokeys[s], -1)
+    conv_old, step = 1.0, 1
+    while not converged:
+        for s in range(N - 1):
+            comp[s] = contract_single(BL[s - 1], BR[s + 1], mps[s], W[s], itokeys[s])
+            _prep_l(comp, s)
+            BL[s] = add_contraction_layer2(BL[s - 1], mps[s], comp[s], W[s], itokeys[s], 1)
+        for s in range(N - 1, 0, -1):
+            comp[s] = contract_single(BL[s - 1], BR[s + 1], mps[s], W[s], itokeys[s])
+            _prep_r(comp, s)
+            BR[s] = add_contraction_layer2(BR[s + 1], mps[s], comp[s], W[s], itokeys[s], -1)
+        n2 = np.sqrt(overlap(comp, comp, itokeys))
+        conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, mps, itokeys))) / (n1 * n1)
+        if conv_old < conv:
+            break
+        conv_old = conv
+        if step >= maxstep or abs(conv) < delta:
+            converged = True
+        step += 1
+    return BL, BR
+
+
+def compress(sites, itokeys, chimax=100, maxstep=5, delta=1e-10, normalize=False):
+    """compress (src/MPSfunctions.hpp:2349-2510) restated: variational single-site compression of psi to
+    bond dimension <= chimax; returns (conv, the prepared psi, the fitted sites).  psi is first swept
+    with prepareSite "l" over 0 .. Nmax-1 and "r" over Nmax-1 .. Nmin (Nmax = N-1, Nmin = 1, or N and 0
+    with normalize, which drops the norm into the dummies); the initial guess is psi truncated to chimax
+    with those lambdas, then swept l and r; after the sweeps site 0 is fitted once more and the fit is
+    swept l and r again.  conv = |fit - psi|^2 / |psi|^2."""
+    N = len(sites)
+    m = [dict(x) for x in sites]
+    lam = {}
+    nmin, nmax = (0, N) if normalize else (1, N - 1)
+    for s in range(nmax):
+        lam[s] = _prep_l(m, s)
+    for s in range(nmax - 1, nmin - 1, -1):
+        lam[s - 1] = _prep_r(m, s)
+    comp = [dict(x) for x in m]
+    _truncate_sites(comp, lam, chimax, delta)
+    for s in range(N - 1):
+        _prep_l(comp, s)
+    for s in range(N - 1, 0, -1):
+        _prep_r(comp, s)
+    n1 = np.sqrt(overlap(m, m, itokeys))
+    idW = [identity_mpo(len(k)) for k in itokeys]
+    BL, BR = _single_site_fit(m, comp, idW, itokeys, n1, maxstep, delta)
+    comp[0] = contract_single(BL[-1], BR[1], m[0], idW[0], itokeys[0])
+    for s in range(N - 1):
+        _prep_l(comp, s)
+    for s in range(N - 1, 0, -1):
+        _prep_r(comp, s)
+    n2 = np.sqrt(overlap(comp, comp, itokeys))
+    conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, m, itokeys))) / (n1 * n1)
+    return conv, m, comp
+
+
+def compress_single_site(sites, W, itokeys, chimax=100, maxstep=5, delta=1e-10):
+    """compressSingleSite (src/MPSfunctions.hpp:2667-2792) restated: variational single-site fit of
+    W|psi>; n1 = |W psi| from the exact product; initial guess W applied to psi truncated to chimax / D
+    (D = W's right bond dimension at site 1) after an l and an r sweep, itself swept l and r.  conv as
+    in compressTwoSite (the overlap term with psi).  Returns (conv, fitted sites)."""
+    N = len(sites)
+    full = apply_mpo(sites, W, itokeys)
+    n1 = np.sqrt(overlap(full, full, itokeys))
+    t = [dict(x) for x in sites]
+    lam = {}
+    for s in range(N - 1):
+        _prep_l(t, s)
+    for s in range(N - 1, 0, -1):
+        lam[s - 1] = _prep_r(t, s)
+    _truncate_sites(t, lam, int(np.floor(chimax / W[1][2])), delta)
+    comp = apply_mpo(t, W, itokeys)
+    for s in range(N - 1):
+        _prep_l(comp, s)
+    for s in range(N - 1, 0, -1):
+        _prep_r(comp, s)
+    _single_site_fit(sites, comp, W, itokeys, n1, maxstep, delta)
+    n2 = np.sqrt(overlap(comp, comp, itokeys))
+    conv = (n1 * n1 + n2 * n2 - 2 * abs(overlap(comp, sites, itokeys))) / (n1 * n1)
+    return conv, comp
 
 # ------------------------------------------------------------------ TEBD (complex FP64)
 def nn_gate(W1, W2, site1, N, dt, d1=2, d2=2):

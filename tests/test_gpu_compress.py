@@ -1,6 +1,6 @@
-"""applyMPO and compressTwoSite on the GPU against the oracle's restatements: the same block structure
-and values for W|psi>, the same convergence measure and the same fitted state (dense amplitudes)
-for a binding and a non-binding bond dimension."""
+"""applyMPO, compressTwoSite, compress and compressSingleSite on the GPU against the oracle's
+restatements: the same block structure and values for W|psi>, the same convergence measures and the
+same fitted states (dense amplitudes) for binding and non-binding bond dimensions."""
 import numpy as np
 import pytest
 
@@ -38,6 +38,34 @@ def test_compress_matches_oracle(ctx, chimax):
                                         tr_weight=1e-12)
     vg, vr = ed.mps_sector_vector(fit_g, N // 2), ed.mps_sector_vector(fit_r, N // 2)
     print(f"chimax {chimax}: conv gpu {conv_g:.12e} oracle {conv_r:.12e}, "
+          f"max amplitude diff {np.abs(vg - vr).max() / np.abs(vr).max():.2e}")
+    assert abs(conv_g - conv_r) <= 1e-9 * max(1.0, abs(conv_r))
+    assert np.abs(vg - vr).max() <= 1e-9 * np.abs(vr).max()
+
+
+@pytest.mark.parametrize("chimax,normalize", [(4, False), (200, False), (6, True)])
+def test_single_site_compress_matches_oracle(ctx, chimax, normalize):
+    W, ik, psi = _case(chi=16)
+    N = len(psi)
+    conv_g, fit_g = api.compress(psi, ik, chimax=chimax, maxstep=3, delta=1e-14, normalize=normalize, ctx=ctx)
+    conv_r, _, fit_r = O.compress(psi, ik, chimax=chimax, maxstep=3, delta=1e-14, normalize=normalize)
+    vg, vr = ed.mps_sector_vector(fit_g, N // 2), ed.mps_sector_vector(fit_r, N // 2)
+    if normalize:  # the sign of the dropped norm is the boundary SVD's choice
+        vg = vg * np.sign(vg @ vr)
+    print(f"compress chimax {chimax} normalize {normalize}: conv gpu {conv_g:.12e} oracle {conv_r:.12e}, "
+          f"max amplitude diff {np.abs(vg - vr).max() / np.abs(vr).max():.2e}")
+    assert abs(conv_g - conv_r) <= 1e-9 * max(1e-3, abs(conv_r))
+    assert np.abs(vg - vr).max() <= 1e-9 * np.abs(vr).max()
+
+
+@pytest.mark.parametrize("chimax", [15, 200])
+def test_compress_single_site_matches_oracle(ctx, chimax):
+    W, ik, psi = _case(chi=16)
+    N = len(psi)
+    conv_g, fit_g = api.compressSingleSite(psi, W, ik, chimax=chimax, maxstep=3, delta=1e-14, ctx=ctx)
+    conv_r, fit_r = O.compress_single_site(psi, W, ik, chimax=chimax, maxstep=3, delta=1e-14)
+    vg, vr = ed.mps_sector_vector(fit_g, N // 2), ed.mps_sector_vector(fit_r, N // 2)
+    print(f"compressSingleSite chimax {chimax}: conv gpu {conv_g:.12e} oracle {conv_r:.12e}, "
           f"max amplitude diff {np.abs(vg - vr).max() / np.abs(vr).max():.2e}")
     assert abs(conv_g - conv_r) <= 1e-9 * max(1.0, abs(conv_r))
     assert np.abs(vg - vr).max() <= 1e-9 * np.abs(vr).max()
