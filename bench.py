@@ -34,6 +34,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DMRG sweep time + matvec TFLOP/s, mixed/batched vs FP64 GPU, dE/E<1e-10"
 L_SITES, NUP, CHI, SEED_MPS, SEED_DELTA = 100, 50, 2048, 12345, 1
+# arithmetic of each Lanczos mode: tensor-core matvec with FP64 recurrence / energies, or plain FP64
+DTYPE = {"fp64": "f64", "auto": "tf32x3+f64", "mixed": "tf32x3+f64"}
 CENTER = L_SITES // 2 - 1
 
 
@@ -263,29 +265,38 @@ def gpu_arm(args):
     value = mv_flops * world / total / 1e12
     steps_rec = eng.steps()[n_steps0:]
 
-    # ------------------------------------------------- the plain FP64 GPU path on the same updates
-    fp64_leg = None
-    if prec != "fp64" and not args.no_fp64_leg:
-        eng64 = api.DMRGengine(sites, W, ik, prec="fp64", ctx=ctx)
-        eng64.build_environments(center)
+    # ------------------------------------------- other precisions (plain FP64 GPU path, AUTO) on the same updates
+    def other_leg(p):
+        e2 = api.DMRGengine(sites, W, ik, prec=p, ctx=ctx)
+        e2.build_environments(center)
         for i in range(args.warmup):
-            eng64.do_step(center, 1 if i % 2 == 0 else -1, args.chi)
-        n64 = len(eng64.steps())
-        t64 = []
+            e2.do_step(center, 1 if i % 2 == 0 else -1, args.chi)
+        n2 = len(e2.steps())
+        t2 = []
         for i in range(args.steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            eng64.do_step(center, 1 if (args.warmup + i) % 2 == 0 else -1, args.chi)
+            e2.do_step(center, 1 if (args.warmup + i) % 2 == 0 else -1, args.chi)
             e1.record(stream)
             e1.synchronize()
-            t64.append(e0.elapsed_time(e1) * 1e-3)
-        e64 = [r["E"] for r in eng64.steps()[n64:]]
-        emix = [r["E"] for r in steps_rec]
-        fp64_leg = {"ms_per_step": float(np.sum(t64)) / args.steps * 1e3, "energies": e64,
-                    "speedup_of_this_line": float(np.sum(t64)) / (total / world),
+            t2.append(e0.elapsed_time(e1) * 1e-3)
+        energies = [r["E"] for r in e2.steps()[n2:]]
+        e2.close()
+        return float(np.sum(t2)), energies
+
+    emix = [r["E"] for r in steps_rec]
+    fp64_leg, auto_leg = None, None
+    if prec != "fp64" and not args.no_fp64_leg:
+        t64, e64 = other_leg("fp64")
+        fp64_leg = {"ms_per_step": t64 / args.steps * 1e3, "energies": e64,
+                    "speedup_of_this_line": t64 / (total / world),
                     "max_rel_energy_diff": max(abs(a - b) / abs(b) for a, b in zip(emix, e64))}
-        eng64.close()
+        if prec == "mixed":
+            ta, ea = other_leg("auto")
+            auto_leg = {"ms_per_step": ta / args.steps * 1e3, "energies": ea,
+                        "speedup_over_fp64": t64 / ta,
+                        "max_rel_energy_diff_vs_fp64": max(abs(a - b) / abs(b) for a, b in zip(ea, e64))}
     lam_c = eng.lam(center)
     lam_all = np.sort(np.concatenate([np.asarray(v) for v in lam_c.values() if len(v)]))[::-1]
     spectrum = {"chi": int(lam_all.size), "s_max": float(lam_all[0]), "s_min_kept": float(lam_all[-1]),
@@ -344,7 +355,7 @@ def gpu_arm(args):
             "matvec_seconds": mv64}
     roof_tc = None
     if prec != "fp64":
-        mv_prec = "tf32x3" if prec == "auto" else prec  # the tensor-core matvec of the mixed Lanczos phase
+        mv_prec = "tf32x3" if prec in ("auto", "mixed") else prec  # the tensor-core matvec of the Lanczos
         info_tc, mv_tc = time_matvec(mv_prec)
         # hardware MMA work per algorithmic FLOP: 3 for hi/lo splits, x2 for TF32 (half the BF16 rate)
         mma_per_flop = (3 if mv_prec.endswith("x3") else 1) * (2 if mv_prec.startswith("tf32") else 1)
@@ -379,14 +390,15 @@ def gpu_arm(args):
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == "fp64" else prec,
+                "scaling": "weak", "vs_baseline": None, "dtype": DTYPE.get(prec, prec),
                 "data": "synthetic", "config": config_dict(args.chi, args.L, prec, args.svd), "clocks": clocks,
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
                 "lanczos_matvecs_per_step": matvecs / args.steps,
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
                 "env_seconds_per_step": (st1["env_seconds"] - st0["env_seconds"]) / args.steps,
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
-                "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg, "roofline_tensor_matvec": roof_tc,
+                "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg, "auto_path": auto_leg,
+                "roofline_tensor_matvec": roof_tc,
                 "matvec_flops_reference_schedule": info["flops_ref"]}
         print(json.dumps(line), flush=True)
     if dist:
@@ -440,7 +452,7 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
         Lo = lib.Tensor(ctx, Lo)
         outs = [U.export_flat(), V.export_flat(), lam.export_flat(), Lo.export_flat()]
         d2h[0] = sum(o[5].nbytes for o in outs)
-        return it.value
+        return it.value + (1 if prec == "mixed" else 0)  # + the FP64 Rayleigh-quotient matvec
 
     for i in range(2):
         step(i)
@@ -585,7 +597,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--chi", type=int, default=CHI)
     ap.add_argument("--L", type=int, default=L_SITES)
-    ap.add_argument("--prec", default="auto", help="fp64 | tf32 | tf32x3 | bf16 | bf16x3 | auto")
+    ap.add_argument("--prec", default=None,
+                    help="fp64 | tf32 | tf32x3 | bf16 | bf16x3 | auto | mixed (default: mixed; chains: auto)")
     ap.add_argument("--svd", default="density_eig", choices=["density", "density_mt", "density_eig", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
@@ -602,6 +615,8 @@ def main():
     ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--seq-chains", type=int, default=8)
     args = ap.parse_args()
+    if args.prec is None:
+        args.prec = "auto" if args.workload == "chains" else "mixed"
     if args.workload == "chains":
         chains_arm(args)
     elif args.workload == "tebd":

@@ -38,8 +38,11 @@ typedef enum {
   MPSG_PREC_TF32X3 = 2,  /* tcgen05 kind::tf32 with hi/lo split (3 products), FP32 accumulate */
   MPSG_PREC_BF16 = 3,    /* tcgen05 kind::f16 (bf16), FP32 accumulate */
   MPSG_PREC_BF16X3 = 4,  /* tcgen05 kind::f16 (bf16) hi/lo split (3 products), FP32 accumulate */
-  MPSG_PREC_AUTO = 5     /* Lanczos only: TF32X3 Lanczos to its precision floor, then the reference's
+  MPSG_PREC_AUTO = 5,    /* Lanczos only: TF32X3 Lanczos to its precision floor, then the reference's
                             FP64 Lanczos restarted from that state (energy test every iteration) */
+  MPSG_PREC_MIXED = 6    /* Lanczos only: TF32X3 Lanczos to its precision floor; the energy is the FP64
+                            Rayleigh quotient <psi|H|psi> / <psi|psi> of its ground state (one FP64
+                            matvec) */
 } mpsg_prec;
 
 typedef struct mpsg_ctx_s* mpsg_ctx;

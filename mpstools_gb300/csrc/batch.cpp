@@ -538,7 +538,7 @@ mpsg_status mpsg_batch_create(mpsg_ctx ctx, int32_t nchains, const mpsg_dmrg* ch
 mpsg_status mpsg_batch_set_options(mpsg_batch b, mpsg_prec prec, int32_t lanmax) {
   API_BEGIN
   MPSG_CHECK(b && b->b, "null batch");
-  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_AUTO, "unknown precision");
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_AUTO, "batched chains: precision must be FP64, TF32(X3), BF16(X3) or AUTO");
   MPSG_CHECK(lanmax >= 1 && lanmax <= 1000, "lanmax must be in [1, 1000]");
   b->b->prec = prec;
   b->b->lanmax = lanmax;

@@ -130,7 +130,7 @@ static void check_matvec_prec(mpsg_prec prec) {
   MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "matvec precision must be FP64, TF32(X3) or BF16(X3)");
 }
 static void check_lanczos_prec(mpsg_prec prec) {
-  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_AUTO, "unknown precision mode");
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_MIXED, "unknown precision mode");
 }
 
 mpsg_status mpsg_contract_twosite(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor theta, const mpsg_mpo* Wl,

@@ -300,9 +300,11 @@ __global__ void k_tri_bounds(const TriOp* __restrict__ ops) {
   const double tnorm = fmax(fabs(lo), fabs(hi));
   lo -= 2.0 * DBL_EPSILON * tnorm + DBL_MIN;
   hi += 2.0 * DBL_EPSILON * tnorm + DBL_MIN;
-  // largest eigenvalue: count(x) <= n - 1 exactly when x <= lambda_max
+  // largest eigenvalue: count(x) <= n - 1 exactly when x <= lambda_max.  It only places the floor
+  // (floor_rel * lambda_max, floor_rel = 32 n eps), so 1e-10 relative is enough: ~7 rounds of 32-point
+  // multisection instead of ~11 to full precision.
   double a = lo, b = hi;
-  for (int round = 0; round < 40 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++round) {
+  for (int round = 0; round < 40 && b - a > 1e-10 * fmax(fabs(a), fabs(b)) + DBL_MIN; ++round) {
     const double x = a + (b - a) * (double)(lane + 1) / 33.0;
     const int c = sturm_count(o.d, o.e2, n, x);
     const unsigned below = __ballot_sync(0xffffffffu, c <= n - 1);

@@ -1897,6 +1897,29 @@ double prec_stall(int prec) {
   }
 }
 
+double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosStats* st) {
+  const int64_t n = psi.nelem;
+  cudaStream_t s = ctx->stream;
+  double* w = (double*)ctx->dmalloc(sizeof(double) * (std::max<int64_t>(n, 2) + 2));
+  double* d_q = w + std::max<int64_t>(n, 2);
+  MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * std::max<int64_t>(n, 2), s));
+  auto t0 = std::chrono::steady_clock::now();
+  mv.run(psi.d, w);
+  launch_dot(psi.d, w, n, ctx->part, d_q, s);
+  launch_dot(psi.d, psi.d, n, ctx->part, d_q + 1, s);
+  double q[2] = {0, 0};
+  MPSG_CUDA(cudaMemcpyAsync(q, d_q, sizeof(q), cudaMemcpyDeviceToHost, s));
+  ctx->sync();
+  ctx->dfree(w);
+  if (st) {
+    st->matvecs += 1;
+    st->matvec_flops += mv.flops;
+    st->matvec_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  MPSG_CHECK(q[1] > 0, "Rayleigh quotient of a zero state");
+  return q[0] / q[1];
+}
+
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
                            double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj) {
@@ -1904,11 +1927,19 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
     return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, 0.0, 5, 0.0, proj);
   }
-  const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_TF32X3 : prec;
+  const int lo = (prec == MPSG_PREC_AUTO || prec == MPSG_PREC_MIXED) ? MPSG_PREC_TF32X3 : prec;
   LanczosResult r;
   {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
     r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo), proj);
+  }
+  if (prec == MPSG_PREC_MIXED) {
+    // the energy measured in FP64: the Rayleigh quotient of the mixed-precision ground state.  The
+    // tensor-core matvec scales H by a systematic factor (FP32 accumulation rounds towards zero; at
+    // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.
+    auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
+    r.E0 = rayleigh_quotient(ctx, *mv64, psi, st);
+    return r;
   }
   if (prec != MPSG_PREC_AUTO) return r;
   // FP64 finish: the reference's Lanczos restarted from the mixed-precision ground state, energy test

@@ -154,6 +154,8 @@ struct LanczosResult {
 // energy-test tolerance and stall level of the Lanczos for a matvec precision (0 for FP64)
 double prec_tol(int prec);
 double prec_stall(int prec);
+// <psi|H|psi> / <psi|psi> with one matvec of the plan (FP64 for MPSG_PREC_MIXED energies).
+double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosStats* st);
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
                       double stall_rel = 0.0, const double* proj = nullptr);

@@ -586,52 +586,129 @@ __global__ void k_trunc_rank(const double* __restrict__ S, int n, int32_t* rank)
   }
   rank[i] = r;
 }
-// out3[0] = truncated weight, out3[1] = kept count, out3[2] = 1/norm of kept values (normalisation)
-__global__ void k_trunc_select(const double* __restrict__ S, int n, const int32_t* __restrict__ sec_of, int nsec,
-                               int chimax, int doTrunc, double tr_weight, const int32_t* __restrict__ rank,
-                               int32_t* order, int32_t* counts, double* out3) {
-  for (int i = threadIdx.x; i < nsec; i += blockDim.x) counts[i] = 0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) order[rank[i]] = i;
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  double tw;
-  int cnt = 0;
-  if (!doTrunc) {
-    tw = 1.0;
-    for (int r = 0; r < n && cnt != chimax; ++r) {
-      const double v = S[order[r]];
-      if (!(fabs(v) > 1e-15)) break;
-      tw -= v * v;
-      counts[sec_of[order[r]]]++;
-      ++cnt;
-    }
-  } else {
-    double nrm2 = 0.0;
-    for (int i = 0; i < n; ++i) nrm2 += S[i] * S[i];
-    const double norm = sqrt(nrm2);
-    tw = norm;
-    for (int r = 0; r < n && fabs(tw) > norm * tr_weight && cnt < chimax; ++r) {
-      const double v = S[order[r]];
-      tw -= (v * v) / norm;
-      counts[sec_of[order[r]]]++;
-      ++cnt;
-    }
-    if (tw < 0 && fabs(tw) < 1e-14) tw = 0.0;
+// out3[0] = truncated weight, out3[1] = kept count, out3[2] = 1/norm of kept values (normalisation).
+// One block.  The floating-point recurrences stay sequential in the reference's order (the norm over
+// the values in storage order, the truncated weight over the values in rank order, the kept norm per
+// sector then over the sectors), run by thread 0 on values the block stages in shared memory chunk by
+// chunk; the scatter of the order, the per-sector counts and the per-sector partial sums run in
+// parallel.  sec_of is non-decreasing (each sector's values contiguous, stored descending).
+constexpr int kTruncThreads = 1024;
+constexpr int kTruncChunk = 2048;
+constexpr int kTruncSecSh = 2048;
+__global__ void __launch_bounds__(kTruncThreads)
+    k_trunc_select(const double* __restrict__ S, int n, const int32_t* __restrict__ sec_of, int nsec, int chimax,
+                   int doTrunc, double tr_weight, const int32_t* __restrict__ rank, int32_t* order, int32_t* counts,
+                   double* out3) {
+  __shared__ double sv[kTruncChunk];
+  __shared__ double part_sh[kTruncSecSh];
+  __shared__ int start_sh[kTruncSecSh];
+  __shared__ int s_stop, s_cnt;
+  __shared__ double s_norm;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < nsec; i += blockDim.x) counts[i] = 0;
+  for (int i = tid; i < n; i += blockDim.x) order[rank[i]] = i;
+  if (tid == 0) {
+    s_stop = 0;
+    s_cnt = 0;
+    s_norm = 0.0;
   }
-  // norm of the kept values, per sector in key order (values of a sector are stored descending)
-  double k2 = 0.0;
-  int i = 0;
-  while (i < n) {
-    const int sec = sec_of[i];
-    int j = i;
-    double part = 0.0;
-    int taken = 0;
-    while (j < n && sec_of[j] == sec) {
-      if (taken < counts[sec]) { part += S[j] * S[j]; ++taken; }
-      ++j;
+  __syncthreads();
+  // norm of all values (truncated-weight mode), summed in storage order
+  double nrm2 = 0.0;
+  if (doTrunc) {
+    for (int c0 = 0; c0 < n; c0 += kTruncChunk) {
+      const int m = min(kTruncChunk, n - c0);
+      for (int j = tid; j < m; j += blockDim.x) sv[j] = S[c0 + j];
+      __syncthreads();
+      if (tid == 0)
+        for (int j = 0; j < m; ++j) nrm2 += sv[j] * sv[j];
+      __syncthreads();
     }
-    k2 += part;
-    i = j;
+    if (tid == 0) s_norm = sqrt(nrm2);
+    __syncthreads();
+  }
+  const double norm = s_norm;
+  // the kept prefix of the rank order
+  double tw = doTrunc ? norm : 1.0;
+  int cnt = 0;
+  for (int c0 = 0; c0 < n; c0 += kTruncChunk) {
+    const int m = min(kTruncChunk, n - c0);
+    for (int j = tid; j < m; j += blockDim.x) sv[j] = S[order[c0 + j]];
+    __syncthreads();
+    if (tid == 0) {
+      int r = 0;
+      if (!doTrunc) {
+        for (; r < m && cnt != chimax; ++r) {
+          const double v = sv[r];
+          if (!(fabs(v) > 1e-15)) {
+            s_stop = 1;
+            break;
+          }
+          tw -= v * v;
+          ++cnt;
+        }
+        if (cnt == chimax) s_stop = 1;
+      } else {
+        for (; r < m && fabs(tw) > norm * tr_weight && cnt < chimax; ++r) {
+          const double v = sv[r];
+          tw -= (v * v) / norm;
+          ++cnt;
+        }
+        if (r < m) s_stop = 1;
+      }
+      s_cnt = cnt;
+    }
+    __syncthreads();
+    const int stop = s_stop;
+    __syncthreads();
+    if (stop) break;
+  }
+  if (doTrunc && tw < 0 && fabs(tw) < 1e-14) tw = 0.0;
+  cnt = s_cnt;
+  for (int r = tid; r < cnt; r += blockDim.x) atomicAdd(&counts[sec_of[order[r]]], 1);
+  __syncthreads();
+  // norm of the kept values: per sector (its first counts[sec] values, in storage order), then over
+  // the sectors in order
+  double k2 = 0.0;
+  if (nsec <= kTruncSecSh) {
+    for (int i = tid; i < nsec; i += blockDim.x) {
+      part_sh[i] = 0.0;
+      start_sh[i] = -1;
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += blockDim.x)
+      if (j == 0 || sec_of[j] != sec_of[j - 1]) start_sh[sec_of[j]] = j;
+    __syncthreads();
+    for (int sec = tid; sec < nsec; sec += blockDim.x) {
+      const int st = start_sh[sec];
+      if (st < 0) continue;
+      const int c = counts[sec];
+      double part = 0.0;
+      for (int t = 0; t < c; ++t) part += S[st + t] * S[st + t];
+      part_sh[sec] = part;
+    }
+    __syncthreads();
+    if (tid != 0) return;
+    for (int sec = 0; sec < nsec; ++sec)
+      if (start_sh[sec] >= 0) k2 += part_sh[sec];
+  } else {
+    if (tid != 0) return;
+    int i = 0;
+    while (i < n) {
+      const int sec = sec_of[i];
+      int j = i;
+      double part = 0.0;
+      int taken = 0;
+      while (j < n && sec_of[j] == sec) {
+        if (taken < counts[sec]) {
+          part += S[j] * S[j];
+          ++taken;
+        }
+        ++j;
+      }
+      k2 += part;
+      i = j;
+    }
   }
   out3[0] = tw;
   out3[1] = (double)cnt;
@@ -643,7 +720,7 @@ void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, in
     k_trunc_rank<<<(n + 255) / 256, 256, 0, s>>>(S, n, rank_scratch);
     LAUNCHED();
   }
-  k_trunc_select<<<1, 256, 0, s>>>(S, n, sec_of, nsec, chimax, doTrunc, tr_weight, rank_scratch,
+  k_trunc_select<<<1, kTruncThreads, 0, s>>>(S, n, sec_of, nsec, chimax, doTrunc, tr_weight, rank_scratch,
                                    rank_scratch + n, counts, out3);
   LAUNCHED();
 }

@@ -12,7 +12,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBPATH = os.path.join(HERE, "libmpsg.so")
 
-PREC = {"fp64": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "auto": 5}
+PREC = {"fp64": 0, "tf32": 1, "tf32x3": 2, "bf16": 3, "bf16x3": 4, "auto": 5, "mixed": 6}
 
 _L = None
 

@@ -3,7 +3,8 @@
 Tolerances: max |mixed - FP64| relative to the largest |FP64| entry of the output:
 TF32X3 2e-5, BF16X3 3e-4, TF32 5e-3, BF16 4e-2 (FP32 accumulation over K <= a few hundred;
 hi/lo splits carry ~22 / ~16 significant bits, single TF32 / BF16 operands 11 / 8 bits).
-Energies of the AUTO path (BF16X3 Lanczos finished in FP64) agree with the FP64 oracle to 1e-10.
+Energies of the AUTO path (TF32X3 Lanczos finished in FP64) and of the MIXED path (TF32X3 Lanczos,
+energy = FP64 Rayleigh quotient of its ground state) agree with the FP64 oracle to 1e-10.
 """
 import numpy as np
 import pytest
@@ -68,7 +69,28 @@ def test_tc_matvec_large_blocks(ctx):
         assert err < TOL[prec], (prec, err)
 
 
-@pytest.mark.parametrize("prec", ["auto", "tf32x3"])
+def test_mixed_lanczos_energy_is_the_fp64_rayleigh_quotient(ctx):
+    g, W, ik = _case()
+    site = 6
+    L, R = g.env("L", site - 1), g.env("R", site + 2)
+    A1, A2 = g.site(site), g.site(site + 1)
+    res = {}
+    for prec in ("fp64", "tf32x3", "mixed"):
+        lz = api.TSLanzcosEngine(L, R, A1, A2, W[site], W[site + 1], ik[site], ik[site + 1], prec=prec, ctx=ctx)
+        n = lz.simulate(500, 1e-12, True)
+        res[prec] = (lz.E(0), lz.getState(0), n)
+    E64 = res["fp64"][0]
+    Em, psi, n = res["mixed"]
+    H = api.contractTwosite(L, R, psi, W[site], W[site + 1], (ik[site], ik[site + 1]), prec="fp64", ctx=ctx)
+    rq = sum(float(np.vdot(psi[k], H[k])) for k in psi) / sum(float(np.vdot(v, v)) for v in psi.values())
+    print(f"fp64 {E64!r} ({res['fp64'][2]} matvecs), tf32x3 Ritz value {res['tf32x3'][0]!r}, "
+          f"mixed {Em!r} ({n} TF32X3 iterations + one FP64 matvec), host Rayleigh quotient {rq!r}")
+    assert n == res["tf32x3"][2]  # the same TF32X3 Lanczos
+    assert abs(Em - rq) <= 1e-13 * abs(rq)
+    assert abs(Em - E64) <= 1e-10 * abs(E64)
+
+
+@pytest.mark.parametrize("prec", ["auto", "tf32x3", "mixed"])
 def test_mixed_dmrg_energy(ctx, prec):
     N = 20
     W = M.heisenberg_mpo(M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N))
@@ -81,7 +103,7 @@ def test_mixed_dmrg_energy(ctx, prec):
     Em = gg.measure_energy()
     rel = abs(Em - go.measure()) / abs(Eo)
     print(f"{prec}: E_lanczos {Eg:.15f} E_measured {Em:.15f} oracle {Eo:.15f} rel {rel:.2e}")
-    if prec == "auto":
+    if prec in ("auto", "mixed"):
         assert abs(Eg - Eo) <= 1e-10 * abs(Eo)
         assert rel <= 1e-10
     else:
