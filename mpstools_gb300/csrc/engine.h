@@ -185,15 +185,10 @@ struct Engine {
     }
     TensorP th = theta_form(ctx, *mps[site], *mps[site + 1], &sx);
     TensorP psi = make_tensor(ctx, 2, sx, true);
-    const bool mixed = prec == MPSG_PREC_MIXED;
     LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], *th, *psi,
-                                    lanmax, delta, testenergy, reorth, (int)prec, &lst, tstate ? tstate->d : nullptr,
-                                    mixed);
+                                    lanmax, delta, testenergy, reorth, (int)prec, &lst, tstate ? tstate->d : nullptr);
     tstate.reset();
     th.reset();
-    // MIXED: the FP64 energy of the ground state runs beside the split and the environment update
-    PendingRQ rq;
-    if (mixed) start_rayleigh_quotient(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], psi, &lst, rq);
     auto t0 = std::chrono::steady_clock::now();
     SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
     ctx->sync();
@@ -207,7 +202,6 @@ struct Engine {
     else R[site + 1] = env_update(ctx, *R[site + 2], *mps[site + 1], mpo[site + 1], ik[site + 1], -1, &env_flops);
     ctx->sync();
     env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
-    if (rq.active()) lr.E0 = rq.resolve();
     StepRec r{site, dir, lr.iterations, sp.chi, lr.E0, sp.tw};
     steps.push_back(r);
     return r;

@@ -1920,77 +1920,9 @@ double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosSta
   return q[0] / q[1];
 }
 
-void start_rayleigh_quotient(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1,
-                             const MPO& W2, const ItoKey& ik0, const ItoKey& ik1, const TensorP& psi, LanczosStats* st,
-                             PendingRQ& out) {
-  MPSG_CHECK(!out.active(), "Rayleigh quotient already pending");
-  out.mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
-  out.ctx = ctx;
-  out.st = st;
-  out.psi = psi;
-  const int64_t n = psi->nelem;
-  out.nw = std::max<int64_t>(n, 2);
-  out.buf = (double*)ctx->dmalloc(sizeof(double) * (out.nw + kRedBlocks + 2));
-  MPSG_CUDA(cudaMemsetAsync(out.buf, 0, sizeof(double) * out.nw, ctx->stream));
-  MPSG_CUDA(cudaEventCreateWithFlags(&out.fork, cudaEventDisableTiming));
-  MPSG_CUDA(cudaEventCreateWithFlags(&out.done, cudaEventDisableTiming));
-  const cudaStream_t ws = ctx->wstreams[ctx->nworkers() - 1];
-  MPSG_CUDA(cudaEventRecord(out.fork, ctx->stream));
-  MPSG_CUDA(cudaStreamWaitEvent(ws, out.fork, 0));
-  const cudaStream_t main_stream = ctx->stream;
-  ctx->stream = ws;  // the plan launches on ctx->stream
-  try {
-    out.mv->run(psi->d, out.buf);
-  } catch (...) {
-    ctx->stream = main_stream;
-    throw;
-  }
-  ctx->stream = main_stream;
-  double* part = out.buf + out.nw;
-  launch_dot(psi->d, out.buf, n, part, part + kRedBlocks, ws);
-  launch_dot(psi->d, psi->d, n, part, part + kRedBlocks + 1, ws);
-  MPSG_CUDA(cudaEventRecord(out.done, ws));
-}
-
-double PendingRQ::resolve() {
-  MPSG_CHECK(active(), "no Rayleigh quotient pending");
-  MPSG_CUDA(cudaStreamWaitEvent(ctx->stream, done, 0));
-  double q[2] = {0, 0};
-  MPSG_CUDA(cudaMemcpyAsync(q, buf + nw + kRedBlocks, sizeof(q), cudaMemcpyDeviceToHost, ctx->stream));
-  ctx->sync();
-  if (st) {
-    st->matvecs += 1;
-    st->matvec_flops += mv->flops;
-  }
-  release();
-  MPSG_CHECK(q[1] > 0, "Rayleigh quotient of a zero state");
-  return q[0] / q[1];
-}
-
-void PendingRQ::release() {
-  if (!ctx) return;
-  cudaStreamWaitEvent(ctx->stream, done, 0);  // frees below are ordered after the worker's reads
-  ctx->dfree(buf);
-  buf = nullptr;
-  mv.reset();
-  psi.reset();
-  cudaEventDestroy(fork);
-  cudaEventDestroy(done);
-  fork = done = nullptr;
-  ctx = nullptr;
-}
-
-PendingRQ::~PendingRQ() {
-  try {
-    release();
-  } catch (...) {
-  }
-}
-
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
-                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj,
-                           bool defer_energy) {
+                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj) {
   if (prec == MPSG_PREC_FP64) {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
     return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, 0.0, 5, 0.0, proj);
@@ -2004,9 +1936,7 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
   if (prec == MPSG_PREC_MIXED) {
     // the energy measured in FP64: the Rayleigh quotient of the mixed-precision ground state.  The
     // tensor-core matvec scales H by a systematic factor (FP32 accumulation rounds towards zero; at
-    // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.  With
-    // defer_energy the caller computes it (start_rayleigh_quotient) and E0 is the TF32X3 Ritz value.
-    if (defer_energy) return r;
+    // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.
     auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
     r.E0 = rayleigh_quotient(ctx, *mv64, psi, st);
     return r;

@@ -156,25 +156,6 @@ double prec_tol(int prec);
 double prec_stall(int prec);
 // <psi|H|psi> / <psi|psi> with one matvec of the plan (FP64 for MPSG_PREC_MIXED energies).
 double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosStats* st);
-// The same FP64 Rayleigh quotient on the last worker stream, overlapping whatever the main stream runs
-// after it (a DMRG step's split and environment update); resolve() makes the main stream wait for it
-// and returns the value.  psi, the plan and the buffers live until then (frees stay stream-ordered).
-struct PendingRQ {
-  Ctx* ctx = nullptr;
-  std::unique_ptr<MatvecPlan> mv;
-  TensorP psi;
-  double* buf = nullptr;  // H psi, reduction partials, the two dots
-  int64_t nw = 0;
-  cudaEvent_t fork = nullptr, done = nullptr;
-  LanczosStats* st = nullptr;
-  bool active() const { return ctx != nullptr; }
-  double resolve();
-  void release();
-  ~PendingRQ();
-};
-void start_rayleigh_quotient(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1,
-                             const MPO& W2, const ItoKey& ik0, const ItoKey& ik1, const TensorP& psi, LanczosStats* st,
-                             PendingRQ& out);
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
                       double stall_rel = 0.0, const double* proj = nullptr);
@@ -184,7 +165,6 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
                            double delta, bool testenergy, bool reorth, int prec, LanczosStats* st,
-                           const double* proj = nullptr,  // proj: state the Krylov space stays orthogonal to
-                           bool defer_energy = false);    // MIXED: leave the FP64 energy to the caller
+                           const double* proj = nullptr);  // proj: state the Krylov space stays orthogonal to
 
 }  // namespace mpsg
