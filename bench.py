@@ -396,6 +396,7 @@ def gpu_arm(args):
                 "lanczos_matvecs_per_step": matvecs / args.steps,
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
                 "env_seconds_per_step": (st1["env_seconds"] - st0["env_seconds"]) / args.steps,
+                "lanczos_seconds_per_step": (st1["lanczos_seconds"] - st0["lanczos_seconds"]) / args.steps,
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
                 "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg, "auto_path": auto_leg,
                 "roofline_tensor_matvec": roof_tc,

@@ -114,8 +114,13 @@ static TcBases tc_bases(MatvecPlan& P, const double* theta_in, double* theta_out
   return B;
 }
 
+void MatvecPlan::use_fp64() {
+  if (!dX) dX = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(xa.nelem, 2));
+  fp64 = true;
+}
+
 void MatvecPlan::run(const double* theta_in, double* theta_out) {
-  if (prec == MPSG_PREC_FP64) {
+  if (prec == MPSG_PREC_FP64 || fp64) {
     const double* bases[8] = {dLt, theta_in, dX, dRt, theta_out, nullptr, nullptr, nullptr};
     stageA.run(bases);
     stageC.run(bases);
@@ -1929,24 +1934,22 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
   }
   const int lo = (prec == MPSG_PREC_AUTO || prec == MPSG_PREC_MIXED) ? MPSG_PREC_TF32X3 : prec;
   LanczosResult r;
-  {
-    auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
-    r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo), proj);
-  }
+  auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, lo);
+  r = lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, prec_tol(lo), 5, prec_stall(lo), proj);
   if (prec == MPSG_PREC_MIXED) {
     // the energy measured in FP64: the Rayleigh quotient of the mixed-precision ground state.  The
     // tensor-core matvec scales H by a systematic factor (FP32 accumulation rounds towards zero; at
     // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.
-    auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
-    r.E0 = rayleigh_quotient(ctx, *mv64, psi, st);
+    mv->use_fp64();
+    r.E0 = rayleigh_quotient(ctx, *mv, psi, st);
     return r;
   }
   if (prec != MPSG_PREC_AUTO) return r;
   // FP64 finish: the reference's Lanczos restarted from the mixed-precision ground state, energy test
   // every iteration, so the final energy carries the same convergence criterion as the FP64 path
-  auto mv64 = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
+  mv->use_fp64();
   TensorP start = tensor_copy(psi);
-  LanczosResult r2 = lanczos(ctx, *mv64, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0, proj);
+  LanczosResult r2 = lanczos(ctx, *mv, *start, psi, itmax, delta, testenergy, reorth, st, 0.0, 1, 0.0, proj);
   r2.iterations += r.iterations;
   return r2;
 }

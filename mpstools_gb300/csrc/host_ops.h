@@ -69,10 +69,14 @@ struct MatvecPlan {
   TcConv* dconv_theta = nullptr;
   int nconv_theta = 0, nimg_theta = 0;
   int* derr = nullptr;
+  // a tensor-core plan also carries the FP64 stage tables (same combined environments and blocks):
+  // use_fp64() switches run() to them, e.g. for an FP64 energy or an FP64 Lanczos finish
+  bool fp64 = false;
+  void use_fp64();
   void run(const double* theta_in, double* theta_out);
   void check_error();  // throws MPSG_ERR_TIMEOUT when a bounded device wait expired
   int launches_per_run() const {
-    if (prec != MPSG_PREC_FP64) return 3;
+    if (prec != MPSG_PREC_FP64 && !fp64) return 3;
     return (stageA.hprob.empty() ? 0 : 1) + (stageC.hprob.empty() ? 0 : 1);
   }
   ~MatvecPlan();
