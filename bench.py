@@ -205,6 +205,16 @@ def count_matvec_flops(L, R, thdims, W1, W2, ik0, ik1):
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def max_over_ranks(x, dist, device):
+    """The largest x over the ranks (a job's time is its slowest rank's); x itself on one process."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def gpu_arm(args):
     import torch
     from mpstools_gb300 import api, lib
@@ -254,10 +264,7 @@ def gpu_arm(args):
     torch.cuda.synchronize()
     clocks = clk.stop()
     total = float(np.sum(times))
-    if dist:
-        t = torch.tensor([total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
+    total = max_over_ranks(total, dist, "cuda")
     st1 = eng.stats()
     launches = ctx.kernel_launches() - launches0
     mv_flops = st1["matvec_flops"] - st0["matvec_flops"]
