@@ -151,8 +151,9 @@ def test_dmrg_small_xxz_matches_oracle(ctx):
     assert len(so) == len(sg)
 
 
-def test_dmrg_config1_heisenberg_L32_chi64(ctx):
-    """Config 1: Heisenberg J=1, L=32, Sz=0, chi=64, 6 sweeps, random N(0,1) MPS (seed 12345)."""
+def test_dmrg_heisenberg_L32_chi64(ctx):
+    """Heisenberg J=1, L=32, Sz=0, chi=64, 6 sweeps from a random N(0,1) MPS (seed 12345): the
+    reference's CPU-sized DMRG run."""
     N = 32
     W = M.heisenberg_mpo(np.ones(N - 1), np.ones(N - 1), np.zeros(N))
     ik = M.u1_itokeys(N)
@@ -192,8 +193,9 @@ def test_split_density_method_matches_oracle(ctx):
     _close_bm(_recompose(U1, l1, V1), _recompose(U0, l0, V0), rtol=1e-8)
 
 
-def test_dmrg_config1_density_svd(ctx):
-    """Config 1 with the density-matrix SVD: energy within 1e-10 relative of the oracle."""
+def test_dmrg_heisenberg_L32_chi64_density_svd(ctx):
+    """The Heisenberg L=32, chi=64 run with the density-matrix SVD: energy within 1e-10 relative of
+    the oracle."""
     N = 32
     W = M.heisenberg_mpo(np.ones(N - 1), np.ones(N - 1), np.zeros(N))
     ik = M.u1_itokeys(N)
