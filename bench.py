@@ -4,8 +4,10 @@ Workload (config: XXZ chain L=100, Jxy=1, Delta_i ~ U[0.5,1.5] from seed 1, U(1)
 MPO bond dimension 5, at the chi=2048 end of the chi ramp): a seeded random U(1) MPS with
 chi=2048 on every bond, left-isometric left of the centre bond and right-isometric right of it.
 One step = one two-site DMRG update at the centre bond (DMRGengine::doStep: theta formation,
-Lanczos to the reference's energy criterion, SVD split with truncation to chi, environment
-update), alternating direction so consecutive steps stay on the same bond.
+Lanczos, SVD split with truncation to chi, environment update), alternating direction so
+consecutive steps stay on the same bond.  Default precision MIXED (TF32X3 tensor-core Lanczos,
+energy = FP64 Rayleigh quotient); the AUTO and plain FP64 paths are timed on the same updates.
+--model tv: the t-V chain instead (L=128, t=1, V_i ~ U[0,2] from seed 2, mu=0, half filling).
 
 value   = algorithmic matvec FLOPs executed inside the timed steps / total device time of the
           steps (TFLOP/s); ms_per_step is the device time of one update.
@@ -39,20 +41,32 @@ DTYPE = {"fp64": "f64", "auto": "tf32x3+f64", "mixed": "tf32x3+f64"}
 CENTER = L_SITES // 2 - 1
 
 
-def workload(chi=CHI, L=L_SITES):
+SEED_V = 2  # t-V chain: V_i ~ U[0,2] from this seed
+MODEL_L = {"xxz": L_SITES, "tv": 128}
+MODEL_TEXT = {"xxz": "XXZ (Heisenberg MPO D=5), Jxy=1, Delta~U[0.5,1.5] seed 1",
+              "tv": "spinless fermions t-V (Jordan-Wigner MPO D=5), t=1, V~U[0,2] seed 2, mu=0"}
+
+
+def workload(chi=CHI, L=L_SITES, model="xxz"):
+    """XXZ chain (Sz_total = 0) or t-V chain at half filling, and a seeded random U(1) MPS of bond
+    dimension chi in mixed-canonical form around the centre bond."""
     from mpstools_gb300 import models as M
     Nup = L // 2
     center = L // 2 - 1
-    W = M.heisenberg_mpo(M.xxz_couplings(L, SEED_DELTA), np.ones(L - 1), np.zeros(L))
+    if model == "tv":
+        W = M.spinless_fermions_mpo(2.0 * M.uniform01(SEED_V, L - 1), np.ones(L - 1), np.zeros(L))
+    else:
+        W = M.heisenberg_mpo(M.xxz_couplings(L, SEED_DELTA), np.ones(L - 1), np.zeros(L))
     ik = M.u1_itokeys(L)
     sites = M.random_mixed_canonical_mps(L, Nup, chi, SEED_MPS, center)
     return W, ik, sites, center
 
 
-def config_dict(chi, L, prec, svd="density"):
-    return {"workload": f"xxz_L{L}_chi{chi}_centre_bond_two_site_update",
-            "model": "XXZ (Heisenberg MPO D=5), Jxy=1, Delta~U[0.5,1.5] seed 1",
-            "L": L, "Sz_total": 0, "chi": chi, "mpo_bond_dim": 5, "state": "seeded random U(1) MPS, mixed canonical",
+def config_dict(chi, L, prec, svd="density", model="xxz"):
+    return {"workload": f"{model}_L{L}_chi{chi}_centre_bond_two_site_update",
+            "model": MODEL_TEXT[model],
+            "L": L, **({"N_particles": L // 2} if model == "tv" else {"Sz_total": 0}), "chi": chi, "mpo_bond_dim": 5,
+            "state": "seeded random U(1) MPS, mixed canonical",
             "lanczos": "delta=1e-12, energy test every 5 iterations, itmax 500", "matvec_precision": prec,
             "svd": svd, "l2": "flushed (512 MiB write) before every timed step and every roofline launch"}
 
@@ -130,7 +144,7 @@ def reference_arm(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    W, ik, sites, center = workload(args.chi, args.L)
+    W, ik, sites, center = workload(args.chi, args.L, args.model)
     from oracle import pyoracle as O
     g = O.DMRG(sites, W, ik, maxthreads=threads, matvec_threads=threads)
     g.build_environments(center)
@@ -149,7 +163,8 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": config_dict(args.chi, args.L, "fp64 (CPU oracle, OpenBLAS dgemm)", "dgesvd (CPU oracle)"),
+            "config": config_dict(args.chi, args.L, "fp64 (CPU oracle, OpenBLAS dgemm)", "dgesvd (CPU oracle)",
+                                  args.model),
             "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} two-site updates at the centre bond (chi={args.chi})"},
             "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -228,7 +243,7 @@ def gpu_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     prec = args.prec
-    W, ik, sites, center = workload(args.chi, args.L)
+    W, ik, sites, center = workload(args.chi, args.L, args.model)
     ctx = lib.Context(local)
     # one explicit stream shared by the library, the L2 flush and the timing events
     stream = torch.cuda.Stream()
@@ -312,7 +327,7 @@ def gpu_arm(args):
     if args.steps_only:  # profiling runs: only warm-up + timed steps (few launches under a profiler)
         if rank == 0:
             print(json.dumps({"metric": METRIC, "steps_only": True, "ms_per_step": total / args.steps * 1e3,
-                              "gpu_launches": int(launches), "config": config_dict(args.chi, args.L, prec, args.svd),
+                              "gpu_launches": int(launches), "config": config_dict(args.chi, args.L, prec, args.svd, args.model),
                               "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
                               "energies": [s["E"] for s in steps_rec]}), flush=True)
         return
@@ -398,7 +413,7 @@ def gpu_arm(args):
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": DTYPE.get(prec, prec),
-                "data": "synthetic", "config": config_dict(args.chi, args.L, prec, args.svd), "clocks": clocks,
+                "data": "synthetic", "config": config_dict(args.chi, args.L, prec, args.svd, args.model), "clocks": clocks,
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
                 "lanczos_matvecs_per_step": matvecs / args.steps,
                 "split_seconds_per_step": (st1["split_seconds"] - st0["split_seconds"]) / args.steps,
@@ -604,7 +619,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--chi", type=int, default=CHI)
-    ap.add_argument("--L", type=int, default=L_SITES)
+    ap.add_argument("--L", type=int, default=None, help="chain length (default: 100 for xxz, 128 for tv)")
+    ap.add_argument("--model", default="xxz", choices=["xxz", "tv"],
+                    help="centre-update workload: XXZ chain or t-V chain at half filling")
     ap.add_argument("--prec", default=None,
                     help="fp64 | tf32 | tf32x3 | bf16 | bf16x3 | auto | mixed (default: mixed; chains: auto)")
     ap.add_argument("--svd", default="density_eig", choices=["density", "density_mt", "density_eig", "jacobi"])
@@ -623,6 +640,8 @@ def main():
     ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--seq-chains", type=int, default=8)
     args = ap.parse_args()
+    if args.L is None:
+        args.L = MODEL_L[args.model]
     if args.prec is None:
         args.prec = "auto" if args.workload == "chains" else "mixed"
     if args.workload == "chains":

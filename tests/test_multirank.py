@@ -78,3 +78,11 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     _check_reference_line(d)
     assert d["n_gpus"] == 2
+
+
+def test_reference_arm_tv_model():
+    lines = _reference_json([sys.executable, "bench.py", "--model", "tv"] + ARGS)
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    _check_reference_line(d)
+    assert d["config"]["workload"].startswith("tv_L12_chi16") and d["config"]["N_particles"] == 6
