@@ -180,3 +180,16 @@ def test_oracle_tebd_matches_dense_trotter():
         got = t.measure_diag(site, [-0.5, 0.5])
         assert abs(got - ref) < 1e-12, (site, got, ref)
     assert abs(ed.sz_expect(psi, 0, N) - (-0.5)) > 1e-3  # the state did evolve
+
+
+def test_oracle_truncation_ties_keep_the_later_sector():
+    """DiagBlockMatrix::truncate (src/BlockTensor.hpp:234-276) walks the values of a reversed
+    std::multimap: by value descending, equal values in reverse insertion order (later charge sector
+    first).  Two 1x1 sectors with the same singular value and chimax = 1: the second one is kept."""
+    th = {(0, 0, 0, 0): np.array([[0.6]]), (0, 1, 1, 0): np.array([[0.6]])}
+    ik = [0, 1]
+    U, Vt, lam, tw, chi = O.split(th, ik, ik, 1, doTrunc=False, tr_weight=1e-12, normalize=True)
+    assert chi == 1
+    kept = {q: v for q, v in lam.items() if len(v)}
+    assert list(kept) == [1] and abs(kept[1][0] - 1.0) < 1e-15
+    assert abs(tw - (1.0 - 0.36)) < 1e-15  # 1 - the kept value squared, before normalisation
