@@ -9,8 +9,9 @@ consecutive steps stay on the same bond.  Default precision MIXED (TF32X3 tensor
 energy = FP64 Rayleigh quotient); the AUTO and plain FP64 paths are timed on the same updates.
 --model tv: the t-V chain instead (L=128, t=1, V_i ~ U[0,2] from seed 2, mu=0, half filling).
 
-value   = algorithmic matvec FLOPs executed inside the timed steps / total device time of the
-          steps (TFLOP/s); ms_per_step is the device time of one update.
+value   = algorithmic FLOPs of the Lanczos matvecs executed inside the timed steps / total device time
+          of the steps (TFLOP/s; MIXED's extra FP64 Rayleigh-quotient matvec is not counted as work);
+          ms_per_step is the device time of one update.
 e2e     = the same metric through the C ABI with host buffers: per step the environments and the
           two site tensors are uploaded (mpsg_tensor_create), the update runs through
           mpsg_lanczos2 + mpsg_split2 + mpsg_add_contraction_layer and the results are
@@ -284,7 +285,10 @@ def gpu_arm(args):
     launches = ctx.kernel_launches() - launches0
     mv_flops = st1["matvec_flops"] - st0["matvec_flops"]
     matvecs = st1["matvecs"] - st0["matvecs"]
-    value = mv_flops * world / total / 1e12
+    # throughput counts the Lanczos matvecs only (the reference's work); MIXED's one FP64
+    # Rayleigh-quotient matvec per update is time spent, not throughput
+    lanczos_mv = matvecs - (args.steps if prec == "mixed" else 0)
+    value = mv_flops * (lanczos_mv / max(matvecs, 1)) * world / total / 1e12
     steps_rec = eng.steps()[n_steps0:]
 
     # ------------------------------------------- other precisions (plain FP64 GPU path, AUTO) on the same updates
@@ -397,17 +401,34 @@ def gpu_arm(args):
                    "mpsg_tensor_export x4 (host buffers, wall clock with device sync)"}
 
     # --------------------------------------------------------------- CPU baseline (bounded sample)
-    cpu = None
+    cpu, oracle_check = None, None
     if rank == 0 and not args.no_cpu:
         envs = (L.to_dict(), R.to_dict())
         sites_c = {center: A1.to_dict(), center + 1: A2.to_dict()}
         threads = os.cpu_count() or 1
-        ts, st = cpu_update_seconds_window(W, ik, sites_c, center, args.chi, 1, threads, envs, args.L)
+        ts, st, g_or = cpu_update_seconds_window(W, ik, sites_c, center, args.chi, 1, threads, envs, args.L,
+                                                 keep=True)
         cpu_mv = sum(s["iters"] for s in st)
         cpu_value = info["flops"] * cpu_mv / sum(ts) / 1e12
         cpu = {"value": cpu_value, "unit": "TFLOP/s", "cores": threads, "kind": "port",
                "sample": f"1 two-site update at the centre bond (chi={args.chi}), {cpu_mv} Lanczos matvecs, "
                          f"{sum(ts):.2f} s"}
+        # the same update (same L, R, site tensors, direction) on the GPU, against the oracle's
+        eng.do_step(center, 1, args.chi)
+        g_rec, o_rec = eng.steps()[-1], st[-1]
+        lg, lo = eng.lam(center), g_or.lam(center)
+        common = set(lg) & set(lo)
+        oracle_check = {"E_gpu": g_rec["E"], "E_oracle": o_rec["E"],
+                        "rel_energy_diff": abs(g_rec["E"] - o_rec["E"]) / abs(o_rec["E"]),
+                        "chi_gpu": g_rec["chi"], "chi_oracle": o_rec["chi"], "tw_gpu": g_rec["tw"],
+                        "tw_oracle": o_rec["tw"],
+                        "kept_per_sector_equal": {q: len(v) for q, v in lg.items()} ==
+                                                 {q: len(v) for q, v in lo.items()},
+                        "lambda_max_abs_diff": max((float(np.abs(np.asarray(lg[q])[:m] - np.asarray(lo[q])[:m]).max())
+                                                    for q in common for m in [min(len(lg[q]), len(lo[q]))] if m),
+                                                   default=0.0),
+                        "what": "one two-site update at the centre bond from the same state (GPU in this "
+                                "line's precision, oracle FP64 with LAPACK dgesvd)"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
@@ -422,14 +443,14 @@ def gpu_arm(args):
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
                 "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg, "auto_path": auto_leg,
                 "roofline_tensor_matvec": roof_tc,
-                "matvec_flops_reference_schedule": info["flops_ref"]}
+                "matvec_flops_reference_schedule": info["flops_ref"], "oracle_check": oracle_check}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
 
 
-def cpu_update_seconds_window(W, ik, sites_c, center, chi, nsteps, threads, envs, N):
+def cpu_update_seconds_window(W, ik, sites_c, center, chi, nsteps, threads, envs, N, keep=False):
     from oracle import pyoracle as O
     window = [sites_c.get(i, {}) for i in range(N)]
     g = O.DMRG(window, W, ik, maxthreads=threads, matvec_threads=threads)
@@ -440,7 +461,7 @@ def cpu_update_seconds_window(W, ik, sites_c, center, chi, nsteps, threads, envs
         t0 = time.perf_counter()
         g.do_step(center, 1 if i % 2 == 0 else -1, chi)
         ts.append(time.perf_counter() - t0)
-    return ts, g.steps()
+    return (ts, g.steps(), g) if keep else (ts, g.steps())
 
 
 def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
@@ -475,7 +496,7 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
         Lo = lib.Tensor(ctx, Lo)
         outs = [U.export_flat(), V.export_flat(), lam.export_flat(), Lo.export_flat()]
         d2h[0] = sum(o[5].nbytes for o in outs)
-        return it.value + (1 if prec == "mixed" else 0)  # + the FP64 Rayleigh-quotient matvec
+        return it.value  # Lanczos matvecs (MIXED's FP64 Rayleigh-quotient matvec is not counted)
 
     for i in range(2):
         step(i)
@@ -491,6 +512,137 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
         secs += time.perf_counter() - a
     return {"matvecs": mvs, "seconds": secs, "steps": n, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h[0])}
+
+
+SWEEP_RAMP = (256, 256, 1024, 1024, 1024, 2048, 2048, 2048)
+
+
+def sweep_workload(L=L_SITES, model="xxz"):
+    """Config of the sweep measurement: the XXZ chain (L=100, Jxy=1, Delta_i ~ U[0.5,1.5] from seed 1,
+    Sz_total=0) or the t-V chain at half filling, from the product state of the reference drivers
+    (every (L/N)-th site occupied, main/mainHeisenberg.cpp:175-191)."""
+    from mpstools_gb300 import models as M
+    if model == "tv":
+        W = M.spinless_fermions_mpo(2.0 * M.uniform01(SEED_V, L - 1), np.ones(L - 1), np.zeros(L))
+    else:
+        W = M.heisenberg_mpo(M.xxz_couplings(L, SEED_DELTA), np.ones(L - 1), np.zeros(L))
+    ik = M.u1_itokeys(L)
+    sites = M.product_state(M.filling_state(L, L // 2), ik)
+    return W, ik, sites
+
+
+def run_sweeps(eng, N, ramp, sync=None, on_sweep=None):
+    """DMRGengine::simulate's sweep loop (src/container.hpp:381-438) with one chimax per sweep:
+    orthonormalize("rl") and the right environments once, then per sweep doStep(site, +1) for
+    site = 0..N-3 and doStep(site, -1) for site = N-2..1; after the last sweep doStep(0, -1).
+    Returns one record per sweep (wall seconds, chi, energy of the sweep's last update)."""
+    recs = []
+    t0 = time.perf_counter()
+    eng.prepare()
+    if sync:
+        sync()
+    t_prep = time.perf_counter() - t0
+    for k, chi in enumerate(ramp):
+        n0 = len(eng.steps())
+        t0 = time.perf_counter()
+        for site in range(N - 2):
+            eng.do_step(site, 1, chi)
+        for site in range(N - 2, 0, -1):
+            eng.do_step(site, -1, chi)
+        if sync:
+            sync()
+        dt = time.perf_counter() - t0
+        st = eng.steps()[n0:]
+        recs.append({"sweep": k + 1, "chi": chi, "seconds": dt, "E": st[-1]["E"], "updates": len(st),
+                     "lanczos_iterations": int(sum(s["iters"] for s in st)),
+                     "max_chi_kept": int(max(s["chi"] for s in st)),
+                     "chi_kept": [int(s["chi"]) for s in st]})
+        if on_sweep:
+            on_sweep(recs[-1])
+    last = eng.do_step(0, -1, ramp[-1])
+    return recs, t_prep, last
+
+
+def sweep_leg(ctx, prec, W, ik, sites, ramp, torch):
+    from mpstools_gb300 import api
+    eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
+    s0 = eng.stats()
+    recs, t_prep, E = run_sweeps(eng, len(sites), ramp, sync=torch.cuda.synchronize)
+    s1 = eng.stats()
+    lam_c = eng.lam(len(sites) // 2 - 1)
+    vals = np.sort(np.concatenate([np.asarray(v) for v in lam_c.values() if len(v)]))[::-1]
+    eng.close()
+    return {"prec": prec, "sweeps": recs, "prepare_seconds": t_prep, "E_final": E,
+            "split_seconds": s1["split_seconds"] - s0["split_seconds"],
+            "env_seconds": s1["env_seconds"] - s0["env_seconds"],
+            "lanczos_seconds": s1["lanczos_seconds"] - s0["lanczos_seconds"],
+            "matvecs": s1["matvecs"] - s0["matvecs"], "matvec_flops": s1["matvec_flops"] - s0["matvec_flops"],
+            "centre_bond": {"chi": int(vals.size), "s_min_kept": float(vals[-1]),
+                            "sectors": {int(q): len(v) for q, v in lam_c.items()}}}
+
+
+def oracle_sweeps(W, ik, sites, ramp, threads):
+    from oracle import pyoracle as O
+    g = O.DMRG(sites, W, ik, maxthreads=threads, matvec_threads=threads)
+    recs = []
+    t0 = time.perf_counter()
+    g.prepare()
+    N = len(sites)
+    for k, chi in enumerate(ramp):
+        n0 = len(g.steps())
+        a = time.perf_counter()
+        for site in range(N - 2):
+            g.do_step(site, 1, chi)
+        for site in range(N - 2, 0, -1):
+            g.do_step(site, -1, chi)
+        st = g.steps()[n0:]
+        recs.append({"sweep": k + 1, "chi": chi, "seconds": time.perf_counter() - a, "E": st[-1]["E"],
+                     "chi_kept": [int(s["chi"]) for s in st]})
+    return recs
+
+
+def sweep_arm(args):
+    """Config 2: XXZ L=100 from the product state, chi ramp 256 (2 sweeps) -> 1024 (3) -> 2048 (3), in
+    MIXED (tensor-core Lanczos) and in plain FP64 on the same GPU; the CPU oracle runs the first
+    --oracle-sweeps sweeps of the same schedule for the energy check."""
+    import torch
+    from mpstools_gb300 import lib
+    ramp = tuple(args.ramp) if args.ramp else SWEEP_RAMP
+    W, ik, sites = sweep_workload(args.L, args.model)
+    ctx = lib.Context(0)
+    ctx.set_svd_method(args.svd)
+    legs = {}
+    clk = ClockSampler()
+    clk.start()
+    for p in ([args.prec] + ([] if args.prec == "fp64" or args.no_fp64_leg else ["fp64"])):
+        legs[p] = sweep_leg(ctx, p, W, ik, sites, ramp, torch)
+    clocks = clk.stop()
+    ora = None
+    if args.oracle_sweeps > 0:
+        ora = oracle_sweeps(W, ik, sites, ramp[:args.oracle_sweeps], os.cpu_count() or 1)
+    main = legs[args.prec]
+    top = max(ramp)
+    t_top = [r["seconds"] for r in main["sweeps"] if r["chi"] == top]
+    out = {"metric": "DMRG sweep time (config-2 chi ramp)", "impl": "ours", "value": float(np.mean(t_top)),
+           "unit": f"s per sweep at chi={top}", "higher_is_better": False, "n_gpus": 1,
+           "dtype": DTYPE.get(args.prec, args.prec), "data": "synthetic",
+           "config": {"workload": f"{args.model}_L{args.L}_product_state_chi_ramp", "ramp": list(ramp),
+                      "model": MODEL_TEXT[args.model], "lanczos": "delta=1e-12, energy test every 5 iterations",
+                      "svd": args.svd}, "clocks": clocks, "legs": legs}
+    if "fp64" in legs and args.prec != "fp64":
+        f = legs["fp64"]
+        t64 = [r["seconds"] for r in f["sweeps"] if r["chi"] == top]
+        out["fp64_speedup_at_top_chi"] = float(np.sum(t64) / np.sum(t_top))
+        out["rel_energy_diff_per_sweep_vs_fp64"] = [abs(a["E"] - b["E"]) / abs(b["E"])
+                                                     for a, b in zip(main["sweeps"], f["sweeps"])]
+        out["rel_energy_diff_final_vs_fp64"] = abs(main["E_final"] - f["E_final"]) / abs(f["E_final"])
+    if ora:
+        out["oracle"] = {"sweeps": ora, "cores": os.cpu_count() or 1}
+        for p, leg in legs.items():
+            out[f"rel_energy_diff_vs_oracle_{p}"] = [abs(a["E"] - b["E"]) / abs(b["E"])
+                                                     for a, b in zip(leg["sweeps"], ora)]
+            out[f"chi_kept_equal_oracle_{p}"] = [a["chi_kept"] == b["chi_kept"] for a, b in zip(leg["sweeps"], ora)]
+    print(json.dumps(out), flush=True)
 
 
 def chains_workload(nchains, chi, seed=3):
@@ -624,16 +776,18 @@ def main():
                     help="centre-update workload: XXZ chain or t-V chain at half filling")
     ap.add_argument("--prec", default=None,
                     help="fp64 | tf32 | tf32x3 | bf16 | bf16x3 | auto | mixed (default: mixed; chains: auto)")
-    ap.add_argument("--svd", default="density_eig", choices=["density", "density_mt", "density_eig", "jacobi"])
+    ap.add_argument("--svd", default="bidiag", choices=["bidiag", "density", "density_mt", "density_eig", "jacobi"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic-bytes", type=float, default=None)
     ap.add_argument("--no-fp64-leg", action="store_true",
                     help="skip the plain FP64 GPU path timed on the same updates (mixed precisions only)")
     ap.add_argument("--steps-only", action="store_true",
                     help="time the DMRG steps only (no roofline / e2e / CPU legs); for profiler launch lists")
-    ap.add_argument("--workload", default="centre_update", choices=["centre_update", "chains", "tebd"],
+    ap.add_argument("--workload", default="centre_update", choices=["centre_update", "sweep", "chains", "tebd"],
                     help="chains: batched independent chains (--nchains, --sweeps, --seq-chains; --chi 256); "
                          "tebd: L=64 TEBD forward + adjoint gradient (--tebd-steps, --fd-bonds)")
+    ap.add_argument("--ramp", type=int, nargs="*", default=None, help="sweep: chimax per sweep")
+    ap.add_argument("--oracle-sweeps", type=int, default=2, help="sweep: sweeps the CPU oracle runs")
     ap.add_argument("--tebd-steps", type=int, default=200)
     ap.add_argument("--fd-bonds", type=int, nargs="*", default=[31])
     ap.add_argument("--nchains", type=int, default=64)
@@ -648,6 +802,8 @@ def main():
         chains_arm(args)
     elif args.workload == "tebd":
         tebd_arm(args)
+    elif args.workload == "sweep":
+        sweep_arm(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

@@ -76,12 +76,16 @@ mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
 mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
-/* Number of charge sectors of splits on the library's own density-matrix eigensolver (svd method 3)
- * that were redone on the exact Jacobi route because their singular vectors were too dependent for
- * CholeskyQR. */
+/* Number of charge sectors of splits on the library's own SVD routes (svd methods 3 and 4) that were
+ * redone on the Jacobi route because their singular vectors were too dependent for CholeskyQR. */
 int64_t mpsg_split_fallbacks(void);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
- * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64; default, exact),
+ * 4 = the library's own exact SVD (default): Householder bidiagonalisation of each charge sector,
+ *     singular values by bisection on the Golub-Kahan tridiagonal (absolute accuracy ~eps ||M||, as
+ *     dgesvd), computed only down to the global truncation cut of the split; singular vectors only
+ *     for the kept values (inverse iteration, CholeskyQR, reflector back-transformation).  Sectors
+ *     wider than 512 fall back to route 0;
+ * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64, exact),
  * 1, 2, 3 = eigen-decomposition of each sector's reduced density matrix G = M^T M (FP64) with the
  *     eigensolver of cuSOLVER batched by size class (1), cuSOLVER per sector on concurrent streams (2)
  *     or the library's own batched eigensolver (3).  The left vectors are re-orthonormalised
@@ -136,8 +140,9 @@ mpsg_status mpsg_matvec2_plan_execute(mpsg_matvec_plan plan, const double* theta
  * It calls no cudaMalloc / cudaFree or other allocating routine: the stage-A intermediate is
  * kept in a fixed 8 MiB device array inside the library (held by every GPU that loads it until
  * the process exits).  FP64 plans only; plans whose intermediate exceeds 1 Mi FP64 elements are
- * rejected with MPSG_ERR_ARG.  The first call on a device resolves the array's device address
- * (cudaGetSymbolAddress) -- make that first call before any stream capture.  All calls share
+ * rejected with MPSG_ERR_ARG.  mpsg_ctx_create resolves the array's device address
+ * (cudaGetSymbolAddress) for its device, which loads the array when the library is set up; a
+ * device reset (cudaDeviceReset) while the library is loaded is not supported.  All calls share
  * the array, so calls that overlap on the GPU (other streams, other threads) race; nothing in
  * it needs clearing, every intermediate block is overwritten before it is read.  Runs on the
  * context's stream, the current device must be the plan's device. */
@@ -193,6 +198,9 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
 /* prec: matvec/environment arithmetic; reorth: full reorthogonalisation in Lanczos;
  * lanmax: Lanczos iteration cap (reference: 500). */
 mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax);
+/* The options in effect (set by mpsg_dmrg_set_options or restored by mpsg_dmrg_load); any output
+ * pointer may be NULL.  No reference counterpart (the reference keeps them as engine members). */
+mpsg_status mpsg_dmrg_get_options(mpsg_dmrg e, int32_t* prec, int32_t* reorth, int32_t* lanmax);
 /* DMRGengine::simulate(maxsteps, EnConv, chimax, doTrunc, tr_weight, delta, testenergy):
  * orthonormalize("rl"), computeR, sweeps, final doStep(0,-1).  E = last Lanczos energy. */
 mpsg_status mpsg_dmrg_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, uint32_t chimax,
@@ -336,7 +344,10 @@ mpsg_status mpsg_dmrg_ss_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv,
  * MPO tensor and the site tensor, then the lambdas.  Format "MPSGCKP1": see checkpoint.cpp; the
  * Python module mpstools_gb300.checkpoint reads and writes the same files (e.g. for states made by
  * the CPU oracle).  mpsg_dmrg_load creates an engine on ctx; simulate() or build_environments()
- * continues from the loaded state. */
+ * continues from the loaded state.  Version-2 files also keep the engine's options (matvec
+ * precision, reorthogonalisation, Lanczos limit), which load restores; version-1 files load with the
+ * FP64 defaults.  The loader rejects (MPSG_ERR_ARG) files whose indices fall outside the declared
+ * MPO / local dimensions or whose declared sizes exceed the file, before allocating for them. */
 mpsg_status mpsg_dmrg_save(mpsg_dmrg e, const char* path);
 mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out);
 

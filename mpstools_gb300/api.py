@@ -236,9 +236,11 @@ class DMRGengine:
         check(self.ctx.L.mpsg_dmrg_save(self.h, os.fsencode(path)))
 
     @classmethod
-    def load(cls, path, prec="fp64", reorth=False, lanmax=500, ctx=None):
+    def load(cls, path, prec=None, reorth=None, lanmax=None, ctx=None):
         """An engine holding the state of an MPSGCKP1 checkpoint (written by save() or by
-        mpstools_gb300.checkpoint.save)."""
+        mpstools_gb300.checkpoint.save).  The run settings stored in the file (matvec precision,
+        reorthogonalisation, Lanczos iteration limit) are restored; arguments that are not None
+        override them."""
         self = cls.__new__(cls)
         self.ctx = ctx or default_context()
         h = C.c_void_p()
@@ -248,8 +250,17 @@ class DMRGengine:
         hdr = checkpoint.read_header(path)
         self.N = hdr["N"]
         self._tensors, self._mpos, self._iks = [], [], []
-        check(self.ctx.L.mpsg_dmrg_set_options(self.h, _prec(prec), int(reorth), int(lanmax)))
+        st = checkpoint.read_settings(path)
+        check(self.ctx.L.mpsg_dmrg_set_options(self.h, st["prec"] if prec is None else _prec(prec),
+                                               st["reorth"] if reorth is None else int(reorth),
+                                               st["lanmax"] if lanmax is None else int(lanmax)))
         return self
+
+    def options(self):
+        """{"prec", "reorth", "lanmax"} in effect (mpsg_dmrg_get_options)."""
+        p, r, m = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.ctx.L.mpsg_dmrg_get_options(self.h, C.byref(p), C.byref(r), C.byref(m)))
+        return {"prec": p.value, "reorth": r.value, "lanmax": m.value}
 
     def simulate(self, maxsteps=5, EnConv=1e-10, chimax=100, doTrunc=False, tr_weight=1e-12, delta=1e-13,
                  testenergy=True):

@@ -1,7 +1,8 @@
 """MPSGCKP1 checkpoints of an MPS with its MPO (the format written by mpsg_dmrg_save and read by
 mpsg_dmrg_load, little-endian):
 
-    char[8] "MPSGCKP1"; u32 version (1); u32 N
+    char[8] "MPSGCKP1"; u32 version (2; version-1 files have no settings record); u32 N
+    version >= 2: u32 prec (mpsg_prec); u32 reorth; u32 lanmax; u64 updates (doStep calls made)
     per site s: u32 d; u64 charge[d]
                 u32 Dl; u32 Dr; u32 nterms; nterms x {u32 wl, wr, out, in; f64 value}
                 u32 nblocks; nblocks x {u64 q0, q1; u32 p; i32 rows, cols}; f64 data (blocks in key
@@ -19,13 +20,18 @@ import struct
 
 import numpy as np
 
-MAGIC, END, VERSION = b"MPSGCKP1", b"MPSGEND!", 1
+MAGIC, END, VERSION = b"MPSGCKP1", b"MPSGEND!", 2
+DEFAULT_SETTINGS = {"prec": 0, "reorth": 0, "lanmax": 500, "updates": 0}
 
 
-def save(path, sites, mpo, itokeys, lambdas=None):
+def save(path, sites, mpo, itokeys, lambdas=None, settings=None):
+    """settings: {"prec", "reorth", "lanmax", "updates"} of the run (default FP64, no
+    reorthogonalisation, 500 Lanczos iterations, 0 updates)."""
     lambdas = lambdas or {}
+    st = dict(DEFAULT_SETTINGS, **(settings or {}))
     with open(path, "wb") as f:
         f.write(MAGIC + struct.pack("<II", VERSION, len(sites)))
+        f.write(struct.pack("<IIIQ", st["prec"], st["reorth"], st["lanmax"], st["updates"]))
         for s, site in enumerate(sites):
             ik = [int(q) for q in itokeys[s]]
             f.write(struct.pack("<I", len(ik)) + struct.pack(f"<{len(ik)}Q", *ik))
@@ -78,6 +84,19 @@ def read_header(path):
     return {"version": version, "N": N}
 
 
+def read_settings(path):
+    """The run settings of a version-2 file (the defaults for a version-1 file)."""
+    with open(path, "rb") as f:
+        head = f.read(36)
+    if head[:8] != MAGIC:
+        raise ValueError("not an MPSG checkpoint file")
+    version, _ = struct.unpack("<II", head[8:16])
+    if version < 2:
+        return dict(DEFAULT_SETTINGS)
+    p, r, lm, u = struct.unpack("<IIIQ", head[16:36])
+    return {"prec": p, "reorth": r, "lanmax": lm, "updates": u}
+
+
 def load(path):
     """Returns (sites, mpo, itokeys, lambdas)."""
     with open(path, "rb") as f:
@@ -85,8 +104,10 @@ def load(path):
     if bytes(rd.take("8s")[0]) != MAGIC:
         raise ValueError("not an MPSG checkpoint file")
     version, N = rd.take("<II")
-    if version != VERSION:
+    if version not in (1, 2):
         raise ValueError("unsupported checkpoint version")
+    if version >= 2:
+        rd.take("<IIIQ")
     sites, mpo, iks = [], [], []
     for _ in range(N):
         (d,) = rd.take("<I")

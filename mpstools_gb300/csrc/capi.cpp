@@ -24,6 +24,9 @@ mpsg_status mpsg_ctx_create(int32_t device, mpsg_ctx* out) {
   mpsg_ctx c = new mpsg_ctx_s;
   try {
     c->c = std::make_shared<Ctx>(device);
+    // place the no-allocation matvec's scratch array now (module load, symbol address), so that
+    // mpsg_matvec2_plan_execute_noalloc itself allocates nothing
+    noalloc_scratch_address(device);
   } catch (...) {
     delete c;
     throw;
@@ -52,14 +55,15 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   API_END
 }
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx) {
-  return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count() + batch_launch_count();
+  return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count() + batch_launch_count() +
+         bidiag_launch_count();
 }
 int64_t mpsg_split_fallbacks(void) { return split_fallback_count(); }
 mpsg_status mpsg_ctx_set_svd_method(mpsg_ctx ctx, int32_t method) {
   API_BEGIN
-  MPSG_CHECK(method >= 0 && method <= 3,
+  MPSG_CHECK(method >= 0 && method <= 4,
              "svd method must be 0 (Jacobi SVD), 1 (density matrix, cuSOLVER batched), 2 (density matrix, "
-             "cuSOLVER concurrent) or 3 (density matrix, own batched eigensolver)");
+             "cuSOLVER concurrent), 3 (density matrix, own batched eigensolver) or 4 (own bidiagonal SVD)");
   C(ctx)->svd_method = method;
   API_END
 }
@@ -320,6 +324,14 @@ mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, i
   e->e->prec = prec;
   e->e->reorth = reorth != 0;
   e->e->lanmax = lanmax;
+  API_END
+}
+mpsg_status mpsg_dmrg_get_options(mpsg_dmrg e, int32_t* prec, int32_t* reorth, int32_t* lanmax) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e, "null engine");
+  if (prec) *prec = (int32_t)e->e->prec;
+  if (reorth) *reorth = e->e->reorth ? 1 : 0;
+  if (lanmax) *lanmax = e->e->lanmax;
   API_END
 }
 mpsg_status mpsg_dmrg_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, uint32_t chimax, int32_t doTrunc,

@@ -4,7 +4,9 @@
 // resume and states can move between the CPU oracle and the GPU engine.
 //
 // File format "MPSGCKP1" (little-endian; tensors FP64, blocks in key order, each block column-major):
-//   char[8] "MPSGCKP1"; u32 version (1); u32 N
+//   char[8] "MPSGCKP1"; u32 version (2; version 1 files lack the settings record and still load);
+//   u32 N
+//   version >= 2: u32 prec (mpsg_prec); u32 reorth; u32 lanmax; u64 updates (doStep calls made)
 //   per site s = 0 .. N-1:
 //     u32 d; u64 charge[d]                                   (i_to_key)
 //     u32 Dl; u32 Dr; u32 nterms; nterms x {u32 wl, wr, out, in; f64 value}   (MPOMat)
@@ -21,7 +23,7 @@ namespace {
 
 constexpr char kMagic[8] = {'M', 'P', 'S', 'G', 'C', 'K', 'P', '1'};
 constexpr char kEnd[8] = {'M', 'P', 'S', 'G', 'E', 'N', 'D', '!'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 
 struct File {
   FILE* f = nullptr;
@@ -36,6 +38,14 @@ struct File {
   }
   void get(void* p, size_t n) {
     if (n && std::fread(p, 1, n, f) != n) throw Err(1, "checkpoint file truncated");
+  }
+  // bytes left after the read position (checked before any allocation sized by the file)
+  int64_t remaining() {
+    const long cur = std::ftell(f);
+    if (cur < 0 || std::fseek(f, 0, SEEK_END) != 0) throw Err(1, "checkpoint file is not seekable");
+    const long end = std::ftell(f);
+    if (end < 0 || std::fseek(f, cur, SEEK_SET) != 0) throw Err(1, "checkpoint file is not seekable");
+    return (int64_t)end - (int64_t)cur;
   }
   template <class T>
   void put(T v) {
@@ -69,8 +79,11 @@ void write_tensor(File& f, const Tensor& t) {
   f.put(data.data(), sizeof(double) * data.size());
 }
 
-TensorP read_tensor(File& f, Ctx* ctx) {
+// Site tensor of local dimension d: block physical indices must be < d, and the data the block
+// table declares must be present in the file before anything is allocated for it.
+TensorP read_tensor(File& f, Ctx* ctx, uint32_t d) {
   const uint32_t n = bounded(f.get<uint32_t>(), 1u << 24, "block count");
+  if ((int64_t)n * 28 > f.remaining()) throw Err(1, "checkpoint file truncated (block table)");
   std::vector<uint64_t> q(2 * (size_t)n);
   std::vector<uint32_t> p(n);
   std::vector<int32_t> r(n), c(n);
@@ -82,9 +95,11 @@ TensorP read_tensor(File& f, Ctx* ctx) {
     r[i] = f.get<int32_t>();
     c[i] = f.get<int32_t>();
     if (r[i] < 0 || c[i] < 0 || r[i] > (1 << 20) || c[i] > (1 << 20)) throw Err(1, "checkpoint: implausible block size");
+    if (p[i] >= d) throw Err(1, "checkpoint: block physical index out of range of the site's itokey");
     total += (int64_t)r[i] * c[i];
   }
   if (total > ((int64_t)1 << 34)) throw Err(1, "checkpoint: implausible tensor size");
+  if (total * (int64_t)sizeof(double) > f.remaining()) throw Err(1, "checkpoint file truncated (block data)");
   std::vector<double> data((size_t)std::max<int64_t>(total, 1));
   f.get(data.data(), sizeof(double) * (size_t)total);
   return tensor_from_host(ctx, 1, (int)n, q.data(), p.data(), r.data(), c.data(), data.data());
@@ -105,6 +120,10 @@ mpsg_status mpsg_dmrg_save(mpsg_dmrg e, const char* path) {
   f.put(kMagic, 8);
   f.put<uint32_t>(kVersion);
   f.put<uint32_t>((uint32_t)x.N);
+  f.put<uint32_t>((uint32_t)x.prec);
+  f.put<uint32_t>(x.reorth ? 1u : 0u);
+  f.put<uint32_t>((uint32_t)x.lanmax);
+  f.put<uint64_t>((uint64_t)x.updates_done());
   for (int s = 0; s < x.N; ++s) {
     f.put<uint32_t>((uint32_t)x.ik[s].size());
     for (Q q : x.ik[s]) f.put<uint64_t>(q);
@@ -148,13 +167,23 @@ mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out) {
   char magic[8];
   f.get(magic, 8);
   MPSG_CHECK(std::memcmp(magic, kMagic, 8) == 0, "not an MPSG checkpoint file");
-  MPSG_CHECK(f.get<uint32_t>() == kVersion, "unsupported checkpoint version");
+  const uint32_t version = f.get<uint32_t>();
+  MPSG_CHECK(version == 1 || version == 2, "unsupported checkpoint version");
   const int N = (int)bounded(f.get<uint32_t>(), 1u << 20, "site count");
   MPSG_CHECK(N >= 3, "DMRG needs at least 3 sites");
   std::unique_ptr<Engine> e(new Engine());
   e->ctx = C(ctx);
   e->keep = e->ctx->shared_from_this();
   e->N = N;
+  if (version >= 2) {  // run settings; a version-1 file resumes with the FP64 defaults
+    const uint32_t prec = f.get<uint32_t>();
+    MPSG_CHECK(prec <= (uint32_t)MPSG_PREC_MIXED, "checkpoint: unknown matvec precision");
+    e->prec = (mpsg_prec)prec;
+    e->reorth = f.get<uint32_t>() != 0;
+    e->lanmax = (int)bounded(f.get<uint32_t>(), 1000, "Lanczos iteration limit");
+    MPSG_CHECK(e->lanmax >= 1, "checkpoint: Lanczos iteration limit must be in [1, 1000]");
+    e->updates_base = (int64_t)f.get<uint64_t>();
+  }
   for (int s = 0; s < N; ++s) {
     const uint32_t d = bounded(f.get<uint32_t>(), 1u << 16, "local dimension");
     ItoKey ik(d);
@@ -166,12 +195,15 @@ mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out) {
     m.Dl = (int32_t)bounded(f.get<uint32_t>(), 1u << 16, "MPO dimension");
     m.Dr = (int32_t)bounded(f.get<uint32_t>(), 1u << 16, "MPO dimension");
     const uint32_t nt = bounded(f.get<uint32_t>(), 1u << 24, "MPO term count");
+    if ((int64_t)nt * 24 > f.remaining()) throw Err(1, "checkpoint file truncated (MPO terms)");
     for (uint32_t t = 0; t < nt; ++t) {
       wl.push_back(f.get<uint32_t>());
       wr.push_back(f.get<uint32_t>());
       o.push_back(f.get<uint32_t>());
       in.push_back(f.get<uint32_t>());
       v.push_back(f.get<double>());
+      if (wl.back() >= (uint32_t)m.Dl || wr.back() >= (uint32_t)m.Dr || o.back() >= d || in.back() >= d)
+        throw Err(1, "checkpoint: MPO term index out of range");
     }
     m.nterms = (int32_t)nt;
     m.wl = wl.data();
@@ -180,12 +212,13 @@ mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out) {
     m.in = in.data();
     m.value = v.data();
     e->mpo.push_back(mpo_from_c(&m));
-    e->mps.push_back(read_tensor(f, e->ctx));
+    e->mps.push_back(read_tensor(f, e->ctx, d));
   }
   const uint32_t nl = bounded(f.get<uint32_t>(), 1u << 20, "lambda count");
   for (uint32_t i = 0; i < nl; ++i) {
     const int32_t bond = f.get<int32_t>();
     const uint32_t n = bounded(f.get<uint32_t>(), 1u << 24, "lambda block count");
+    if ((int64_t)n * 12 > f.remaining()) throw Err(1, "checkpoint file truncated (lambda table)");
     std::vector<uint64_t> q(2 * (size_t)n);
     std::vector<uint32_t> p(n, 0);
     std::vector<int32_t> r(n), c(n, 1);
@@ -196,6 +229,7 @@ mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out) {
       if (r[j] < 0 || r[j] > (1 << 20)) throw Err(1, "checkpoint: implausible lambda size");
       total += r[j];
     }
+    if (total * (int64_t)sizeof(double) > f.remaining()) throw Err(1, "checkpoint file truncated (lambda data)");
     std::vector<double> data((size_t)std::max<int64_t>(total, 1));
     f.get(data.data(), sizeof(double) * (size_t)total);
     e->lam[bond] = tensor_from_host(e->ctx, 0, (int)n, q.data(), p.data(), r.data(), c.data(), data.data());

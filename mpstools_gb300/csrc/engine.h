@@ -27,6 +27,8 @@ struct Engine {
   bool reorth = false;
   int lanmax = 500;
   std::vector<StepRec> steps;
+  int64_t updates_base = 0;  // doStep calls made before this engine was loaded from a checkpoint
+  int64_t updates_done() const { return updates_base + (int64_t)steps.size(); }
   LanczosStats lst;
   double env_seconds = 0, split_seconds = 0, env_flops = 0, wall = 0;
 

@@ -1,5 +1,6 @@
 // Host core of libmpsg: context, device memory, block-sparse tensors, MPO terms and the
 // grouped-GEMM / linear-combination plans that the contractions are built from.
+#include <cstdio>
 #include "host_core.h"
 
 #include <algorithm>
@@ -44,7 +45,12 @@ void* Ctx::dmalloc(size_t bytes) {
   return p;
 }
 void Ctx::dfree(void* p) {
-  if (p) cudaFreeAsync(p, stream);
+  if (!p) return;
+  const cudaError_t e = cudaFreeAsync(p, stream);
+  if (e != cudaSuccess) {  // a library bug: report it here instead of at the next unrelated status check
+    cudaGetLastError();
+    std::fprintf(stderr, "libmpsg: cudaFreeAsync failed: %s\n", cudaGetErrorString(e));
+  }
 }
 cusolverDnHandle_t Ctx::svd_handle() {
   if (!solver) {

@@ -18,7 +18,7 @@ struct Ctx : std::enable_shared_from_this<Ctx> {
   gesvdjInfo_t svdp = nullptr;
   double* part = nullptr;     // reduction partials (kRedBlocks) + 64 scalars
   double* hscal = nullptr;    // pinned host scalars
-  int svd_method = 0;         // 0: Jacobi SVD (gesvdj), 1: density matrix (Gram + syevd)
+  int svd_method = 4;         // 4: own bidiagonal SVD; 0: Jacobi SVD (gesvdj); 1-3: density matrix
   explicit Ctx(int dev);
   ~Ctx();
   void* dmalloc(size_t bytes);

@@ -633,6 +633,7 @@ struct SvdBatch {
   int64_t nS = 0;
   explicit SvdBatch(Ctx* c) : ctx(c) {}
   ~SvdBatch() {
+    bidiag_free();
     ctx->dfree(dM);
     ctx->dfree(dU);
     ctx->dfree(dV);
@@ -1124,7 +1125,7 @@ struct SvdBatch {
   // multiplied by R_jj of the first pass (the norm of y_j after removing its components along the
   // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
   // failed (optional): sectors whose Cholesky met a non-positive pivot are appended instead of throwing
-  void cholqr(bool left, int passes, std::vector<int>* failed = nullptr) {
+  void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true) {
     std::vector<int> idx;
     int kmax = 0;
     for (size_t i = 0; i < s.size(); ++i)
@@ -1162,7 +1163,7 @@ struct SvdBatch {
       zd.push_back(CholOp{dC + offC[i], nullptr, kc, kc});
       const int CL = chol_cluster_size(kc);
       for (int pass = 0; pass < 2; ++pass)
-        byCL[pass][CL].push_back(CholQROp{dC + offC[i], dR + s[i].offS, (pass == 0 && left) ? dS + s[i].offS : nullptr,
+        byCL[pass][CL].push_back(CholQROp{dC + offC[i], dR + s[i].offS, (pass == 0 && left && scale_s) ? dS + s[i].offS : nullptr,
                                           dinf + t, kc, kc});
       kmaxCL[CL] = std::max(kmaxCL[CL], kc);
     }
@@ -1255,10 +1256,260 @@ struct SvdBatch {
     int nmax = 0;
     for (auto& x : s) nmax = std::max(nmax, x.k > 0 ? x.ns : 0);
     if (method != 0 && nmax > chol_max_k()) method = 0;  // the density routes' CholeskyQR covers widths <= 512
+    if (method == 4 && !bidiag_fits()) method = 0;
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
     else if (method == 3) run_gram_custom();
+    else if (method == 4) run_bidiag_all();
     else run_jacobi();
+  }
+
+  // ---------------------------------------------------------------- bidiagonal route (svd_bidiag.cu)
+  // Exact route on the library's own kernels: Householder bidiagonalisation of every sector on a
+  // thread-block cluster, singular values by bisection on the Golub-Kahan tridiagonal, restricted to
+  // the values at or above the truncation cut of each segment; singular vectors only for the values
+  // the truncation keeps (inverse iteration, CholeskyQR of U_B and V_B, reflector back-transformation).
+  struct Bidiag {
+    double *d = nullptr, *e = nullptr, *tq = nullptr, *tp = nullptr, *Pr = nullptr, *b = nullptr, *b2 = nullptr,
+           *meta = nullptr, *Z = nullptr, *xlo = nullptr, *Mcopy = nullptr;
+    int32_t *kcomp = nullptr, *seg = nullptr, *kept = nullptr;
+    GkOp* ops_d = nullptr;
+    std::vector<GkOp> ops;
+    std::vector<int> idx;  // sector of each op
+    std::vector<int64_t> offPr, offB;
+  } bd;
+  bool bidiag_fits() const {  // cluster bidiagonalisation and CholeskyQR widths
+    for (auto& x : s)
+      if (x.k > 0 && (gebrd_cluster_size(x.ms, x.ns) == 0 || x.ns > chol_max_k())) return false;
+    return true;
+  }
+  void bidiag_free() {
+    for (double* p : {bd.d, bd.e, bd.tq, bd.tp, bd.Pr, bd.b, bd.b2, bd.meta, bd.Z, bd.xlo, bd.Mcopy}) ctx->dfree(p);
+    ctx->dfree(bd.kcomp);  // kept and seg live in the same allocation
+    ctx->dfree(bd.ops_d);
+    bd = Bidiag();
+  }
+  // Singular values at or above each segment's cut into dS (descending, 0 past the computed ones).
+  // seg_first[c] = first sector of segment c (size nseg + 1, ascending); chimax: values kept per
+  // segment at most; floor_abs: values below it are never kept (the reference drops <= 1e-15).
+  void bidiag_values(const std::vector<int>& seg_first, int chimax, double floor_abs) {
+    cudaStream_t st = ctx->stream;
+    MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(s.size(), 1), st));
+    MPSG_CUDA(cudaMemsetAsync(dS, 0, sizeof(double) * std::max<int64_t>(nS, 2), st));
+    bd.idx.clear();
+    int64_t oPr = 0, oB = 0;
+    for (size_t i = 0; i < s.size(); ++i) {
+      bd.offPr.push_back(oPr);
+      bd.offB.push_back(oB);
+      if (s[i].k == 0) continue;
+      bd.idx.push_back((int)i);
+      oPr += ((int64_t)s[i].ns * s[i].ns + kAlign - 1) / kAlign * kAlign;
+      oB += 2 * (int64_t)s[i].ns;
+    }
+    const int nop = (int)bd.idx.size();
+    if (nop == 0) return;
+    auto alloc = [&](int64_t n) { return (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(n, 2)); };
+    bd.d = alloc(nS);
+    bd.e = alloc(nS);
+    bd.tq = alloc(nS);
+    bd.tp = alloc(nS);
+    bd.Pr = alloc(oPr);
+    bd.b = alloc(oB);
+    bd.b2 = alloc(oB);
+    bd.meta = alloc(4 * (int64_t)nop);
+    const int nseg = (int)seg_first.size() - 1;
+    bd.xlo = alloc(nseg);
+    // the sector matrices, kept for sectors whose vectors have to be redone on the Jacobi route (the
+    // bidiagonalisation overwrites them with its reflectors)
+    const int64_t nM = s.empty() ? 0 : s.back().offM + (int64_t)s.back().ms * s.back().ns;
+    bd.Mcopy = alloc(nM);
+    if (nM) MPSG_CUDA(cudaMemcpyAsync(bd.Mcopy, dM, sizeof(double) * nM, cudaMemcpyDeviceToDevice, st));
+    bd.kcomp = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (size_t)nop * 2 + sizeof(int32_t) * (nseg + 1));
+    bd.kept = bd.kcomp + nop;
+    bd.seg = bd.kept + nop;
+    // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first)
+    {
+      std::map<int, std::vector<GebrdOp>> byCL;
+      std::map<int, std::pair<int, int>> mx;
+      for (int i : bd.idx) {
+        const Sec& x = s[i];
+        const int CL = gebrd_cluster_size(x.ms, x.ns);
+        byCL[CL].push_back(GebrdOp{dM + x.offM, bd.d + x.offS, bd.e + x.offS, bd.tq + x.offS, bd.tp + x.offS,
+                                   bd.Pr + bd.offPr[i], x.ms, x.ns, x.ms});
+        auto& p = mx[CL];
+        p.first = std::max(p.first, x.ms);
+        p.second = std::max(p.second, x.ns);
+      }
+      std::vector<std::pair<int, GebrdOp*>> bufs;
+      for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) {
+        GebrdOp* dptr = (GebrdOp*)ctx->dmalloc(sizeof(GebrdOp) * it->second.size());
+        MPSG_CUDA(cudaMemcpyAsync(dptr, it->second.data(), sizeof(GebrdOp) * it->second.size(), cudaMemcpyHostToDevice,
+                                  st));
+        bufs.push_back({it->first, dptr});
+      }
+      const int nw = std::min<int>((int)bufs.size(), ctx->nworkers());
+      ctx->fork(nw);
+      for (size_t j = 0; j < bufs.size(); ++j)
+        launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, mx[bufs[j].first].first,
+                     mx[bufs[j].first].second, ctx->wstreams[j % nw]);
+      ctx->join(nw);
+      for (auto& b : bufs) ctx->dfree(b.second);
+    }
+    // 2.-4. Golub-Kahan matrices, the cut of each segment, the singular values above it
+    std::vector<int32_t> segop(nseg + 1, 0);
+    {
+      int t = 0;
+      for (int c = 0; c <= nseg; ++c) {
+        while (t < nop && bd.idx[t] < seg_first[c]) ++t;
+        segop[c] = t;
+      }
+      segop[nseg] = nop;
+    }
+    std::vector<int> seg_of_op(nop, 0);
+    for (int c = 0; c < nseg; ++c)
+      for (int t = segop[c]; t < segop[c + 1]; ++t) seg_of_op[t] = c;
+    bd.ops.clear();
+    std::vector<int32_t> op_of, k_of;
+    for (int t = 0; t < nop; ++t) {
+      const Sec& x = s[bd.idx[t]];
+      GkOp g;
+      g.d = bd.d + x.offS;
+      g.e = bd.e + x.offS;
+      g.b = bd.b + bd.offB[bd.idx[t]];
+      g.b2 = bd.b2 + bd.offB[bd.idx[t]];
+      g.S = dS + x.offS;
+      g.Z = nullptr;
+      g.meta = bd.meta + 4 * t;
+      g.xlo = bd.xlo + seg_of_op[t];
+      g.kcomp = bd.kcomp + t;
+      g.n = x.ns;
+      g.ldz = 2 * x.ns;
+      bd.ops.push_back(g);
+      for (int k = 0; k < x.ns; ++k) {
+        op_of.push_back(t);
+        k_of.push_back(k);
+      }
+    }
+    const int nth = (int)op_of.size();
+    bd.ops_d = (GkOp*)ctx->dmalloc(sizeof(GkOp) * nop);
+    int32_t* dmap = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * (size_t)nth);
+    MPSG_CUDA(cudaMemcpyAsync(bd.ops_d, bd.ops.data(), sizeof(GkOp) * nop, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(bd.seg, segop.data(), sizeof(int32_t) * (nseg + 1), cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap + nth, k_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
+    launch_gk_setup(bd.ops_d, nop, st);
+    launch_gk_cut(bd.ops_d, bd.seg, nseg, chimax, floor_abs, bd.xlo, st);
+    launch_gk_bisect(bd.ops_d, dmap, dmap + nth, nth, st);
+    ctx->dfree(dmap);
+  }
+  // Singular vectors of the kept values (kept[i] per sector, from the truncation): U (ms x kept) and
+  // V (ns x kept) in dU / dV, FixPhase applied.  Sectors whose vectors CholeskyQR cannot
+  // orthonormalise are redone on the exact Jacobi route.
+  void bidiag_vectors(const std::vector<int32_t>& kept) {
+    cudaStream_t st = ctx->stream;
+    const int nop = (int)bd.idx.size();
+    kr.assign(s.size(), 0);
+    for (int i : bd.idx) kr[i] = kept[i];
+    if (nop == 0) return;
+    std::vector<int32_t> kk(nop);
+    int64_t oZ = 0, scr = 0;
+    std::vector<int64_t> offZ(nop);
+    std::vector<int32_t> op_of, k_of;
+    std::vector<int64_t> soff;
+    int lenmax = 0;
+    for (int t = 0; t < nop; ++t) {
+      const Sec& x = s[bd.idx[t]];
+      kk[t] = kept[bd.idx[t]];
+      offZ[t] = oZ;
+      oZ += 2 * (int64_t)x.ns * kk[t];
+      for (int k = 0; k < kk[t]; ++k) {
+        op_of.push_back(t);
+        k_of.push_back(k);
+        soff.push_back(scr);
+        scr += 5 * 2 * (int64_t)x.ns;
+      }
+      lenmax = std::max(lenmax, x.ms);
+    }
+    const int nth = (int)op_of.size();
+    if (nth == 0) return;
+    bd.Z = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oZ, 2));
+    for (int t = 0; t < nop; ++t) bd.ops[t].Z = bd.Z + offZ[t];
+    double* dscr = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(scr, 2));
+    int32_t* dmap = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * (size_t)nth);
+    int64_t* dsoff = (int64_t*)ctx->dmalloc(sizeof(int64_t) * (size_t)nth);
+    MPSG_CUDA(cudaMemcpyAsync(bd.ops_d, bd.ops.data(), sizeof(GkOp) * nop, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(bd.kept, kk.data(), sizeof(int32_t) * nop, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dmap + nth, k_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(dsoff, soff.data(), sizeof(int64_t) * nth, cudaMemcpyHostToDevice, st));
+    // 5./6. eigenvectors of T for the kept values, split into U_B (first ns rows of U) and V_B
+    launch_gk_invit(bd.ops_d, dmap, dmap + nth, bd.kept, nth, dscr, dsoff, st);
+    {
+      std::vector<GkVecOp> vo;
+      for (int t = 0; t < nop; ++t) {
+        const Sec& x = s[bd.idx[t]];
+        for (int k = 0; k < kk[t]; ++k)
+          vo.push_back(GkVecOp{bd.Z + offZ[t], dU + x.offU, dV + x.offV, x.ns, x.ms, 2 * x.ns, x.ms, x.ns, k});
+      }
+      GkVecOp* dv = (GkVecOp*)ctx->dmalloc(sizeof(GkVecOp) * vo.size());
+      MPSG_CUDA(cudaMemcpyAsync(dv, vo.data(), sizeof(GkVecOp) * vo.size(), cudaMemcpyHostToDevice, st));
+      launch_gk_vectors(dv, (int)vo.size(), st);
+      ctx->dfree(dv);
+    }
+    ctx->dfree(dscr);
+    ctx->dfree(dsoff);
+    ctx->dfree(dmap);
+    // orthonormal to rounding: inverse iteration leaves ~eps ||T|| / gap between close values
+    std::vector<int> failed;
+    cholqr(true, 2, &failed, false);
+    cholqr(false, 2, &failed, false);
+    // 7. U = Q [U_B; 0], V = P V_B
+    {
+      std::vector<ReflOp> ro;
+      for (int i : bd.idx) {
+        const Sec& x = s[i];
+        for (int c0 = 0; c0 < kr[i]; c0 += 8) {
+          const int c1 = std::min(c0 + 8, kr[i]);
+          ro.push_back(ReflOp{dM + x.offM, bd.tq + x.offS, dU + x.offU, x.ms, x.ns, 0, x.ms, x.ms, c0, c1});
+          ro.push_back(ReflOp{bd.Pr + bd.offPr[i], bd.tp + x.offS, dV + x.offV, x.ns, x.ns - 1, 1, x.ns, x.ns, c0, c1});
+        }
+      }
+      if (!ro.empty()) {
+        ReflOp* dr = (ReflOp*)ctx->dmalloc(sizeof(ReflOp) * ro.size());
+        MPSG_CUDA(cudaMemcpyAsync(dr, ro.data(), sizeof(ReflOp) * ro.size(), cudaMemcpyHostToDevice, st));
+        launch_apply_refl(dr, (int)ro.size(), lenmax, st);
+        ctx->dfree(dr);
+      }
+    }
+    fixphase();
+    if (!failed.empty()) {
+      std::sort(failed.begin(), failed.end());
+      failed.erase(std::unique(failed.begin(), failed.end()), failed.end());
+      g_split_fallbacks.fetch_add((int64_t)failed.size());
+      if (std::getenv("MPSG_VERBOSE"))
+        for (int i : failed)
+          std::fprintf(stderr, "libmpsg: bidiagonal SVD vectors of sector %d (%d x %d) redone on the Jacobi route\n", i,
+                       s[i].ms, s[i].ns);
+      for (int i : failed) {  // the sector matrix back from the copy, all its columns from gesvdj
+        MPSG_CUDA(cudaMemcpyAsync(dM + s[i].offM, bd.Mcopy + s[i].offM, sizeof(double) * (size_t)s[i].ms * s[i].ns,
+                                  cudaMemcpyDeviceToDevice, st));
+        kr[i] = s[i].k;
+      }
+      run_jacobi(&failed);
+    }
+    bidiag_free();
+  }
+  // the whole SVD on the bidiagonal route without truncation: every value >= 1e-16 with its vectors
+  void run_bidiag_all() {
+    std::vector<int> seg_first = {0, (int)s.size()};
+    bidiag_values(seg_first, INT32_MAX, 1e-16);
+    std::vector<int32_t> kc(bd.idx.size());
+    if (!kc.empty())
+      MPSG_CUDA(cudaMemcpyAsync(kc.data(), bd.kcomp, sizeof(int32_t) * kc.size(), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    std::vector<int32_t> kept(s.size(), 0);
+    for (size_t t = 0; t < bd.idx.size(); ++t) kept[bd.idx[t]] = kc[t];
+    bidiag_vectors(kept);
   }
 
   // only (optional): the sectors to decompose (the others keep their factors)
@@ -1301,11 +1552,11 @@ struct SvdBatch {
       p.Pm = Pp((int)i, &lp);
       p.m = s[i].m;
       p.n = s[i].n;
-      p.k = s[i].k;
+      p.k = kcols(i);
       p.ldq = lq;
       p.ldp = lp;
       ph.push_back(p);
-      maxk = std::max(maxk, s[i].k);
+      maxk = std::max(maxk, kcols(i));
     }
     if (!ph.empty()) {
       PhaseOp* d = (PhaseOp*)ctx->dmalloc(sizeof(PhaseOp) * ph.size());
@@ -1366,7 +1617,6 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
     }
   }
   run_copyops(ctx, gops);
-  sv.run(ctx->svd_method);
   // global truncation; with segments (a direct sum of independent chains, chain c holding the
   // centre charges in [seg_q0[c], seg_q0[c + 1])) one truncation per chain over its own sectors
   const int nseg = seg_q0 ? (int)seg_q0->size() : 1;
@@ -1381,6 +1631,11 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   }
   for (int si = (int)qcs.size() - 1; si >= 0; --si) s0[seg_of_sec[si]] = si;
   for (int c = nseg - 1; c >= 0; --c) s0[c] = std::min(s0[c], s0[c + 1]);
+  // the bidiagonal route computes only the values at or above each segment's truncation cut here, and
+  // the singular vectors of the kept ones after the truncation; every other route decomposes fully
+  const bool bidiag = ctx->svd_method == 4 && sv.bidiag_fits() && !sv.s.empty();
+  if (bidiag) sv.bidiag_values(s0, chimax, 1e-15);
+  else sv.run(ctx->svd_method == 4 ? 0 : ctx->svd_method);
   std::vector<int32_t> sec_of(sv.nS);
   for (size_t si = 0; si < qcs.size(); ++si)
     for (int j = 0; j < sv.s[si].k; ++j) sec_of[sv.s[si].offS + j] = (int32_t)si - s0[seg_of_sec[si]];
@@ -1416,6 +1671,11 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   const double tw = R.tw_seg[0];
   const int chi = R.chi_seg[0];
   ctx->dfree(dsec);
+  if (bidiag) {
+    std::vector<int32_t> kept(qcs.size());
+    for (size_t si = 0; si < qcs.size(); ++si) kept[si] = std::max(counts[si], 0);
+    sv.bidiag_vectors(kept);
+  }
   // result layouts (dropDangling: sectors without kept values vanish, blocks cut to the kept count)
   Layout lu, lv, ll;
   for (size_t si = 0; si < qcs.size(); ++si) {

@@ -83,6 +83,8 @@ struct MatvecPlan {
 };
 // FP64 plan applied with the stage-A intermediate in the library's fixed device array (noalloc.cu)
 void matvec_noalloc(MatvecPlan& P, const double* theta_in, double* theta_out);
+// device address of that array on `device` (the current device); resolved once per device
+double* noalloc_scratch_address(int device);
 std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& th_in,
                                          const MPO& W1, const MPO& W2, const ItoKey& ik0, const ItoKey& ik1,
                                          const Layout* out_layout, int prec = MPSG_PREC_FP64);

@@ -575,16 +575,29 @@ void launch_tri_lowest_seg(const double* alpha, const double* beta, const int* n
 // ============================================================================ truncation
 // rank[i] = position of value i when all values are ordered by (value desc, later insertion first),
 // the iteration order of the reference's reversed std::multimap (src/BlockTensor.hpp:236-258).
-__global__ void k_trunc_rank(const double* __restrict__ S, int n, int32_t* rank) {
+// rank[i] = number of values ordered before value i: larger ones, and equal ones stored later (the
+// reversed multimap).  Singular values are >= +0, so their IEEE bit patterns order like the values:
+// the comparisons run on the integer pipe (an FP64 compare occupies this GPU's FP64 pipe for 16
+// cycles per warp), over tiles of the values staged in shared memory.
+constexpr int kRankTile = 2048;
+__global__ void __launch_bounds__(256) k_trunc_rank(const double* __restrict__ S, int n, int32_t* rank) {
+  __shared__ long long key[kRankTile];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double v = S[i];
+  constexpr long long kAbs = 0x7fffffffffffffffll;  // -0 orders as +0
+  const long long v = i < n ? (__double_as_longlong(S[i]) & kAbs) : 0;
   int r = 0;
-  for (int j = 0; j < n; ++j) {
-    const double w = S[j];
-    r += (w > v) || (w == v && j > i);
+  for (int t0 = 0; t0 < n; t0 += kRankTile) {
+    const int tn = min(kRankTile, n - t0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < tn; j += blockDim.x) key[j] = __double_as_longlong(S[t0 + j]) & kAbs;
+    __syncthreads();
+    if (i < n)
+      for (int j = 0; j < tn; ++j) {
+        const long long w = key[j];
+        r += (w > v) | ((w == v) & (t0 + j > i));
+      }
   }
-  rank[i] = r;
+  if (i < n) rank[i] = r;
 }
 // out3[0] = truncated weight, out3[1] = kept count, out3[2] = 1/norm of kept values (normalisation).
 // One block.  The floating-point recurrences stay sequential in the reference's order (the norm over

@@ -186,6 +186,41 @@ struct TrsmRowsOp {  // rows [r0, r1) of X (ldx) <- X R^-1, R upper (ldr), k col
   const double* rdiag;
   int32_t k, ldx, ldr, r0, r1;
 };
+// ---- bidiagonal SVD of the split (svd_bidiag.cu)
+struct GebrdOp {  // m x n (m >= n) sector matrix A (lda) -> B = Q^T A P upper bidiagonal (d, e)
+  double* A;      // overwritten: column j below the diagonal = tail of left reflector j (unit at row j)
+  double* d;      // n
+  double* e;      // n (e[n-1] unused)
+  double* tauq;   // n
+  double* taup;   // n (taup[n-1] unused)
+  double* Pr;     // n x n (ld n): column j = tail of right reflector j at rows j+2.. (unit at row j+1)
+  int32_t m, n, lda;
+};
+struct GkOp {  // Golub-Kahan tridiagonal [[0, B], [B^T, 0]] (interleaved, zero diagonal) of one sector
+  const double* d;    // n (bidiagonal)
+  const double* e;    // n - 1
+  double* b;          // 2n - 1 off-diagonals, scaled by 2^-p (max |b| in [1, 2))
+  double* b2;         // their squares
+  double* S;          // n: singular values (unscaled), descending; 0 past the computed ones
+  double* Z;          // 2n x kept: eigenvectors (v0, u0, v1, u1, ...) of the kept values
+  double* meta;       // [0] 2^p, [1] 2^-p, [2] Gershgorin bound of the scaled matrix
+  const double* xlo;  // the segment's cut: singular values >= *xlo are computed
+  int32_t* kcomp;     // number of singular values >= *xlo
+  int32_t n, ldz;
+};
+struct GkVecOp {  // split the GK eigenvector of kept value k into V (n x k) and U (m x k, zero rows >= n)
+  const double* Z;
+  double* U;
+  double* V;
+  int32_t n, m, ldz, ldu, ldv, k;
+};
+struct ReflOp {  // columns [c0, c1) of X (len rows, ldx) <- H_0 H_1 ... H_{nref-1} X,
+                 // H_j = I - tau_j r_j r_j^T, r_j = unit at row j + off, R(i, j) below it
+  const double* R;
+  const double* tau;
+  double* X;
+  int32_t len, nref, off, ldr, ldx, c0, c1;
+};
 // ---- complex (TEBD) path (tebd_kernels.cu); planar blocks: re at p, im at p + plane offset
 struct CGatherOp {  // interleaved dst(i, j) = re(i, j) + i im(i, j); conj_trans: dst(j, i) = conj(...)
   const double* re;
@@ -299,6 +334,22 @@ void launch_saxpy3(double* out, const double* w, const double* v, const double* 
                    cudaStream_t s);
 void launch_scombine(double* y, const double* const* V, const int* nv_of, const double* z, int zstride,
                      const int64_t* segoff, int nseg, cudaStream_t s);
+// bidiagonal SVD (svd_bidiag.cu)
+int gebrd_cluster_size(int m, int n);  // 0: the sector does not fit the cluster kernel
+void launch_gebrd(const GebrdOp* ops, int nops, int CL, int mmax, int nmax, cudaStream_t s);
+void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s);
+// one CTA per segment [seg[c], seg[c + 1]) of ops: xlo[c] = cut such that at least chimax values of the
+// segment are >= it (or floor_abs when fewer than chimax exceed floor_abs); kcomp per op
+void launch_gk_cut(const GkOp* ops, const int32_t* seg, int nseg, int chimax, double floor_abs, double* xlo,
+                   cudaStream_t s);
+// S[k] of every (op_of[t], k_of[t]) with k < kcomp; 0 past kcomp
+void launch_gk_bisect(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, int nthreads, cudaStream_t s);
+// Z column k for every listed (op, k), k < kept[op]; scratch: 5 * 2n doubles per listed thread
+void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept, int nthreads,
+                     double* scratch, const int64_t* scratch_off, cudaStream_t s);
+void launch_gk_vectors(const GkVecOp* ops, int nops, cudaStream_t s);
+void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s);
+int64_t bidiag_launch_count();
 // global truncation over concatenated singular values (see kernels.cu)
 void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, int chimax, int doTrunc,
                      double tr_weight, int32_t* rank_scratch, int32_t* counts, double* out3, cudaStream_t s);

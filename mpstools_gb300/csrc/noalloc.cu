@@ -28,7 +28,10 @@ double* g_noalloc_addr[256] = {};  // device address of g_noalloc_scratch per de
 }  // namespace
 
 // Resolves (once per device, with that device current) the device address of the scratch array.
-static double* noalloc_scratch_address(int device) {
+// mpsg_ctx_create calls it for the context's device, so this module is loaded and the array placed
+// when the library is set up; an execute call then only reads the cached address.  The cache is
+// never invalidated: a device reset (cudaDeviceReset) while the library is loaded is not supported.
+double* noalloc_scratch_address(int device) {
   MPSG_CHECK(device >= 0 && device < 256, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if (!g_noalloc_addr[device]) {

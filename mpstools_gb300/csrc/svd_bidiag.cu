@@ -1,0 +1,561 @@
+// Batched FP64 singular value decomposition of the split's sector matrices through the bidiagonal
+// form, with the global truncation decided before any singular vector is computed.  Every stage is
+// one launch over all sectors of the split:
+//   1. k_gebrd<CL>   Householder bidiagonalisation A = Q B P^T (Golub & Kahan; Golub & Van Loan,
+//                    Matrix Computations, section 5.4.8).  One thread-block cluster of CL CTAs per
+//                    sector, the columns round-robin in shared memory; per column two cluster barriers:
+//                    the left reflector is pulled from the CTA that owns the column, the right
+//                    reflector of the row is formed from partial products every CTA pushes through
+//                    distributed shared memory.
+//   2. k_gk_setup    the Golub-Kahan tridiagonal T = [[0, B], [B^T, 0]] (rows interleaved, zero
+//                    diagonal; eigenvalues +-sigma), scaled by a power of two.
+//   3. k_gk_cut      one CTA per truncation segment: Sturm counts of all sectors at 32 points per
+//                    round (log scale) locate a cut x with at least chimax singular values >= x; only
+//                    the values above the cut can be kept, and only they are computed.
+//   4. k_gk_bisect   those singular values by multisection on Sturm counts of T.
+//   5. k_gk_invit    eigenvectors of T for the values the truncation keeps (inverse iteration).
+//   6. k_gk_vectors  (v, u) halves of each eigenvector: right and left singular vectors of B.
+//   7. k_apply_refl  U = Q [U_B; 0] and V = P V_B with the stored reflectors.
+// The singular values carry the absolute accuracy of a backward-stable SVD (~eps ||A||), like the
+// LAPACK dgesvd of the reference, because T is formed from B without squaring A (the Gram-matrix
+// route cannot resolve values below ~sqrt(eps) ||A||).  Sturm counts and inverse iteration follow
+// Wilkinson, The Algebraic Eigenvalue Problem, chapter 5.  No wait in these kernels spins: cluster
+// barriers are hardware barriers.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cstdlib>
+
+#include "mpsg_internal.h"
+#include "eig_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace mpsg {
+
+static std::atomic<int64_t> g_bd_launches{0};
+int64_t bidiag_launch_count() { return g_bd_launches.load(); }
+
+// ----------------------------------------------------------------------------- 1. bidiagonalisation
+// Shared memory of one CTA: own columns (ncol x m) | v (m) | zp (m) | cb (m) | z (m) | ub (ncol) | scal (8)
+static __host__ __device__ size_t gebrd_smem_doubles(int m, int n, int CL) {
+  const int ncol = (n + CL - 1) / CL;
+  return (size_t)ncol * m + 4 * (size_t)m + (size_t)ncol + 8;
+}
+static size_t gebrd_smem_bytes(int m, int n, int CL) { return sizeof(double) * gebrd_smem_doubles(m, n, CL); }
+
+// Left reflector of column j (the calling warp's CTA holds it as `col`; rows j..m-1 are current):
+// v (v[j] = 1) into the CTA's v buffer, tau into scal[0]; the reflector's tail into column j of A,
+// tauq[j] and d[j] = beta.
+__device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v, double* scal, int lane) {
+  const int m = o.m;
+  double s2 = 0.0;
+  for (int i = j + 1 + lane; i < m; i += 32) s2 = fma(col[i], col[i], s2);
+  s2 = warp_sum(s2);
+  const double alpha = col[j];
+  double tau = 0.0, beta = alpha, scale = 0.0;
+  if (s2 > 0.0) {
+    beta = -copysign(sqrt(fma(alpha, alpha, s2)), alpha);
+    tau = (beta - alpha) / beta;
+    scale = 1.0 / (alpha - beta);
+  }
+  for (int i = j + lane; i < m; i += 32) {
+    const double x = (i == j) ? 1.0 : col[i] * scale;
+    v[i] = x;
+    if (i > j) o.A[i + (int64_t)j * o.lda] = x;
+  }
+  if (lane == 0) {
+    scal[0] = tau;
+    o.tauq[j] = tau;
+    o.d[j] = beta;
+  }
+}
+
+template <int CL>
+__global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const GebrdOp o = ops[blockIdx.x / CL];
+  const int m = o.m, n = o.n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  extern __shared__ double sm[];
+  const int ncol_max = (n + CL - 1) / CL;
+  const int ncol = (n - r + CL - 1) / CL;  // own columns: global column r + lc * CL
+  double* cols = sm;
+  double* v = cols + (size_t)ncol_max * m;  // current left reflector
+  double* zp = v + m;                       // this CTA's partial products for the right reflector
+  double* cb = zp + m;                      // column j+1 before the right update (its owner)
+  double* z = cb + m;                       // right-update coefficients
+  double* ub = z + m;                       // right reflector entries of the own columns
+  double* scal = ub + ncol_max;             // [0] tau, [1] partial |row|^2, [2] alpha, [3] |row|^2, [4] alpha
+  for (int lc = warp; lc < ncol; lc += nwarp) {
+    const int c = r + lc * CL;
+    for (int i = lane; i < m; i += 32) cols[(size_t)lc * m + i] = o.A[i + (int64_t)c * o.lda];
+  }
+  __syncthreads();
+  if (r == 0 && warp == 0) gebrd_left(o, cols, 0, v, scal, lane);
+  cluster.sync();  // every CTA runs (distributed shared memory is addressable), reflector 0 exists
+  for (int j = 0; j + 1 < n; ++j) {
+    // (a) left reflector j from the owner of column j; applied to the own columns c > j
+    const int oj = j % CL;
+    if (r != oj) {
+      const double* rv = cluster.map_shared_rank(v, oj);
+      for (int i = j + tid; i < m; i += blockDim.x) v[i] = rv[i];
+      if (tid == 0) scal[0] = *cluster.map_shared_rank(scal, oj);
+    }
+    __syncthreads();
+    const double tau = scal[0];
+    const int lc1 = (j + CL - r) / CL;      // first own column with c >= j + 1
+    const int lc2 = (j + 1 + CL - r) / CL;  // first own column with c >= j + 2
+    if (tau != 0.0) {
+      for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
+        double* a = cols + (size_t)lc * m;
+        double s = 0.0;
+        for (int i = j + lane; i < m; i += 32) s = fma(v[i], a[i], s);
+        const double w = warp_sum(s) * tau;
+        for (int i = j + lane; i < m; i += 32) a[i] = fma(-v[i], w, a[i]);
+      }
+    }
+    __syncthreads();
+    // (b) partial products of the right reflector of row j: zp_i = sum over own c >= j+2 of
+    //     A(i, c) A(j, c), and the partial |A(j, c >= j+2)|^2; the owner of column j+1 stages it
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+      double acc = 0.0;
+      for (int lc = lc2; lc < ncol; ++lc) acc = fma(cols[(size_t)lc * m + i], cols[(size_t)lc * m + j], acc);
+      zp[i] = acc;
+    }
+    if (warp == 0) {
+      double s = 0.0;
+      for (int lc = lc2 + lane; lc < ncol; lc += 32) {
+        const double x = cols[(size_t)lc * m + j];
+        s = fma(x, x, s);
+      }
+      s = warp_sum(s);
+      if (lane == 0) scal[1] = s;
+    }
+    const int on = (j + 1) % CL, lnext = (j + 1) / CL;
+    if (r == on) {
+      const double* a = cols + (size_t)lnext * m;
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = a[i];
+      if (tid == 0) scal[2] = a[j];
+    }
+    cluster.sync();  // #1: partials and column j+1 visible to the cluster
+    // (c) the right reflector u (u_{j+1} = 1) zeroing A(j, j+2..): every CTA sums the partials
+    if (warp == 0) {
+      double s = lane < CL ? *cluster.map_shared_rank(scal + 1, lane) : 0.0;
+      s = warp_sum(s);
+      if (lane == 0) {
+        scal[3] = s;
+        scal[4] = *cluster.map_shared_rank(scal + 2, on);
+      }
+    }
+    __syncthreads();
+    const double nrm2 = scal[3], alpha = scal[4];
+    double taup = 0.0, beta = alpha, sc = 0.0;
+    if (nrm2 > 0.0) {
+      beta = -copysign(sqrt(fma(alpha, alpha, nrm2)), alpha);
+      taup = (beta - alpha) / beta;
+      sc = 1.0 / (alpha - beta);
+    }
+    if (taup != 0.0) {
+      // z_i = taup (A(i, j+1) + sum_{c >= j+2} A(i, c) u_c), u_c = A(j, c) sc
+      const double* rcb = cluster.map_shared_rank(cb, on);
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+        double zs = 0.0;
+#pragma unroll 4
+        for (int q = 0; q < CL; ++q) zs += cluster.map_shared_rank(zp, q)[i];
+        z[i] = taup * fma(sc, zs, rcb[i]);
+      }
+      for (int lc = lc2 + tid; lc < ncol; lc += blockDim.x) {
+        const double u = cols[(size_t)lc * m + j] * sc;
+        ub[lc] = u;
+        o.Pr[(r + lc * CL) + (int64_t)j * o.n] = u;
+      }
+    }
+    __syncthreads();
+    // (d) A(i, c) -= z_i u_c for i > j on the own columns c >= j+1; the owner of column j+1 updates
+    //     that column first and computes left reflector j+1 (lookahead) while its other warps go on
+    const bool own_next = (r == on);
+    if (own_next && warp == 0) {
+      double* a = cols + (size_t)lnext * m;
+      if (taup != 0.0)
+        for (int i = j + 1 + lane; i < m; i += 32) a[i] -= z[i];
+      __syncwarp();
+      if (lane == 0) {
+        o.e[j] = beta;
+        o.taup[j] = taup;
+      }
+      gebrd_left(o, a, j + 1, v, scal, lane);
+    }
+    const int p0 = own_next ? 32 : 0;  // threads of the update (all but the lookahead warp)
+    if (taup != 0.0 && tid >= p0) {
+      for (int i = j + 1 + tid - p0; i < m; i += (int)blockDim.x - p0) {
+        const double zi = z[i];
+        for (int lc = lc2; lc < ncol; ++lc) cols[(size_t)lc * m + i] = fma(-zi, ub[lc], cols[(size_t)lc * m + i]);
+      }
+    }
+    cluster.sync();  // #2: columns updated, reflector j+1 ready on its owner, partials consumed
+  }
+}
+
+template <int CL>
+static void launch_gebrd_cl(const GebrdOp* ops, int nops, int mmax, int nmax, cudaStream_t s) {
+  const size_t smem = gebrd_smem_bytes(mmax, nmax, CL);
+  MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nops * CL);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_gebrd<CL>, ops));
+  g_bd_launches.fetch_add(1);
+}
+
+static int gebrd_cl_cap() {
+  static int cap = [] {
+    const char* e = std::getenv("MPSG_GEBRD_MAX_CLUSTER");
+    const int v = e ? std::atoi(e) : 16;
+    return (v == 1 || v == 2 || v == 4 || v == 8) ? v : 16;
+  }();
+  return cap;
+}
+
+int gebrd_cluster_size(int m, int n) {
+  int CL = n <= 48 ? 1 : n <= 96 ? 2 : n <= 192 ? 4 : n <= 320 ? 8 : 16;
+  CL = std::min(CL, gebrd_cl_cap());
+  while (CL <= 16 && gebrd_smem_bytes(m, n, CL) > 220 * 1024) CL *= 2;
+  return CL <= 16 ? CL : 0;
+}
+
+void launch_gebrd(const GebrdOp* ops, int nops, int CL, int mmax, int nmax, cudaStream_t s) {
+  if (nops <= 0) return;
+  MPSG_CHECK(gebrd_smem_bytes(mmax, nmax, CL) <= 227 * 1024, "bidiagonalisation: sector too large for the cluster");
+  switch (CL) {
+    case 1: launch_gebrd_cl<1>(ops, nops, mmax, nmax, s); break;
+    case 2: launch_gebrd_cl<2>(ops, nops, mmax, nmax, s); break;
+    case 4: launch_gebrd_cl<4>(ops, nops, mmax, nmax, s); break;
+    case 8: launch_gebrd_cl<8>(ops, nops, mmax, nmax, s); break;
+    case 16: launch_gebrd_cl<16>(ops, nops, mmax, nmax, s); break;
+    default: throw Err(1, "bidiagonalisation: unsupported cluster size");
+  }
+}
+
+// ----------------------------------------------------------------------------- 2. Golub-Kahan matrix
+// b = (d0, e0, d1, e1, ..., d_{n-1}) * 2^-p with 2^p <= max |b| < 2^(p+1) (exact scaling: the
+// division-free Sturm counts below assume entries of order one); meta = (2^p, 2^-p, Gershgorin bound).
+__global__ void __launch_bounds__(128) k_gk_setup(const GkOp* __restrict__ ops) {
+  const GkOp o = ops[blockIdx.x];
+  const int n = o.n, N = 2 * n;
+  double mx = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    mx = fmax(mx, fabs(o.d[i]));
+    if (i + 1 < n) mx = fmax(mx, fabs(o.e[i]));
+  }
+  mx = warp_max(mx);
+  __shared__ double red[4];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
+  if (!(mx > 0.0) || !isfinite(mx)) {  // a zero sector: no singular value above any floor
+    for (int k = threadIdx.x; k + 1 < N; k += blockDim.x) o.b[k] = o.b2[k] = 0.0;
+    if (threadIdx.x == 0) o.meta[0] = o.meta[1] = o.meta[2] = 0.0;
+    return;
+  }
+  const int p = ilogb(mx);
+  const double sc = ldexp(1.0, -p);
+  double rs = 0.0;
+  for (int k = threadIdx.x; k + 1 < N; k += blockDim.x) {
+    const double x = ((k & 1) ? o.e[k >> 1] : o.d[k >> 1]) * sc;
+    o.b[k] = x;
+    o.b2[k] = x * x;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < N; k += blockDim.x)
+    rs = fmax(rs, (k > 0 ? fabs(o.b[k - 1]) : 0.0) + (k + 1 < N ? fabs(o.b[k]) : 0.0));
+  rs = warp_max(rs);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rs;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    rs = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
+    o.meta[0] = ldexp(1.0, p);
+    o.meta[1] = sc;
+    o.meta[2] = rs * (1.0 + 8.0 * DBL_EPSILON) + DBL_MIN;
+  }
+}
+void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_gk_setup<<<nops, 128, 0, s>>>(ops);
+  g_bd_launches.fetch_add(1);
+}
+
+// Number of eigenvalues of the zero-diagonal tridiagonal matrix (squared off-diagonals b2, order N)
+// below x, from the sign changes of p_i = -x p_{i-1} - b2_{i-1} p_{i-2}, rescaled by exact powers of
+// two (no division).  A zero p_i counts as a sign change.
+__device__ int gk_count(const double* __restrict__ b2, int N, double x) {
+  auto neg = [](double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); };
+  double p0 = 1.0, p1 = -x;
+  if (p1 == 0.0) p1 = -DBL_MIN;
+  int c = neg(p1);
+  int i = 1;
+  while (i < N) {
+    const int iend = min(N, i + 4);
+    for (; i < iend; ++i) {
+      double p2 = fma(-x, p1, -b2[i - 1] * p0);
+      if ((__double_as_longlong(p2) << 1) == 0) p2 = neg(p1) ? DBL_MIN : -DBL_MIN;
+      c += neg(p2) ^ neg(p1);
+      p0 = p1;
+      p1 = p2;
+    }
+    const int ex = (int)((__double_as_longlong(p1) >> 52) & 0x7ff) - 1023;
+    if (ex > 400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
+    else if (ex < -400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
+  }
+  return c;
+}
+// singular values of the sector >= x (unscaled x)
+__device__ __forceinline__ int gk_ge(const GkOp& o, double x) {
+  if (!(o.meta[0] > 0.0)) return 0;
+  const double xs = x * o.meta[1];
+  if (xs >= o.meta[2]) return 0;
+  return 2 * o.n - gk_count(o.b2, 2 * o.n, xs);
+}
+
+// ----------------------------------------------------------------------------- 3. the cut
+__global__ void __launch_bounds__(1024) k_gk_cut(const GkOp* __restrict__ ops, const int32_t* __restrict__ seg,
+                                                 int chimax, double floor_abs, double* __restrict__ xlo_out) {
+  const int s0 = seg[blockIdx.x], s1 = seg[blockIdx.x + 1];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  __shared__ int tot[32];
+  __shared__ double red[32];
+  __shared__ double ivl[2];
+  double hb = 0.0;
+  for (int q = s0 + tid; q < s1; q += blockDim.x) hb = fmax(hb, ops[q].meta[2] * ops[q].meta[0]);
+  hb = warp_max(hb);
+  if (lane == 0) red[warp] = hb;
+  if (tid < 32) tot[tid] = 0;
+  __syncthreads();
+  double hmax = 0.0;
+  for (int w = 0; w < nwarp; ++w) hmax = fmax(hmax, red[w]);
+  int cnt = 0;
+  for (int q = s0 + tid; q < s1; q += blockDim.x) cnt += gk_ge(ops[q], floor_abs);
+  if (cnt) atomicAdd(&tot[0], cnt);
+  __syncthreads();
+  double xlo = floor_abs;
+  if (tot[0] > chimax && hmax > floor_abs) {
+    // multisection in log2(x): 32 points per round; the interval [lo, hi) keeps total(lo) >= chimax
+    double lo = log2(floor_abs), hi = log2(hmax) + 1.0;
+    for (int round = 0; round < 7; ++round) {
+      __syncthreads();
+      if (tid < 32) tot[tid] = 0;
+      __syncthreads();
+      const double x = exp2(lo + (hi - lo) * (double)(lane + 1) / 33.0);
+      int c = 0;
+      for (int q = s0 + warp; q < s1; q += nwarp) c += gk_ge(ops[q], x);
+      if (c) atomicAdd(&tot[lane], c);
+      __syncthreads();
+      if (tid == 0) {
+        int best = -1;  // the counts fall with x
+        for (int i = 0; i < 32; ++i)
+          if (tot[i] >= chimax) best = i;
+        double nlo = lo, nhi = lo + (hi - lo) * 1.0 / 33.0;
+        if (best >= 0) {
+          nlo = lo + (hi - lo) * (double)(best + 1) / 33.0;
+          nhi = best < 31 ? lo + (hi - lo) * (double)(best + 2) / 33.0 : hi;
+        }
+        ivl[0] = nlo;
+        ivl[1] = nhi;
+      }
+      __syncthreads();
+      lo = ivl[0];
+      hi = ivl[1];
+    }
+    xlo = exp2(lo);
+  }
+  for (int q = s0 + tid; q < s1; q += blockDim.x) *ops[q].kcomp = gk_ge(ops[q], xlo);
+  if (tid == 0) xlo_out[blockIdx.x] = xlo;
+}
+void launch_gk_cut(const GkOp* ops, const int32_t* seg, int nseg, int chimax, double floor_abs, double* xlo,
+                   cudaStream_t s) {
+  if (nseg <= 0) return;
+  k_gk_cut<<<nseg, 1024, 0, s>>>(ops, seg, chimax, floor_abs, xlo);
+  g_bd_launches.fetch_add(1);
+}
+
+// ----------------------------------------------------------------------------- 4. singular values
+// LN lanes per (sector, k): the k-th largest singular value (the eigenvalue of T with exactly
+// 2n - 1 - k smaller ones) for k < kcomp, by multisection on [cut, Gershgorin bound]; S[k] = 0 past
+// kcomp.  S is unscaled and descending.
+constexpr int kGkLanes = 4;
+template <int LN>
+__global__ void k_gk_bisect(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
+                            const int32_t* __restrict__ k_of, int nthreads) {
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt / LN, g = gt % LN;
+  if (t >= nthreads) return;  // whole lane groups leave together (blockDim.x is a multiple of LN)
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << LN) - 1u) << (lane & ~(LN - 1));
+  const GkOp o = ops[op_of[t]];
+  const int k = k_of[t];
+  if (k >= *o.kcomp) {
+    if (g == 0) o.S[k] = 0.0;
+    return;
+  }
+  const int N = 2 * o.n;
+  const int m = N - 1 - k;
+  const double frac = (double)(g + 1) / (double)(LN + 1);
+  double a = *o.xlo * o.meta[1], b = o.meta[2];
+  for (int it = 0; it < 100 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++it) {
+    const double x = fma(b - a, frac, a);
+    const unsigned above = (__ballot_sync(gmask, gk_count(o.b2, N, x) > m) >> (lane & ~(LN - 1))) & ((1u << LN) - 1u);
+    const int first = above ? __ffs(above) - 1 : LN;
+    const double xb = __shfl_sync(gmask, x, first < LN ? first : LN - 1, LN);
+    const double xa = __shfl_sync(gmask, x, first > 0 ? first - 1 : 0, LN);
+    if (first < LN) b = xb;
+    if (first > 0) a = xa;
+  }
+  if (g == 0) o.S[k] = 0.5 * (a + b) * o.meta[0];
+}
+void launch_gk_bisect(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, int nthreads, cudaStream_t s) {
+  if (nthreads <= 0) return;
+  const int64_t lanes = (int64_t)kGkLanes * nthreads;
+  k_gk_bisect<kGkLanes><<<(unsigned)((lanes + 127) / 128), 128, 0, s>>>(ops, op_of, k_of, nthreads);
+  g_bd_launches.fetch_add(1);
+}
+
+// ----------------------------------------------------------------------------- 5. eigenvectors of T
+// One thread per kept singular value: three inverse iterations with one pivoted LU of T - sigma I from
+// a deterministic pseudo-random start.  Values that bisection cannot tell apart (within
+// kGkClusterGap * ||T|| of their predecessor) are handled in groups of at most kGkGroup: the group's
+// first thread computes its members one after another, each orthogonalised against the group's
+// earlier ones (modified Gram-Schmidt).  The vectors are re-orthonormalised afterwards (CholeskyQR of
+// the singular-vector matrices).
+constexpr double kGkClusterGap = 16.0 * DBL_EPSILON;
+constexpr int kGkGroup = 32;
+
+__device__ __forceinline__ bool gk_same_cluster(const GkOp& o, int j) {
+  return j > 0 && (o.S[j - 1] - o.S[j]) * o.meta[1] <= kGkClusterGap * o.meta[2];
+}
+
+__device__ void gk_invit_one(const GkOp& o, int k, int k_first, double* x, double* base) {
+  const int N = 2 * o.n;
+  double *u0 = base, *u1 = base + N, *u2 = base + 2 * N, *mul = base + 3 * N;
+  unsigned char* piv = (unsigned char*)(base + 4 * N);
+  for (int i = 0; i < N; ++i) x[i] = hash_unit(k, i);
+  tri_shift_factor(nullptr, o.b, N, o.S[k] * o.meta[1], o.meta[2], u0, u1, u2, mul, piv);
+  for (int it = 0; it < 3; ++it) {
+    tri_shift_solve(N, x, u0, u1, u2, mul, piv);
+    for (int j = k - 1; j >= k_first; --j) {
+      const double* y = o.Z + (int64_t)j * o.ldz;
+      double dot = 0.0;
+      for (int i = 0; i < N; ++i) dot = fma(y[i], x[i], dot);
+      for (int i = 0; i < N; ++i) x[i] = fma(-dot, y[i], x[i]);
+    }
+    double amax = 0.0;
+    for (int i = 0; i < N; ++i) amax = fmax(amax, fabs(x[i]));
+    const double inv = amax > 0.0 ? 1.0 / amax : 0.0;
+    for (int i = 0; i < N; ++i) x[i] *= inv;
+  }
+  double nrm = 0.0;
+  for (int i = 0; i < N; ++i) nrm = fma(x[i], x[i], nrm);
+  const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
+  for (int i = 0; i < N; ++i) x[i] *= inv;
+}
+
+// threads list (op, k) for k < kept(op); kept counts come from the host (kcnt per op)
+__global__ void k_gk_invit(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
+                           const int32_t* __restrict__ k_of, const int32_t* __restrict__ kept, int nthreads,
+                           double* scratch, const int64_t* __restrict__ scratch_off) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nthreads) return;
+  const int op = op_of[t];
+  const GkOp o = ops[op];
+  const int k = k_of[t], kk = kept[op];
+  int c0 = k;
+  while (gk_same_cluster(o, c0)) --c0;
+  if ((k - c0) % kGkGroup != 0) return;  // computed by the first thread of its group
+  double* base = scratch + scratch_off[t];
+  for (int mm = k; mm < kk && mm < k + kGkGroup && (mm == k || gk_same_cluster(o, mm)); ++mm)
+    gk_invit_one(o, mm, k, o.Z + (int64_t)mm * o.ldz, base);
+}
+void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept,
+                          int nthreads, double* scratch, const int64_t* scratch_off, cudaStream_t s) {
+  if (nthreads <= 0) return;
+  k_gk_invit<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, kept, nthreads, scratch, scratch_off);
+  g_bd_launches.fetch_add(1);
+}
+
+// ----------------------------------------------------------------------------- 6. (v, u) halves
+// One warp per kept vector: x = (v0, u0, v1, u1, ...) -> V(:, k) = v / |v|, U(:, k) = (u / |u|; 0).
+__global__ void __launch_bounds__(256) k_gk_vectors(const GkVecOp* __restrict__ ops, int nops) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= nops) return;
+  const GkVecOp o = ops[w];
+  const double* x = o.Z + (int64_t)o.k * o.ldz;
+  double sv = 0.0, su = 0.0;
+  for (int i = lane; i < o.n; i += 32) {
+    sv = fma(x[2 * i], x[2 * i], sv);
+    su = fma(x[2 * i + 1], x[2 * i + 1], su);
+  }
+  sv = warp_sum(sv);
+  su = warp_sum(su);
+  const double iv = sv > 0.0 ? 1.0 / sqrt(sv) : 0.0, iu = su > 0.0 ? 1.0 / sqrt(su) : 0.0;
+  double* V = o.V + (int64_t)o.k * o.ldv;
+  double* U = o.U + (int64_t)o.k * o.ldu;
+  for (int i = lane; i < o.n; i += 32) V[i] = x[2 * i] * iv;
+  for (int i = lane; i < o.m; i += 32) U[i] = i < o.n ? x[2 * i + 1] * iu : 0.0;
+}
+void launch_gk_vectors(const GkVecOp* ops, int nops, cudaStream_t s) {
+  if (nops <= 0) return;
+  k_gk_vectors<<<(nops + 7) / 8, 256, 0, s>>>(ops, nops);
+  g_bd_launches.fetch_add(1);
+}
+
+// ----------------------------------------------------------------------------- 7. back-transformation
+// X <- H_0 H_1 ... H_{nref-1} X for columns [c0, c1): the reflectors applied last to first, one warp
+// per column of X held in shared memory (8 columns per CTA).
+__global__ void __launch_bounds__(256) k_apply_refl(const ReflOp* __restrict__ ops) {
+  const ReflOp o = ops[blockIdx.x];
+  const int len = o.len;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  extern __shared__ double xs[];  // 8 columns x len
+  const int c = o.c0 + warp;
+  if (c >= o.c1) return;  // no block-wide synchronisation below: each warp owns its column
+  double* x = xs + (size_t)warp * len;
+  double* X = o.X + (int64_t)c * o.ldx;
+  for (int i = lane; i < len; i += 32) x[i] = X[i];
+  __syncwarp();
+  for (int j = o.nref - 1; j >= 0; --j) {
+    const double tau = o.tau[j];
+    if (tau == 0.0) continue;
+    const int r0 = j + o.off;
+    const double* rj = o.R + (int64_t)j * o.ldr;
+    double s = lane == 0 ? x[r0] : 0.0;
+    for (int i = r0 + 1 + lane; i < len; i += 32) s = fma(rj[i], x[i], s);
+    s = warp_sum(s) * tau;
+    if (lane == 0) x[r0] -= s;
+    for (int i = r0 + 1 + lane; i < len; i += 32) x[i] = fma(-s, rj[i], x[i]);
+    __syncwarp();
+  }
+  for (int i = lane; i < len; i += 32) X[i] = x[i];
+}
+void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s) {
+  if (nops <= 0) return;
+  const size_t smem = sizeof(double) * 8 * (size_t)std::max(lenmax, 1);
+  MPSG_CUDA(cudaFuncSetAttribute(k_apply_refl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_apply_refl<<<nops, 256, smem, s>>>(ops);
+  g_bd_launches.fetch_add(1);
+}
+
+}  // namespace mpsg

@@ -516,7 +516,7 @@ struct TebdEngine {
         ctx->dfree(d);
       }
     }
-    if (ctx->svd_method != 0) {
+    if (ctx->svd_method != 0 && ctx->svd_method != 4) {  // 4 (real bidiagonal route): exact gesvdj here
       density_svd(secs, dM, dU, dV, dS);
     } else {
       cusolverDnHandle_t h = ctx->svd_handle();

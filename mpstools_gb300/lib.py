@@ -58,6 +58,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_lanczos2.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, f64, i32, i32, i32, P(vp), P(f64), P(i32)]
     L.mpsg_dmrg_create.argtypes = [vp, i32, vp, vp, vp, P(vp)]
     L.mpsg_dmrg_set_options.argtypes = [vp, i32, i32, i32]
+    L.mpsg_dmrg_get_options.argtypes = [vp, P(i32), P(i32), P(i32)]
     L.mpsg_dmrg_simulate.argtypes = [vp, u32, f64, u32, i32, f64, f64, i32, P(f64)]
     L.mpsg_dmrg_prepare.argtypes = [vp]
     L.mpsg_dmrg_do_step.argtypes = [vp, i32, i32, u32, i32, f64, f64, i32, P(f64)]
@@ -124,6 +125,10 @@ def ptr(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None and a.size else None
 
 
+# the SVD route a new context starts with (mpsg_ctx_set_svd_method)
+DEFAULT_SVD = "bidiag"
+
+
 class Context:
     """mpsg_ctx: one GPU, one stream, the device memory pool and the solver handles."""
 
@@ -140,9 +145,9 @@ class Context:
         return int(self.L.mpsg_ctx_kernel_launches(self.h))
 
     def set_svd_method(self, method):
-        """'jacobi' (0, default), 'density' (1), 'density_mt' (2), 'density_eig' (3): see
+        """'bidiag' (4, default), 'jacobi' (0), 'density' (1), 'density_mt' (2), 'density_eig' (3): see
         mpsg_ctx_set_svd_method."""
-        m = {"jacobi": 0, "density": 1, "density_mt": 2, "density_eig": 3}.get(method, method)
+        m = {"jacobi": 0, "density": 1, "density_mt": 2, "density_eig": 3, "bidiag": 4}.get(method, method)
         check(self.L.mpsg_ctx_set_svd_method(self.h, int(m)))
 
     def set_stream(self, stream_ptr: int | None):

@@ -23,7 +23,8 @@ def test_roundtrip_of_an_oracle_state(tmp_path):
     p = str(tmp_path / "state.mpsg")
     checkpoint.save(p, sites, W, ik, lam)
     s2, W2, ik2, lam2 = checkpoint.load(p)
-    assert checkpoint.read_header(p) == {"version": 1, "N": len(sites)}
+    assert checkpoint.read_header(p) == {"version": 2, "N": len(sites)}
+    assert checkpoint.read_settings(p) == checkpoint.DEFAULT_SETTINGS
     assert ik2 == [list(map(int, k)) for k in ik]
     for a, b in zip(sites, s2):
         assert set(a) == set(b)
@@ -48,3 +49,20 @@ def test_truncated_file_is_rejected(tmp_path):
     (tmp_path / "cut.mpsg").write_bytes(data[: len(data) // 2])
     with pytest.raises(ValueError):
         checkpoint.load(str(tmp_path / "cut.mpsg"))
+
+
+def test_settings_record_and_version_1_files(tmp_path):
+    g, sites, W, ik, lam = _state(N=6, chi=4)
+    p = tmp_path / "state.mpsg"
+    st = {"prec": 6, "reorth": 1, "lanmax": 123, "updates": 77}
+    checkpoint.save(str(p), sites, W, ik, lam, settings=st)
+    assert checkpoint.read_settings(str(p)) == st
+    # the same file as version 1: no settings record, read with the defaults
+    data = p.read_bytes()
+    v1 = data[:8] + (1).to_bytes(4, "little") + data[12:16] + data[36:]
+    (tmp_path / "v1.mpsg").write_bytes(v1)
+    assert checkpoint.read_settings(str(tmp_path / "v1.mpsg")) == checkpoint.DEFAULT_SETTINGS
+    s2, W2, ik2, lam2 = checkpoint.load(str(tmp_path / "v1.mpsg"))
+    for a, b in zip(sites, s2):
+        for k in a:
+            assert np.array_equal(np.asarray(a[k]), b[k])

@@ -49,3 +49,33 @@ def test_engine_checkpoint_roundtrip_and_resume(ctx, tmp_path):
     assert abs(Ea - Eb) <= 1e-12 * abs(Ea)
     a.close()
     b.close()
+
+
+def test_options_are_restored_and_corrupt_files_are_rejected(ctx, tmp_path):
+    import ctypes as C
+    from mpstools_gb300 import lib
+    N, chi = 10, 8
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 4), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    a = api.DMRGengine(M.random_u1_mps(N, N // 2, chi, 13), W, ik, prec="mixed", lanmax=321, ctx=ctx)
+    a.simulate(maxsteps=1, EnConv=1e-300, chimax=chi, delta=1e-12)
+    p = tmp_path / "mixed.mpsg"
+    a.save(str(p))
+    assert checkpoint.read_settings(str(p))["prec"] == lib.PREC["mixed"]
+    b = api.DMRGengine.load(str(p), ctx=ctx)
+    assert b.options() == {"prec": lib.PREC["mixed"], "reorth": 0, "lanmax": 321}
+    b.close()
+    a.close()
+    # an MPO term whose wl index exceeds Dl, and a file cut inside the block data: MPSG_ERR_ARG
+    sites, W2, ik2, lam = checkpoint.load(str(p))
+    bad = list(W2)
+    terms, Dl, Dr = bad[3]
+    bad[3] = ([(Dl + 2,) + tuple(terms[0][1:])] + list(terms[1:]), Dl, Dr)
+    checkpoint.save(str(tmp_path / "bad.mpsg"), sites, bad, ik2, lam)
+    h = C.c_void_p()
+    assert ctx.L.mpsg_dmrg_load(ctx.h, str(tmp_path / "bad.mpsg").encode(), C.byref(h)) == 1
+    assert b"out of range" in ctx.L.mpsg_last_error()
+    data = p.read_bytes()
+    (tmp_path / "cut.mpsg").write_bytes(data[: len(data) * 2 // 3])
+    assert ctx.L.mpsg_dmrg_load(ctx.h, str(tmp_path / "cut.mpsg").encode(), C.byref(h)) == 1
+    assert b"truncated" in ctx.L.mpsg_last_error()

@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from mpstools_gb300 import api, models as M
+from mpstools_gb300 import api, lib, models as M
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
@@ -185,7 +185,7 @@ def test_split_density_method_matches_oracle(ctx):
     try:
         U1, V1, l1, tw1, chi1 = api.split(psi, (ik[site], ik[site + 1]), 8, ctx=ctx)
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
     assert chi1 == chi0 and abs(tw1 - tw0) < 1e-10
     assert set(l1) == set(l0)
     for q in l0:
@@ -208,7 +208,7 @@ def test_dmrg_heisenberg_L32_chi64_density_svd(ctx):
         Eg = gg.simulate(maxsteps=6, EnConv=1e-300, chimax=64, delta=1e-12)
         Em = gg.measure_energy()
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
     print(f"density svd: E {Eg:.15f} measured {Em:.15f} oracle {Eo:.15f}")
     assert abs(Eg - Eo) <= 1e-10 * abs(Eo)
     assert abs(Em - go.measure()) <= 1e-10 * abs(Eo)

@@ -1,11 +1,13 @@
-"""GPU tests of the three SVD routes of split / canonicalisation against the oracle.
+"""GPU tests of the SVD routes of split / canonicalisation against the oracle.
 
+method 4: the library's own bidiagonal SVD (default), exact;
 method 0: one-sided Jacobi SVD (cuSOLVER gesvdj), exact;
 method 1: density matrix (FP64 Gram + batched eigensolver per size class);
 method 2: density matrix (FP64 Gram + concurrent per-sector eigensolvers);
 method 3: density matrix (FP64 Gram + the library's own batched eigensolver).
 Checks: singular values, orthonormality of the kept left / right vectors and right-canonical form
-after orthonormalize("rl").  The Jacobi route is exact (1e-10 everywhere).  The density routes square
+after orthonormalize("rl").  The exact routes (bidiagonal, Jacobi) keep the oracle's block structure
+(the same chi, the same sectors with the same kept counts) and every kept value to 1e-10.  The density routes square
 the condition number: eigenvalues of M^T M below 32 n eps lambda_max are dropped (fewer kept values
 than the oracle at most), a kept singular value s agrees with the oracle to 1e-10 + 64 n eps s_max^2 / s
 (the Gram matrix's resolution), and both U and V are orthonormal to 1e-10 (CholeskyQR2 on U).
@@ -13,7 +15,7 @@ than the oracle at most), a kept singular value s agrees with the oracle to 1e-1
 import numpy as np
 import pytest
 
-from mpstools_gb300 import api, models as M
+from mpstools_gb300 import api, lib, models as M
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
@@ -50,7 +52,10 @@ def _right_ortho_err(V):
     return max(np.abs(np.hstack(g) @ np.hstack(g).T - np.eye(g[0].shape[0])).max() for g in groups.values())
 
 
-@pytest.mark.parametrize("method", ["jacobi", "density", "density_mt", "density_eig"])
+EXACT = ("bidiag", "jacobi")
+
+
+@pytest.mark.parametrize("method", ["bidiag", "jacobi", "density", "density_mt", "density_eig"])
 @pytest.mark.parametrize("chimax,N,chi,site", [(10, 12, 16, 4), (200, 12, 16, 4), (100, 14, 128, 6), (1000, 14, 128, 6)])
 def test_split_methods(ctx, method, chimax, N, chi, site):
     """Sector widths up to 16 (one eigensolver size class) and up to 70 (classes 32, 64, 128)."""
@@ -63,12 +68,16 @@ def test_split_methods(ctx, method, chimax, N, chi, site):
     try:
         U1, V1, l1, tw1, chi1 = api.split(psi, (ik[site], ik[site + 1]), chimax, ctx=ctx)
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
     eu, ev = _left_ortho_err(U1), _right_ortho_err(V1)
     nmax = max(np.vstack(g).shape[0] for g in _by_centre(U1).values())
     smax = max(v.max() for v in l0.values() if len(v))
-    tol = 1e-10 if method == "jacobi" else None
+    tol = 1e-10 if method in EXACT else None
     ratio = 0.0
+    if method in EXACT:  # the reference's block structure: same sectors, same kept count in each
+        assert set(l1) == set(l0)
+        assert {q: len(v) for q, v in l1.items()} == {q: len(v) for q, v in l0.items()}
+        assert set(U1) == set(U0) and set(V1) == set(V0)
     for q in l1:
         if q not in l0:
             continue
@@ -80,13 +89,14 @@ def test_split_methods(ctx, method, chimax, N, chi, site):
           f"U ortho {eu:.2e} V ortho {ev:.2e}")
     assert eu < 1e-10 and ev < 1e-10
     assert ratio <= 1.0
-    if method == "jacobi":
+    if method in EXACT:
         assert chi1 == chi0
+        assert abs(tw1 - tw0) <= 1e-12
     else:
         assert chi1 <= chi0
 
 
-@pytest.mark.parametrize("method", ["jacobi", "density", "density_mt", "density_eig"])
+@pytest.mark.parametrize("method", ["bidiag", "jacobi", "density", "density_mt", "density_eig"])
 def test_orthonormalize_methods(ctx, method):
     """orthonormalize("rl") of a random MPS: every site right-canonical."""
     N = 10
@@ -99,7 +109,7 @@ def test_orthonormalize_methods(ctx, method):
         e.prepare()
         errs = [_right_ortho_err(e.site(s)) for s in range(1, N)]
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
     print(f"{method}: max right-canonical error {max(errs):.2e}")
     assert max(errs) < 1e-10
 
@@ -116,16 +126,18 @@ def test_density_eig_badly_scaled_sectors(ctx, log2_scale):
     ik = [0, 0]
     out = {}
     L = ctx.L
-    for method in ("jacobi", "density_eig"):
+    for method in ("jacobi", "density_eig", "bidiag"):
         ctx.set_svd_method(method)
         f0 = L.mpsg_split_fallbacks()
         U, Vt, lam, tw, chi = api.split(th, (ik, ik), 1000, doTrunc=False, normalize=False, ctx=ctx)
         out[method] = (lam, L.mpsg_split_fallbacks() - f0)
-    ctx.set_svd_method("jacobi")
-    assert out["density_eig"][1] == 0
-    lj, ld = out["jacobi"][0], out["density_eig"][0]
-    assert set(lj) == set(ld)
-    for q in lj:
-        a, b = np.sort(np.asarray(lj[q]))[::-1], np.sort(np.asarray(ld[q]))[::-1]
-        assert len(a) == len(b)
-        assert np.abs(a - b).max() <= 1e-10 * a[0], (q, np.abs(a - b).max() / a[0])
+    ctx.set_svd_method(lib.DEFAULT_SVD)
+    assert out["density_eig"][1] == 0 and out["bidiag"][1] == 0
+    lj = out["jacobi"][0]
+    for other in ("density_eig", "bidiag"):
+        ld = out[other][0]
+        assert set(lj) == set(ld)
+        for q in lj:
+            a, b = np.sort(np.asarray(lj[q]))[::-1], np.sort(np.asarray(ld[q]))[::-1]
+            assert len(a) == len(b)
+            assert np.abs(a - b).max() <= 1e-10 * a[0], (other, q, np.abs(a - b).max() / a[0])

@@ -9,7 +9,7 @@ the GPU), and Gamma = U / lambda then amplifies that noise; that setting is not 
 import numpy as np
 import pytest
 
-from mpstools_gb300 import api, models as M
+from mpstools_gb300 import api, lib, models as M
 from oracle import pyoracle as O
 
 pytestmark = pytest.mark.gpu
@@ -82,7 +82,7 @@ def test_tebd_density_split_matches_oracle(ctx, N, steps, chimax):
         assert err_sz < 1e-8 and err_lam < 1e-8
         got.close()
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
 
 
 @pytest.mark.parametrize("svd", ["jacobi", "density"])
@@ -109,4 +109,4 @@ def test_tebd_layer_batching_matches_bond_by_bond(ctx, svd):
                 assert len(a[q]) == len(b[q])
                 assert np.abs(np.sort(a[q]) - np.sort(b[q])).max() < 1e-12
     finally:
-        ctx.set_svd_method("jacobi")
+        ctx.set_svd_method(lib.DEFAULT_SVD)
