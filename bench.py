@@ -15,7 +15,7 @@ value   = algorithmic FLOPs of the Lanczos matvecs executed inside the timed ste
 e2e     = the same metric through the C ABI with host buffers: per step the environments and the
           two site tensors are uploaded (mpsg_tensor_create), the update runs through
           mpsg_lanczos2 + mpsg_split2 + mpsg_add_contraction_layer and the results are
-          downloaded (mpsg_tensor_export).
+          downloaded (mpsg_tensor_export); the host buffers are pinned.
 roofline: the grouped matvec GEMM timed alone with CUDA events, L2 flushed before each launch.
 --impl reference: the CPU oracle (restatement of the reference's C++/BLAS path) on the same
           workload, one two-site update per step, all host threads.
@@ -468,10 +468,25 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
     """Two-site update through the reference-facing C ABI from host buffers."""
     import ctypes as C
     from mpstools_gb300 import lib
-    Lh = eng.env_tensor("L", center - 1).export_flat()
-    Rh = eng.env_tensor("R", center + 2).export_flat()
-    A1h = eng.site_tensor(center).export_flat()
-    A2h = eng.site_tensor(center + 1).export_flat()
+    # host buffers of the inputs and results are pinned (page-locked), as an integration that streams
+    # tensors through the library would allocate them
+    pool = {}
+
+    def pinned(n, tag):
+        key = (tag, n)
+        if key not in pool:
+            pool[key] = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        return pool[key]
+
+    def pin_flat(flat, tag):
+        buf = pinned(flat[5].size, tag)
+        buf[:] = flat[5]
+        return flat[:5] + (buf,)
+
+    Lh = pin_flat(eng.env_tensor("L", center - 1).export_flat(), "L")
+    Rh = pin_flat(eng.env_tensor("R", center + 2).export_flat(), "R")
+    A1h = pin_flat(eng.site_tensor(center).export_flat(), "A1")
+    A2h = pin_flat(eng.site_tensor(center + 1).export_flat(), "A2")
     w1, w2 = lib.MPOArg(W[center]), lib.MPOArg(W[center + 1])
     k0, k1 = lib.ItoKeyArg(ik[center]), lib.ItoKeyArg(ik[center + 1])
     h2d = sum(x[5].nbytes + x[1].nbytes + x[2].nbytes + x[3].nbytes * 2 for x in (Lh, Rh, A1h, A2h))
@@ -494,7 +509,8 @@ def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):
         lib.check(ctx.L.mpsg_add_contraction_layer(ctx.h, tL.h, U.h, w1.ref(), k0.ref(), 1, lib.PREC["fp64"],
                                                    C.byref(Lo)))
         Lo = lib.Tensor(ctx, Lo)
-        outs = [U.export_flat(), V.export_flat(), lam.export_flat(), Lo.export_flat()]
+        outs = [t.export_flat(lambda n, tag=tag: pinned(n, tag))
+                for t, tag in ((U, "U"), (V, "V"), (lam, "lam"), (Lo, "Lo"))]
         d2h[0] = sum(o[5].nbytes for o in outs)
         return it.value  # Lanczos matvecs (MIXED's FP64 Rayleigh-quotient matvec is not counted)
 

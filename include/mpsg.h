@@ -362,7 +362,9 @@ typedef struct mpsg_batch_s* mpsg_batch;
 /* chains: engines created with mpsg_dmrg_create on ctx (charges below 2^32, the same i_to_key at the
  * sites that update together); they must outlive the batch and are updated in place. */
 mpsg_status mpsg_batch_create(mpsg_ctx ctx, int32_t nchains, const mpsg_dmrg* chains, mpsg_batch* out);
-/* matvec precision (FP64, a mixed mode or AUTO) and the Lanczos iteration cap of every chain. */
+/* matvec precision (FP64, a mixed mode, AUTO or MIXED: per chain the FP64 Rayleigh quotient of its
+ * TF32X3 ground state, one FP64 matvec of the direct sum for all chains) and the Lanczos iteration
+ * cap of every chain. */
 mpsg_status mpsg_batch_set_options(mpsg_batch b, mpsg_prec prec, int32_t lanmax);
 /* DMRGengine::simulate of every chain with exactly `sweeps` sweeps (orthonormalize("rl"), then the
  * sweeps, then the final doStep(0, -1)); energies[c] = the last step's energy of chain c.  Each

@@ -105,6 +105,40 @@ struct SegLanczos {
   std::vector<int> iters;
 };
 
+// <psi_c|H|psi_c> / <psi_c|psi_c> of every chain c of a direct sum (segments [segoff[c], segoff[c+1])
+// of the block-diagonal problem): one matvec, two segmented dot products.
+std::vector<double> rayleigh_quotient_seg(Ctx* ctx, MatvecPlan& mv, const Tensor& psi,
+                                          const std::vector<int64_t>& segoff, LanczosStats* st) {
+  const int C = (int)segoff.size() - 1;
+  const int64_t n = psi.nelem;
+  cudaStream_t s = ctx->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  double* w = (double*)ctx->dmalloc(sizeof(double) * (std::max<int64_t>(n, 2) + 2 * (size_t)C));
+  double* q = w + std::max<int64_t>(n, 2);
+  double* part = (double*)ctx->dmalloc(sizeof(double) * (size_t)C * seg_chunks());
+  int64_t* dseg = (int64_t*)ctx->dmalloc(sizeof(int64_t) * (C + 1));
+  MPSG_CUDA(cudaMemcpyAsync(dseg, segoff.data(), sizeof(int64_t) * (C + 1), cudaMemcpyHostToDevice, s));
+  MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * std::max<int64_t>(n, 2), s));
+  mv.run(psi.d, w);
+  launch_sdot(psi.d, w, dseg, C, part, q, 1, s);
+  launch_sdot(psi.d, psi.d, dseg, C, part, q + C, 1, s);
+  std::vector<double> h(2 * (size_t)C);
+  MPSG_CUDA(cudaMemcpyAsync(h.data(), q, sizeof(double) * 2 * C, cudaMemcpyDeviceToHost, s));
+  ctx->sync();
+  mv.check_error();
+  ctx->dfree(w);
+  ctx->dfree(part);
+  ctx->dfree(dseg);
+  if (st) {
+    st->matvecs += 1;
+    st->matvec_flops += mv.flops;
+    st->matvec_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  std::vector<double> E(C, 0.0);
+  for (int c = 0; c < C; ++c) E[c] = h[C + c] > 0 ? h[c] / h[C + c] : 0.0;
+  return E;
+}
+
 // TSLanzcosEngine::simulate (src/lanzcos.hpp:165-278) for every chain of a direct sum at once: the
 // same recurrence as the single-chain Lanczos with per-chain scalars, the energy test per chain, and
 // a chain that has stopped riding along (its later vectors are never used).
@@ -313,20 +347,25 @@ struct BatchEngine {
       lr = lanczos_seg(ctx, *mv, *th, *psi, segoff, lanmax, delta, testenergy, 0.0, 5, 0.0, &lst);
       matvec_launches += (lst.matvecs - m0) * mv->launches_per_run();
     } else {
-      const int lo = (prec == MPSG_PREC_AUTO) ? MPSG_PREC_TF32X3 : prec;
-      {
-        auto mv = build_matvec(ctx, *Lt, *Rt, sx, W1t, W2t, ik0, ik1, &sx, lo);
-        const int64_t m0 = lst.matvecs;
-        lr = lanczos_seg(ctx, *mv, *th, *psi, segoff, lanmax, delta, testenergy, prec_tol(lo), 5, prec_stall(lo),
-                         &lst);
+      const bool two_phase = prec == MPSG_PREC_AUTO || prec == MPSG_PREC_MIXED;
+      const int lo = two_phase ? MPSG_PREC_TF32X3 : prec;
+      auto mv = build_matvec(ctx, *Lt, *Rt, sx, W1t, W2t, ik0, ik1, &sx, lo);
+      int64_t m0 = lst.matvecs;
+      lr = lanczos_seg(ctx, *mv, *th, *psi, segoff, lanmax, delta, testenergy, prec_tol(lo), 5, prec_stall(lo), &lst);
+      matvec_launches += (lst.matvecs - m0) * mv->launches_per_run();
+      // the FP64 phase runs on the FP64 stage tables the tensor-core plan carries (no second plan)
+      if (two_phase) mv->use_fp64();
+      if (prec == MPSG_PREC_MIXED) {
+        // per chain, the FP64 Rayleigh quotient of its mixed-precision ground state (one FP64 matvec
+        // of the direct sum serves every chain), as the single-chain MIXED
+        m0 = lst.matvecs;
+        lr.E0 = rayleigh_quotient_seg(ctx, *mv, *psi, segoff, &lst);
         matvec_launches += (lst.matvecs - m0) * mv->launches_per_run();
-      }
-      if (prec == MPSG_PREC_AUTO) {
-        auto mv64 = build_matvec(ctx, *Lt, *Rt, sx, W1t, W2t, ik0, ik1, &sx, MPSG_PREC_FP64);
+      } else if (prec == MPSG_PREC_AUTO) {
         TensorP start = tensor_copy(*psi);
-        const int64_t m0 = lst.matvecs;
-        SegLanczos r2 = lanczos_seg(ctx, *mv64, *start, *psi, segoff, lanmax, delta, testenergy, 0.0, 1, 0.0, &lst);
-        matvec_launches += (lst.matvecs - m0) * mv64->launches_per_run();
+        m0 = lst.matvecs;
+        SegLanczos r2 = lanczos_seg(ctx, *mv, *start, *psi, segoff, lanmax, delta, testenergy, 0.0, 1, 0.0, &lst);
+        matvec_launches += (lst.matvecs - m0) * mv->launches_per_run();
         for (int i = 0; i < n; ++i) r2.iters[i] += lr.iters[i];
         lr = r2;
       }
@@ -538,7 +577,8 @@ mpsg_status mpsg_batch_create(mpsg_ctx ctx, int32_t nchains, const mpsg_dmrg* ch
 mpsg_status mpsg_batch_set_options(mpsg_batch b, mpsg_prec prec, int32_t lanmax) {
   API_BEGIN
   MPSG_CHECK(b && b->b, "null batch");
-  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_AUTO, "batched chains: precision must be FP64, TF32(X3), BF16(X3) or AUTO");
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_MIXED,
+             "batched chains: precision must be FP64, TF32(X3), BF16(X3), AUTO or MIXED");
   MPSG_CHECK(lanmax >= 1 && lanmax <= 1000, "lanmax must be in [1, 1000]");
   b->b->prec = prec;
   b->b->lanmax = lanmax;

@@ -103,11 +103,7 @@ mpsg_status mpsg_tensor_export(mpsg_tensor t, uint64_t* q, uint32_t* p, int32_t*
     if (rows) rows[i] = x.b[i].r;
     if (cols) cols[i] = x.b[i].c;
   }
-  if (host_data) {
-    std::vector<double> h;
-    tensor_to_host(x, h);
-    if (!h.empty()) std::memcpy(host_data, h.data(), sizeof(double) * h.size());
-  }
+  if (host_data) tensor_pack_to_host(x, host_data);
   API_END
 }
 mpsg_status mpsg_tensor_device_view(mpsg_tensor t, double** dptr, int64_t* offsets) {

@@ -169,24 +169,46 @@ TensorP tensor_from_host(Ctx* ctx, int nphys, int n, const uint64_t* q, const ui
   for (int i = 0; i < n; ++i) srcpos[lay.b[i].k] = src_off[i];
   lay.finalize();
   TensorP t = make_tensor(ctx, nphys, lay, true);
-  if (data && n) {
-    std::vector<double> host(std::max<int64_t>(t->nelem, 2), 0.0);
+  if (data && n && so > 0) {
+    // the caller's packed buffer goes up in one copy (DMA straight from it when the caller pinned it)
+    // and a gather kernel places the blocks at their aligned arena offsets
+    double* stage = (double*)ctx->dmalloc(sizeof(double) * (size_t)so);
+    MPSG_CUDA(cudaMemcpyAsync(stage, data, sizeof(double) * (size_t)so, cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<CopyOp> ops;
     for (auto& b : t->b) {
-      const int64_t s = srcpos[b.k];
-      std::memcpy(host.data() + b.off, data + s, sizeof(double) * (size_t)b.r * b.c);
+      if (!b.r || !b.c) continue;
+      ops.push_back(CopyOp{stage + srcpos[b.k], t->d + b.off, nullptr, nullptr, b.r, b.c, b.r, b.r, 0, 1.0});
     }
-    MPSG_CUDA(cudaMemcpyAsync(t->d, host.data(), sizeof(double) * t->nelem, cudaMemcpyHostToDevice, ctx->stream));
+    run_copyops(ctx, ops);
+    ctx->dfree(stage);
     ctx->sync();
   }
   return t;
 }
 
+void tensor_pack_to_host(const Tensor& t, double* dst) {
+  int64_t total = 0;
+  for (auto& b : t.b) total += (int64_t)b.r * b.c;
+  if (total == 0) return;
+  Ctx* ctx = t.ctx;
+  double* stage = (double*)ctx->dmalloc(sizeof(double) * (size_t)total);
+  std::vector<CopyOp> ops;
+  int64_t o = 0;
+  for (auto& b : t.b) {
+    if (b.r && b.c) ops.push_back(CopyOp{t.d + b.off, stage + o, nullptr, nullptr, b.r, b.c, b.r, b.r, 0, 1.0});
+    o += (int64_t)b.r * b.c;
+  }
+  run_copyops(ctx, ops);
+  MPSG_CUDA(cudaMemcpyAsync(dst, stage, sizeof(double) * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream));
+  ctx->dfree(stage);
+  ctx->sync();
+}
+
 void tensor_to_host(const Tensor& t, std::vector<double>& packed) {
-  std::vector<double> arena(std::max<int64_t>(t.nelem, 2));
-  MPSG_CUDA(cudaMemcpyAsync(arena.data(), t.d, sizeof(double) * t.nelem, cudaMemcpyDeviceToHost, t.ctx->stream));
-  t.ctx->sync();
-  packed.clear();
-  for (auto& b : t.b) packed.insert(packed.end(), arena.begin() + b.off, arena.begin() + b.off + (int64_t)b.r * b.c);
+  int64_t total = 0;
+  for (auto& b : t.b) total += (int64_t)b.r * b.c;
+  packed.assign((size_t)total, 0.0);
+  tensor_pack_to_host(t, packed.data());
 }
 
 TensorP tensor_copy(const Tensor& t) {

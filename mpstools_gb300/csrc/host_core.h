@@ -48,6 +48,8 @@ Layout layout_of(const Tensor& t);
 TensorP tensor_from_host(Ctx* ctx, int nphys, int n, const uint64_t* q, const uint32_t* p, const int32_t* rows,
                          const int32_t* cols, const double* data);
 void tensor_to_host(const Tensor& t, std::vector<double>& packed);  // blocks in key order, concatenated
+// the same packed layout written straight into dst (device gather, one device-to-host copy)
+void tensor_pack_to_host(const Tensor& t, double* dst);
 TensorP tensor_copy(const Tensor& t);
 
 // ---------------------------------------------------------------- MPO (MPOMat<1,T>)

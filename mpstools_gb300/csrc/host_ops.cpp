@@ -1125,7 +1125,8 @@ struct SvdBatch {
   // multiplied by R_jj of the first pass (the norm of y_j after removing its components along the
   // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
   // failed (optional): sectors whose Cholesky met a non-positive pivot are appended instead of throwing
-  void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true) {
+  // ub_rows: the left matrix holds U_B (ns rows, zero below): only its first ns rows are processed
+  void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true, bool ub_rows = false) {
     std::vector<int> idx;
     int kmax = 0;
     for (size_t i = 0; i < s.size(); ++i)
@@ -1137,7 +1138,8 @@ struct SvdBatch {
     MPSG_CHECK(kmax <= chol_max_k(), "CholeskyQR: sector wider than the cluster kernel's limit (512)");
     cudaStream_t st = ctx->stream;
     double* X = left ? dU : dV;
-    auto rows = [&](int i) { return left ? s[i].ms : s[i].ns; };
+    auto rows = [&](int i) { return left && !ub_rows ? s[i].ms : s[i].ns; };
+    auto ldx = [&](int i) { return left ? s[i].ms : s[i].ns; };
     auto offX = [&](int i) { return left ? s[i].offU : s[i].offV; };
     std::vector<int64_t> offC(s.size(), 0);
     int64_t oC = 0;
@@ -1152,7 +1154,7 @@ struct SvdBatch {
     GemmPlan g;
     for (int i : idx)
       g.add_problem(2, offC[i], kcols(i), kcols(i), kcols(i), false,
-                    {GSegH{0, 0, offX(i), offX(i), rows(i), rows(i), rows(i), 1, 0, 1.0}});
+                    {GSegH{0, 0, offX(i), offX(i), ldx(i), ldx(i), rows(i), 1, 0, 1.0}});
     g.upload(ctx);
     std::vector<CholOp> zd;
     std::map<int, std::vector<CholQROp>> byCL[2];
@@ -1180,11 +1182,11 @@ struct SvdBatch {
         if (c0 >= kc) continue;
         const int bw = std::min(kTB, kc - c0);
         if (b > 0)
-          upd[b]->add_problem(2, offX(i) + (int64_t)c0 * rows(i), rows(i), rows(i), bw, true,
-                              {GSegH{0, 1, offX(i), offC[i] + (int64_t)c0 * kc, rows(i), kc, c0, 0, 0, -1.0}});
+          upd[b]->add_problem(2, offX(i) + (int64_t)c0 * ldx(i), ldx(i), rows(i), bw, true,
+                              {GSegH{0, 1, offX(i), offC[i] + (int64_t)c0 * kc, ldx(i), kc, c0, 0, 0, -1.0}});
         for (int r0 = 0; r0 < rows(i); r0 += 32)
-          tr[b].push_back(TrsmRowsOp{X + offX(i) + (int64_t)c0 * rows(i), dC + offC[i] + c0 + (int64_t)c0 * kc,
-                                     dR + s[i].offS + c0, bw, rows(i), kc, r0, std::min(r0 + 32, rows(i))});
+          tr[b].push_back(TrsmRowsOp{X + offX(i) + (int64_t)c0 * ldx(i), dC + offC[i] + c0 + (int64_t)c0 * kc,
+                                     dR + s[i].offS + c0, bw, ldx(i), kc, r0, std::min(r0 + 32, rows(i))});
       }
       upd[b]->upload(ctx);
     }
@@ -1272,7 +1274,7 @@ struct SvdBatch {
   struct Bidiag {
     double *d = nullptr, *e = nullptr, *tq = nullptr, *tp = nullptr, *Pr = nullptr, *b = nullptr, *b2 = nullptr,
            *meta = nullptr, *Z = nullptr, *xlo = nullptr, *Mcopy = nullptr;
-    int32_t *kcomp = nullptr, *seg = nullptr, *kept = nullptr;
+    int32_t *kcomp = nullptr, *seg = nullptr, *kept = nullptr, *opseg = nullptr;
     GkOp* ops_d = nullptr;
     std::vector<GkOp> ops;
     std::vector<int> idx;  // sector of each op
@@ -1318,15 +1320,16 @@ struct SvdBatch {
     bd.b2 = alloc(oB);
     bd.meta = alloc(4 * (int64_t)nop);
     const int nseg = (int)seg_first.size() - 1;
-    bd.xlo = alloc(nseg);
+    bd.xlo = (double*)ctx->dmalloc(gk_cut_state_bytes() * std::max(nseg, 1));  // per-segment cut state
     // the sector matrices, kept for sectors whose vectors have to be redone on the Jacobi route (the
     // bidiagonalisation overwrites them with its reflectors)
     const int64_t nM = s.empty() ? 0 : s.back().offM + (int64_t)s.back().ms * s.back().ns;
     bd.Mcopy = alloc(nM);
     if (nM) MPSG_CUDA(cudaMemcpyAsync(bd.Mcopy, dM, sizeof(double) * nM, cudaMemcpyDeviceToDevice, st));
-    bd.kcomp = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (size_t)nop * 2 + sizeof(int32_t) * (nseg + 1));
+    bd.kcomp = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (size_t)nop * 3 + sizeof(int32_t) * (nseg + 1));
     bd.kept = bd.kcomp + nop;
-    bd.seg = bd.kept + nop;
+    bd.opseg = bd.kept + nop;
+    bd.seg = bd.opseg + nop;
     // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first)
     {
       std::map<int, std::vector<GebrdOp>> byCL;
@@ -1365,7 +1368,7 @@ struct SvdBatch {
       }
       segop[nseg] = nop;
     }
-    std::vector<int> seg_of_op(nop, 0);
+    std::vector<int32_t> seg_of_op(nop, 0);
     for (int c = 0; c < nseg; ++c)
       for (int t = segop[c]; t < segop[c + 1]; ++t) seg_of_op[t] = c;
     bd.ops.clear();
@@ -1380,7 +1383,7 @@ struct SvdBatch {
       g.S = dS + x.offS;
       g.Z = nullptr;
       g.meta = bd.meta + 4 * t;
-      g.xlo = bd.xlo + seg_of_op[t];
+      g.xlo = gk_cut_xlo(bd.xlo, seg_of_op[t]);
       g.kcomp = bd.kcomp + t;
       g.n = x.ns;
       g.ldz = 2 * x.ns;
@@ -1395,10 +1398,11 @@ struct SvdBatch {
     int32_t* dmap = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * (size_t)nth);
     MPSG_CUDA(cudaMemcpyAsync(bd.ops_d, bd.ops.data(), sizeof(GkOp) * nop, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(bd.seg, segop.data(), sizeof(int32_t) * (nseg + 1), cudaMemcpyHostToDevice, st));
+    MPSG_CUDA(cudaMemcpyAsync(bd.opseg, seg_of_op.data(), sizeof(int32_t) * nop, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(dmap + nth, k_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
     launch_gk_setup(bd.ops_d, nop, st);
-    launch_gk_cut(bd.ops_d, bd.seg, nseg, chimax, floor_abs, bd.xlo, st);
+    launch_gk_cut(bd.ops_d, bd.seg, bd.opseg, nop, nseg, chimax, floor_abs, bd.xlo, st);
     launch_gk_bisect(bd.ops_d, dmap, dmap + nth, nth, st);
     ctx->dfree(dmap);
   }
@@ -1412,11 +1416,10 @@ struct SvdBatch {
     for (int i : bd.idx) kr[i] = kept[i];
     if (nop == 0) return;
     std::vector<int32_t> kk(nop);
-    int64_t oZ = 0, scr = 0;
+    int64_t oZ = 0;
     std::vector<int64_t> offZ(nop);
     std::vector<int32_t> op_of, k_of;
-    std::vector<int64_t> soff;
-    int lenmax = 0;
+    int lenmax = 0, nmax2 = 2;
     for (int t = 0; t < nop; ++t) {
       const Sec& x = s[bd.idx[t]];
       kk[t] = kept[bd.idx[t]];
@@ -1425,25 +1428,22 @@ struct SvdBatch {
       for (int k = 0; k < kk[t]; ++k) {
         op_of.push_back(t);
         k_of.push_back(k);
-        soff.push_back(scr);
-        scr += 5 * 2 * (int64_t)x.ns;
       }
       lenmax = std::max(lenmax, x.ms);
+      if (kk[t] > 0) nmax2 = std::max(nmax2, 2 * x.ns);
     }
     const int nth = (int)op_of.size();
     if (nth == 0) return;
     bd.Z = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oZ, 2));
     for (int t = 0; t < nop; ++t) bd.ops[t].Z = bd.Z + offZ[t];
-    double* dscr = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(scr, 2));
+    double* dscr = (double*)ctx->dmalloc(sizeof(double) * 6 * (size_t)nmax2 * nth);
     int32_t* dmap = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * (size_t)nth);
-    int64_t* dsoff = (int64_t*)ctx->dmalloc(sizeof(int64_t) * (size_t)nth);
     MPSG_CUDA(cudaMemcpyAsync(bd.ops_d, bd.ops.data(), sizeof(GkOp) * nop, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(bd.kept, kk.data(), sizeof(int32_t) * nop, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(dmap + nth, k_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
-    MPSG_CUDA(cudaMemcpyAsync(dsoff, soff.data(), sizeof(int64_t) * nth, cudaMemcpyHostToDevice, st));
     // 5./6. eigenvectors of T for the kept values, split into U_B (first ns rows of U) and V_B
-    launch_gk_invit(bd.ops_d, dmap, dmap + nth, bd.kept, nth, dscr, dsoff, st);
+    launch_gk_invit(bd.ops_d, dmap, dmap + nth, bd.kept, nth, nmax2, dscr, st);
     {
       std::vector<GkVecOp> vo;
       for (int t = 0; t < nop; ++t) {
@@ -1457,12 +1457,13 @@ struct SvdBatch {
       ctx->dfree(dv);
     }
     ctx->dfree(dscr);
-    ctx->dfree(dsoff);
     ctx->dfree(dmap);
-    // orthonormal to rounding: inverse iteration leaves ~eps ||T|| / gap between close values
+    // orthonormal to rounding: inverse iteration leaves ~eps ||T|| / gap between close values (far
+    // below one for values bisection tells apart, which the groups above cover), so one CholeskyQR pass
+    // (error ~eps cond^2) suffices; U_B's rows past ns are zero and are left out
     std::vector<int> failed;
-    cholqr(true, 2, &failed, false);
-    cholqr(false, 2, &failed, false);
+    cholqr(true, 1, &failed, false, true);
+    cholqr(false, 1, &failed, false);
     // 7. U = Q [U_B; 0], V = P V_B
     {
       std::vector<ReflOp> ro;

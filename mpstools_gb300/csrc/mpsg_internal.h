@@ -338,15 +338,20 @@ void launch_scombine(double* y, const double* const* V, const int* nv_of, const 
 int gebrd_cluster_size(int m, int n);  // 0: the sector does not fit the cluster kernel
 void launch_gebrd(const GebrdOp* ops, int nops, int CL, int mmax, int nmax, cudaStream_t s);
 void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s);
-// one CTA per segment [seg[c], seg[c + 1]) of ops: xlo[c] = cut such that at least chimax values of the
-// segment are >= it (or floor_abs when fewer than chimax exceed floor_abs); kcomp per op
-void launch_gk_cut(const GkOp* ops, const int32_t* seg, int nseg, int chimax, double floor_abs, double* xlo,
-                   cudaStream_t s);
+// per segment [seg[c], seg[c + 1]) of ops (op_seg: segment of each op): the cut x of the segment such
+// that at least chimax of its values are >= x (or floor_abs when fewer than chimax exceed it), kept in
+// the segment's state (gk_cut_state_bytes() per segment; the ops' xlo point at gk_cut_xlo(state, c));
+// kcomp per op
+void launch_gk_cut(const GkOp* ops, const int32_t* seg, const int32_t* op_seg, int nops, int nseg, int chimax,
+                   double floor_abs, void* state, cudaStream_t s);
+size_t gk_cut_state_bytes();
+double* gk_cut_xlo(void* state, int c);
 // S[k] of every (op_of[t], k_of[t]) with k < kcomp; 0 past kcomp
 void launch_gk_bisect(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, int nthreads, cudaStream_t s);
-// Z column k for every listed (op, k), k < kept[op]; scratch: 5 * 2n doubles per listed thread
+// Z column k for every listed (op, k), k < kept[op]; nmax2 = the largest 2n; scratch: 6 * nmax2 doubles
+// per listed thread
 void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept, int nthreads,
-                     double* scratch, const int64_t* scratch_off, cudaStream_t s);
+                     int nmax2, double* scratch, cudaStream_t s);
 void launch_gk_vectors(const GkVecOp* ops, int nops, cudaStream_t s);
 void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s);
 int64_t bidiag_launch_count();

@@ -9,9 +9,9 @@
 //                    distributed shared memory.
 //   2. k_gk_setup    the Golub-Kahan tridiagonal T = [[0, B], [B^T, 0]] (rows interleaved, zero
 //                    diagonal; eigenvalues +-sigma), scaled by a power of two.
-//   3. k_gk_cut      one CTA per truncation segment: Sturm counts of all sectors at 32 points per
-//                    round (log scale) locate a cut x with at least chimax singular values >= x; only
-//                    the values above the cut can be kept, and only they are computed.
+//   3. k_gk_cut_*    per truncation segment: Sturm counts of all sectors at 32 points per round
+//                    (log scale, one warp per sector) locate a cut x with at least chimax singular
+//                    values >= x; only the values above the cut can be kept, and only they are computed.
 //   4. k_gk_bisect   those singular values by multisection on Sturm counts of T.
 //   5. k_gk_invit    eigenvectors of T for the values the truncation keeps (inverse iteration).
 //   6. k_gk_vectors  (v, u) halves of each eigenvector: right and left singular vectors of B.
@@ -164,9 +164,12 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
       // z_i = taup (A(i, j+1) + sum_{c >= j+2} A(i, c) u_c), u_c = A(j, c) sc
       const double* rcb = cluster.map_shared_rank(cb, on);
       for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+        double part[CL];  // all CL remote loads in flight before the (fixed-order) sum
+#pragma unroll
+        for (int q = 0; q < CL; ++q) part[q] = cluster.map_shared_rank(zp, q)[i];
         double zs = 0.0;
-#pragma unroll 4
-        for (int q = 0; q < CL; ++q) zs += cluster.map_shared_rank(zp, q)[i];
+#pragma unroll
+        for (int q = 0; q < CL; ++q) zs += part[q];
         z[i] = taup * fma(sc, zs, rcb[i]);
       }
       for (int lc = lc2 + tid; lc < ncol; lc += blockDim.x) {
@@ -303,25 +306,34 @@ void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s) {
 // Number of eigenvalues of the zero-diagonal tridiagonal matrix (squared off-diagonals b2, order N)
 // below x, from the sign changes of p_i = -x p_{i-1} - b2_{i-1} p_{i-2}, rescaled by exact powers of
 // two (no division).  A zero p_i counts as a sign change.
-__device__ int gk_count(const double* __restrict__ b2, int N, double x) {
+// The off-diagonals are loaded kGkBlk steps ahead of the dependent chain (one load latency per block
+// instead of per step); with |b| < 2 and x <= 4 a block of 8 steps grows |p| by at most 2^24, so the
+// magnitude check once per block keeps p inside [2^-1000, 2^1000].
+constexpr int kGkBlk = 8;
+__device__ __forceinline__ void gk_step(double x, double b2, double& p0, double& p1, int& c) {
   auto neg = [](double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); };
+  double p2 = fma(-x, p1, -b2 * p0);
+  if ((__double_as_longlong(p2) << 1) == 0) p2 = neg(p1) ? DBL_MIN : -DBL_MIN;  // zero: a sign change
+  c += neg(p2) ^ neg(p1);
+  p0 = p1;
+  p1 = p2;
+}
+__device__ int gk_count(const double* __restrict__ b2, int N, double x) {
   double p0 = 1.0, p1 = -x;
   if (p1 == 0.0) p1 = -DBL_MIN;
-  int c = neg(p1);
+  int c = (int)((unsigned long long)__double_as_longlong(p1) >> 63);
   int i = 1;
-  while (i < N) {
-    const int iend = min(N, i + 4);
-    for (; i < iend; ++i) {
-      double p2 = fma(-x, p1, -b2[i - 1] * p0);
-      if ((__double_as_longlong(p2) << 1) == 0) p2 = neg(p1) ? DBL_MIN : -DBL_MIN;
-      c += neg(p2) ^ neg(p1);
-      p0 = p1;
-      p1 = p2;
-    }
+  for (; i + kGkBlk <= N; i += kGkBlk) {
+    double bb[kGkBlk];
+#pragma unroll
+    for (int u = 0; u < kGkBlk; ++u) bb[u] = __ldg(b2 + i - 1 + u);
+#pragma unroll
+    for (int u = 0; u < kGkBlk; ++u) gk_step(x, bb[u], p0, p1, c);
     const int ex = (int)((__double_as_longlong(p1) >> 52) & 0x7ff) - 1023;
     if (ex > 400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
     else if (ex < -400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
   }
+  for (; i < N; ++i) gk_step(x, __ldg(b2 + i - 1), p0, p1, c);
   return c;
 }
 // singular values of the sector >= x (unscaled x)
@@ -333,74 +345,116 @@ __device__ __forceinline__ int gk_ge(const GkOp& o, double x) {
 }
 
 // ----------------------------------------------------------------------------- 3. the cut
-__global__ void __launch_bounds__(1024) k_gk_cut(const GkOp* __restrict__ ops, const int32_t* __restrict__ seg,
-                                                 int chimax, double floor_abs, double* __restrict__ xlo_out) {
-  const int s0 = seg[blockIdx.x], s1 = seg[blockIdx.x + 1];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-  __shared__ int tot[32];
-  __shared__ double red[32];
-  __shared__ double ivl[2];
+// Per truncation segment a cut x such that at least chimax of the segment's singular values are >= x
+// (or the floor when fewer than chimax exceed it): multisection on log2(x), 32 points per round; each
+// round counts every sector at the 32 points with one warp per sector over the whole GPU (a Sturm
+// count is a dependent FP64 chain; a single CTA would run all of them through one SM's FP64 pipe),
+// then one thread per segment keeps the part of the interval where the count still reaches chimax.
+// Four rounds narrow log2(x) by 33^4: the values computed beyond the kept chimax are those within a
+// relative 1e-4 or so of the cut.
+struct CutState {
+  double lo, hi, xlo;
+  int32_t tot[32];
+  int32_t floor_tot, done, pad;
+};
+constexpr int kCutRounds = 4;
+
+__global__ void k_gk_cut_init(const GkOp* __restrict__ ops, const int32_t* __restrict__ seg, double floor_abs,
+                              CutState* st) {
+  const int c = blockIdx.x, s0 = seg[c], s1 = seg[c + 1];
   double hb = 0.0;
-  for (int q = s0 + tid; q < s1; q += blockDim.x) hb = fmax(hb, ops[q].meta[2] * ops[q].meta[0]);
+  for (int q = s0 + threadIdx.x; q < s1; q += blockDim.x) hb = fmax(hb, ops[q].meta[2] * ops[q].meta[0]);
   hb = warp_max(hb);
-  if (lane == 0) red[warp] = hb;
-  if (tid < 32) tot[tid] = 0;
+  __shared__ double red[8];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = hb;
   __syncthreads();
-  double hmax = 0.0;
-  for (int w = 0; w < nwarp; ++w) hmax = fmax(hmax, red[w]);
-  int cnt = 0;
-  for (int q = s0 + tid; q < s1; q += blockDim.x) cnt += gk_ge(ops[q], floor_abs);
-  if (cnt) atomicAdd(&tot[0], cnt);
-  __syncthreads();
-  double xlo = floor_abs;
-  if (tot[0] > chimax && hmax > floor_abs) {
-    // multisection in log2(x): 32 points per round; the interval [lo, hi) keeps total(lo) >= chimax
-    double lo = log2(floor_abs), hi = log2(hmax) + 1.0;
-    for (int round = 0; round < 7; ++round) {
-      __syncthreads();
-      if (tid < 32) tot[tid] = 0;
-      __syncthreads();
-      const double x = exp2(lo + (hi - lo) * (double)(lane + 1) / 33.0);
-      int c = 0;
-      for (int q = s0 + warp; q < s1; q += nwarp) c += gk_ge(ops[q], x);
-      if (c) atomicAdd(&tot[lane], c);
-      __syncthreads();
-      if (tid == 0) {
-        int best = -1;  // the counts fall with x
-        for (int i = 0; i < 32; ++i)
-          if (tot[i] >= chimax) best = i;
-        double nlo = lo, nhi = lo + (hi - lo) * 1.0 / 33.0;
-        if (best >= 0) {
-          nlo = lo + (hi - lo) * (double)(best + 1) / 33.0;
-          nhi = best < 31 ? lo + (hi - lo) * (double)(best + 2) / 33.0 : hi;
-        }
-        ivl[0] = nlo;
-        ivl[1] = nhi;
-      }
-      __syncthreads();
-      lo = ivl[0];
-      hi = ivl[1];
-    }
-    xlo = exp2(lo);
+  if (threadIdx.x == 0) {
+    double h = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) h = fmax(h, red[w]);
+    CutState& x = st[c];
+    x.lo = log2(floor_abs);
+    x.hi = h > 0.0 ? log2(h) + 1.0 : x.lo;
+    x.xlo = floor_abs;
+    x.floor_tot = 0;
+    x.done = h > floor_abs ? 0 : 1;
+    for (int i = 0; i < 32; ++i) x.tot[i] = 0;
   }
-  for (int q = s0 + tid; q < s1; q += blockDim.x) *ops[q].kcomp = gk_ge(ops[q], xlo);
-  if (tid == 0) xlo_out[blockIdx.x] = xlo;
 }
-void launch_gk_cut(const GkOp* ops, const int32_t* seg, int nseg, int chimax, double floor_abs, double* xlo,
-                   cudaStream_t s) {
-  if (nseg <= 0) return;
-  k_gk_cut<<<nseg, 1024, 0, s>>>(ops, seg, chimax, floor_abs, xlo);
-  g_bd_launches.fetch_add(1);
+// singular values >= the floor, per segment (one thread per sector)
+__global__ void k_gk_cut_floor(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_seg, int nops,
+                               double floor_abs, CutState* st) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nops) return;
+  const int c = gk_ge(ops[q], floor_abs);
+  if (c) atomicAdd(&st[op_seg[q]].floor_tot, c);
 }
+// one warp per sector: lane i counts at the i-th of 32 interior points of the segment's interval
+__global__ void k_gk_cut_round(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_seg, CutState* st) {
+  const int q = blockIdx.x, lane = threadIdx.x;
+  CutState& x = st[op_seg[q]];
+  if (x.done) return;
+  const double lo = x.lo, hi = x.hi;
+  const int c = gk_ge(ops[q], exp2(lo + (hi - lo) * (double)(lane + 1) / 33.0));
+  if (c) atomicAdd(&x.tot[lane], c);
+}
+// one thread per segment: after the floor count (round < 0) or a multisection round
+__global__ void k_gk_cut_pick(CutState* st, int nseg, int chimax, int round) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nseg) return;
+  CutState& x = st[c];
+  if (x.done) return;
+  if (round < 0) {
+    if (x.floor_tot <= chimax) x.done = 1;  // every value above the floor can be kept
+    return;
+  }
+  int best = -1;  // the counts fall with x
+  for (int i = 0; i < 32; ++i)
+    if (x.tot[i] >= chimax) best = i;
+  const double lo = x.lo, hi = x.hi;
+  double nlo = lo, nhi = lo + (hi - lo) * 1.0 / 33.0;
+  if (best >= 0) {
+    nlo = lo + (hi - lo) * (double)(best + 1) / 33.0;
+    nhi = best < 31 ? lo + (hi - lo) * (double)(best + 2) / 33.0 : hi;
+  }
+  x.lo = nlo;
+  x.hi = nhi;
+  for (int i = 0; i < 32; ++i) x.tot[i] = 0;
+  if (round == kCutRounds - 1) x.xlo = exp2(nlo);  // total(>= 2^nlo) >= chimax by construction
+}
+__global__ void k_gk_cut_final(const GkOp* __restrict__ ops, int nops) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nops) return;
+  *ops[q].kcomp = gk_ge(ops[q], *ops[q].xlo);
+}
+void launch_gk_cut(const GkOp* ops, const int32_t* seg, const int32_t* op_seg, int nops, int nseg, int chimax,
+                   double floor_abs, void* state, cudaStream_t s) {
+  if (nseg <= 0 || nops <= 0) return;
+  CutState* st = (CutState*)state;
+  k_gk_cut_init<<<nseg, 256, 0, s>>>(ops, seg, floor_abs, st);
+  k_gk_cut_floor<<<(nops + 63) / 64, 64, 0, s>>>(ops, op_seg, nops, floor_abs, st);
+  k_gk_cut_pick<<<(nseg + 63) / 64, 64, 0, s>>>(st, nseg, chimax, -1);
+  for (int r = 0; r < kCutRounds; ++r) {
+    k_gk_cut_round<<<nops, 32, 0, s>>>(ops, op_seg, st);
+    k_gk_cut_pick<<<(nseg + 63) / 64, 64, 0, s>>>(st, nseg, chimax, r);
+  }
+  k_gk_cut_final<<<(nops + 63) / 64, 64, 0, s>>>(ops, nops);
+  g_bd_launches.fetch_add(4 + 2 * kCutRounds);
+}
+size_t gk_cut_state_bytes() { return sizeof(CutState); }
+double* gk_cut_xlo(void* state, int c) { return &((CutState*)state)[c].xlo; }
 
 // ----------------------------------------------------------------------------- 4. singular values
 // LN lanes per (sector, k): the k-th largest singular value (the eigenvalue of T with exactly
-// 2n - 1 - k smaller ones) for k < kcomp, by multisection on [cut, Gershgorin bound]; S[k] = 0 past
-// kcomp.  S is unscaled and descending.
-constexpr int kGkLanes = 4;
+// 2n - 1 - k smaller ones) for k < kcomp by multisection on [cut, Gershgorin bound]; S[k] = 0 past
+// kcomp.  The LN interior points of each round are spaced evenly in the bit patterns of the bounds
+// (positive doubles order like their bits): geometric spacing while the interval spans binades,
+// linear within one, so every value needs about the same number of rounds however small it is.
+// One warp per block: the groups spread over all SMs (the counts are dependent FP64 chains).
+// S is unscaled and descending.
+constexpr int kGkLanes = 2;
 template <int LN>
-__global__ void k_gk_bisect(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
-                            const int32_t* __restrict__ k_of, int nthreads) {
+__global__ void __launch_bounds__(32) k_gk_bisect(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
+                                                  const int32_t* __restrict__ k_of, int nthreads) {
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
   const int t = gt / LN, g = gt % LN;
   if (t >= nthreads) return;  // whole lane groups leave together (blockDim.x is a multiple of LN)
@@ -414,69 +468,157 @@ __global__ void k_gk_bisect(const GkOp* __restrict__ ops, const int32_t* __restr
   }
   const int N = 2 * o.n;
   const int m = N - 1 - k;
-  const double frac = (double)(g + 1) / (double)(LN + 1);
-  double a = *o.xlo * o.meta[1], b = o.meta[2];
-  for (int it = 0; it < 100 && b - a > 2.0 * DBL_EPSILON * fmax(fabs(a), fabs(b)) + DBL_MIN; ++it) {
-    const double x = fma(b - a, frac, a);
-    const unsigned above = (__ballot_sync(gmask, gk_count(o.b2, N, x) > m) >> (lane & ~(LN - 1))) & ((1u << LN) - 1u);
+  long long ia = __double_as_longlong(*o.xlo * o.meta[1]), ib = __double_as_longlong(o.meta[2]);
+  for (int it = 0; it < 200 && ib - ia > 2; ++it) {
+    const long long ix = ia + ((ib - ia) / (LN + 1)) * (g + 1);
+    const unsigned above =
+        (__ballot_sync(gmask, gk_count(o.b2, N, __longlong_as_double(ix)) > m) >> (lane & ~(LN - 1))) &
+        ((1u << LN) - 1u);
+    // the counts grow with x: the first point above the eigenvalue bounds it from above, the one
+    // before it from below
     const int first = above ? __ffs(above) - 1 : LN;
-    const double xb = __shfl_sync(gmask, x, first < LN ? first : LN - 1, LN);
-    const double xa = __shfl_sync(gmask, x, first > 0 ? first - 1 : 0, LN);
-    if (first < LN) b = xb;
-    if (first > 0) a = xa;
+    const long long xb = __shfl_sync(gmask, ix, first < LN ? first : LN - 1, LN);
+    const long long xa = __shfl_sync(gmask, ix, first > 0 ? first - 1 : 0, LN);
+    if (first < LN) ib = xb;
+    if (first > 0) ia = xa;
   }
-  if (g == 0) o.S[k] = 0.5 * (a + b) * o.meta[0];
+  if (g == 0) o.S[k] = 0.5 * (__longlong_as_double(ia) + __longlong_as_double(ib)) * o.meta[0];
 }
 void launch_gk_bisect(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, int nthreads, cudaStream_t s) {
   if (nthreads <= 0) return;
   const int64_t lanes = (int64_t)kGkLanes * nthreads;
-  k_gk_bisect<kGkLanes><<<(unsigned)((lanes + 127) / 128), 128, 0, s>>>(ops, op_of, k_of, nthreads);
+  k_gk_bisect<kGkLanes><<<(unsigned)((lanes + 31) / 32), 32, 0, s>>>(ops, op_of, k_of, nthreads);
   g_bd_launches.fetch_add(1);
 }
 
 // ----------------------------------------------------------------------------- 5. eigenvectors of T
-// One thread per kept singular value: three inverse iterations with one pivoted LU of T - sigma I from
-// a deterministic pseudo-random start.  Values that bisection cannot tell apart (within
-// kGkClusterGap * ||T|| of their predecessor) are handled in groups of at most kGkGroup: the group's
-// first thread computes its members one after another, each orthogonalised against the group's
-// earlier ones (modified Gram-Schmidt).  The vectors are re-orthonormalised afterwards (CholeskyQR of
-// the singular-vector matrices).
+// One thread per kept singular value: three inverse iterations with one partially pivoted LU of
+// T - sigma I (zero diagonal) from a deterministic pseudo-random start.  The LU factors and the iterate
+// live in a scratch interleaved across the threads of the launch (element i of thread t at
+// i * stride + t), so that a warp's loads of step i are contiguous; the solves carry their running
+// values in registers.  Values above the noise level (4 N eps ||T||) that bisection cannot tell apart
+// (within kGkClusterGap * ||T|| of their predecessor) are handled in groups of at most kGkGroup: the
+// group's first thread computes its members one after another, each orthogonalised against the
+// group's earlier ones (modified Gram-Schmidt).  Values at the noise level have no well-defined
+// vectors: any orthonormal completion is an exact SVD to rounding, so they are computed independently
+// (each iterate lies in the near-null space of T).  The vectors are re-orthonormalised afterwards
+// (CholeskyQR of the singular-vector matrices).
 constexpr double kGkClusterGap = 16.0 * DBL_EPSILON;
 constexpr int kGkGroup = 32;
 
 __device__ __forceinline__ bool gk_same_cluster(const GkOp& o, int j) {
-  return j > 0 && (o.S[j - 1] - o.S[j]) * o.meta[1] <= kGkClusterGap * o.meta[2];
+  if (j <= 0) return false;
+  const double tn = o.meta[2], noise = 4.0 * (2 * o.n) * DBL_EPSILON * tn;
+  const double a = o.S[j - 1] * o.meta[1], b = o.S[j] * o.meta[1];
+  return b > noise && a - b <= kGkClusterGap * tn;
 }
 
-__device__ void gk_invit_one(const GkOp& o, int k, int k_first, double* x, double* base) {
+// partially pivoted LU of T - lam I (zero diagonal, off-diagonals b) into strided factors: reciprocal
+// pivots u0, superdiagonals u1, u2, multipliers, interchange flags (rows i, i+1 swapped when the
+// subdiagonal entry is larger than the pivot; zero pivots replaced by eps * tnorm)
+__device__ void gk_factor(const double* __restrict__ b, int N, double lam, double tnorm, double* __restrict__ f,
+                          int64_t st) {
+  double *u0 = f, *u1 = f + N * st, *u2 = f + 2 * N * st, *mul = f + 3 * N * st, *piv = f + 4 * N * st;
+  const double tiny = DBL_EPSILON * fmax(tnorm, DBL_MIN);
+  double dd = -lam, du = N > 1 ? b[0] : 0.0;
+  for (int i = 0; i + 1 < N; ++i) {
+    const double sub = b[i];
+    const double dnext = -lam;
+    const double dunext = i + 2 < N ? b[i + 1] : 0.0;
+    const int64_t o = i * st;
+    if (fabs(dd) >= fabs(sub)) {
+      if (dd == 0.0) dd = tiny;
+      const double inv = 1.0 / dd;
+      const double l = sub * inv;
+      u0[o] = inv; u1[o] = du; u2[o] = 0.0; mul[o] = l; piv[o] = 0.0;
+      dd = dnext - l * du;
+      du = dunext;
+    } else {
+      const double l = dd / sub;
+      u0[o] = 1.0 / sub; u1[o] = dnext; u2[o] = dunext; mul[o] = l; piv[o] = 1.0;
+      dd = du - l * dnext;
+      du = -l * dunext;
+    }
+  }
+  if (dd == 0.0) dd = tiny;
+  u0[(N - 1) * st] = 1.0 / dd;
+}
+// x <- c (T - lam I)^-1 x with the factors of gk_factor, c > 0 (the iterate is rescaled by 2^-166
+// whenever an entry passes 2^166; the caller normalises)
+__device__ void gk_solve(int N, double* __restrict__ x, const double* __restrict__ f, int64_t st) {
+  const double *u0 = f, *u1 = f + N * st, *u2 = f + 2 * N * st, *mul = f + 3 * N * st, *piv = f + 4 * N * st;
+  // forward: L^-1 with the interchanges; cur = x_i as updated so far
+  double cur = x[0];
+  for (int i = 0; i + 1 < N; ++i) {
+    const int64_t o = i * st;
+    const double nxt = x[o + st], m = mul[o];
+    double xi, xn;
+    if (piv[o] != 0.0) {
+      xi = nxt;
+      xn = cur - m * nxt;
+    } else {
+      xi = cur;
+      xn = nxt - m * cur;
+    }
+    x[o] = xi;
+    cur = xn;
+    if (fabs(xn) > 0x1p+166) {  // the whole vector
+      for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
+      cur *= 0x1p-166;
+    }
+  }
+  // backward: U^-1, x_{i+1} and x_{i+2} carried in registers
+  double x1 = cur * u0[(N - 1) * st], x2 = 0.0;
+  if (fabs(x1) > 0x1p+166) {
+    for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
+    x1 *= 0x1p-166;
+  }
+  x[(N - 1) * st] = x1;
+  for (int i = N - 2; i >= 0; --i) {
+    const int64_t o = i * st;
+    double xi = (x[o] - u1[o] * x1 - u2[o] * x2) * u0[o];
+    if (fabs(xi) > 0x1p+166) {  // the whole vector, its register copies included
+      for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
+      xi *= 0x1p-166;
+      x1 *= 0x1p-166;
+      x2 *= 0x1p-166;
+    }
+    x[o] = xi;
+    x2 = x1;
+    x1 = xi;
+  }
+}
+
+// member k of a group whose first member is k_first; x: strided iterate; the result goes to Z column k
+__device__ void gk_invit_one(const GkOp& o, int k, int k_first, double* x, double* f, int64_t st) {
   const int N = 2 * o.n;
-  double *u0 = base, *u1 = base + N, *u2 = base + 2 * N, *mul = base + 3 * N;
-  unsigned char* piv = (unsigned char*)(base + 4 * N);
-  for (int i = 0; i < N; ++i) x[i] = hash_unit(k, i);
-  tri_shift_factor(nullptr, o.b, N, o.S[k] * o.meta[1], o.meta[2], u0, u1, u2, mul, piv);
+  for (int i = 0; i < N; ++i) x[i * st] = hash_unit(k, i);
+  gk_factor(o.b, N, o.S[k] * o.meta[1], o.meta[2], f, st);
   for (int it = 0; it < 3; ++it) {
-    tri_shift_solve(N, x, u0, u1, u2, mul, piv);
+    gk_solve(N, x, f, st);
     for (int j = k - 1; j >= k_first; --j) {
       const double* y = o.Z + (int64_t)j * o.ldz;
       double dot = 0.0;
-      for (int i = 0; i < N; ++i) dot = fma(y[i], x[i], dot);
-      for (int i = 0; i < N; ++i) x[i] = fma(-dot, y[i], x[i]);
+      for (int i = 0; i < N; ++i) dot = fma(y[i], x[i * st], dot);
+      for (int i = 0; i < N; ++i) x[i * st] = fma(-dot, y[i], x[i * st]);
     }
     double amax = 0.0;
-    for (int i = 0; i < N; ++i) amax = fmax(amax, fabs(x[i]));
+    for (int i = 0; i < N; ++i) amax = fmax(amax, fabs(x[i * st]));
     const double inv = amax > 0.0 ? 1.0 / amax : 0.0;
-    for (int i = 0; i < N; ++i) x[i] *= inv;
+    for (int i = 0; i < N; ++i) x[i * st] *= inv;
   }
   double nrm = 0.0;
-  for (int i = 0; i < N; ++i) nrm = fma(x[i], x[i], nrm);
+  for (int i = 0; i < N; ++i) nrm = fma(x[i * st], x[i * st], nrm);
   const double inv = nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0;
-  for (int i = 0; i < N; ++i) x[i] *= inv;
+  double* z = o.Z + (int64_t)k * o.ldz;
+  for (int i = 0; i < N; ++i) z[i] = x[i * st] * inv;
 }
 
-// threads list (op, k) for k < kept(op); kept counts come from the host (kcnt per op)
+// threads list (op, k) for k < kept(op), kept counts from the truncation; scratch: 6 * nmax2 doubles
+// per listed thread, interleaved with stride nthreads
 __global__ void k_gk_invit(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
-                           const int32_t* __restrict__ k_of, const int32_t* __restrict__ kept, int nthreads,
-                           double* scratch, const int64_t* __restrict__ scratch_off) {
+                           const int32_t* __restrict__ k_of, const int32_t* __restrict__ kept, int nthreads, int nmax2,
+                           double* scratch) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nthreads) return;
   const int op = op_of[t];
@@ -485,14 +627,16 @@ __global__ void k_gk_invit(const GkOp* __restrict__ ops, const int32_t* __restri
   int c0 = k;
   while (gk_same_cluster(o, c0)) --c0;
   if ((k - c0) % kGkGroup != 0) return;  // computed by the first thread of its group
-  double* base = scratch + scratch_off[t];
+  const int64_t st = nthreads;
+  double* x = scratch + t;
+  double* f = scratch + (int64_t)nmax2 * st + t;
   for (int mm = k; mm < kk && mm < k + kGkGroup && (mm == k || gk_same_cluster(o, mm)); ++mm)
-    gk_invit_one(o, mm, k, o.Z + (int64_t)mm * o.ldz, base);
+    gk_invit_one(o, mm, k, x, f, st);
 }
-void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept,
-                          int nthreads, double* scratch, const int64_t* scratch_off, cudaStream_t s) {
+void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept, int nthreads,
+                     int nmax2, double* scratch, cudaStream_t s) {
   if (nthreads <= 0) return;
-  k_gk_invit<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, kept, nthreads, scratch, scratch_off);
+  k_gk_invit<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, kept, nthreads, nmax2, scratch);
   g_bd_launches.fetch_add(1);
 }
 

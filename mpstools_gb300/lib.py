@@ -215,13 +215,14 @@ class Tensor:
         check(self.ctx.L.mpsg_tensor_device_view(self.h, C.byref(d), ptr(offs)))
         return d.value, offs[:nb]
 
-    def export_flat(self):
+    def export_flat(self, alloc=None):
+        """(nphys, q, p, rows, cols, data); alloc(n) may supply the data buffer (e.g. pinned memory)."""
         nphys, n, ne = self.shape()
         q = np.zeros(2 * max(n, 1), np.uint64)
         p = np.zeros(max(1, nphys) * max(n, 1), np.uint32)
         rows = np.zeros(max(n, 1), np.int32)
         cols = np.zeros(max(n, 1), np.int32)
-        data = np.zeros(max(ne, 1))
+        data = alloc(max(ne, 1)) if alloc else np.zeros(max(ne, 1))
         check(self.ctx.L.mpsg_tensor_export(self.h, ptr(q), ptr(p), ptr(rows), ptr(cols), ptr(data)))
         return (nphys, q, p, rows[:n], cols[:n], data)
 
