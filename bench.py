@@ -583,7 +583,16 @@ def sweep_leg(ctx, prec, W, ik, sites, ramp, torch):
     from mpstools_gb300 import api
     eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
     s0 = eng.stats()
-    recs, t_prep, E = run_sweeps(eng, len(sites), ramp, sync=torch.cuda.synchronize)
+
+    def progress(r):  # one line per sweep on stderr, so that a run cut short still leaves its record
+        st = eng.stats()
+        print(json.dumps({"prec": prec, "sweep": r["sweep"], "chi": r["chi"], "seconds": r["seconds"], "E": r["E"],
+                          "max_chi_kept": r["max_chi_kept"], "lanczos_iterations": r["lanczos_iterations"],
+                          "split_seconds_total": st["split_seconds"] - s0["split_seconds"],
+                          "lanczos_seconds_total": st["lanczos_seconds"] - s0["lanczos_seconds"],
+                          "env_seconds_total": st["env_seconds"] - s0["env_seconds"]}), file=sys.stderr, flush=True)
+
+    recs, t_prep, E = run_sweeps(eng, len(sites), ramp, sync=torch.cuda.synchronize, on_sweep=progress)
     s1 = eng.stats()
     lam_c = eng.lam(len(sites) // 2 - 1)
     vals = np.sort(np.concatenate([np.asarray(v) for v in lam_c.values() if len(v)]))[::-1]

@@ -1280,9 +1280,9 @@ struct SvdBatch {
     std::vector<int> idx;  // sector of each op
     std::vector<int64_t> offPr, offB;
   } bd;
-  bool bidiag_fits() const {  // cluster bidiagonalisation and CholeskyQR widths
+  bool bidiag_fits() const {  // the cluster bidiagonalisation (shared- or global-memory variant)
     for (auto& x : s)
-      if (x.k > 0 && (gebrd_cluster_size(x.ms, x.ns) == 0 || x.ns > chol_max_k())) return false;
+      if (x.k > 0 && gebrd_cluster_size(x.ms, x.ns) == 0) return false;
     return true;
   }
   void bidiag_free() {
@@ -1462,6 +1462,11 @@ struct SvdBatch {
     // below one for values bisection tells apart, which the groups above cover), so one CholeskyQR pass
     // (error ~eps cond^2) suffices; U_B's rows past ns are zero and are left out
     std::vector<int> failed;
+    for (int i : bd.idx)  // more kept vectors than the cluster Cholesky takes: the Jacobi route below
+      if (kr[i] > chol_max_k()) {
+        failed.push_back(i);
+        kr[i] = 0;
+      }
     cholqr(true, 1, &failed, false, true);
     cholqr(false, 1, &failed, false);
     // 7. U = Q [U_B; 0], V = P V_B
@@ -1469,8 +1474,9 @@ struct SvdBatch {
       std::vector<ReflOp> ro;
       for (int i : bd.idx) {
         const Sec& x = s[i];
-        for (int c0 = 0; c0 < kr[i]; c0 += 8) {
-          const int c1 = std::min(c0 + 8, kr[i]);
+        const int cb = apply_refl_cols_per_block(lenmax);
+        for (int c0 = 0; c0 < kr[i]; c0 += cb) {
+          const int c1 = std::min(c0 + cb, kr[i]);
           ro.push_back(ReflOp{dM + x.offM, bd.tq + x.offS, dU + x.offU, x.ms, x.ns, 0, x.ms, x.ms, c0, c1});
           ro.push_back(ReflOp{bd.Pr + bd.offPr[i], bd.tp + x.offS, dV + x.offV, x.ns, x.ns - 1, 1, x.ns, x.ns, c0, c1});
         }

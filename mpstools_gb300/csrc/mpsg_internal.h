@@ -354,6 +354,7 @@ void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of,
                      int nmax2, double* scratch, cudaStream_t s);
 void launch_gk_vectors(const GkVecOp* ops, int nops, cudaStream_t s);
 void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s);
+int apply_refl_cols_per_block(int lenmax);  // columns of X per ReflOp (c1 - c0 at most)
 int64_t bidiag_launch_count();
 // global truncation over concatenated singular values (see kernels.cu)
 void launch_truncate(const double* S, int n, const int32_t* sec_of, int nsec, int chimax, int doTrunc,

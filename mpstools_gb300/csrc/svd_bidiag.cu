@@ -46,15 +46,25 @@ static __host__ __device__ size_t gebrd_smem_doubles(int m, int n, int CL) {
   return (size_t)ncol * m + 4 * (size_t)m + (size_t)ncol + 8;
 }
 static size_t gebrd_smem_bytes(int m, int n, int CL) { return sizeof(double) * gebrd_smem_doubles(m, n, CL); }
+// the global-memory variant keeps only the reduction buffers in shared memory
+static __host__ __device__ size_t gebrd_gm_smem_doubles(int m, int n, int CL) {
+  return 4 * (size_t)m + (size_t)((n + CL - 1) / CL) + 8;
+}
+constexpr int kGebrdGlobal = 100;  // cluster-size code offset of the global-memory variant
 
 // Left reflector of column j (the calling warp's CTA holds it as `col`; rows j..m-1 are current):
 // v (v[j] = 1) into the CTA's v buffer, tau into scal[0]; the reflector's tail into column j of A,
 // tauq[j] and d[j] = beta.
 __device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v, double* scal, int lane) {
   const int m = o.m;
-  double s2 = 0.0;
-  for (int i = j + 1 + lane; i < m; i += 32) s2 = fma(col[i], col[i], s2);
-  s2 = warp_sum(s2);
+  double s2a = 0.0, s2b = 0.0;
+  int i0 = j + 1 + lane;
+  for (; i0 + 32 < m; i0 += 64) {
+    s2a = fma(col[i0], col[i0], s2a);
+    s2b = fma(col[i0 + 32], col[i0 + 32], s2b);
+  }
+  if (i0 < m) s2a = fma(col[i0], col[i0], s2a);
+  const double s2 = warp_sum(s2a + s2b);
   const double alpha = col[j];
   double tau = 0.0, beta = alpha, scale = 0.0;
   if (s2 > 0.0) {
@@ -74,7 +84,10 @@ __device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v
   }
 }
 
-template <int CL>
+// GM = false: the CTA's columns live in shared memory; GM = true (sectors too large for that): they
+// are worked on in place in the sector matrix in global memory (L2-resident), only the reduction
+// buffers stay in shared memory.  The arithmetic is the same.
+template <int CL, bool GM>
 __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) {
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
@@ -84,17 +97,19 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
   extern __shared__ double sm[];
   const int ncol_max = (n + CL - 1) / CL;
   const int ncol = (n - r + CL - 1) / CL;  // own columns: global column r + lc * CL
-  double* cols = sm;
-  double* v = cols + (size_t)ncol_max * m;  // current left reflector
+  const int64_t ldc = GM ? (int64_t)CL * o.lda : m;  // stride between own columns
+  double* cols = GM ? o.A + (int64_t)r * o.lda : sm;
+  double* v = GM ? sm : cols + (size_t)ncol_max * m;  // current left reflector
   double* zp = v + m;                       // this CTA's partial products for the right reflector
   double* cb = zp + m;                      // column j+1 before the right update (its owner)
   double* z = cb + m;                       // right-update coefficients
   double* ub = z + m;                       // right reflector entries of the own columns
   double* scal = ub + ncol_max;             // [0] tau, [1] partial |row|^2, [2] alpha, [3] |row|^2, [4] alpha
-  for (int lc = warp; lc < ncol; lc += nwarp) {
-    const int c = r + lc * CL;
-    for (int i = lane; i < m; i += 32) cols[(size_t)lc * m + i] = o.A[i + (int64_t)c * o.lda];
-  }
+  if (!GM)
+    for (int lc = warp; lc < ncol; lc += nwarp) {
+      const int c = r + lc * CL;
+      for (int i = lane; i < m; i += 32) cols[(size_t)lc * m + i] = o.A[i + (int64_t)c * o.lda];
+    }
   __syncthreads();
   if (r == 0 && warp == 0) gebrd_left(o, cols, 0, v, scal, lane);
   cluster.sync();  // every CTA runs (distributed shared memory is addressable), reflector 0 exists
@@ -112,7 +127,7 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     const int lc2 = (j + 1 + CL - r) / CL;  // first own column with c >= j + 2
     if (tau != 0.0) {
       for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
-        double* a = cols + (size_t)lc * m;
+        double* a = cols + (size_t)lc * ldc;
         double s = 0.0;
         for (int i = j + lane; i < m; i += 32) s = fma(v[i], a[i], s);
         const double w = warp_sum(s) * tau;
@@ -122,15 +137,22 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     __syncthreads();
     // (b) partial products of the right reflector of row j: zp_i = sum over own c >= j+2 of
     //     A(i, c) A(j, c), and the partial |A(j, c >= j+2)|^2; the owner of column j+1 stages it
-    for (int i = j + 1 + tid; i < m; i += blockDim.x) {
-      double acc = 0.0;
-      for (int lc = lc2; lc < ncol; ++lc) acc = fma(cols[(size_t)lc * m + i], cols[(size_t)lc * m + j], acc);
-      zp[i] = acc;
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) {  // four independent partial sums per row
+      double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+      int lc = lc2;
+      for (; lc + 3 < ncol; lc += 4) {
+        acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
+        acc1 = fma(cols[(size_t)(lc + 1) * ldc + i], cols[(size_t)(lc + 1) * ldc + j], acc1);
+        acc2 = fma(cols[(size_t)(lc + 2) * ldc + i], cols[(size_t)(lc + 2) * ldc + j], acc2);
+        acc3 = fma(cols[(size_t)(lc + 3) * ldc + i], cols[(size_t)(lc + 3) * ldc + j], acc3);
+      }
+      for (; lc < ncol; ++lc) acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
+      zp[i] = (acc0 + acc1) + (acc2 + acc3);
     }
     if (warp == 0) {
       double s = 0.0;
       for (int lc = lc2 + lane; lc < ncol; lc += 32) {
-        const double x = cols[(size_t)lc * m + j];
+        const double x = cols[(size_t)lc * ldc + j];
         s = fma(x, x, s);
       }
       s = warp_sum(s);
@@ -138,7 +160,7 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     }
     const int on = (j + 1) % CL, lnext = (j + 1) / CL;
     if (r == on) {
-      const double* a = cols + (size_t)lnext * m;
+      const double* a = cols + (size_t)lnext * ldc;
       for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = a[i];
       if (tid == 0) scal[2] = a[j];
     }
@@ -173,7 +195,7 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
         z[i] = taup * fma(sc, zs, rcb[i]);
       }
       for (int lc = lc2 + tid; lc < ncol; lc += blockDim.x) {
-        const double u = cols[(size_t)lc * m + j] * sc;
+        const double u = cols[(size_t)lc * ldc + j] * sc;
         ub[lc] = u;
         o.Pr[(r + lc * CL) + (int64_t)j * o.n] = u;
       }
@@ -183,7 +205,7 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     //     that column first and computes left reflector j+1 (lookahead) while its other warps go on
     const bool own_next = (r == on);
     if (own_next && warp == 0) {
-      double* a = cols + (size_t)lnext * m;
+      double* a = cols + (size_t)lnext * ldc;
       if (taup != 0.0)
         for (int i = j + 1 + lane; i < m; i += 32) a[i] -= z[i];
       __syncwarp();
@@ -197,18 +219,18 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     if (taup != 0.0 && tid >= p0) {
       for (int i = j + 1 + tid - p0; i < m; i += (int)blockDim.x - p0) {
         const double zi = z[i];
-        for (int lc = lc2; lc < ncol; ++lc) cols[(size_t)lc * m + i] = fma(-zi, ub[lc], cols[(size_t)lc * m + i]);
+        for (int lc = lc2; lc < ncol; ++lc) cols[(size_t)lc * ldc + i] = fma(-zi, ub[lc], cols[(size_t)lc * ldc + i]);
       }
     }
     cluster.sync();  // #2: columns updated, reflector j+1 ready on its owner, partials consumed
   }
 }
 
-template <int CL>
+template <int CL, bool GM>
 static void launch_gebrd_cl(const GebrdOp* ops, int nops, int mmax, int nmax, cudaStream_t s) {
-  const size_t smem = gebrd_smem_bytes(mmax, nmax, CL);
-  MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  const size_t smem = sizeof(double) * (GM ? gebrd_gm_smem_doubles(mmax, nmax, CL) : gebrd_smem_doubles(mmax, nmax, CL));
+  MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nops * CL);
   cfg.blockDim = dim3(256);
@@ -221,7 +243,7 @@ static void launch_gebrd_cl(const GebrdOp* ops, int nops, int mmax, int nmax, cu
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_gebrd<CL>, ops));
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_gebrd<CL, GM>, ops));
   g_bd_launches.fetch_add(1);
 }
 
@@ -234,22 +256,36 @@ static int gebrd_cl_cap() {
   return cap;
 }
 
+// Cluster size of a sector: CL in 1..16 for the shared-memory kernel, kGebrdGlobal + CL for the
+// global-memory one (sectors whose columns do not fit the cluster's shared memory), 0 if neither fits.
 int gebrd_cluster_size(int m, int n) {
   int CL = n <= 48 ? 1 : n <= 96 ? 2 : n <= 192 ? 4 : n <= 320 ? 8 : 16;
   CL = std::min(CL, gebrd_cl_cap());
-  while (CL <= 16 && gebrd_smem_bytes(m, n, CL) > 220 * 1024) CL *= 2;
-  return CL <= 16 ? CL : 0;
+  int c = CL;
+  while (c <= 16 && gebrd_smem_bytes(m, n, c) > 220 * 1024) c *= 2;
+  if (c <= 16) return c;
+  c = std::min(16, gebrd_cl_cap());
+  return sizeof(double) * gebrd_gm_smem_doubles(m, n, c) <= 220 * 1024 ? kGebrdGlobal + c : 0;
 }
 
-void launch_gebrd(const GebrdOp* ops, int nops, int CL, int mmax, int nmax, cudaStream_t s) {
+void launch_gebrd(const GebrdOp* ops, int nops, int code, int mmax, int nmax, cudaStream_t s) {
   if (nops <= 0) return;
-  MPSG_CHECK(gebrd_smem_bytes(mmax, nmax, CL) <= 227 * 1024, "bidiagonalisation: sector too large for the cluster");
-  switch (CL) {
-    case 1: launch_gebrd_cl<1>(ops, nops, mmax, nmax, s); break;
-    case 2: launch_gebrd_cl<2>(ops, nops, mmax, nmax, s); break;
-    case 4: launch_gebrd_cl<4>(ops, nops, mmax, nmax, s); break;
-    case 8: launch_gebrd_cl<8>(ops, nops, mmax, nmax, s); break;
-    case 16: launch_gebrd_cl<16>(ops, nops, mmax, nmax, s); break;
+  const bool gm = code > kGebrdGlobal;
+  const int CL = gm ? code - kGebrdGlobal : code;
+  MPSG_CHECK(sizeof(double) * (gm ? gebrd_gm_smem_doubles(mmax, nmax, CL) : gebrd_smem_doubles(mmax, nmax, CL)) <=
+                 227 * 1024,
+             "bidiagonalisation: sector too large for the cluster");
+  switch (code) {
+    case 1: launch_gebrd_cl<1, false>(ops, nops, mmax, nmax, s); break;
+    case 2: launch_gebrd_cl<2, false>(ops, nops, mmax, nmax, s); break;
+    case 4: launch_gebrd_cl<4, false>(ops, nops, mmax, nmax, s); break;
+    case 8: launch_gebrd_cl<8, false>(ops, nops, mmax, nmax, s); break;
+    case 16: launch_gebrd_cl<16, false>(ops, nops, mmax, nmax, s); break;
+    case kGebrdGlobal + 1: launch_gebrd_cl<1, true>(ops, nops, mmax, nmax, s); break;
+    case kGebrdGlobal + 2: launch_gebrd_cl<2, true>(ops, nops, mmax, nmax, s); break;
+    case kGebrdGlobal + 4: launch_gebrd_cl<4, true>(ops, nops, mmax, nmax, s); break;
+    case kGebrdGlobal + 8: launch_gebrd_cl<8, true>(ops, nops, mmax, nmax, s); break;
+    case kGebrdGlobal + 16: launch_gebrd_cl<16, true>(ops, nops, mmax, nmax, s); break;
     default: throw Err(1, "bidiagonalisation: unsupported cluster size");
   }
 }
@@ -310,30 +346,42 @@ void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s) {
 // instead of per step); with |b| < 2 and x <= 4 a block of 8 steps grows |p| by at most 2^24, so the
 // magnitude check once per block keeps p inside [2^-1000, 2^1000].
 constexpr int kGkBlk = 8;
-__device__ __forceinline__ void gk_step(double x, double b2, double& p0, double& p1, int& c) {
-  auto neg = [](double v) { return (int)((unsigned long long)__double_as_longlong(v) >> 63); };
-  double p2 = fma(-x, p1, -b2 * p0);
-  if ((__double_as_longlong(p2) << 1) == 0) p2 = neg(p1) ? DBL_MIN : -DBL_MIN;  // zero: a sign change
-  c += neg(p2) ^ neg(p1);
-  p0 = p1;
-  p1 = p2;
-}
 __device__ int gk_count(const double* __restrict__ b2, int N, double x) {
+  // signs from the high words (32-bit integer operations; 64-bit integer operations on the bit
+  // patterns measured twice as slow); an exact zero counts as a sign change (it is replaced by the
+  // smallest normal number of the sign opposite to its predecessor)
   double p0 = 1.0, p1 = -x;
   if (p1 == 0.0) p1 = -DBL_MIN;
-  int c = (int)((unsigned long long)__double_as_longlong(p1) >> 63);
+  int s1 = (int)((unsigned)__double2hiint(p1) >> 31);
+  int c = s1;
   int i = 1;
+  auto step = [&](double b2v) {
+    double p2 = fma(-x, p1, -b2v * p0);
+    const int hi = __double2hiint(p2);
+    int s2 = (int)((unsigned)hi >> 31);
+    if (((hi & 0x7fffffff) | __double2loint(p2)) == 0) {
+      p2 = s1 ? DBL_MIN : -DBL_MIN;
+      s2 = s1 ^ 1;
+    }
+    c += s1 ^ s2;
+    s1 = s2;
+    p0 = p1;
+    p1 = p2;
+  };
   for (; i + kGkBlk <= N; i += kGkBlk) {
     double bb[kGkBlk];
 #pragma unroll
     for (int u = 0; u < kGkBlk; ++u) bb[u] = __ldg(b2 + i - 1 + u);
 #pragma unroll
-    for (int u = 0; u < kGkBlk; ++u) gk_step(x, bb[u], p0, p1, c);
-    const int ex = (int)((__double_as_longlong(p1) >> 52) & 0x7ff) - 1023;
-    if (ex > 400) { p0 *= 0x1p-400; p1 *= 0x1p-400; }
-    else if (ex < -400) { p0 *= 0x1p+400; p1 *= 0x1p+400; }
+    for (int u = 0; u < kGkBlk; ++u) step(bb[u]);
+    const int ex = ((__double2hiint(p1) >> 20) & 0x7ff) - 1023;
+    if (ex > 400 || ex < -400) {
+      const double f = ex > 0 ? 0x1p-400 : 0x1p+400;
+      p0 *= f;
+      p1 *= f;
+    }
   }
-  for (; i < N; ++i) gk_step(x, __ldg(b2 + i - 1), p0, p1, c);
+  for (; i < N; ++i) step(__ldg(b2 + i - 1));
   return c;
 }
 // singular values of the sector >= x (unscaled x)
@@ -543,14 +591,56 @@ __device__ void gk_factor(const double* __restrict__ b, int N, double lam, doubl
   if (dd == 0.0) dd = tiny;
   u0[(N - 1) * st] = 1.0 / dd;
 }
-// x <- c (T - lam I)^-1 x with the factors of gk_factor, c > 0 (the iterate is rescaled by 2^-166
-// whenever an entry passes 2^166; the caller normalises)
+// Whole-vector rescaling by a power of two (exact) when an entry passed 2^166: brings the largest
+// entry back to ~2^100 (the caller normalises the result).
+__device__ __forceinline__ double gk_rescale_factor(double amax) { return ldexp(1.0, 100 - ilogb(amax)); }
+__device__ void gk_scale_all(int N, double* x, int64_t st, double f) {
+  for (int k = 0; k < N; ++k) x[k * st] *= f;
+}
+
+// x <- c (T - lam I)^-1 x with the factors of gk_factor, c > 0.  The loads of each block of kGkRows
+// rows are issued before its dependent chain (the chain is what bounds this kernel: a dependent FP64
+// operation takes ~64 cycles on this GPU), and the magnitude is checked once per block: partial
+// pivoting keeps |mul| <= 1 (growth <= 2 per forward step) and the pivots >= eps ||T|| (growth
+// <= 2^53 per backward step), so no entry leaves the range within a block.
+constexpr int kGkRows = 8;
 __device__ void gk_solve(int N, double* __restrict__ x, const double* __restrict__ f, int64_t st) {
   const double *u0 = f, *u1 = f + N * st, *u2 = f + 2 * N * st, *mul = f + 3 * N * st, *piv = f + 4 * N * st;
   // forward: L^-1 with the interchanges; cur = x_i as updated so far
   double cur = x[0];
-  for (int i = 0; i + 1 < N; ++i) {
-    const int64_t o = i * st;
+  int i = 0;
+  for (; i + kGkRows < N; i += kGkRows) {
+    double nx[kGkRows], mm[kGkRows], pv[kGkRows];
+#pragma unroll
+    for (int u = 0; u < kGkRows; ++u) {
+      const int64_t o = (int64_t)(i + u) * st;
+      nx[u] = x[o + st];
+      mm[u] = mul[o];
+      pv[u] = piv[o];
+    }
+    double amax = 0.0;
+#pragma unroll
+    for (int u = 0; u < kGkRows; ++u) {
+      double xi, xn;
+      if (pv[u] != 0.0) {
+        xi = nx[u];
+        xn = cur - mm[u] * nx[u];
+      } else {
+        xi = cur;
+        xn = nx[u] - mm[u] * cur;
+      }
+      x[(int64_t)(i + u) * st] = xi;
+      cur = xn;
+      amax = fmax(amax, fabs(xn));
+    }
+    if (amax > 0x1p+166) {
+      const double sc = gk_rescale_factor(amax);
+      gk_scale_all(N, x, st, sc);
+      cur *= sc;
+    }
+  }
+  for (; i + 1 < N; ++i) {
+    const int64_t o = (int64_t)i * st;
     const double nxt = x[o + st], m = mul[o];
     double xi, xn;
     if (piv[o] != 0.0) {
@@ -562,26 +652,55 @@ __device__ void gk_solve(int N, double* __restrict__ x, const double* __restrict
     }
     x[o] = xi;
     cur = xn;
-    if (fabs(xn) > 0x1p+166) {  // the whole vector
-      for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
-      cur *= 0x1p-166;
-    }
+  }
+  if (fabs(cur) > 0x1p+166) {
+    const double sc = gk_rescale_factor(fabs(cur));
+    gk_scale_all(N, x, st, sc);
+    cur *= sc;
   }
   // backward: U^-1, x_{i+1} and x_{i+2} carried in registers
-  double x1 = cur * u0[(N - 1) * st], x2 = 0.0;
+  double x1 = cur * u0[(int64_t)(N - 1) * st], x2 = 0.0;
   if (fabs(x1) > 0x1p+166) {
-    for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
-    x1 *= 0x1p-166;
+    const double sc = gk_rescale_factor(fabs(x1));
+    gk_scale_all(N, x, st, sc);
+    x1 *= sc;
   }
-  x[(N - 1) * st] = x1;
-  for (int i = N - 2; i >= 0; --i) {
-    const int64_t o = i * st;
+  x[(int64_t)(N - 1) * st] = x1;
+  i = N - 2;
+  for (; i - kGkRows + 1 >= 0; i -= kGkRows) {
+    double xv[kGkRows], a0[kGkRows], a1[kGkRows], a2[kGkRows];
+#pragma unroll
+    for (int u = 0; u < kGkRows; ++u) {
+      const int64_t o = (int64_t)(i - u) * st;
+      xv[u] = x[o];
+      a0[u] = u0[o];
+      a1[u] = u1[o];
+      a2[u] = u2[o];
+    }
+    double amax = 0.0;
+#pragma unroll
+    for (int u = 0; u < kGkRows; ++u) {
+      const double xi = (xv[u] - a1[u] * x1 - a2[u] * x2) * a0[u];
+      x[(int64_t)(i - u) * st] = xi;
+      x2 = x1;
+      x1 = xi;
+      amax = fmax(amax, fabs(xi));
+    }
+    if (amax > 0x1p+166) {  // the whole vector, its register copies included
+      const double sc = gk_rescale_factor(amax);
+      gk_scale_all(N, x, st, sc);
+      x1 *= sc;
+      x2 *= sc;
+    }
+  }
+  for (; i >= 0; --i) {
+    const int64_t o = (int64_t)i * st;
     double xi = (x[o] - u1[o] * x1 - u2[o] * x2) * u0[o];
-    if (fabs(xi) > 0x1p+166) {  // the whole vector, its register copies included
-      for (int k = 0; k < N; ++k) x[k * st] *= 0x1p-166;
-      xi *= 0x1p-166;
-      x1 *= 0x1p-166;
-      x2 *= 0x1p-166;
+    if (fabs(xi) > 0x1p+166) {
+      const double sc = gk_rescale_factor(fabs(xi));
+      gk_scale_all(N, x, st, sc);
+      xi *= sc;
+      x1 *= sc;
     }
     x[o] = xi;
     x2 = x1;
@@ -694,12 +813,20 @@ __global__ void __launch_bounds__(256) k_apply_refl(const ReflOp* __restrict__ o
   }
   for (int i = lane; i < len; i += 32) X[i] = x[i];
 }
+// warps (columns) per CTA for columns of lenmax rows (at most 8, within 220 KB of shared memory)
+static int apply_refl_warps(int lenmax) {
+  const int w = (int)((220 * 1024) / (sizeof(double) * (size_t)std::max(lenmax, 1)));
+  return std::max(1, std::min(8, w));
+}
 void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s) {
   if (nops <= 0) return;
-  const size_t smem = sizeof(double) * 8 * (size_t)std::max(lenmax, 1);
+  const int nw = apply_refl_warps(lenmax);
+  const size_t smem = sizeof(double) * nw * (size_t)std::max(lenmax, 1);
+  MPSG_CHECK(smem <= 227 * 1024, "back-transformation: sector too tall for the shared-memory column block");
   MPSG_CUDA(cudaFuncSetAttribute(k_apply_refl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_apply_refl<<<nops, 256, smem, s>>>(ops);
+  k_apply_refl<<<nops, 32 * nw, smem, s>>>(ops);
   g_bd_launches.fetch_add(1);
 }
+int apply_refl_cols_per_block(int lenmax) { return apply_refl_warps(lenmax); }
 
 }  // namespace mpsg
