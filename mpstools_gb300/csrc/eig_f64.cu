@@ -493,7 +493,9 @@ static __host__ __device__ size_t chol_smem_doubles(int k, int CL) {
 }
 size_t chol_smem_bytes(int k, int CL) { return sizeof(double) * chol_smem_doubles(k, CL); }
 
-template <int CL>
+// GM = true (k beyond the cluster's shared memory): the own panels are factorised and updated in place
+// in C in global memory (L2-resident); only the copied panel lives in shared memory.
+template <int CL, bool GM>
 __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) {
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
@@ -504,15 +506,21 @@ __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) 
   const int nb = (k + kPanel - 1) / kPanel;
   const int nbl_max = (nb + CL - 1) / CL;
   double* cols = sm;                                        // local panel p (global panel r + p*CL): kPanel x k
-  double* pbuf = cols + (size_t)nbl_max * kPanel * k;       // current panel, copied from its owner
-  auto colptr = [&](double* base, int lp, int jj) { return base + ((size_t)lp * kPanel + jj) * k; };
+  double* pbuf = GM ? sm : cols + (size_t)nbl_max * kPanel * k;  // current panel, copied from its owner
+  // column jj of local panel lp (GM: the column of C itself; padding columns past k are never used
+  // in GM mode, which works on the k real columns only)
+  auto colptr = [&](double* base, int lp, int jj) -> double* {
+    if (GM) return o.C + (int64_t)((r + lp * CL) * kPanel + jj) * o.ld;
+    return base + ((size_t)lp * kPanel + jj) * k;
+  };
   const int nbl = (nb - r + CL - 1) / CL;
-  for (int lp = 0; lp < nbl; ++lp)
-    for (int jj = warp; jj < kPanel; jj += nwarp) {
-      const int c = (r + lp * CL) * kPanel + jj;
-      double* dst = colptr(cols, lp, jj);
-      for (int i = lane; i < k; i += 32) dst[i] = c < k ? o.C[i + (int64_t)c * o.ld] : 0.0;
-    }
+  if (!GM)
+    for (int lp = 0; lp < nbl; ++lp)
+      for (int jj = warp; jj < kPanel; jj += nwarp) {
+        const int c = (r + lp * CL) * kPanel + jj;
+        double* dst = colptr(cols, lp, jj);
+        for (int i = lane; i < k; i += 32) dst[i] = c < k ? o.C[i + (int64_t)c * o.ld] : 0.0;
+      }
   cluster.sync();
   for (int b = 0; b < nb; ++b) {
     const int j0 = b * kPanel, jn = min(kPanel, k - j0);
@@ -555,8 +563,13 @@ __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) 
     }
     cluster.sync();  // panel b factorised
     if (b + 1 == nb) break;
-    // copy panel b (rows >= j0 + jn) from the owner's shared memory
-    {
+    // copy panel b (rows >= j0 + jn) from the owner's shared memory (GM: from C)
+    if (GM) {
+      for (int idx = tid; idx < jn * k; idx += blockDim.x) {
+        const int i = idx % k, q = idx / k;
+        if (i >= j0 + jn) pbuf[idx] = o.C[i + (int64_t)(j0 + q) * o.ld];
+      }
+    } else {
       const double* src = cluster.map_shared_rank(colptr(cols, b / CL, 0), owner);
       for (int idx = tid; idx < jn * k; idx += blockDim.x) {
         const int i = idx % k;
@@ -588,11 +601,11 @@ __global__ void __launch_bounds__(256) k_chol(const CholQROp* __restrict__ ops) 
   cluster.sync();  // no CTA leaves while another may still read its panels
 }
 
-template <int CL>
+template <int CL, bool GM>
 static void launch_chol_cl(const CholQROp* ops, int nops, int kmax, cudaStream_t s) {
-  const size_t smem = chol_smem_bytes(kmax, CL);
-  MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  const size_t smem = GM ? sizeof(double) * ((size_t)kPanel * kmax + 8) : chol_smem_bytes(kmax, CL);
+  MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL, GM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_chol<CL, GM>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nops * CL);
   cfg.blockDim = dim3(256);
@@ -605,25 +618,30 @@ static void launch_chol_cl(const CholQROp* ops, int nops, int kmax, cudaStream_t
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_chol<CL>, ops));
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_chol<CL, GM>, ops));
   g_eig_launches.fetch_add(1);
 }
-int chol_max_k() { return 512; }
+// the shared-memory cluster kernel up to k = 512; beyond, the global-memory variant (its copied panel,
+// 16 x k doubles, has to fit in shared memory)
+constexpr int kCholGlobal = 100;
+int chol_max_k() { return 1600; }
 int chol_cluster_size(int k) {
   // smallest cluster whose shared memory holds the panels (<= 200 KB per CTA)
   for (int CL : {1, 2, 4, 8, 16})
     if (chol_smem_bytes(k, CL) <= 200 * 1024 && (CL >= 16 || k <= 48 * CL)) return CL;
-  return 16;
+  if (chol_smem_bytes(k, 16) <= 227 * 1024) return 16;
+  return kCholGlobal + 16;
 }
-void launch_chol(const CholQROp* ops, int nops, int CL, int kmax, cudaStream_t s) {
+void launch_chol(const CholQROp* ops, int nops, int code, int kmax, cudaStream_t s) {
   if (nops <= 0) return;
-  MPSG_CHECK(chol_smem_bytes(kmax, CL) <= 227 * 1024, "Cholesky: sector too large for the cluster kernel");
-  switch (CL) {
-    case 1: launch_chol_cl<1>(ops, nops, kmax, s); break;
-    case 2: launch_chol_cl<2>(ops, nops, kmax, s); break;
-    case 4: launch_chol_cl<4>(ops, nops, kmax, s); break;
-    case 8: launch_chol_cl<8>(ops, nops, kmax, s); break;
-    case 16: launch_chol_cl<16>(ops, nops, kmax, s); break;
+  MPSG_CHECK(kmax <= chol_max_k(), "Cholesky: sector wider than the cluster kernel's limit");
+  switch (code) {
+    case 1: launch_chol_cl<1, false>(ops, nops, kmax, s); break;
+    case 2: launch_chol_cl<2, false>(ops, nops, kmax, s); break;
+    case 4: launch_chol_cl<4, false>(ops, nops, kmax, s); break;
+    case 8: launch_chol_cl<8, false>(ops, nops, kmax, s); break;
+    case 16: launch_chol_cl<16, false>(ops, nops, kmax, s); break;
+    case kCholGlobal + 16: launch_chol_cl<16, true>(ops, nops, kmax, s); break;
     default: throw Err(1, "Cholesky: unsupported cluster size");
   }
 }

@@ -817,7 +817,7 @@ struct SvdBatch {
         nmax = std::max(nmax, s[i].ns);
       }
     if (idx.empty()) return;
-    MPSG_CHECK(nmax <= sytrd_max_n() && nmax <= chol_max_k(), "density split: sector too wide");
+    MPSG_CHECK(nmax <= sytrd_max_n() && nmax <= 512, "density split: sector too wide");
     cudaStream_t st = ctx->stream;
     MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(s.size(), 1), st));  // no solver status
     std::vector<int64_t> offG(s.size(), 0);
@@ -1135,7 +1135,7 @@ struct SvdBatch {
         kmax = std::max(kmax, kcols(i));
       }
     if (idx.empty()) return;
-    MPSG_CHECK(kmax <= chol_max_k(), "CholeskyQR: sector wider than the cluster kernel's limit (512)");
+    MPSG_CHECK(kmax <= chol_max_k(), "CholeskyQR: sector wider than the cluster kernel's limit");
     cudaStream_t st = ctx->stream;
     double* X = left ? dU : dV;
     auto rows = [&](int i) { return left && !ub_rows ? s[i].ms : s[i].ns; };
@@ -1257,7 +1257,7 @@ struct SvdBatch {
   void run(int method) {
     int nmax = 0;
     for (auto& x : s) nmax = std::max(nmax, x.k > 0 ? x.ns : 0);
-    if (method != 0 && nmax > chol_max_k()) method = 0;  // the density routes' CholeskyQR covers widths <= 512
+    if (method >= 1 && method <= 3 && nmax > 512) method = 0;  // the density routes cover widths <= 512
     if (method == 4 && !bidiag_fits()) method = 0;
     if (method == 1) run_gram();
     else if (method == 2) run_gram_mt();
@@ -1333,15 +1333,13 @@ struct SvdBatch {
     // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first)
     {
       std::map<int, std::vector<GebrdOp>> byCL;
-      std::map<int, std::pair<int, int>> mx;
+      std::map<int, size_t> smem;  // per cluster-size code, the largest of its sectors' needs
       for (int i : bd.idx) {
         const Sec& x = s[i];
         const int CL = gebrd_cluster_size(x.ms, x.ns);
         byCL[CL].push_back(GebrdOp{dM + x.offM, bd.d + x.offS, bd.e + x.offS, bd.tq + x.offS, bd.tp + x.offS,
                                    bd.Pr + bd.offPr[i], x.ms, x.ns, x.ms});
-        auto& p = mx[CL];
-        p.first = std::max(p.first, x.ms);
-        p.second = std::max(p.second, x.ns);
+        smem[CL] = std::max(smem[CL], gebrd_smem(x.ms, x.ns, CL));
       }
       std::vector<std::pair<int, GebrdOp*>> bufs;
       for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) {
@@ -1353,8 +1351,8 @@ struct SvdBatch {
       const int nw = std::min<int>((int)bufs.size(), ctx->nworkers());
       ctx->fork(nw);
       for (size_t j = 0; j < bufs.size(); ++j)
-        launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, mx[bufs[j].first].first,
-                     mx[bufs[j].first].second, ctx->wstreams[j % nw]);
+        launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, smem[bufs[j].first],
+                     ctx->wstreams[j % nw]);
       ctx->join(nw);
       for (auto& b : bufs) ctx->dfree(b.second);
     }
@@ -2066,10 +2064,55 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   double eold = 1e100, dE_prev = 1e100;
   bool done = false;
   float mv_ms_total = 0;
+  // Batches after the first hold ndiag iterations each and end on an energy checkpoint: they are
+  // captured once as a CUDA graph (iteration index on the device, matvec on fixed buffers) and the
+  // graph is replayed for every later batch.  Projected and reorthogonalised runs stay launch by launch.
+  bool graphs = !proj && !reorth && !std::getenv("MPSG_NO_LANCZOS_GRAPH");
+  cudaGraphExec_t gexec = nullptr;
+  size_t gnodes = 0;
+  int* d_j = nullptr;
+  double* xin = nullptr;
   while (!done) {
     // batch up to the next energy checkpoint (it % ndiag == 0, it != 0) or itmax-1
     int ck = it;
     while (!((ck % ndiag == 0 && ck != 0) || ck >= itmax - 1)) ++ck;
+    if (graphs && it > 0 && ck - it + 1 == ndiag && ck % ndiag == 0 && !gexec) {
+      slot(ck + 1);
+      d_j = (int*)ctx->dmalloc(sizeof(int) * 4);
+      xin = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(n, 2));
+      lz_prepare_attributes(itmax);
+      cudaGraph_t g = nullptr;
+      const int64_t launched0 = kernel_launch_count() + tc_launch_count();  // captured, not run
+      cudaError_t ce = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+      if (ce == cudaSuccess) {
+        for (int u = 0; u < ndiag; ++u) {
+          launch_lz_pre(dV, d_j, d_norm2, delta, d_beta, xin, n, s);
+          mv.run(xin, w);
+          launch_lz_post(dV, d_j, w, xin, d_alpha, d_beta, d_norm2, d_E, ndiag, testenergy && u == ndiag - 1, itmax,
+                         n, ctx->part, s);
+        }
+        ce = cudaStreamEndCapture(s, &g);
+      }
+      count_graph_launches(launched0 - (kernel_launch_count() + tc_launch_count()));
+      if (ce == cudaSuccess && g && cudaGraphGetNodes(g, nullptr, &gnodes) == cudaSuccess &&
+          cudaGraphInstantiate(&gexec, g, 0) == cudaSuccess) {
+      } else {  // capture not possible on this stream: the launch-by-launch path
+        cudaGetLastError();
+        gexec = nullptr;
+        graphs = false;
+        if (std::getenv("MPSG_VERBOSE")) std::fprintf(stderr, "libmpsg: Lanczos graph capture failed (%s)\n", cudaGetErrorString(ce));
+      }
+      if (g) cudaGraphDestroy(g);
+    }
+    if (gexec && it > 0 && ck - it + 1 == ndiag && ck % ndiag == 0) {
+      slot(ck + 1);  // the batch's Krylov vectors exist (and are in the device table) before the graph runs
+      int* hj = reinterpret_cast<int*>(ctx->hscal + 4095);  // pinned, past the scalars read back below
+      hj[0] = it;
+      MPSG_CUDA(cudaMemcpyAsync(d_j, hj, sizeof(int), cudaMemcpyHostToDevice, s));
+      MPSG_CUDA(cudaEventRecord(e0, s));
+      MPSG_CUDA(cudaGraphLaunch(gexec, s));
+      count_graph_launches((int64_t)gnodes);
+    } else {
     MPSG_CUDA(cudaEventRecord(e0, s));
     for (int j = it; j <= ck; ++j) {
       slot(j + 1);
@@ -2091,6 +2134,7 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
         }
         launch_dot(V[j + 1], V[j + 1], n, ctx->part, d_norm2 + j + 1, s);
       }
+    }
     }
     MPSG_CUDA(cudaEventRecord(e1, s));
     MPSG_CUDA(cudaMemcpyAsync(ctx->hscal, dsc, sizeof(double) * (size_t)na * 4, cudaMemcpyDeviceToHost, s));
@@ -2136,6 +2180,9 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (gexec) cudaGraphExecDestroy(gexec);
+  ctx->dfree(d_j);
+  ctx->dfree(xin);
   for (double* p : V) ctx->dfree(p);
   ctx->dfree(w);
   ctx->dfree(dV);

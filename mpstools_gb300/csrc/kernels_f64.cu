@@ -554,6 +554,85 @@ void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E
   k_tri_lowest<<<1, 32, sh, s>>>(alpha, beta, n, E0, z);
   LAUNCHED();
 }
+// ============================================================================ graph-replayed Lanczos
+// The Lanczos iterations between two energy checkpoints are captured once as a CUDA graph and replayed
+// for every later batch: the iteration index j lives on the device (*jp), the kernels below read it
+// and address the Krylov vectors through the device table V; the matvec works on fixed buffers (xin
+// holds the normalised V[j]).  The arithmetic is that of the launch-by-launch kernels above.
+__global__ void k_lz_scale(double* const* __restrict__ V, const int* __restrict__ jp, const double* __restrict__ norm2,
+                           double delta, double* beta, double* __restrict__ xin, int64_t n) {
+  const int j = *jp;
+  double* x = V[j];
+  const double k = sqrt(norm2[j]);
+  const double sc = (k < delta) ? 0.0 : 1.0 / k;
+  if (blockIdx.x == 0 && threadIdx.x == 0) beta[j] = k;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i] * sc;
+    x[i] = v;
+    xin[i] = v;
+  }
+}
+// base[*jp + offset] = sum of the block partials; incr: then *jp += 1
+__global__ void k_lz_sum(const double* part, int np, double* base, int* jp, int offset, int incr) {
+  const int j = *jp;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s += part[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    base[j + offset] = s;
+    if (incr) *jp = j + 1;
+  }
+}
+__global__ void k_lz_axpy3(double* const* __restrict__ V, const int* __restrict__ jp, const double* __restrict__ w,
+                           const double* __restrict__ v, const double* alpha, const double* beta, int64_t n,
+                           double* part) {
+  const int j = *jp;
+  double* __restrict__ out = V[j + 1];
+  const double* __restrict__ vp = j > 0 ? V[j - 1] : nullptr;
+  const double a = -alpha[j];
+  const double b = vp ? -beta[j] : 0.0;
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double o = v[i] * a + w[i];
+    if (vp) o = o + vp[i] * b;
+    out[i] = o;
+    s = fma(o, o, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+__global__ void k_lz_tri_lowest(const double* __restrict__ a_g, const double* __restrict__ b, const int* jp, int ndiag,
+                                double* E) {
+  const int j = *jp;
+  tri_lowest_dev(a_g, b, j + 1, E + j / ndiag, nullptr);
+}
+// one Lanczos iteration on the device index: scale V[j] (and copy it to xin), the caller's matvec
+// xin -> w, alpha[j], the optional energy checkpoint, V[j+1] and its squared norm, j += 1
+void launch_lz_pre(double* const* V, const int* jp, const double* norm2, double delta, double* beta, double* xin,
+                   int64_t n, cudaStream_t s) {
+  k_lz_scale<<<kRedBlocks, 256, 0, s>>>(V, jp, norm2, delta, beta, xin, n);
+  LAUNCHED();
+}
+void launch_lz_post(double* const* V, int* jp, const double* w, const double* xin, double* alpha, double* beta,
+                    double* norm2, double* E, int ndiag, bool checkpoint, int itmax, int64_t n, double* part,
+                    cudaStream_t s) {
+  k_dot_part<<<kRedBlocks, 256, 0, s>>>(w, xin, n, part);
+  k_lz_sum<<<1, 256, 0, s>>>(part, kRedBlocks, alpha, jp, 0, 0);
+  if (checkpoint) {
+    const size_t sh = (size_t)(itmax + 1) * 8 * sizeof(double) + 16;
+    k_lz_tri_lowest<<<1, 32, sh, s>>>(alpha, beta, jp, ndiag, E);
+  }
+  k_lz_axpy3<<<kRedBlocks, 256, 0, s>>>(V, jp, w, xin, alpha, beta, n, part);
+  k_lz_sum<<<1, 256, 0, s>>>(part, kRedBlocks, norm2, jp, 1, 1);
+  g_launches.fetch_add(checkpoint ? 5 : 4);
+}
+void lz_prepare_attributes(int itmax) {
+  const size_t sh = (size_t)(itmax + 1) * 8 * sizeof(double) + 16;
+  if (sh > 48 * 1024)
+    MPSG_CUDA(cudaFuncSetAttribute(k_lz_tri_lowest, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh));
+}
+void count_graph_launches(int64_t n) { g_launches.fetch_add(n); }
+
 // One block per chain c: the lowest eigenpair of chain c's tridiagonal (alpha / beta at c * stride,
 // n_of[c] rows; chains with n_of[c] <= 0 are skipped); E0 at c * estride, z at c * stride.
 __global__ void k_tri_lowest_seg(const double* __restrict__ alpha, const double* __restrict__ beta,

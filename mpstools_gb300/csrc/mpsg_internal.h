@@ -317,6 +317,14 @@ void launch_combine(double* y, const double* const* V, int nv, const double* c, 
 // c[j] = <V_j, x> for j < nv (block partials reduced deterministically); part_nv holds 64*nv doubles
 void launch_project(const double* const* V, int nv, const double* x, int64_t n, double* part_nv, double* c,
                     cudaStream_t s);
+// graph-replayed Lanczos iteration (kernels_f64.cu): the iteration index *jp on the device
+void launch_lz_pre(double* const* V, const int* jp, const double* norm2, double delta, double* beta, double* xin,
+                   int64_t n, cudaStream_t s);
+void launch_lz_post(double* const* V, int* jp, const double* w, const double* xin, double* alpha, double* beta,
+                    double* norm2, double* E, int ndiag, bool checkpoint, int itmax, int64_t n, double* part,
+                    cudaStream_t s);
+void lz_prepare_attributes(int itmax);
+void count_graph_launches(int64_t n);  // kernels a graph replay ran (for the launch statistics)
 // lowest eigenpair of the symmetric tridiagonal (alpha[0..n), offdiag beta[1..n)); z may be null
 void launch_tri_lowest(const double* alpha, const double* beta, int n, double* E0, double* z, cudaStream_t s);
 void launch_tri_lowest_seg(const double* alpha, const double* beta, const int* n_of, int nchains, int nmax, int stride,
@@ -336,7 +344,8 @@ void launch_scombine(double* y, const double* const* V, const int* nv_of, const 
                      const int64_t* segoff, int nseg, cudaStream_t s);
 // bidiagonal SVD (svd_bidiag.cu)
 int gebrd_cluster_size(int m, int n);  // 0: the sector does not fit the cluster kernel
-void launch_gebrd(const GebrdOp* ops, int nops, int CL, int mmax, int nmax, cudaStream_t s);
+size_t gebrd_smem(int m, int n, int code);  // dynamic shared memory of one sector's CTAs
+void launch_gebrd(const GebrdOp* ops, int nops, int code, size_t smem, cudaStream_t s);
 void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s);
 // per segment [seg[c], seg[c + 1]) of ops (op_seg: segment of each op): the cut x of the segment such
 // that at least chimax of its values are >= x (or floor_abs when fewer than chimax exceed it), kept in

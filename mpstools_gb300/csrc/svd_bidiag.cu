@@ -227,8 +227,7 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
 }
 
 template <int CL, bool GM>
-static void launch_gebrd_cl(const GebrdOp* ops, int nops, int mmax, int nmax, cudaStream_t s) {
-  const size_t smem = sizeof(double) * (GM ? gebrd_gm_smem_doubles(mmax, nmax, CL) : gebrd_smem_doubles(mmax, nmax, CL));
+static void launch_gebrd_cl(const GebrdOp* ops, int nops, size_t smem, cudaStream_t s) {
   MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
@@ -268,24 +267,27 @@ int gebrd_cluster_size(int m, int n) {
   return sizeof(double) * gebrd_gm_smem_doubles(m, n, c) <= 220 * 1024 ? kGebrdGlobal + c : 0;
 }
 
-void launch_gebrd(const GebrdOp* ops, int nops, int code, int mmax, int nmax, cudaStream_t s) {
-  if (nops <= 0) return;
+// dynamic shared memory of one sector's CTAs (a launch takes the largest over its sectors)
+size_t gebrd_smem(int m, int n, int code) {
   const bool gm = code > kGebrdGlobal;
   const int CL = gm ? code - kGebrdGlobal : code;
-  MPSG_CHECK(sizeof(double) * (gm ? gebrd_gm_smem_doubles(mmax, nmax, CL) : gebrd_smem_doubles(mmax, nmax, CL)) <=
-                 227 * 1024,
-             "bidiagonalisation: sector too large for the cluster");
+  return sizeof(double) * (gm ? gebrd_gm_smem_doubles(m, n, CL) : gebrd_smem_doubles(m, n, CL));
+}
+
+void launch_gebrd(const GebrdOp* ops, int nops, int code, size_t smem, cudaStream_t s) {
+  if (nops <= 0) return;
+  MPSG_CHECK(smem <= 227 * 1024, "bidiagonalisation: sector too large for the cluster");
   switch (code) {
-    case 1: launch_gebrd_cl<1, false>(ops, nops, mmax, nmax, s); break;
-    case 2: launch_gebrd_cl<2, false>(ops, nops, mmax, nmax, s); break;
-    case 4: launch_gebrd_cl<4, false>(ops, nops, mmax, nmax, s); break;
-    case 8: launch_gebrd_cl<8, false>(ops, nops, mmax, nmax, s); break;
-    case 16: launch_gebrd_cl<16, false>(ops, nops, mmax, nmax, s); break;
-    case kGebrdGlobal + 1: launch_gebrd_cl<1, true>(ops, nops, mmax, nmax, s); break;
-    case kGebrdGlobal + 2: launch_gebrd_cl<2, true>(ops, nops, mmax, nmax, s); break;
-    case kGebrdGlobal + 4: launch_gebrd_cl<4, true>(ops, nops, mmax, nmax, s); break;
-    case kGebrdGlobal + 8: launch_gebrd_cl<8, true>(ops, nops, mmax, nmax, s); break;
-    case kGebrdGlobal + 16: launch_gebrd_cl<16, true>(ops, nops, mmax, nmax, s); break;
+    case 1: launch_gebrd_cl<1, false>(ops, nops, smem, s); break;
+    case 2: launch_gebrd_cl<2, false>(ops, nops, smem, s); break;
+    case 4: launch_gebrd_cl<4, false>(ops, nops, smem, s); break;
+    case 8: launch_gebrd_cl<8, false>(ops, nops, smem, s); break;
+    case 16: launch_gebrd_cl<16, false>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 1: launch_gebrd_cl<1, true>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 2: launch_gebrd_cl<2, true>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 4: launch_gebrd_cl<4, true>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 8: launch_gebrd_cl<8, true>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 16: launch_gebrd_cl<16, true>(ops, nops, smem, s); break;
     default: throw Err(1, "bidiagonalisation: unsupported cluster size");
   }
 }

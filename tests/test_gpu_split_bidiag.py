@@ -128,3 +128,31 @@ def test_bidiag_split_weight_truncation_and_tiny_sectors(ctx):
     for q in l0:
         assert np.abs(np.asarray(l1[q]) - np.asarray(l0[q])).max(initial=0.0) <= 1e-13
     assert abs(tw1 - tw0) <= 1e-13
+
+
+def test_bidiag_split_sector_with_more_than_512_kept_vectors(ctx):
+    """One 1016 x 792 sector (as converged chi = 2048 sweeps produce) whose 792 values are all kept:
+    beyond the shared-memory Cholesky of a 16-CTA cluster, the CholeskyQR runs on its global-memory
+    variant (no fallback to the Jacobi route)."""
+    rng = np.random.default_rng(8)
+    m, n = 1016, 792
+    U = np.linalg.qr(rng.standard_normal((m, n)))[0]
+    V = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    s = np.sort(10.0 ** rng.uniform(-10.0, 0.0, n))[::-1]
+    th = {(0, 0, 0, 0): (U * s) @ V.T}
+    ik = [0, 0]
+    U0, V0, l0, tw0, chi0 = O.split(th, ik, ik, 1000, normalize=False)
+    ctx.set_svd_method("bidiag")
+    f0 = ctx.L.mpsg_split_fallbacks()
+    try:
+        U1, V1, l1, tw1, chi1 = api.split(th, (ik, ik), 1000, normalize=False, ctx=ctx)
+    finally:
+        ctx.set_svd_method(lib.DEFAULT_SVD)
+    assert ctx.L.mpsg_split_fallbacks() == f0
+    assert chi1 == chi0 == n
+    assert np.abs(np.asarray(l1[0]) - np.asarray(l0[0])).max() <= 1e-13
+    Ug = U1[(0, 0, 0)]
+    Vg = V1[(0, 0, 0)]
+    assert np.abs(Ug.T @ Ug - np.eye(n)).max() < 1e-12
+    assert np.abs(Vg @ Vg.T - np.eye(n)).max() < 1e-12
+    assert np.abs((Ug * np.asarray(l1[0])) @ Vg - th[(0, 0, 0, 0)]).max() < 1e-12
