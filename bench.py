@@ -583,6 +583,7 @@ def sweep_leg(ctx, prec, W, ik, sites, ramp, torch):
     from mpstools_gb300 import api
     eng = api.DMRGengine(sites, W, ik, prec=prec, ctx=ctx)
     s0 = eng.stats()
+    f0 = int(ctx.L.mpsg_split_fallbacks())
 
     def progress(r):  # one line per sweep on stderr, so that a run cut short still leaves its record
         st = eng.stats()
@@ -590,7 +591,12 @@ def sweep_leg(ctx, prec, W, ik, sites, ramp, torch):
                           "max_chi_kept": r["max_chi_kept"], "lanczos_iterations": r["lanczos_iterations"],
                           "split_seconds_total": st["split_seconds"] - s0["split_seconds"],
                           "lanczos_seconds_total": st["lanczos_seconds"] - s0["lanczos_seconds"],
-                          "env_seconds_total": st["env_seconds"] - s0["env_seconds"]}), file=sys.stderr, flush=True)
+                          "matvec_seconds_total": st["lanczos_iter_seconds"] - s0["lanczos_iter_seconds"],
+                          "env_seconds_total": st["env_seconds"] - s0["env_seconds"],
+                          "prep_seconds_total": st["prep_seconds"] - s0["prep_seconds"],
+                          "lanczos_call_seconds_total": st["lanczos_call_seconds"] - s0["lanczos_call_seconds"],
+                          "split_fallbacks_to_jacobi": int(ctx.L.mpsg_split_fallbacks()) - f0}),
+              file=sys.stderr, flush=True)
 
     recs, t_prep, E = run_sweeps(eng, len(sites), ramp, sync=torch.cuda.synchronize, on_sweep=progress)
     s1 = eng.stats()

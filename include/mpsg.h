@@ -225,6 +225,10 @@ mpsg_status mpsg_dmrg_steps(mpsg_dmrg e, int32_t* site, int32_t* dir, int32_t* i
  * seconds, [5] Lanczos seconds (wall), [6] env-update FLOPs, [7] wall seconds of simulate,
  * [8] device seconds of all doStep calls (events), [9] number of doStep calls. */
 mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* stats10);
+/* The counters of mpsg_dmrg_stats followed by [10] wall seconds of doStep before the eigensolver
+ * (theta layout, closure and formation) and [11] wall seconds of the eigensolver calls (matvec plan,
+ * Lanczos, MIXED's FP64 energy, AUTO's FP64 finish); the first min(n, 12) entries are written. */
+mpsg_status mpsg_dmrg_stats_ext(mpsg_dmrg e, double* stats, int32_t n);
 mpsg_status mpsg_dmrg_site(mpsg_dmrg e, int32_t site, mpsg_tensor* out);
 mpsg_status mpsg_dmrg_lambda(mpsg_dmrg e, int32_t bond, mpsg_tensor* out);
 /* MPO::measure(mps) in FP64 on the GPU  -- src/MPOTypes.hpp:990-1020. */

@@ -287,10 +287,11 @@ class DMRGengine:
                      tw=float(tw[i])) for i in range(n)]
 
     def stats(self):
-        s = np.zeros(10)
-        check(self.ctx.L.mpsg_dmrg_stats(self.h, lib.ptr(s)))
+        s = np.zeros(12)
+        check(self.ctx.L.mpsg_dmrg_stats_ext(self.h, lib.ptr(s), 12))
         keys = ["matvecs", "matvec_flops", "lanczos_iter_seconds", "env_seconds", "split_seconds",
-                "lanczos_seconds", "env_flops", "wall_seconds", "step_device_seconds", "step_calls"]
+                "lanczos_seconds", "env_flops", "wall_seconds", "step_device_seconds", "step_calls",
+                "prep_seconds", "lanczos_call_seconds"]
         return dict(zip(keys, s.tolist()))
 
     def build_environments(self, center):

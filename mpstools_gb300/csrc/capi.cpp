@@ -385,6 +385,16 @@ mpsg_status mpsg_dmrg_stats(mpsg_dmrg e, double* st) {
   st[9] = (double)g.nstep_calls;
   API_END
 }
+mpsg_status mpsg_dmrg_stats_ext(mpsg_dmrg e, double* st, int32_t n) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e && st && n >= 0, "null argument");
+  Engine& g = *e->e;
+  const double v[12] = {(double)g.lst.matvecs, g.lst.matvec_flops, g.lst.matvec_seconds, g.env_seconds,
+                        g.split_seconds, g.lst.seconds, g.env_flops, g.wall, g.step_device_seconds,
+                        (double)g.nstep_calls, g.prep_seconds, g.lanczos_call_seconds};
+  for (int i = 0; i < n && i < 12; ++i) st[i] = v[i];
+  API_END
+}
 mpsg_status mpsg_dmrg_build_environments(mpsg_dmrg e, int32_t center) {
   API_BEGIN
   MPSG_CHECK(e && e->e, "null engine");

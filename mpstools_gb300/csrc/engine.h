@@ -31,6 +31,9 @@ struct Engine {
   int64_t updates_done() const { return updates_base + (int64_t)steps.size(); }
   LanczosStats lst;
   double env_seconds = 0, split_seconds = 0, env_flops = 0, wall = 0;
+  // wall seconds of doStep before the eigensolver (theta layout, closure and formation) and of the
+  // eigensolver call as a whole (matvec plan, Lanczos, the FP64 energy of MIXED, AUTO's finish)
+  double prep_seconds = 0, lanczos_call_seconds = 0;
 
   static TensorP lmin(Ctx* ctx) {  // getLMin: (0,0;0) = [[1]]
     uint64_t q[2] = {0, 0};
@@ -147,6 +150,7 @@ struct Engine {
                        bool testenergy) {
     MPSG_CHECK(site >= 0 && site + 1 < N, "site out of range");
     MPSG_CHECK(L.count(site - 1) && R.count(site + 2), "environments missing (call prepare first)");
+    const auto tp0 = std::chrono::steady_clock::now();
     const Tensor& Le = *L[site - 1];
     const Tensor& Re = *R[site + 2];
     // theta structure: blocks of BlockMatrix<2>(mps[site], mps[site+1]) and everything the matvec reaches
@@ -187,15 +191,27 @@ struct Engine {
     }
     TensorP th = theta_form(ctx, *mps[site], *mps[site + 1], &sx);
     TensorP psi = make_tensor(ctx, 2, sx, true);
+    const auto tp1 = std::chrono::steady_clock::now();
+    prep_seconds += std::chrono::duration<double>(tp1 - tp0).count();
+    // MIXED: the FP64 energy of psi runs on the side stream beside the split (both only read psi)
+    EnergyJob energy;
     LanczosResult lr = lanczos_prec(ctx, Le, Re, sx, mpo[site], mpo[site + 1], ik[site], ik[site + 1], *th, *psi,
-                                    lanmax, delta, testenergy, reorth, (int)prec, &lst, tstate ? tstate->d : nullptr);
+                                    lanmax, delta, testenergy, reorth, (int)prec, &lst, tstate ? tstate->d : nullptr,
+                                    &energy);
     tstate.reset();
     th.reset();
     auto t0 = std::chrono::steady_clock::now();
+    lanczos_call_seconds += std::chrono::duration<double>(t0 - tp1).count();
     SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
     ctx->sync();
     auto t1 = std::chrono::steady_clock::now();
     split_seconds += std::chrono::duration<double>(t1 - t0).count();
+    if (energy.pending()) {
+      lr.E0 = energy.finish();
+      const auto t2 = std::chrono::steady_clock::now();
+      lanczos_call_seconds += std::chrono::duration<double>(t2 - t1).count();
+      t1 = t2;
+    }
     psi.reset();
     mps[site] = sp.U;
     mps[site + 1] = sp.Vt;

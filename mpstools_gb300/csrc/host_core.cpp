@@ -11,9 +11,20 @@ namespace mpsg {
 thread_local std::string g_last_error;
 
 // ============================================================================ context
+// The library's streams are created at the highest priority, so that kernels queued on the
+// lowest-priority side stream (Ctx::side_stream) only take SMs the main work leaves idle.
+static int stream_priority(bool highest) {
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return highest ? greatest : least;
+}
+
 Ctx::Ctx(int dev) : device(dev) {
   MPSG_CUDA(cudaSetDevice(dev));
-  MPSG_CUDA(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+  MPSG_CUDA(cudaStreamCreateWithPriority(&own, cudaStreamNonBlocking, stream_priority(true)));
   stream = own;
   cudaMemPool_t pool;
   MPSG_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
@@ -30,6 +41,10 @@ Ctx::~Ctx() {
   for (auto h : wblas) cublasDestroy(h);
   if (blas) cublasDestroy(blas);
   for (auto s : wstreams) cudaStreamDestroy(s);
+  if (side) {
+    cudaStreamSynchronize(side);
+    cudaStreamDestroy(side);
+  }
   for (auto e : wevents) cudaEventDestroy(e);
   if (fork_event) cudaEventDestroy(fork_event);
   if (part) cudaFreeAsync(part, stream);
@@ -75,7 +90,7 @@ int Ctx::nworkers() {
   constexpr int kWorkers = 8;
   while ((int)wstreams.size() < kWorkers) {
     cudaStream_t s;
-    MPSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    MPSG_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, stream_priority(true)));
     cusolverDnHandle_t h;
     if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) throw Err(3, "cusolverDnCreate failed");
     cusolverDnSetStream(h, s);
@@ -87,6 +102,10 @@ int Ctx::nworkers() {
     wblas.push_back(b);
   }
   return kWorkers;
+}
+cudaStream_t Ctx::side_stream() {
+  if (!side) MPSG_CUDA(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, stream_priority(false)));
+  return side;
 }
 void Ctx::fork(int n) {
   MPSG_CHECK(n >= 0 && n <= nworkers(), "fork: more streams than workers");

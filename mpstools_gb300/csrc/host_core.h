@@ -40,6 +40,10 @@ struct Ctx : std::enable_shared_from_this<Ctx> {
   void fork(int n);
   void join(int n);
   void sync();
+  // side stream at the lowest priority (the library's own streams run at the highest): work queued
+  // there fills the SMs that the main stream's kernels leave idle
+  cudaStream_t side = nullptr;
+  cudaStream_t side_stream();
 };
 
 // ---------------------------------------------------------------- tensors

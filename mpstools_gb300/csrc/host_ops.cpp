@@ -2,6 +2,7 @@
 // global truncation, right canonicalisation and the GPU Lanczos driver.
 #include "host_ops.h"
 
+#include <limits>
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -2239,9 +2240,76 @@ double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosSta
   return q[0] / q[1];
 }
 
+void EnergyJob::start(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& psi, LanczosStats* s) {
+  release();
+  ctx = c;
+  mv = std::move(plan);
+  st = s;
+  const int64_t n = std::max<int64_t>(psi.nelem, 2);
+  nw = n;
+  buf = (double*)ctx->dmalloc(sizeof(double) * (n + kRedBlocks + 64 + 2));
+  double* w = buf;
+  double* part = buf + n;
+  double* dq = part + kRedBlocks + 64;
+  MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * n, ctx->stream));
+  for (auto& e : ev) MPSG_CUDA(cudaEventCreate(&e));
+  // the side stream starts after everything queued so far (psi, the plan's FP64 tables, buf)
+  cudaStream_t side = ctx->side_stream();
+  MPSG_CUDA(cudaEventRecord(ev[2], ctx->stream));
+  MPSG_CUDA(cudaStreamWaitEvent(side, ev[2], 0));
+  cudaStream_t main = ctx->stream;
+  ctx->stream = side;  // the plan launches on ctx->stream
+  try {
+    MPSG_CUDA(cudaEventRecord(ev[0], side));
+    mv->run(psi.d, w);
+    MPSG_CUDA(cudaEventRecord(ev[1], side));
+    launch_dot(psi.d, w, psi.nelem, part, dq, side);
+    launch_dot(psi.d, psi.d, psi.nelem, part, dq + 1, side);
+    MPSG_CUDA(cudaEventRecord(ev[2], side));
+  } catch (...) {
+    ctx->stream = main;
+    throw;
+  }
+  ctx->stream = main;
+}
+
+double EnergyJob::finish() {
+  MPSG_CHECK(pending(), "energy job not started");
+  MPSG_CUDA(cudaEventSynchronize(ev[2]));
+  float ms = 0;
+  MPSG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+  double q[2] = {0, 0};
+  cudaStream_t side = ctx->side_stream();
+  MPSG_CUDA(cudaMemcpyAsync(q, buf + nw + kRedBlocks + 64, sizeof(q), cudaMemcpyDeviceToHost, side));
+  MPSG_CUDA(cudaStreamSynchronize(side));
+  if (st) {
+    st->matvecs += 1;
+    st->matvec_flops += mv->flops;
+    st->matvec_seconds += ms * 1e-3;
+  }
+  release();
+  MPSG_CHECK(q[1] > 0, "Rayleigh quotient of a zero state");
+  return q[0] / q[1];
+}
+
+void EnergyJob::release() {
+  if (!ctx) return;
+  cudaStreamSynchronize(ctx->side_stream());
+  for (auto& e : ev)
+    if (e) {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
+  ctx->dfree(buf);
+  buf = nullptr;
+  mv.reset();
+  ctx = nullptr;
+}
+
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
-                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj) {
+                           double delta, bool testenergy, bool reorth, int prec, LanczosStats* st, const double* proj,
+                           EnergyJob* energy) {
   if (prec == MPSG_PREC_FP64) {
     auto mv = build_matvec(ctx, L, R, sx, W1, W2, ik0, ik1, &sx, MPSG_PREC_FP64);
     return lanczos(ctx, *mv, th_init, psi, itmax, delta, testenergy, reorth, st, 0.0, 5, 0.0, proj);
@@ -2255,7 +2323,12 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
     // tensor-core matvec scales H by a systematic factor (FP32 accumulation rounds towards zero; at
     // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.
     mv->use_fp64();
-    r.E0 = rayleigh_quotient(ctx, *mv, psi, st);
+    if (energy) {
+      energy->start(ctx, std::move(mv), psi, st);
+      r.E0 = std::numeric_limits<double>::quiet_NaN();
+    } else {
+      r.E0 = rayleigh_quotient(ctx, *mv, psi, st);
+    }
     return r;
   }
   if (prec != MPSG_PREC_AUTO) return r;

@@ -162,6 +162,22 @@ double prec_tol(int prec);
 double prec_stall(int prec);
 // <psi|H|psi> / <psi|psi> with one matvec of the plan (FP64 for MPSG_PREC_MIXED energies).
 double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosStats* st);
+// The same Rayleigh quotient queued on the context's low-priority side stream, so that it runs on
+// the SMs the work queued after it (the split of psi) leaves idle.  psi must stay alive and
+// unchanged until finish(), which waits for the result.
+struct EnergyJob {
+  Ctx* ctx = nullptr;
+  std::unique_ptr<MatvecPlan> mv;
+  LanczosStats* st = nullptr;
+  double* buf = nullptr;  // H psi (nw) | reduction partials | the two dot products
+  int64_t nw = 0;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // matvec start / end, dots done
+  bool pending() const { return ctx != nullptr; }
+  void start(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& psi, LanczosStats* s);
+  double finish();
+  void release();
+  ~EnergyJob() { release(); }
+};
 LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& psi, int itmax, double delta,
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
                       double stall_rel = 0.0, const double* proj = nullptr);
@@ -171,6 +187,7 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
                            double delta, bool testenergy, bool reorth, int prec, LanczosStats* st,
-                           const double* proj = nullptr);  // proj: state the Krylov space stays orthogonal to
+                           const double* proj = nullptr,  // proj: state the Krylov space stays orthogonal to
+                           EnergyJob* energy = nullptr);  // MIXED: E0 left to energy->finish()
 
 }  // namespace mpsg

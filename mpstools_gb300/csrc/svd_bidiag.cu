@@ -3,10 +3,11 @@
 // one launch over all sectors of the split:
 //   1. k_gebrd<CL>   Householder bidiagonalisation A = Q B P^T (Golub & Kahan; Golub & Van Loan,
 //                    Matrix Computations, section 5.4.8).  One thread-block cluster of CL CTAs per
-//                    sector, the columns round-robin in shared memory; per column two cluster barriers:
-//                    the left reflector is pulled from the CTA that owns the column, the right
-//                    reflector of the row is formed from partial products every CTA pushes through
-//                    distributed shared memory.
+//                    sector, the columns round-robin in shared memory (in global memory for sectors
+//                    too large for that); per column two or three cluster barriers: the left
+//                    reflector is pulled from the CTA that owns the column, the right reflector of
+//                    the row is formed from partial products every CTA pushes through distributed
+//                    shared memory, each CTA summing the partials of a slice of the rows.
 //   2. k_gk_setup    the Golub-Kahan tridiagonal T = [[0, B], [B^T, 0]] (rows interleaved, zero
 //                    diagonal; eigenvalues +-sigma), scaled by a power of two.
 //   3. k_gk_cut_*    per truncation segment: Sturm counts of all sectors at 32 points per round
@@ -87,8 +88,8 @@ __device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v
 // GM = false: the CTA's columns live in shared memory; GM = true (sectors too large for that): they
 // are worked on in place in the sector matrix in global memory (L2-resident), only the reduction
 // buffers stay in shared memory.  The arithmetic is the same.
-template <int CL, bool GM>
-__global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) {
+template <int CL, bool GM, int NT>
+__global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
   const GebrdOp o = ops[blockIdx.x / CL];
@@ -128,10 +129,27 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     if (tau != 0.0) {
       for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
         double* a = cols + (size_t)lc * ldc;
-        double s = 0.0;
-        for (int i = j + lane; i < m; i += 32) s = fma(v[i], a[i], s);
-        const double w = warp_sum(s) * tau;
-        for (int i = j + lane; i < m; i += 32) a[i] = fma(-v[i], w, a[i]);
+        // four independent loads and partial sums in flight per lane (the global-memory variant waits
+        // on L2 latency otherwise)
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int i = j + lane;
+        for (; i + 96 < m; i += 128) {
+          s0 = fma(v[i], a[i], s0);
+          s1 = fma(v[i + 32], a[i + 32], s1);
+          s2 = fma(v[i + 64], a[i + 64], s2);
+          s3 = fma(v[i + 96], a[i + 96], s3);
+        }
+        for (; i < m; i += 32) s0 = fma(v[i], a[i], s0);
+        const double w = warp_sum((s0 + s1) + (s2 + s3)) * tau;
+        i = j + lane;
+        for (; i + 96 < m; i += 128) {
+          const double a0 = a[i], a1 = a[i + 32], a2 = a[i + 64], a3 = a[i + 96];
+          a[i] = fma(-v[i], w, a0);
+          a[i + 32] = fma(-v[i + 32], w, a1);
+          a[i + 64] = fma(-v[i + 64], w, a2);
+          a[i + 96] = fma(-v[i + 96], w, a3);
+        }
+        for (; i < m; i += 32) a[i] = fma(-v[i], w, a[i]);
       }
     }
     __syncthreads();
@@ -182,10 +200,18 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
       taup = (beta - alpha) / beta;
       sc = 1.0 / (alpha - beta);
     }
+    // z_i = taup (A(i, j+1) + sum_{c >= j+2} A(i, c) u_c), u_c = A(j, c) sc.  With 8 or more CTAs
+    // each sums the partials of one slice of the rows (the sum of CL partials per row is FP64 work
+    // of the order of the update itself) and the slices are exchanged after a cluster barrier;
+    // smaller clusters sum all rows in every CTA.  Either way z_i is the same fixed-order sum.
+    constexpr bool kSliced = CL >= 8;
+    const int zlen = m - (j + 1);
+    const int zcs = kSliced ? (zlen + CL - 1) / CL : zlen;
     if (taup != 0.0) {
-      // z_i = taup (A(i, j+1) + sum_{c >= j+2} A(i, c) u_c), u_c = A(j, c) sc
       const double* rcb = cluster.map_shared_rank(cb, on);
-      for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+      const int i0 = j + 1 + (kSliced ? r * zcs : 0);
+      const int i1 = kSliced ? min(m, i0 + zcs) : m;
+      for (int i = i0 + tid; i < i1; i += blockDim.x) {
         double part[CL];  // all CL remote loads in flight before the (fixed-order) sum
 #pragma unroll
         for (int q = 0; q < CL; ++q) part[q] = cluster.map_shared_rank(zp, q)[i];
@@ -199,6 +225,14 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
         ub[lc] = u;
         o.Pr[(r + lc * CL) + (int64_t)j * o.n] = u;
       }
+    }
+    if (kSliced) {
+      cluster.sync();  // #1b: every CTA's slice of z (taup is the same in every CTA)
+      if (taup != 0.0)
+        for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+          const int q = (i - (j + 1)) / zcs;
+          if (q != r) z[i] = cluster.map_shared_rank(z, q)[i];
+        }
     }
     __syncthreads();
     // (d) A(i, c) -= z_i u_c for i > j on the own columns c >= j+1; the owner of column j+1 updates
@@ -219,20 +253,29 @@ __global__ void __launch_bounds__(256) k_gebrd(const GebrdOp* __restrict__ ops) 
     if (taup != 0.0 && tid >= p0) {
       for (int i = j + 1 + tid - p0; i < m; i += (int)blockDim.x - p0) {
         const double zi = z[i];
-        for (int lc = lc2; lc < ncol; ++lc) cols[(size_t)lc * ldc + i] = fma(-zi, ub[lc], cols[(size_t)lc * ldc + i]);
+        int lc = lc2;
+        for (; lc + 3 < ncol; lc += 4) {  // four loads in flight before the stores
+          double* a = cols + (size_t)lc * ldc + i;
+          const double a0 = a[0], a1 = a[ldc], a2 = a[2 * ldc], a3 = a[3 * ldc];
+          a[0] = fma(-zi, ub[lc], a0);
+          a[ldc] = fma(-zi, ub[lc + 1], a1);
+          a[2 * ldc] = fma(-zi, ub[lc + 2], a2);
+          a[3 * ldc] = fma(-zi, ub[lc + 3], a3);
+        }
+        for (; lc < ncol; ++lc) cols[(size_t)lc * ldc + i] = fma(-zi, ub[lc], cols[(size_t)lc * ldc + i]);
       }
     }
     cluster.sync();  // #2: columns updated, reflector j+1 ready on its owner, partials consumed
   }
 }
 
-template <int CL, bool GM>
+template <int CL, bool GM, int NT = 256>
 static void launch_gebrd_cl(const GebrdOp* ops, int nops, size_t smem, cudaStream_t s) {
-  MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_gebrd<CL, GM, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nops * CL);
-  cfg.blockDim = dim3(256);
+  cfg.blockDim = dim3(NT);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
@@ -242,7 +285,7 @@ static void launch_gebrd_cl(const GebrdOp* ops, int nops, size_t smem, cudaStrea
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_gebrd<CL, GM>, ops));
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_gebrd<CL, GM, NT>, ops));
   g_bd_launches.fetch_add(1);
 }
 
@@ -253,6 +296,23 @@ static int gebrd_cl_cap() {
     return (v == 1 || v == 2 || v == 4 || v == 8) ? v : 16;
   }();
   return cap;
+}
+
+static int gebrd_gm_threads() {
+  static int nt = [] {
+    const char* e = std::getenv("MPSG_GEBRD_GM_THREADS");
+    const int v = e ? std::atoi(e) : 512;
+    return (v == 256 || v == 1024) ? v : 512;
+  }();
+  return nt;
+}
+static int gebrd_sm_threads() {
+  static int nt = [] {
+    const char* e = std::getenv("MPSG_GEBRD_THREADS");
+    const int v = e ? std::atoi(e) : 256;
+    return v == 512 ? 512 : 256;
+  }();
+  return nt;
 }
 
 // Cluster size of a sector: CL in 1..16 for the shared-memory kernel, kGebrdGlobal + CL for the
@@ -281,13 +341,26 @@ void launch_gebrd(const GebrdOp* ops, int nops, int code, size_t smem, cudaStrea
     case 1: launch_gebrd_cl<1, false>(ops, nops, smem, s); break;
     case 2: launch_gebrd_cl<2, false>(ops, nops, smem, s); break;
     case 4: launch_gebrd_cl<4, false>(ops, nops, smem, s); break;
-    case 8: launch_gebrd_cl<8, false>(ops, nops, smem, s); break;
-    case 16: launch_gebrd_cl<16, false>(ops, nops, smem, s); break;
+    case 8:
+      if (gebrd_sm_threads() == 512) launch_gebrd_cl<8, false, 512>(ops, nops, smem, s);
+      else launch_gebrd_cl<8, false>(ops, nops, smem, s);
+      break;
+    case 16:
+      if (gebrd_sm_threads() == 512) launch_gebrd_cl<16, false, 512>(ops, nops, smem, s);
+      else launch_gebrd_cl<16, false>(ops, nops, smem, s);
+      break;
     case kGebrdGlobal + 1: launch_gebrd_cl<1, true>(ops, nops, smem, s); break;
     case kGebrdGlobal + 2: launch_gebrd_cl<2, true>(ops, nops, smem, s); break;
     case kGebrdGlobal + 4: launch_gebrd_cl<4, true>(ops, nops, smem, s); break;
     case kGebrdGlobal + 8: launch_gebrd_cl<8, true>(ops, nops, smem, s); break;
-    case kGebrdGlobal + 16: launch_gebrd_cl<16, true>(ops, nops, smem, s); break;
+    case kGebrdGlobal + 16:
+      // threads of the global-memory variant: more warps hide the L2 latency of its column accesses
+      switch (gebrd_gm_threads()) {
+        case 256: launch_gebrd_cl<16, true, 256>(ops, nops, smem, s); break;
+        case 512: launch_gebrd_cl<16, true, 512>(ops, nops, smem, s); break;
+        default: launch_gebrd_cl<16, true, 1024>(ops, nops, smem, s); break;
+      }
+      break;
     default: throw Err(1, "bidiagonalisation: unsupported cluster size");
   }
 }

@@ -65,6 +65,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_nsteps.argtypes = [vp]
     L.mpsg_dmrg_steps.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.mpsg_dmrg_stats.argtypes = [vp, vp]
+    L.mpsg_dmrg_stats_ext.argtypes = [vp, vp, C.c_int32]
     L.mpsg_dmrg_site.argtypes = [vp, i32, P(vp)]
     L.mpsg_dmrg_lambda.argtypes = [vp, i32, P(vp)]
     L.mpsg_dmrg_measure_energy.argtypes = [vp, P(f64)]
