@@ -1127,48 +1127,69 @@ struct SvdBatch {
   // larger pairs); otherwise X = Vst (ns x ns).  Each pass leaves X orthonormal to ~eps cond(X)^2.
   // failed (optional): sectors whose Cholesky met a non-positive pivot are appended instead of throwing
   // ub_rows: the left matrix holds U_B (ns rows, zero below): only its first ns rows are processed
+  struct CholSide {
+    bool left, scale_s, ub_rows;
+  };
   void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true, bool ub_rows = false) {
-    std::vector<int> idx;
+    cholqr_sides({CholSide{left, scale_s, ub_rows}}, passes, failed);
+  }
+  // CholeskyQR of several sides (U and / or V of every sector) in the same launches: the Gram
+  // matrices in one grouped GEMM, the Cholesky factorisations in one launch per cluster size, the
+  // blocked substitution in one GEMM + one substitution launch per 64-column block.
+  void cholqr_sides(const std::vector<CholSide>& sides, int passes, std::vector<int>* failed) {
+    struct Prob {
+      int i;  // sector
+      const CholSide* sd;
+      int base;  // operand slot of X: 0 = dU, 3 = dV
+      int64_t offX, offC, offR;
+      int ldx, rows, kc;
+    };
+    std::vector<Prob> ps;
     int kmax = 0;
-    for (size_t i = 0; i < s.size(); ++i)
-      if (kcols(i) > 0) {
-        idx.push_back((int)i);
-        kmax = std::max(kmax, kcols(i));
+    int64_t oC = 0, oR = 0;
+    for (const CholSide& sd : sides)
+      for (size_t i = 0; i < s.size(); ++i) {
+        const int kc = kcols(i);
+        if (kc <= 0) continue;
+        Prob p;
+        p.i = (int)i;
+        p.sd = &sd;
+        p.base = sd.left ? 0 : 3;
+        p.offX = sd.left ? s[i].offU : s[i].offV;
+        p.ldx = sd.left ? s[i].ms : s[i].ns;
+        p.rows = sd.left && !sd.ub_rows ? s[i].ms : s[i].ns;
+        p.kc = kc;
+        p.offC = oC;
+        oC += ((int64_t)kc * kc + kAlign - 1) / kAlign * kAlign;
+        p.offR = oR;
+        oR += kc;
+        ps.push_back(p);
+        kmax = std::max(kmax, kc);
       }
-    if (idx.empty()) return;
+    if (ps.empty()) return;
     MPSG_CHECK(kmax <= chol_max_k(), "CholeskyQR: sector wider than the cluster kernel's limit");
     cudaStream_t st = ctx->stream;
-    double* X = left ? dU : dV;
-    auto rows = [&](int i) { return left && !ub_rows ? s[i].ms : s[i].ns; };
-    auto ldx = [&](int i) { return left ? s[i].ms : s[i].ns; };
-    auto offX = [&](int i) { return left ? s[i].offU : s[i].offV; };
-    std::vector<int64_t> offC(s.size(), 0);
-    int64_t oC = 0;
-    for (int i : idx) {
-      offC[i] = oC;
-      oC += ((int64_t)kcols(i) * kcols(i) + kAlign - 1) / kAlign * kAlign;
-    }
     double* dC = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
-    double* dR = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nS, 2));  // 1 / R_jj
-    int* dinf = (int*)ctx->dmalloc(sizeof(int) * idx.size());
-    MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * idx.size(), st));
+    double* dR = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oR, 2));  // 1 / R_jj
+    int* dinf = (int*)ctx->dmalloc(sizeof(int) * ps.size());
+    MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * ps.size(), st));
     GemmPlan g;
-    for (int i : idx)
-      g.add_problem(2, offC[i], kcols(i), kcols(i), kcols(i), false,
-                    {GSegH{0, 0, offX(i), offX(i), ldx(i), ldx(i), rows(i), 1, 0, 1.0}});
+    for (const Prob& p : ps)
+      g.add_problem(2, p.offC, p.kc, p.kc, p.kc, false,
+                    {GSegH{p.base, p.base, p.offX, p.offX, p.ldx, p.ldx, p.rows, 1, 0, 1.0}});
     g.upload(ctx);
     std::vector<CholOp> zd;
     std::map<int, std::vector<CholQROp>> byCL[2];
     std::map<int, int> kmaxCL;
-    for (size_t t = 0; t < idx.size(); ++t) {
-      const int i = idx[t];
-      const int kc = kcols(i);
-      zd.push_back(CholOp{dC + offC[i], nullptr, kc, kc});
-      const int CL = chol_cluster_size(kc);
+    for (size_t t = 0; t < ps.size(); ++t) {
+      const Prob& p = ps[t];
+      zd.push_back(CholOp{dC + p.offC, nullptr, p.kc, p.kc});
+      const int CL = chol_cluster_size(p.kc);
       for (int pass = 0; pass < 2; ++pass)
-        byCL[pass][CL].push_back(CholQROp{dC + offC[i], dR + s[i].offS, (pass == 0 && left && scale_s) ? dS + s[i].offS : nullptr,
-                                          dinf + t, kc, kc});
-      kmaxCL[CL] = std::max(kmaxCL[CL], kc);
+        byCL[pass][CL].push_back(CholQROp{dC + p.offC, dR + p.offR,
+                                          (pass == 0 && p.sd->left && p.sd->scale_s) ? dS + s[p.i].offS : nullptr,
+                                          dinf + t, p.kc, p.kc});
+      kmaxCL[CL] = std::max(kmaxCL[CL], p.kc);
     }
     // X <- X R^-1 by 64-column blocks: X_b -= X_<b R_<b,b (grouped GEMM), then X_b <- X_b R_bb^-1
     // (row-parallel substitution over 64 columns)
@@ -1178,16 +1199,17 @@ struct SvdBatch {
     std::vector<std::vector<TrsmRowsOp>> tr(nblk);
     for (int b = 0; b < nblk; ++b) {
       upd[b].reset(new GemmPlan());
-      for (int i : idx) {
-        const int c0 = b * kTB, kc = kcols(i);
+      for (const Prob& p : ps) {
+        const int c0 = b * kTB, kc = p.kc;
         if (c0 >= kc) continue;
         const int bw = std::min(kTB, kc - c0);
+        double* X = p.base == 0 ? dU : dV;
         if (b > 0)
-          upd[b]->add_problem(2, offX(i) + (int64_t)c0 * ldx(i), ldx(i), rows(i), bw, true,
-                              {GSegH{0, 1, offX(i), offC[i] + (int64_t)c0 * kc, ldx(i), kc, c0, 0, 0, -1.0}});
-        for (int r0 = 0; r0 < rows(i); r0 += 32)
-          tr[b].push_back(TrsmRowsOp{X + offX(i) + (int64_t)c0 * ldx(i), dC + offC[i] + c0 + (int64_t)c0 * kc,
-                                     dR + s[i].offS + c0, bw, ldx(i), kc, r0, std::min(r0 + 32, rows(i))});
+          upd[b]->add_problem(p.base, p.offX + (int64_t)c0 * p.ldx, p.ldx, p.rows, bw, true,
+                              {GSegH{p.base, 1, p.offX, p.offC + (int64_t)c0 * kc, p.ldx, kc, c0, 0, 0, -1.0}});
+        for (int r0 = 0; r0 < p.rows; r0 += 32)
+          tr[b].push_back(TrsmRowsOp{X + p.offX + (int64_t)c0 * p.ldx, dC + p.offC + c0 + (int64_t)c0 * kc,
+                                     dR + p.offR + c0, bw, p.ldx, kc, r0, std::min(r0 + 32, p.rows)});
       }
       upd[b]->upload(ctx);
     }
@@ -1212,8 +1234,8 @@ struct SvdBatch {
       for (auto& c : byCL[pass]) dch[pass][c.first] = (CholQROp*)put(c.second.data(), sizeof(CholQROp) * c.second.size());
     MPSG_CHECK(off <= bytes + 64, "CholeskyQR descriptor overflow");
     MPSG_CUDA(cudaMemcpyAsync(dops, hops.data(), off, cudaMemcpyHostToDevice, st));
+    const double* bases[8] = {dU, dC, dC, dV, nullptr, nullptr, nullptr, nullptr};
     for (int pass = 0; pass < passes; ++pass) {
-      const double* bases[8] = {X, nullptr, dC, nullptr, nullptr, nullptr, nullptr, nullptr};
       g.run(bases);
       launch_chol_unit_zero_diag(dzd, (int)zd.size(), st);
       const int which = pass == 0 ? 0 : 1;
@@ -1226,30 +1248,30 @@ struct SvdBatch {
                       ctx->wstreams[j % nw]);
         ctx->join(nw);
       }
-      const double* tb[8] = {X, dC, X, nullptr, nullptr, nullptr, nullptr, nullptr};
       for (int b = 0; b < nblk; ++b) {
-        if (b > 0) upd[b]->run(tb);
+        if (b > 0) upd[b]->run(bases);
         launch_trsm_rows(dtr[b], (int)tr[b].size(), kTB, st);
       }
     }
-    std::vector<int> inf(idx.size(), 0);
+    std::vector<int> inf(ps.size(), 0);
     MPSG_CUDA(cudaMemcpyAsync(inf.data(), dinf, sizeof(int) * inf.size(), cudaMemcpyDeviceToHost, st));
     ctx->sync();
     ctx->dfree(dops);
     ctx->dfree(dinf);
     ctx->dfree(dR);
     ctx->dfree(dC);
-    for (size_t t = 0; t < idx.size(); ++t)
+    for (size_t t = 0; t < ps.size(); ++t)
       if (inf[t] != 0) {
+        const Prob& p = ps[t];
         if (failed) {
-          failed->push_back(idx[t]);
+          failed->push_back(p.i);
           continue;
         }
-        const Sec& x = s[idx[t]];
-        throw Err(3, std::string("CholeskyQR of ") + (left ? "U" : "V") +
+        const Sec& x = s[p.i];
+        throw Err(3, std::string("CholeskyQR of ") + (p.sd->left ? "U" : "V") +
                          ": the Gram matrix of the singular vectors is not positive definite (sector " +
-                         std::to_string(idx[t]) + " of " + std::to_string(s.size()) + ", " + std::to_string(x.ms) +
-                         " x " + std::to_string(x.ns) + ", " + std::to_string(kcols(idx[t])) +
+                         std::to_string(p.i) + " of " + std::to_string(s.size()) + ", " + std::to_string(x.ms) +
+                         " x " + std::to_string(x.ns) + ", " + std::to_string(kcols(p.i)) +
                          " resolved columns, column " + std::to_string(inf[t] - 1) + ")");
       }
   }
@@ -1466,8 +1488,7 @@ struct SvdBatch {
         failed.push_back(i);
         kr[i] = 0;
       }
-    cholqr(true, 1, &failed, false, true);
-    cholqr(false, 1, &failed, false);
+    cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed);
     // 7. U = Q [U_B; 0], V = P V_B
     {
       std::vector<ReflOp> ro;
