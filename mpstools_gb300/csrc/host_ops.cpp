@@ -1353,30 +1353,95 @@ struct SvdBatch {
     bd.kept = bd.kcomp + nop;
     bd.opseg = bd.kept + nop;
     bd.seg = bd.opseg + nop;
-    // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first)
+    // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first);
+    //    the largest global-memory sectors on two clusters each, in a launch of their own
     {
       std::map<int, std::vector<GebrdOp>> byCL;
       std::map<int, size_t> smem;  // per cluster-size code, the largest of its sectors' needs
+      std::vector<GebrdOp> mc;
+      std::vector<int> mc_sec;
+      size_t mc_smem = 0;
       for (int i : bd.idx) {
         const Sec& x = s[i];
+        const GebrdOp op{dM + x.offM, bd.d + x.offS, bd.e + x.offS, bd.tq + x.offS, bd.tp + x.offS,
+                         bd.Pr + bd.offPr[i], x.ms, x.ns, x.ms};
+        if (gebrd_mc_clusters(x.ms, x.ns) == 2 && (int)mc.size() < gebrd_mc_capacity()) {
+          mc.push_back(op);
+          mc_sec.push_back(i);
+          mc_smem = std::max(mc_smem, gebrd_mc_smem(x.ms, x.ns, 2));
+          continue;
+        }
         const int CL = gebrd_cluster_size(x.ms, x.ns);
-        byCL[CL].push_back(GebrdOp{dM + x.offM, bd.d + x.offS, bd.e + x.offS, bd.tq + x.offS, bd.tp + x.offS,
-                                   bd.Pr + bd.offPr[i], x.ms, x.ns, x.ms});
+        byCL[CL].push_back(op);
         smem[CL] = std::max(smem[CL], gebrd_smem(x.ms, x.ns, CL));
       }
+      // two-cluster sectors: exchange buffers, barrier counters (zero) and the error flag
+      double* mcbuf = nullptr;
+      unsigned* mcctr = nullptr;
+      if (!mc.empty()) {
+        size_t nxg = 0;
+        for (auto& op : mc) nxg += gebrd_mc_xg_doubles(op.m, 2);
+        mcbuf = (double*)ctx->dmalloc(sizeof(double) * nxg + sizeof(unsigned) * (mc.size() + 1) + 16);
+        mcctr = (unsigned*)(mcbuf + nxg);
+        MPSG_CUDA(cudaMemsetAsync(mcctr, 0, sizeof(unsigned) * (mc.size() + 1), st));
+        size_t o = 0;
+        for (size_t t = 0; t < mc.size(); ++t) {
+          mc[t].xg = mcbuf + o;
+          o += gebrd_mc_xg_doubles(mc[t].m, 2);
+          mc[t].ctr = mcctr + t;
+          mc[t].err = (int*)(mcctr + mc.size());
+        }
+      }
       std::vector<std::pair<int, GebrdOp*>> bufs;
-      for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) {
-        GebrdOp* dptr = (GebrdOp*)ctx->dmalloc(sizeof(GebrdOp) * it->second.size());
-        MPSG_CUDA(cudaMemcpyAsync(dptr, it->second.data(), sizeof(GebrdOp) * it->second.size(), cudaMemcpyHostToDevice,
-                                  st));
-        bufs.push_back({it->first, dptr});
+      if (!mc.empty()) bufs.push_back({-2, nullptr});
+      for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) bufs.push_back({it->first, nullptr});
+      for (auto& b : bufs) {
+        const std::vector<GebrdOp>& v = b.first == -2 ? mc : byCL[b.first];
+        b.second = (GebrdOp*)ctx->dmalloc(sizeof(GebrdOp) * v.size());
+        MPSG_CUDA(cudaMemcpyAsync(b.second, v.data(), sizeof(GebrdOp) * v.size(), cudaMemcpyHostToDevice, st));
       }
       const int nw = std::min<int>((int)bufs.size(), ctx->nworkers());
       ctx->fork(nw);
-      for (size_t j = 0; j < bufs.size(); ++j)
-        launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, smem[bufs[j].first],
-                     ctx->wstreams[j % nw]);
+      for (size_t j = 0; j < bufs.size(); ++j) {
+        if (bufs[j].first == -2) launch_gebrd_mc(bufs[j].second, (int)mc.size(), 2, mc_smem, ctx->wstreams[j % nw]);
+        else
+          launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, smem[bufs[j].first],
+                       ctx->wstreams[j % nw]);
+      }
       ctx->join(nw);
+      if (!mc.empty()) {
+        // a two-cluster sector whose barrier wait expired is redone on one cluster from the copy
+        int err = 0;
+        MPSG_CUDA(cudaMemcpyAsync(&err, mcctr + mc.size(), sizeof(int), cudaMemcpyDeviceToHost, st));
+        ctx->sync();
+        if (err) {
+          g_split_fallbacks.fetch_add((int64_t)mc.size());
+          if (std::getenv("MPSG_VERBOSE"))
+            std::fprintf(stderr, "libmpsg: two-cluster bidiagonalisation timed out; redone on one cluster\n");
+          std::map<int, std::vector<GebrdOp>> re;
+          std::map<int, size_t> resm;
+          for (size_t t = 0; t < mc.size(); ++t) {
+            const Sec& x = s[mc_sec[t]];
+            MPSG_CUDA(cudaMemcpyAsync(dM + x.offM, bd.Mcopy + x.offM, sizeof(double) * (size_t)x.ms * x.ns,
+                                      cudaMemcpyDeviceToDevice, st));
+            const int CL = gebrd_cluster_size(x.ms, x.ns);
+            GebrdOp op = mc[t];
+            op.xg = nullptr;
+            op.ctr = nullptr;
+            op.err = nullptr;
+            re[CL].push_back(op);
+            resm[CL] = std::max(resm[CL], gebrd_smem(x.ms, x.ns, CL));
+          }
+          for (auto& kv : re) {
+            GebrdOp* dp = (GebrdOp*)ctx->dmalloc(sizeof(GebrdOp) * kv.second.size());
+            MPSG_CUDA(cudaMemcpyAsync(dp, kv.second.data(), sizeof(GebrdOp) * kv.second.size(), cudaMemcpyHostToDevice,
+                                      st));
+            launch_gebrd(dp, (int)kv.second.size(), kv.first, resm[kv.first], st);
+            ctx->dfree(dp);
+          }
+        }
+        ctx->dfree(mcbuf);
+      }
       for (auto& b : bufs) ctx->dfree(b.second);
     }
     // 2.-4. Golub-Kahan matrices, the cut of each segment, the singular values above it

@@ -195,6 +195,11 @@ struct GebrdOp {  // m x n (m >= n) sector matrix A (lda) -> B = Q^T A P upper b
   double* taup;   // n (taup[n-1] unused)
   double* Pr;     // n x n (ld n): column j = tail of right reflector j at rows j+2.. (unit at row j+1)
   int32_t m, n, lda;
+  // sectors spread over several clusters (k_gebrd_mc): exchange buffers (gebrd_mc_xg_doubles), the
+  // sector's barrier counter (zero at launch) and the launch's error flag (set when a wait expired)
+  double* xg = nullptr;
+  unsigned int* ctr = nullptr;
+  int* err = nullptr;
 };
 struct GkOp {  // Golub-Kahan tridiagonal [[0, B], [B^T, 0]] (interleaved, zero diagonal) of one sector
   const double* d;    // n (bidiagonal)
@@ -344,6 +349,13 @@ void launch_scombine(double* y, const double* const* V, const int* nv_of, const 
                      const int64_t* segoff, int nseg, cudaStream_t s);
 // bidiagonal SVD (svd_bidiag.cu)
 int gebrd_cluster_size(int m, int n);  // 0: the sector does not fit the cluster kernel
+// clusters of 16 CTAs for a global-memory sector (1 or 2) and the doubles of its exchange buffers
+int gebrd_mc_clusters(int m, int n);
+size_t gebrd_mc_xg_doubles(int m, int clusters);
+size_t gebrd_mc_smem(int m, int n, int clusters);  // dynamic shared memory of one sector's CTAs
+int gebrd_mc_capacity();  // two-cluster sectors that can be resident at once
+// the sectors of ops (all with gebrd_mc_clusters == clusters) on clusters x 16 CTAs each
+void launch_gebrd_mc(const GebrdOp* ops, int nops, int clusters, size_t smem, cudaStream_t s);
 size_t gebrd_smem(int m, int n, int code);  // dynamic shared memory of one sector's CTAs
 void launch_gebrd(const GebrdOp* ops, int nops, int code, size_t smem, cudaStream_t s);
 void launch_gk_setup(const GkOp* ops, int nops, cudaStream_t s);

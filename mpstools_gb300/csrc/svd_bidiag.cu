@@ -41,22 +41,24 @@ static std::atomic<int64_t> g_bd_launches{0};
 int64_t bidiag_launch_count() { return g_bd_launches.load(); }
 
 // ----------------------------------------------------------------------------- 1. bidiagonalisation
-// Shared memory of one CTA: own columns (ncol x m) | v (m) | zp (m) | cb (m) | z (m) | ub (ncol) | scal (8)
+// Shared memory of one CTA: own columns (ncol x m) | v (m) | zp (m) | cb (m) | z (m) | ub (ncol) | scal (16)
 static __host__ __device__ size_t gebrd_smem_doubles(int m, int n, int CL) {
   const int ncol = (n + CL - 1) / CL;
-  return (size_t)ncol * m + 4 * (size_t)m + (size_t)ncol + 8;
+  return (size_t)ncol * m + 4 * (size_t)m + (size_t)ncol + 16;
 }
 static size_t gebrd_smem_bytes(int m, int n, int CL) { return sizeof(double) * gebrd_smem_doubles(m, n, CL); }
 // the global-memory variant keeps only the reduction buffers in shared memory
 static __host__ __device__ size_t gebrd_gm_smem_doubles(int m, int n, int CL) {
-  return 4 * (size_t)m + (size_t)((n + CL - 1) / CL) + 8;
+  return 4 * (size_t)m + (size_t)((n + CL - 1) / CL) + 16;
 }
 constexpr int kGebrdGlobal = 100;  // cluster-size code offset of the global-memory variant
 
-// Left reflector of column j (the calling warp's CTA holds it as `col`; rows j..m-1 are current):
-// v (v[j] = 1) into the CTA's v buffer, tau into scal[0]; the reflector's tail into column j of A,
-// tauq[j] and d[j] = beta.
-__device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v, double* scal, int lane) {
+// Left reflector of column j (`col`, rows j..m-1 current): v (v[j] = 1) into the CTA's v buffer, tau
+// into scal[0]; with store (the owner of the column) the reflector's tail into column j of A,
+// tauq[j] and d[j] = beta.  Every CTA computes the reflector from the same values with the same
+// operations, so the copies agree bit for bit.
+__device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v, double* scal, int lane,
+                           bool store = true) {
   const int m = o.m;
   double s2a = 0.0, s2b = 0.0;
   int i0 = j + 1 + lane;
@@ -76,12 +78,90 @@ __device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v
   for (int i = j + lane; i < m; i += 32) {
     const double x = (i == j) ? 1.0 : col[i] * scale;
     v[i] = x;
-    if (i > j) o.A[i + (int64_t)j * o.lda] = x;
+    if (store && i > j) o.A[i + (int64_t)j * o.lda] = x;
   }
   if (lane == 0) {
     scal[0] = tau;
-    o.tauq[j] = tau;
-    o.d[j] = beta;
+    if (store) {
+      o.tauq[j] = tau;
+      o.d[j] = beta;
+    }
+  }
+}
+
+// Column passes shared by the bidiagonalisation kernels.  The CTA's own columns are cols + lc * ldc,
+// lc < ncol; lc1 / lc2 = first own column at or past global column j + 1 / j + 2.
+// (a) A(j:m, c) -= v tau (v^T A(j:m, c)) on the own columns lc >= lc1, one warp per column; four
+//     independent loads and partial sums in flight per lane (the global-memory variants wait on L2
+//     latency otherwise).
+__device__ __forceinline__ void gebrd_apply_left(double* cols, int64_t ldc, const double* v, double tau, int j, int m,
+                                                 int lc1, int ncol, int warp, int nwarp, int lane) {
+  for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
+    double* a = cols + (size_t)lc * ldc;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = j + lane;
+    for (; i + 96 < m; i += 128) {
+      s0 = fma(v[i], a[i], s0);
+      s1 = fma(v[i + 32], a[i + 32], s1);
+      s2 = fma(v[i + 64], a[i + 64], s2);
+      s3 = fma(v[i + 96], a[i + 96], s3);
+    }
+    for (; i < m; i += 32) s0 = fma(v[i], a[i], s0);
+    const double w = warp_sum((s0 + s1) + (s2 + s3)) * tau;
+    i = j + lane;
+    for (; i + 96 < m; i += 128) {
+      const double a0 = a[i], a1 = a[i + 32], a2 = a[i + 64], a3 = a[i + 96];
+      a[i] = fma(-v[i], w, a0);
+      a[i + 32] = fma(-v[i + 32], w, a1);
+      a[i + 64] = fma(-v[i + 64], w, a2);
+      a[i + 96] = fma(-v[i + 96], w, a3);
+    }
+    for (; i < m; i += 32) a[i] = fma(-v[i], w, a[i]);
+  }
+}
+// (b) zp_i = sum over the own columns lc >= lc2 of A(i, c) A(j, c), rows j < i < m, thread t of nt
+//     (four independent partial sums per row)
+__device__ __forceinline__ void gebrd_row_partials(const double* cols, int64_t ldc, double* zp, int j, int m, int lc2,
+                                                   int ncol, int t, int nt) {
+  for (int i = j + 1 + t; i < m; i += nt) {
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+    int lc = lc2;
+    for (; lc + 3 < ncol; lc += 4) {
+      acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
+      acc1 = fma(cols[(size_t)(lc + 1) * ldc + i], cols[(size_t)(lc + 1) * ldc + j], acc1);
+      acc2 = fma(cols[(size_t)(lc + 2) * ldc + i], cols[(size_t)(lc + 2) * ldc + j], acc2);
+      acc3 = fma(cols[(size_t)(lc + 3) * ldc + i], cols[(size_t)(lc + 3) * ldc + j], acc3);
+    }
+    for (; lc < ncol; ++lc) acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
+    zp[i] = (acc0 + acc1) + (acc2 + acc3);
+  }
+}
+// the own part of |A(j, c >= j+2)|^2 (one warp; the sum is in every lane)
+__device__ __forceinline__ double gebrd_row_norm_partial(const double* cols, int64_t ldc, int j, int lc2, int ncol,
+                                                         int lane) {
+  double s = 0.0;
+  for (int lc = lc2 + lane; lc < ncol; lc += 32) {
+    const double x = cols[(size_t)lc * ldc + j];
+    s = fma(x, x, s);
+  }
+  return warp_sum(s);
+}
+// (d) A(i, c) -= z_i u_c for rows j < i < m on the own columns lc >= lc2, thread t of nt (four loads
+//     in flight before the stores)
+__device__ __forceinline__ void gebrd_apply_right(double* cols, int64_t ldc, const double* z, const double* ub, int j,
+                                                  int m, int lc2, int ncol, int t, int nt) {
+  for (int i = j + 1 + t; i < m; i += nt) {
+    const double zi = z[i];
+    int lc = lc2;
+    for (; lc + 3 < ncol; lc += 4) {
+      double* a = cols + (size_t)lc * ldc + i;
+      const double a0 = a[0], a1 = a[ldc], a2 = a[2 * ldc], a3 = a[3 * ldc];
+      a[0] = fma(-zi, ub[lc], a0);
+      a[ldc] = fma(-zi, ub[lc + 1], a1);
+      a[2 * ldc] = fma(-zi, ub[lc + 2], a2);
+      a[3 * ldc] = fma(-zi, ub[lc + 3], a3);
+    }
+    for (; lc < ncol; ++lc) cols[(size_t)lc * ldc + i] = fma(-zi, ub[lc], cols[(size_t)lc * ldc + i]);
   }
 }
 
@@ -89,7 +169,7 @@ __device__ void gebrd_left(const GebrdOp& o, const double* col, int j, double* v
 // are worked on in place in the sector matrix in global memory (L2-resident), only the reduction
 // buffers stay in shared memory.  The arithmetic is the same.
 template <int CL, bool GM, int NT>
-__global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
+__global__ void __launch_bounds__(NT, 1) k_gebrd(const GebrdOp* __restrict__ ops) {
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
   const GebrdOp o = ops[blockIdx.x / CL];
@@ -102,7 +182,8 @@ __global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
   double* cols = GM ? o.A + (int64_t)r * o.lda : sm;
   double* v = GM ? sm : cols + (size_t)ncol_max * m;  // current left reflector
   double* zp = v + m;                       // this CTA's partial products for the right reflector
-  double* cb = zp + m;                      // column j+1 before the right update (its owner)
+  double* cb = zp + m;                      // column j+1 after the left update (staged by its owner,
+                                            // copied by the others)
   double* z = cb + m;                       // right-update coefficients
   double* ub = z + m;                       // right reflector entries of the own columns
   double* scal = ub + ncol_max;             // [0] tau, [1] partial |row|^2, [2] alpha, [3] |row|^2, [4] alpha
@@ -114,70 +195,29 @@ __global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
   __syncthreads();
   if (r == 0 && warp == 0) gebrd_left(o, cols, 0, v, scal, lane);
   cluster.sync();  // every CTA runs (distributed shared memory is addressable), reflector 0 exists
+  if (r != 0) {    // reflector 0 from its owner; every later one is computed in every CTA
+    const double* rv = cluster.map_shared_rank(v, 0);
+    for (int i = tid; i < m; i += blockDim.x) v[i] = rv[i];
+    if (tid == 0) scal[0] = *cluster.map_shared_rank(scal, 0);
+  }
   for (int j = 0; j + 1 < n; ++j) {
-    // (a) left reflector j from the owner of column j; applied to the own columns c > j
-    const int oj = j % CL;
-    if (r != oj) {
-      const double* rv = cluster.map_shared_rank(v, oj);
-      for (int i = j + tid; i < m; i += blockDim.x) v[i] = rv[i];
-      if (tid == 0) scal[0] = *cluster.map_shared_rank(scal, oj);
-    }
-    __syncthreads();
+    __syncthreads();  // left reflector j in v, scal[0]
+    // (a) left reflector j applied to the own columns c > j
     const double tau = scal[0];
     const int lc1 = (j + CL - r) / CL;      // first own column with c >= j + 1
     const int lc2 = (j + 1 + CL - r) / CL;  // first own column with c >= j + 2
-    if (tau != 0.0) {
-      for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
-        double* a = cols + (size_t)lc * ldc;
-        // four independent loads and partial sums in flight per lane (the global-memory variant waits
-        // on L2 latency otherwise)
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        int i = j + lane;
-        for (; i + 96 < m; i += 128) {
-          s0 = fma(v[i], a[i], s0);
-          s1 = fma(v[i + 32], a[i + 32], s1);
-          s2 = fma(v[i + 64], a[i + 64], s2);
-          s3 = fma(v[i + 96], a[i + 96], s3);
-        }
-        for (; i < m; i += 32) s0 = fma(v[i], a[i], s0);
-        const double w = warp_sum((s0 + s1) + (s2 + s3)) * tau;
-        i = j + lane;
-        for (; i + 96 < m; i += 128) {
-          const double a0 = a[i], a1 = a[i + 32], a2 = a[i + 64], a3 = a[i + 96];
-          a[i] = fma(-v[i], w, a0);
-          a[i + 32] = fma(-v[i + 32], w, a1);
-          a[i + 64] = fma(-v[i + 64], w, a2);
-          a[i + 96] = fma(-v[i + 96], w, a3);
-        }
-        for (; i < m; i += 32) a[i] = fma(-v[i], w, a[i]);
-      }
-    }
+    if (tau != 0.0) gebrd_apply_left(cols, ldc, v, tau, j, m, lc1, ncol, warp, nwarp, lane);
     __syncthreads();
     // (b) partial products of the right reflector of row j: zp_i = sum over own c >= j+2 of
     //     A(i, c) A(j, c), and the partial |A(j, c >= j+2)|^2; the owner of column j+1 stages it
-    for (int i = j + 1 + tid; i < m; i += blockDim.x) {  // four independent partial sums per row
-      double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
-      int lc = lc2;
-      for (; lc + 3 < ncol; lc += 4) {
-        acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
-        acc1 = fma(cols[(size_t)(lc + 1) * ldc + i], cols[(size_t)(lc + 1) * ldc + j], acc1);
-        acc2 = fma(cols[(size_t)(lc + 2) * ldc + i], cols[(size_t)(lc + 2) * ldc + j], acc2);
-        acc3 = fma(cols[(size_t)(lc + 3) * ldc + i], cols[(size_t)(lc + 3) * ldc + j], acc3);
-      }
-      for (; lc < ncol; ++lc) acc0 = fma(cols[(size_t)lc * ldc + i], cols[(size_t)lc * ldc + j], acc0);
-      zp[i] = (acc0 + acc1) + (acc2 + acc3);
-    }
+    gebrd_row_partials(cols, ldc, zp, j, m, lc2, ncol, tid, blockDim.x);
     if (warp == 0) {
-      double s = 0.0;
-      for (int lc = lc2 + lane; lc < ncol; lc += 32) {
-        const double x = cols[(size_t)lc * ldc + j];
-        s = fma(x, x, s);
-      }
-      s = warp_sum(s);
-      if (lane == 0) scal[1] = s;
+      const double s2 = gebrd_row_norm_partial(cols, ldc, j, lc2, ncol, lane);
+      if (lane == 0) scal[1] = s2;
     }
     const int on = (j + 1) % CL, lnext = (j + 1) / CL;
-    if (r == on) {
+    const bool own_next = (r == on);
+    if (own_next) {
       const double* a = cols + (size_t)lnext * ldc;
       for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = a[i];
       if (tid == 0) scal[2] = a[j];
@@ -207,8 +247,8 @@ __global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
     constexpr bool kSliced = CL >= 8;
     const int zlen = m - (j + 1);
     const int zcs = kSliced ? (zlen + CL - 1) / CL : zlen;
+    const double* rcb = cluster.map_shared_rank(cb, on);
     if (taup != 0.0) {
-      const double* rcb = cluster.map_shared_rank(cb, on);
       const int i0 = j + 1 + (kSliced ? r * zcs : 0);
       const int i1 = kSliced ? min(m, i0 + zcs) : m;
       for (int i = i0 + tid; i < i1; i += blockDim.x) {
@@ -226,47 +266,225 @@ __global__ void __launch_bounds__(NT) k_gebrd(const GebrdOp* __restrict__ ops) {
         o.Pr[(r + lc * CL) + (int64_t)j * o.n] = u;
       }
     }
-    if (kSliced) {
-      cluster.sync();  // #1b: every CTA's slice of z (taup is the same in every CTA)
-      if (taup != 0.0)
-        for (int i = j + 1 + tid; i < m; i += blockDim.x) {
-          const int q = (i - (j + 1)) / zcs;
-          if (q != r) z[i] = cluster.map_shared_rank(z, q)[i];
-        }
-    }
+    // column j+1 of the other CTAs: a copy of the owner's (read before the barrier below, so that the
+    // owner may stage the next column without a further barrier)
+    if (!own_next)
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = rcb[i];
+    if (kSliced) cluster.sync();  // #1b: every CTA's slice of z, every copy of column j+1 taken
+    if (kSliced && taup != 0.0)
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+        const int q = (i - (j + 1)) / zcs;
+        if (q != r) z[i] = cluster.map_shared_rank(z, q)[i];
+      }
+    if (!kSliced) cluster.sync();  // every copy of column j+1 taken
     __syncthreads();
-    // (d) A(i, c) -= z_i u_c for i > j on the own columns c >= j+1; the owner of column j+1 updates
-    //     that column first and computes left reflector j+1 (lookahead) while its other warps go on
-    const bool own_next = (r == on);
-    if (own_next && warp == 0) {
-      double* a = cols + (size_t)lnext * ldc;
+    // (d) A(i, c) -= z_i u_c for i > j on the own columns c >= j+2; warp 0 of every CTA forms column
+    //     j+1 after the update (the owner in place) and left reflector j+1 from it (the owner stores it)
+    if (warp == 0) {
+      double* a = own_next ? cols + (size_t)lnext * ldc : cb;
       if (taup != 0.0)
         for (int i = j + 1 + lane; i < m; i += 32) a[i] -= z[i];
       __syncwarp();
-      if (lane == 0) {
+      if (own_next && lane == 0) {
         o.e[j] = beta;
         o.taup[j] = taup;
       }
-      gebrd_left(o, a, j + 1, v, scal, lane);
+      gebrd_left(o, a, j + 1, v, scal, lane, own_next);
     }
-    const int p0 = own_next ? 32 : 0;  // threads of the update (all but the lookahead warp)
-    if (taup != 0.0 && tid >= p0) {
-      for (int i = j + 1 + tid - p0; i < m; i += (int)blockDim.x - p0) {
-        const double zi = z[i];
-        int lc = lc2;
-        for (; lc + 3 < ncol; lc += 4) {  // four loads in flight before the stores
-          double* a = cols + (size_t)lc * ldc + i;
-          const double a0 = a[0], a1 = a[ldc], a2 = a[2 * ldc], a3 = a[3 * ldc];
-          a[0] = fma(-zi, ub[lc], a0);
-          a[ldc] = fma(-zi, ub[lc + 1], a1);
-          a[2 * ldc] = fma(-zi, ub[lc + 2], a2);
-          a[3 * ldc] = fma(-zi, ub[lc + 3], a3);
-        }
-        for (; lc < ncol; ++lc) cols[(size_t)lc * ldc + i] = fma(-zi, ub[lc], cols[(size_t)lc * ldc + i]);
+    if (taup != 0.0 && tid >= 32) gebrd_apply_right(cols, ldc, z, ub, j, m, lc2, ncol, tid - 32, (int)blockDim.x - 32);
+  }
+  cluster.sync();  // no CTA leaves while the others may still read its shared memory
+}
+
+
+// ----------------------------------------------------------------------------- 1b. two-cluster sectors
+// Sectors too large for one cluster's shared memory run in global memory; the largest of them are
+// spread over G clusters of CL CTAs (CTA R = g CL + r owns the columns c = R mod G CL), so that
+// G CL SMs share their FP64 work.  Per column: the left update, each CTA's partial products of the
+// right reflector into global memory, one barrier over the G clusters, each cluster sums the
+// partials of its rows (one slice per CTA, exchanged through distributed shared memory), the right
+// update, and in every CTA the next left reflector from the copy of the next column.  The barriers count on a per-sector counter in global memory; every
+// wait is bounded (~2 s of globaltimer), after which the CTA records *err and all CTAs of its
+// cluster leave together (the other clusters' waits then expire as well); the host redoes the
+// split on the Jacobi route.  All G clusters of a sector must be resident together: the host
+// launches these sectors alone on their stream, at most 2 x 16 CTAs each.
+__device__ __forceinline__ uint64_t gebrd_globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned gebrd_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+// Barrier of the NC = G CL CTAs of a sector; false (in every CTA of the cluster) once a wait expired.
+template <int CL>
+__device__ bool gebrd_sector_sync(cg::cluster_group& cluster, unsigned* ctr, unsigned target, int* err, int* flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // this CTA's global writes (ordered before by the CTA barrier) are visible
+    atomicAdd(ctr, 1u);
+    const uint64_t t0 = gebrd_globaltimer();
+    bool ok = true;
+    while (gebrd_ld_acquire(ctr) < target) {
+      if (gebrd_globaltimer() - t0 > 2000000000ull) {
+        ok = false;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (!ok) {
+      atomicExch(err, 1);
+      for (int q = 0; q < CL; ++q) *cluster.map_shared_rank(flag, q) = 1;
+    }
+    __threadfence();
+  }
+  cluster.sync();
+  return flag[0] == 0;
+}
+size_t gebrd_mc_xg_doubles(int m, int clusters) {
+  const size_t nc = (size_t)16 * clusters;
+  return 2 * (nc * (size_t)m + nc + (size_t)m + 8);  // two sets: partials | row norms | column j+1 | alpha
+}
+// shared memory of a CTA: v (m) | z (m) | cb (m) | ub (ncol) | scal (8) | flag
+size_t gebrd_mc_smem(int m, int n, int clusters) {
+  const int NC = 16 * clusters;
+  return sizeof(double) * (3 * (size_t)m + (size_t)((n + NC - 1) / NC) + 8) + 16;
+}
+
+template <int CL, int G, int NT>
+__global__ void __launch_bounds__(NT, 1) k_gebrd_mc(const GebrdOp* __restrict__ ops) {
+  constexpr int NC = CL * G;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int g = (int)(blockIdx.x / CL) % G;
+  const int R = g * CL + r;
+  const GebrdOp o = ops[blockIdx.x / NC];
+  const int m = o.m, n = o.n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = NT / 32;
+  extern __shared__ double sm[];
+  const int ncol_max = (n + NC - 1) / NC;
+  const int ncol = (n - R + NC - 1) / NC;  // own columns: global column R + lc * NC
+  const int64_t ldc = (int64_t)NC * o.lda;
+  double* cols = o.A + (int64_t)R * o.lda;
+  double* v = sm;                // current left reflector
+  double* z = v + m;             // right-update coefficients
+  double* cb = z + m;            // column j+1 (copy)
+  double* ub = cb + m;           // right reflector entries of the own columns
+  double* scal = ub + ncol_max;  // [0] tau, [3] |row|^2, [4] alpha
+  int* flag = (int*)(scal + 8);
+  // exchange buffers, two sets used in alternate columns (a CTA can be at most one column ahead of
+  // another's reads): partial products (NC x m) | row-norm partials (NC) | column j+1 (m) | alpha
+  const size_t xset = (size_t)NC * m + NC + m + 8;
+  unsigned nb = 0;
+  if (tid == 0) flag[0] = 0;
+  if (R == 0 && warp == 0) gebrd_left(o, cols, 0, v, scal, lane);
+  if (!gebrd_sector_sync<CL>(cluster, o.ctr, NC * ++nb, o.err, flag)) return;
+  if (R != 0) {  // reflector 0 from the sector matrix; every later one is computed in every CTA
+    for (int i = tid; i < m; i += NT) v[i] = i == 0 ? 1.0 : __ldcg(o.A + i);
+    if (tid == 0) scal[0] = __ldcg(o.tauq);
+  }
+  for (int j = 0; j + 1 < n; ++j) {
+    double* zpg = o.xg + (size_t)(j & 1) * xset;
+    double* nrg = zpg + (size_t)NC * m;
+    double* cbuf = nrg + NC;
+    double* galpha = cbuf + m;
+    __syncthreads();  // left reflector j in v, scal[0]
+    // (a) left reflector j applied to the own columns c > j
+    const double tau = scal[0];
+    const int lc1 = (j + NC - R) / NC;      // first own column with c >= j + 1
+    const int lc2 = (j + 1 + NC - R) / NC;  // first own column with c >= j + 2
+    if (tau != 0.0) gebrd_apply_left(cols, ldc, v, tau, j, m, lc1, ncol, warp, nwarp, lane);
+    __syncthreads();
+    // (b) partial products and row-norm partial of this CTA into global memory; the owner of column
+    //     j+1 copies it there
+    gebrd_row_partials(cols, ldc, zpg + (size_t)R * m, j, m, lc2, ncol, tid, NT);
+    if (warp == 0) {
+      const double s2 = gebrd_row_norm_partial(cols, ldc, j, lc2, ncol, lane);
+      if (lane == 0) nrg[R] = s2;
+    }
+    const int on = (j + 1) % NC, lnext = (j + 1) / NC;
+    const bool own_next = (R == on);
+    if (own_next) {
+      const double* a = cols + (size_t)lnext * ldc;
+      for (int i = j + 1 + tid; i < m; i += NT) cbuf[i] = a[i];
+      if (tid == 0) galpha[0] = a[j];
+    }
+    if (!gebrd_sector_sync<CL>(cluster, o.ctr, NC * ++nb, o.err, flag)) return;
+    // (c) the right reflector from the NC partials (fixed order); z for this CTA's slice of the rows
+    if (warp == 0) {
+      double s2 = 0.0;
+      for (int q = lane; q < NC; q += 32) s2 += __ldcg(nrg + q);
+      s2 = warp_sum(s2);
+      if (lane == 0) {
+        scal[3] = s2;
+        scal[4] = __ldcg(galpha);
       }
     }
-    cluster.sync();  // #2: columns updated, reflector j+1 ready on its owner, partials consumed
+    __syncthreads();
+    const double nrm2 = scal[3], alpha = scal[4];
+    double taup = 0.0, beta = alpha, sc = 0.0;
+    if (nrm2 > 0.0) {
+      beta = -copysign(sqrt(fma(alpha, alpha, nrm2)), alpha);
+      taup = (beta - alpha) / beta;
+      sc = 1.0 / (alpha - beta);
+    }
+    const int zlen = m - (j + 1);
+    const int zcs = (zlen + CL - 1) / CL;
+    if (taup != 0.0) {
+      // 8 lanes per row, each summing NC / 8 partials (all loads in flight at once), then a fixed
+      // butterfly over the 8 lanes: one L2 round trip per row
+      constexpr int TPR = 8, PPT = NC / TPR;
+      static_assert(NC % TPR == 0, "partials per lane");
+      const int i0 = j + 1 + r * zcs, i1 = min(m, i0 + zcs);
+      for (int k0 = warp * 32; k0 < zcs * TPR; k0 += NT) {  // whole warps per iteration
+        const int k = k0 + lane;
+        const int i = i0 + k / TPR, t = k % TPR;
+        double zs = 0.0;
+        if (i < i1) {
+          double part[PPT];
+#pragma unroll
+          for (int u = 0; u < PPT; ++u) part[u] = __ldcg(zpg + (size_t)(t * PPT + u) * m + i);
+#pragma unroll
+          for (int u = 0; u < PPT; ++u) zs += part[u];
+        }
+        zs += __shfl_xor_sync(0xffffffffu, zs, 1);
+        zs += __shfl_xor_sync(0xffffffffu, zs, 2);
+        zs += __shfl_xor_sync(0xffffffffu, zs, 4);
+        if (t == 0 && i < i1) z[i] = taup * fma(sc, zs, __ldcg(cbuf + i));
+      }
+      for (int lc = lc2 + tid; lc < ncol; lc += NT) {
+        const double u = cols[(size_t)lc * ldc + j] * sc;
+        ub[lc] = u;
+        o.Pr[(R + lc * NC) + (int64_t)j * o.n] = u;
+      }
+    }
+    if (!own_next)
+      for (int i = j + 1 + tid; i < m; i += NT) cb[i] = __ldcg(cbuf + i);
+    cluster.sync();  // the cluster's slices of z
+    if (taup != 0.0)
+      for (int i = j + 1 + tid; i < m; i += NT) {
+        const int q = (i - (j + 1)) / zcs;
+        if (q != r) z[i] = cluster.map_shared_rank(z, q)[i];
+      }
+    __syncthreads();
+    // (d) the right update; warp 0 of every CTA forms column j+1 after it (the owner in place) and
+    //     left reflector j+1 from it (the owner stores it)
+    if (warp == 0) {
+      double* a = own_next ? cols + (size_t)lnext * ldc : cb;
+      if (taup != 0.0)
+        for (int i = j + 1 + lane; i < m; i += 32) a[i] -= z[i];
+      __syncwarp();
+      if (own_next && lane == 0) {
+        o.e[j] = beta;
+        o.taup[j] = taup;
+      }
+      gebrd_left(o, a, j + 1, v, scal, lane, own_next);
+    }
+    if (taup != 0.0 && tid >= 32) gebrd_apply_right(cols, ldc, z, ub, j, m, lc2, ncol, tid - 32, NT - 32);
   }
+  cluster.sync();  // no CTA leaves while the others may still read its shared memory
 }
 
 template <int CL, bool GM, int NT = 256>
@@ -325,6 +543,85 @@ int gebrd_cluster_size(int m, int n) {
   if (c <= 16) return c;
   c = std::min(16, gebrd_cl_cap());
   return sizeof(double) * gebrd_gm_smem_doubles(m, n, c) <= 220 * 1024 ? kGebrdGlobal + c : 0;
+}
+
+
+// Sectors whose FP64 work is worth two clusters: global-memory sectors with m n^2 above 3e8
+// (about 670 x 670); MPSG_GEBRD_CLUSTERS=1 keeps every sector on one cluster.
+int gebrd_mc_clusters(int m, int n) {
+  static const int cap = [] {
+    const char* e = std::getenv("MPSG_GEBRD_CLUSTERS");
+    return e && std::atoi(e) == 1 ? 1 : 2;
+  }();
+  if (cap < 2 || gebrd_cl_cap() < 16) return 1;
+  const int code = gebrd_cluster_size(m, n);
+  if (code <= kGebrdGlobal) return 1;
+  return (double)m * n * n > 3e8 ? 2 : 1;
+}
+
+template <int G>
+static void launch_gebrd_mc_g(const GebrdOp* ops, int nops, size_t smem, cudaStream_t s) {
+  constexpr int CL = 16, NT = 512;
+  auto kern = k_gebrd_mc<CL, G, NT>;
+  MPSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MPSG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nops * CL * G);
+  cfg.blockDim = dim3(NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  // every cluster of the launch must be able to be resident at once (the clusters of a sector wait
+  // on each other)
+  int active = 0;
+  MPSG_CUDA(cudaOccupancyMaxActiveClusters(&active, (void*)kern, &cfg));
+  MPSG_CHECK(active >= nops * G, "bidiagonalisation: the two-cluster sectors cannot all be resident");
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, kern, ops));
+  g_bd_launches.fetch_add(1);
+}
+
+// two-cluster sectors resident at once: the active 16-CTA clusters of the kernel (one per GPC of at
+// least 16 SMs) over two, at the kernel's largest shared memory
+int gebrd_mc_capacity() {
+  static const int cap = [] {
+    auto kern = k_gebrd_mc<16, 2, 512>;
+    const size_t smem = 227 * 1024;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(32);
+    cfg.blockDim = dim3(512);
+    cfg.dynamicSmemBytes = 16 * 1024;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int active = 0;
+    if (cudaOccupancyMaxActiveClusters(&active, (void*)kern, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    return active / 2;
+  }();
+  return cap;
+}
+
+void launch_gebrd_mc(const GebrdOp* ops, int nops, int clusters, size_t smem, cudaStream_t s) {
+  if (nops <= 0) return;
+  MPSG_CHECK(clusters == 2, "bidiagonalisation: unsupported cluster count");
+  launch_gebrd_mc_g<2>(ops, nops, smem, s);
 }
 
 // dynamic shared memory of one sector's CTAs (a launch takes the largest over its sectors)
@@ -574,7 +871,7 @@ double* gk_cut_xlo(void* state, int c) { return &((CutState*)state)[c].xlo; }
 // linear within one, so every value needs about the same number of rounds however small it is.
 // One warp per block: the groups spread over all SMs (the counts are dependent FP64 chains).
 // S is unscaled and descending.
-constexpr int kGkLanes = 2;
+constexpr int kGkLanes = 8;
 template <int LN>
 __global__ void __launch_bounds__(32) k_gk_bisect(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
                                                   const int32_t* __restrict__ k_of, int nthreads) {
@@ -593,7 +890,10 @@ __global__ void __launch_bounds__(32) k_gk_bisect(const GkOp* __restrict__ ops, 
   const int m = N - 1 - k;
   long long ia = __double_as_longlong(*o.xlo * o.meta[1]), ib = __double_as_longlong(o.meta[2]);
   for (int it = 0; it < 200 && ib - ia > 2; ++it) {
-    const long long ix = ia + ((ib - ia) / (LN + 1)) * (g + 1);
+    // LN points strictly inside (ia, ib); once the interval holds fewer than LN + 1 patterns some of
+    // them coincide (the counts stay monotone in the point, so the bracketing below still holds)
+    const long long step = (ib - ia) / (LN + 1) > 0 ? (ib - ia) / (LN + 1) : 1;
+    const long long ix = min(ia + step * (g + 1), ib - 1);
     const unsigned above =
         (__ballot_sync(gmask, gk_count(o.b2, N, __longlong_as_double(ix)) > m) >> (lane & ~(LN - 1))) &
         ((1u << LN) - 1u);
@@ -607,10 +907,22 @@ __global__ void __launch_bounds__(32) k_gk_bisect(const GkOp* __restrict__ ops, 
   }
   if (g == 0) o.S[k] = 0.5 * (__longlong_as_double(ia) + __longlong_as_double(ib)) * o.meta[0];
 }
+static int gk_lanes() {
+  static const int v = [] {
+    const char* e = std::getenv("MPSG_GK_LANES");
+    const int x = e ? std::atoi(e) : kGkLanes;
+    return (x == 2 || x == 4 || x == 8) ? x : kGkLanes;
+  }();
+  return v;
+}
 void launch_gk_bisect(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, int nthreads, cudaStream_t s) {
   if (nthreads <= 0) return;
-  const int64_t lanes = (int64_t)kGkLanes * nthreads;
-  k_gk_bisect<kGkLanes><<<(unsigned)((lanes + 31) / 32), 32, 0, s>>>(ops, op_of, k_of, nthreads);
+  const int ln = gk_lanes();
+  const int64_t lanes = (int64_t)ln * nthreads;
+  const unsigned grid = (unsigned)((lanes + 31) / 32);
+  if (ln == 2) k_gk_bisect<2><<<grid, 32, 0, s>>>(ops, op_of, k_of, nthreads);
+  else if (ln == 4) k_gk_bisect<4><<<grid, 32, 0, s>>>(ops, op_of, k_of, nthreads);
+  else k_gk_bisect<8><<<grid, 32, 0, s>>>(ops, op_of, k_of, nthreads);
   g_bd_launches.fetch_add(1);
 }
 
