@@ -612,6 +612,99 @@ def sweep_leg(ctx, prec, W, ik, sites, ramp, torch):
                             "sectors": {int(q): len(v) for q, v in lam_c.items()}}}
 
 
+SPLIT_RAMP = (256, 256, 1024, 1024, 1024, 2048)
+
+
+def split_arm(args):
+    """--workload split: the split alone (mpsg_split2 with --svd) of the two-site ground state at the
+    centre bond of the XXZ chain (L=100, Jxy=1, Delta_i ~ U[0.5,1.5] seed 1) after a chi ramp
+    (--ramp, default 256, 256, 1024, 1024, 1024, 2048: chi grows about fourfold per sweep from the
+    product state; MIXED): the sector structure of a converged
+    chi=2048 state (sector matrices up to ~1000 x 1000).  The FP64 Lanczos ground state at the centre
+    bond is formed once; --warmup + --steps splits of it follow, the timed ones inside the NVTX range
+    "split" (profiler launch lists: ncu --nvtx --nvtx-include split/).  The oracle's split (LAPACK
+    dgesvd) of the same state checks the singular values and the kept count of every sector."""
+    import ctypes as C
+    import torch
+    from mpstools_gb300 import lib, api
+    ramp = tuple(args.ramp) if args.ramp else SPLIT_RAMP
+    chimax = ramp[-1]
+    W, ik, sites = sweep_workload(args.L, args.model)
+    ctx = lib.Context(0)
+    ctx.set_svd_method(args.svd)
+    eng = api.DMRGengine(sites, W, ik, prec="mixed", ctx=ctx)
+    t0 = time.perf_counter()
+    run_sweeps(eng, args.L, ramp, sync=torch.cuda.synchronize)
+    c = args.L // 2 - 1
+    for site in range(c):
+        eng.do_step(site, 1, chimax)
+    t_ramp = time.perf_counter() - t0
+    Lt, Rt = eng.env_tensor("L", c - 1), eng.env_tensor("R", c + 2)
+    A1, A2 = eng.site_tensor(c), eng.site_tensor(c + 1)
+    w1, w2 = lib.MPOArg(W[c]), lib.MPOArg(W[c + 1])
+    k0, k1 = lib.ItoKeyArg(ik[c]), lib.ItoKeyArg(ik[c + 1])
+    st, E0, it = C.c_void_p(), C.c_double(), C.c_int32()
+    lib.check(ctx.L.mpsg_lanczos2(ctx.h, Lt.h, Rt.h, A1.h, A2.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), 500, 1e-12, 1,
+                                  lib.PREC["fp64"], 0, C.byref(st), C.byref(E0), C.byref(it)))
+    psi = lib.Tensor(ctx, st)
+
+    def split_once():
+        U, V, lam = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tw, chi = C.c_double(), C.c_uint32()
+        lib.check(ctx.L.mpsg_split2(ctx.h, psi.h, k0.ref(), k1.ref(), chimax, 0, 1e-12, 1, C.byref(U), C.byref(V),
+                                    C.byref(lam), C.byref(tw), C.byref(chi)))
+        return lib.Tensor(ctx, U), lib.Tensor(ctx, V), lib.Tensor(ctx, lam), tw.value, chi.value
+
+    f0 = int(ctx.L.mpsg_split_fallbacks())
+    for _ in range(max(args.warmup, 1)):
+        out = split_once()
+    clk = ClockSampler()
+    clk.start()
+    times = []
+    torch.cuda.nvtx.range_push("split")
+    for _ in range(args.steps):
+        del out
+        ctx.sync()
+        a = time.perf_counter()
+        out = split_once()
+        ctx.sync()
+        times.append(time.perf_counter() - a)
+    torch.cuda.nvtx.range_pop()
+    clocks = clk.stop()
+    U, V, lam, tw, chi = out
+    lam_d, u_d, v_d = lam.to_dict(), U.to_dict(), V.to_dict()
+    rows, cols = {}, {}
+    for (a, qc, s1), blk in u_d.items():
+        rows[qc] = rows.get(qc, 0) + blk.shape[0]
+    for (qc, b, s2), blk in v_d.items():
+        cols[qc] = cols.get(qc, 0) + blk.shape[1]
+    sectors = sorted(([int(rows[q]), int(cols[q]), len(lam_d[q])] for q in lam_d if q in rows and q in cols),
+                     key=lambda x: -x[0] * x[1])
+    line = {"metric": "split time of a converged chi=2048 two-site state", "value": float(np.median(times)) * 1e3,
+            "unit": "ms", "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{args.model}_L{args.L}_centre_bond_split_after_ramp", "ramp": list(ramp),
+                       "svd": args.svd, "state": "FP64 Lanczos ground state at the centre bond after the ramp",
+                       "ramp_seconds": t_ramp},
+            "ms_each": [t * 1e3 for t in times], "chi": int(chi), "truncated_weight": tw,
+            "sectors_m_n_kept": sectors, "split_fallbacks_to_jacobi": int(ctx.L.mpsg_split_fallbacks()) - f0,
+            "clocks": clocks}
+    if not args.no_cpu:
+        from oracle import pyoracle as O
+        th = psi.to_dict()
+        a = time.perf_counter()
+        U0, V0, l0, tw0, chi0 = O.split(th, ik[c], ik[c + 1], chimax, nthreads=os.cpu_count() or 1)
+        t_or = time.perf_counter() - a
+        kept_eq = {q: len(v) for q, v in l0.items() if len(v)} == {q: len(v) for q, v in lam_d.items() if len(v)}
+        dl = max((float(np.abs(np.asarray(lam_d[q]) - np.asarray(l0[q])).max())
+                  for q in l0 if len(l0[q]) and q in lam_d and len(lam_d[q]) == len(l0[q])), default=0.0)
+        line["oracle_check"] = {"chi_oracle": int(chi0), "kept_per_sector_equal": bool(kept_eq),
+                                "lambda_max_abs_diff": dl, "tw_oracle": tw0, "oracle_seconds": t_or}
+        line["cpu_baseline"] = {"value": t_or * 1e3, "unit": "ms", "cores": os.cpu_count() or 1, "kind": "port",
+                                "sample": "the same split in the oracle (LAPACK dgesvd per sector, all threads)"}
+    print(json.dumps(line), flush=True)
+
+
 def oracle_sweeps(W, ik, sites, ramp, threads):
     from oracle import pyoracle as O
     g = O.DMRG(sites, W, ik, maxthreads=threads, matvec_threads=threads)
@@ -814,9 +907,11 @@ def main():
                     help="skip the plain FP64 GPU path timed on the same updates (mixed precisions only)")
     ap.add_argument("--steps-only", action="store_true",
                     help="time the DMRG steps only (no roofline / e2e / CPU legs); for profiler launch lists")
-    ap.add_argument("--workload", default="centre_update", choices=["centre_update", "sweep", "chains", "tebd"],
+    ap.add_argument("--workload", default="centre_update",
+                    choices=["centre_update", "sweep", "split", "chains", "tebd"],
                     help="chains: batched independent chains (--nchains, --sweeps, --seq-chains; --chi 256); "
-                         "tebd: L=64 TEBD forward + adjoint gradient (--tebd-steps, --fd-bonds)")
+                         "tebd: L=64 TEBD forward + adjoint gradient (--tebd-steps, --fd-bonds); "
+                         "split: the split of a converged chi=2048 centre-bond state (--ramp)")
     ap.add_argument("--ramp", type=int, nargs="*", default=None, help="sweep: chimax per sweep")
     ap.add_argument("--oracle-sweeps", type=int, default=2, help="sweep: sweeps the CPU oracle runs")
     ap.add_argument("--tebd-steps", type=int, default=200)
@@ -835,6 +930,8 @@ def main():
         tebd_arm(args)
     elif args.workload == "sweep":
         sweep_arm(args)
+    elif args.workload == "split":
+        split_arm(args)
     elif args.impl == "reference":
         reference_arm(args)
     else:

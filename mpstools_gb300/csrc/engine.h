@@ -202,7 +202,15 @@ struct Engine {
     th.reset();
     auto t0 = std::chrono::steady_clock::now();
     lanczos_call_seconds += std::chrono::duration<double>(t0 - tp1).count();
-    SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1);
+    // the energy matvec is queued once the bidiagonalisation launches are (their clusters are placed
+    // first), or after the split when it takes another route
+    std::function<void(cudaEvent_t)> hook;
+    if (energy.pending())
+      hook = [&energy](cudaEvent_t after) {
+        if (!energy.launched) energy.launch(after);
+      };
+    SplitResult sp = split2(ctx, *psi, ik[site], ik[site + 1], chimax, doTrunc, tr_weight, true, dir > 0 ? 1 : -1,
+                            nullptr, nullptr, hook);
     ctx->sync();
     auto t1 = std::chrono::steady_clock::now();
     split_seconds += std::chrono::duration<double>(t1 - t0).count();

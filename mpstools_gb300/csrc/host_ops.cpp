@@ -632,6 +632,7 @@ struct SvdBatch {
   double *dM = nullptr, *dU = nullptr, *dV = nullptr, *dS = nullptr;
   int* dinfo = nullptr;
   int64_t nS = 0;
+  std::function<void(cudaEvent_t)> on_bidiag;  // see split2
   explicit SvdBatch(Ctx* c) : ctx(c) {}
   ~SvdBatch() {
     bidiag_free();
@@ -1408,6 +1409,7 @@ struct SvdBatch {
           launch_gebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, smem[bufs[j].first],
                        ctx->wstreams[j % nw]);
       }
+      if (on_bidiag) on_bidiag(ctx->fork_event);  // ready together with the launches above
       ctx->join(nw);
       if (!mc.empty()) {
         // a two-cluster sector whose barrier wait expired is redone on one cluster from the copy
@@ -1671,7 +1673,7 @@ struct SvdBatch {
 // ============================================================================ split
 SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
                    double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
-                   const std::vector<int>* seg_absorb) {
+                   const std::vector<int>* seg_absorb, const std::function<void(cudaEvent_t)>& on_bidiag) {
   struct SecInfo {
     std::map<uint32_t, std::pair<int, int>> rx, ry;  // index -> (start, size)
     std::vector<int> blocks;
@@ -1699,6 +1701,7 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   if (!chimax && doTrunc) chimax = 100;
   if (!chimax && !doTrunc) chimax = 200;
   SvdBatch sv(ctx);
+  sv.on_bidiag = on_bidiag;
   sv.plan(mn);
   std::vector<CopyOp> gops;
   for (size_t si = 0; si < qcs.size(); ++si) {
@@ -2326,31 +2329,37 @@ double rayleigh_quotient(Ctx* ctx, MatvecPlan& mv, const Tensor& psi, LanczosSta
   return q[0] / q[1];
 }
 
-void EnergyJob::start(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& psi, LanczosStats* s) {
+void EnergyJob::prepare(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& state, LanczosStats* s) {
   release();
   ctx = c;
   mv = std::move(plan);
   st = s;
-  const int64_t n = std::max<int64_t>(psi.nelem, 2);
-  nw = n;
-  buf = (double*)ctx->dmalloc(sizeof(double) * (n + kRedBlocks + 64 + 2));
-  double* w = buf;
-  double* part = buf + n;
-  double* dq = part + kRedBlocks + 64;
-  MPSG_CUDA(cudaMemsetAsync(w, 0, sizeof(double) * n, ctx->stream));
+  psi = &state;
+  launched = false;
+  nw = std::max<int64_t>(state.nelem, 2);
+  buf = (double*)ctx->dmalloc(sizeof(double) * (nw + kRedBlocks + 64 + 2));
+  MPSG_CUDA(cudaMemsetAsync(buf, 0, sizeof(double) * nw, ctx->stream));
   for (auto& e : ev) MPSG_CUDA(cudaEventCreate(&e));
-  // the side stream starts after everything queued so far (psi, the plan's FP64 tables, buf)
+  MPSG_CUDA(cudaEventRecord(ev[2], ctx->stream));  // psi, the plan's FP64 tables, buf
+}
+
+void EnergyJob::launch(cudaEvent_t after) {
+  MPSG_CHECK(pending() && !launched, "energy job not prepared");
+  launched = true;
+  double* w = buf;
+  double* part = buf + nw;
+  double* dq = part + kRedBlocks + 64;
   cudaStream_t side = ctx->side_stream();
-  MPSG_CUDA(cudaEventRecord(ev[2], ctx->stream));
   MPSG_CUDA(cudaStreamWaitEvent(side, ev[2], 0));
+  if (after) MPSG_CUDA(cudaStreamWaitEvent(side, after, 0));
   cudaStream_t main = ctx->stream;
   ctx->stream = side;  // the plan launches on ctx->stream
   try {
     MPSG_CUDA(cudaEventRecord(ev[0], side));
-    mv->run(psi.d, w);
+    mv->run(psi->d, w);
     MPSG_CUDA(cudaEventRecord(ev[1], side));
-    launch_dot(psi.d, w, psi.nelem, part, dq, side);
-    launch_dot(psi.d, psi.d, psi.nelem, part, dq + 1, side);
+    launch_dot(psi->d, w, psi->nelem, part, dq, side);
+    launch_dot(psi->d, psi->d, psi->nelem, part, dq + 1, side);
     MPSG_CUDA(cudaEventRecord(ev[2], side));
   } catch (...) {
     ctx->stream = main;
@@ -2361,6 +2370,7 @@ void EnergyJob::start(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& ps
 
 double EnergyJob::finish() {
   MPSG_CHECK(pending(), "energy job not started");
+  if (!launched) launch(nullptr);
   MPSG_CUDA(cudaEventSynchronize(ev[2]));
   float ms = 0;
   MPSG_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
@@ -2410,7 +2420,7 @@ LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Lay
     // chi = 2048 about 1 - 5e-6), which shifts the Ritz value but not the eigenvector.
     mv->use_fp64();
     if (energy) {
-      energy->start(ctx, std::move(mv), psi, st);
+      energy->prepare(ctx, std::move(mv), psi, st);
       r.E0 = std::numeric_limits<double>::quiet_NaN();
     } else {
       r.E0 = rayleigh_quotient(ctx, *mv, psi, st);

@@ -1,5 +1,6 @@
 // Contraction plans and algorithms of the DMRG hot path (host orchestration of the kernels).
 #pragma once
+#include <functional>
 #include <memory>
 
 #include "host_core.h"
@@ -131,9 +132,13 @@ struct SplitResult {
 // number of charge sectors of density-matrix splits (own eigensolver) redone on the exact Jacobi
 // route because the CholeskyQR of their singular vectors failed
 int64_t split_fallback_count();
+// on_bidiag (optional): called once the bidiagonalisation launches are queued (bidiagonal route), with
+// the event those launches wait for; work queued on other streams after that event becomes ready
+// together with them, so that the higher-priority cluster launches are placed first.
 SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
                    double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0 = nullptr,
-                   const std::vector<int>* seg_absorb = nullptr);  // per-segment absorb
+                   const std::vector<int>* seg_absorb = nullptr,  // per-segment absorb
+                   const std::function<void(cudaEvent_t)>& on_bidiag = {});
 
 // prepareMatrix(BL1, lambda, BL2, "r", multiply=true, truncate=true, delta): right-orthonormalise BL2,
 // multiply U*D into BL1 (BL1 may be null at the left edge).
@@ -169,11 +174,16 @@ struct EnergyJob {
   Ctx* ctx = nullptr;
   std::unique_ptr<MatvecPlan> mv;
   LanczosStats* st = nullptr;
+  const Tensor* psi = nullptr;
+  bool launched = false;
   double* buf = nullptr;  // H psi (nw) | reduction partials | the two dot products
   int64_t nw = 0;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};  // matvec start / end, dots done
   bool pending() const { return ctx != nullptr; }
-  void start(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& psi, LanczosStats* s);
+  // prepare: take the plan and the state (nothing queued); launch: queue the matvec and the dot
+  // products on the side stream after `after` (an event of the main stream's work; nullptr: all of it)
+  void prepare(Ctx* c, std::unique_ptr<MatvecPlan> plan, const Tensor& psi, LanczosStats* s);
+  void launch(cudaEvent_t after);
   double finish();
   void release();
   ~EnergyJob() { release(); }

@@ -1122,10 +1122,14 @@ __device__ void gk_invit_one(const GkOp& o, int k, int k_first, double* x, doubl
 
 // threads list (op, k) for k < kept(op), kept counts from the truncation; scratch: 6 * nmax2 doubles
 // per listed thread, interleaved with stride nthreads
+// cpw chains per warp (lanes cpw..31 idle): a warp's FP64 instruction occupies its SMSP's FP64 pipe for
+// the same time however few lanes are active, so fewer chains per warp spread them over more SMSPs
 __global__ void k_gk_invit(const GkOp* __restrict__ ops, const int32_t* __restrict__ op_of,
                            const int32_t* __restrict__ k_of, const int32_t* __restrict__ kept, int nthreads, int nmax2,
-                           double* scratch) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+                           double* scratch, int cpw) {
+  const int lane = threadIdx.x & 31;
+  if (lane >= cpw) return;
+  const int t = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * cpw + lane;
   if (t >= nthreads) return;
   const int op = op_of[t];
   const GkOp o = ops[op];
@@ -1142,7 +1146,13 @@ __global__ void k_gk_invit(const GkOp* __restrict__ ops, const int32_t* __restri
 void launch_gk_invit(const GkOp* ops, const int32_t* op_of, const int32_t* k_of, const int32_t* kept, int nthreads,
                      int nmax2, double* scratch, cudaStream_t s) {
   if (nthreads <= 0) return;
-  k_gk_invit<<<(nthreads + 31) / 32, 32, 0, s>>>(ops, op_of, k_of, kept, nthreads, nmax2, scratch);
+  static const int cpw = [] {
+    const char* e = std::getenv("MPSG_INVIT_CPW");
+    const int v = e ? std::atoi(e) : 8;
+    return (v == 1 || v == 2 || v == 4 || v == 16 || v == 32) ? v : 8;
+  }();
+  const int nwarps = (nthreads + cpw - 1) / cpw;
+  k_gk_invit<<<nwarps, 32, 0, s>>>(ops, op_of, k_of, kept, nthreads, nmax2, scratch, cpw);
   g_bd_launches.fetch_add(1);
 }
 
