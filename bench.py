@@ -647,6 +647,10 @@ def split_arm(args):
     lib.check(ctx.L.mpsg_lanczos2(ctx.h, Lt.h, Rt.h, A1.h, A2.h, w1.ref(), w2.ref(), k0.ref(), k1.ref(), 500, 1e-12, 1,
                                   lib.PREC["fp64"], 0, C.byref(st), C.byref(E0), C.byref(it)))
     psi = lib.Tensor(ctx, st)
+    # only the state stays on the device (the engine, its environments and site tensors are released)
+    del Lt, Rt, A1, A2
+    eng.close()
+    ctx.trim()
 
     def split_once():
         U, V, lam = C.c_void_p(), C.c_void_p(), C.c_void_p()

@@ -74,6 +74,9 @@ const char* mpsg_last_error(void);
 /* stream: a cudaStream_t (NULL = the library's own non-blocking stream). */
 mpsg_status mpsg_ctx_set_stream(mpsg_ctx ctx, void* stream);
 mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
+/* Waits for the context's work and returns the device memory the library's stream-ordered
+ * allocations keep cached (the default memory pool of the device) to the driver. */
+mpsg_status mpsg_ctx_trim(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
 /* Number of charge sectors of splits on the library's own SVD routes (svd methods 3 and 4) that were

@@ -54,6 +54,16 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx) {
   C(ctx)->sync();
   API_END
 }
+mpsg_status mpsg_ctx_trim(mpsg_ctx ctx) {
+  API_BEGIN
+  Ctx* c = C(ctx);
+  c->sync();
+  if (c->side) MPSG_CUDA(cudaStreamSynchronize(c->side));
+  cudaMemPool_t pool;
+  MPSG_CUDA(cudaDeviceGetDefaultMemPool(&pool, c->device));
+  MPSG_CUDA(cudaMemPoolTrimTo(pool, 0));
+  API_END
+}
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx) {
   return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count() + batch_launch_count() +
          bidiag_launch_count();

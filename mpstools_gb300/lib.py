@@ -39,6 +39,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_ctx_destroy.restype = None
     L.mpsg_ctx_set_stream.argtypes = [vp, vp]
     L.mpsg_ctx_sync.argtypes = [vp]
+    L.mpsg_ctx_trim.argtypes = [vp]
     L.mpsg_ctx_kernel_launches.argtypes = [vp]
     L.mpsg_ctx_kernel_launches.restype = i64
     L.mpsg_ctx_set_svd_method.argtypes = [vp, i32]
@@ -141,6 +142,9 @@ class Context:
 
     def sync(self):
         check(self.L.mpsg_ctx_sync(self.h))
+
+    def trim(self):
+        check(self.L.mpsg_ctx_trim(self.h))
 
     def kernel_launches(self) -> int:
         return int(self.L.mpsg_ctx_kernel_launches(self.h))
