@@ -391,6 +391,13 @@ def gpu_arm(args):
                    "kernel": f"k_tc_gemm<{mv_prec}> (conversion + stage A + stage C of one matvec)",
                    "matvec_seconds": mv_tc, "bf16_equivalent_mma_per_algorithmic_flop": mma_per_flop,
                    "tensor_issue_frac": ach * mma_per_flop / pk["bf16_tflops"]}
+        tuned, hits, sched, ms6 = ctx.tc_autotune_info()
+        names = ["round_robin", "snake", "lpt"]
+        roof_tc["block_schedule_autotuner"] = {
+            "signatures_timed": tuned, "plans_from_cache": hits,
+            "stage_a": names[sched[0]] if sched[0] >= 0 else None,
+            "stage_c": names[sched[1]] if sched[1] >= 0 else None,
+            "last_timing_ms": {"stage_a": dict(zip(names, ms6[:3])), "stage_c": dict(zip(names, ms6[3:]))}}
 
     # --------------------------------------------------------------- e2e through the C ABI, host buffers
     e2e_raw = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)

@@ -79,6 +79,12 @@ mpsg_status mpsg_ctx_sync(mpsg_ctx ctx);
 mpsg_status mpsg_ctx_trim(mpsg_ctx ctx);
 /* Number of kernels this library launched on ctx since creation. */
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
+/* The tensor-core matvec's block-schedule autotuner (process-wide): signatures timed, plans served
+ * from its cache, the schedule of each stage of the most recent tensor-core plan (0 round robin,
+ * 1 snake, 2 greedy longest-processing-time) and, of the most recent timing, the best time in ms of
+ * each schedule for stage A (entries 0-2) and stage C (3-5; -1 where not timed).  Any pointer may be
+ * null. */
+void mpsg_tc_autotune_info(int64_t* tuned, int64_t* cache_hits, int32_t* last_schedule2, float* last_timing6);
 /* Number of charge sectors of splits on the library's own SVD routes (svd methods 3 and 4) that were
  * redone on the Jacobi route because their singular vectors were too dependent for CholeskyQR. */
 int64_t mpsg_split_fallbacks(void);

@@ -64,6 +64,14 @@ mpsg_status mpsg_ctx_trim(mpsg_ctx ctx) {
   MPSG_CUDA(cudaMemPoolTrimTo(pool, 0));
   API_END
 }
+void mpsg_tc_autotune_info(int64_t* tuned, int64_t* cache_hits, int32_t* last_schedule2, float* last_timing6) {
+  tc_autotune_counts(tuned, cache_hits);
+  if (last_schedule2) tc_last_schedules(last_schedule2, last_timing6);
+  else if (last_timing6) {
+    int32_t tmp[2];
+    tc_last_schedules(tmp, last_timing6);
+  }
+}
 int64_t mpsg_ctx_kernel_launches(mpsg_ctx) {
   return kernel_launch_count() + tc_launch_count() + eig_launch_count() + tebd_launch_count() + batch_launch_count() +
          bidiag_launch_count();

@@ -3,6 +3,8 @@
 #include "host_ops.h"
 
 #include <limits>
+#include <mutex>
+#include <queue>
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -129,8 +131,8 @@ void MatvecPlan::run(const double* theta_in, double* theta_out) {
   }
   const TcBases B = tc_bases(*this, theta_in, theta_out);
   launch_tc_convert(kind, nprod == 3 ? 2 : 1, dconv_theta, nconv_theta, nimg_theta, B, ctx->stream);
-  launch_tc_gemm(kind, nprod, dprob[0], dseg[0], dtile[0], ntile[0], B, nsm, ctx->stream);
-  launch_tc_gemm(kind, nprod, dprob[1], dseg[1], dtile[1], ntile[1], B, nsm, ctx->stream);
+  launch_tc_gemm(kind, nprod, dprob[0], dseg[0], dtile[0], ntile[0], B, nsm, ctx->stream, tgrid[0]);
+  launch_tc_gemm(kind, nprod, dprob[1], dseg[1], dtile[1], ntile[1], B, nsm, ctx->stream, tgrid[1]);
 }
 
 void MatvecPlan::check_error() {
@@ -150,6 +152,92 @@ static int64_t add_images(std::map<K, int64_t>& off, const K& key, int rows, int
   off[key] = total;
   total += nimg * 16384;
   return off[key];
+}
+
+// ---- block schedules of the tcgen05 stages and their autotuner
+static std::atomic<int64_t> g_tc_tuned{0}, g_tc_hits{0};
+void tc_autotune_counts(int64_t* tuned, int64_t* cache_hits) {
+  if (tuned) *tuned = g_tc_tuned.load();
+  if (cache_hits) *cache_hits = g_tc_hits.load();
+}
+static std::atomic<int32_t> g_tc_last[2] = {{-1}, {-1}};
+static std::mutex g_tc_ms_mu;
+static float g_tc_ms[6] = {-1, -1, -1, -1, -1, -1};
+void tc_last_schedules(int32_t* sched2, float* timing6) {
+  sched2[0] = g_tc_last[0].load();
+  sched2[1] = g_tc_last[1].load();
+  if (timing6) {
+    std::lock_guard<std::mutex> g(g_tc_ms_mu);
+    for (int i = 0; i < 6; ++i) timing6[i] = g_tc_ms[i];
+  }
+}
+const char* tc_schedule_name(int s) {
+  return s == 0 ? "round_robin" : s == 1 ? "snake" : s == 2 ? "lpt" : "?";
+}
+constexpr int kTcSchedules = 3;
+// Tile layout of schedule `sched` for `grid` persistent CTAs (CTA b runs positions b, b + grid, ...).
+// tiles: (K chunks, tile), longest first.  A tile's estimated cost is its K chunks plus the fill and
+// drain of the operand ring (about four chunks).
+static std::vector<TcTile> tc_layout(const std::vector<std::pair<int, TcTile>>& tiles, int grid, int sched) {
+  std::vector<TcTile> out;
+  const int n = (int)tiles.size();
+  if (sched == 0) {
+    for (auto& t : tiles) out.push_back(t.second);
+  } else if (sched == 1) {
+    for (int r0 = 0; r0 < n; r0 += grid) {
+      const int r1 = std::min(n, r0 + grid);
+      const bool rev = ((r0 / grid) & 1) != 0;
+      if (!rev || r1 - r0 < grid) {
+        for (int i = r0; i < r1; ++i) out.push_back(tiles[i].second);
+      } else {
+        for (int i = r1 - 1; i >= r0; --i) out.push_back(tiles[i].second);
+      }
+    }
+  } else {
+    std::vector<std::vector<TcTile>> lists(grid);
+    std::priority_queue<std::pair<int64_t, int>, std::vector<std::pair<int64_t, int>>, std::greater<>> load;
+    for (int b = 0; b < grid; ++b) load.push({0, b});
+    for (auto& t : tiles) {
+      auto top = load.top();
+      load.pop();
+      lists[top.second].push_back(t.second);
+      load.push({top.first + t.first + 4, top.second});
+    }
+    size_t len = 0;
+    for (auto& l : lists) len = std::max(len, l.size());
+    const TcTile pad{-1, 0, 0};
+    for (size_t r = 0; r < len; ++r)
+      for (int b = 0; b < grid; ++b) out.push_back(r < lists[b].size() ? lists[b][r] : pad);
+  }
+  return out;
+}
+// coarse signature of a stage: precision, stage, and the tile count / K chunks in ~20 % buckets
+static uint64_t tc_signature(int kind, int nprod, int st, const std::vector<std::pair<int, TcTile>>& tiles) {
+  auto bucket = [](double x) { return (uint64_t)std::lround(std::log(std::max(x, 1.0)) / std::log(1.2)); };
+  int64_t ksum = 0;
+  int kmax = 0;
+  for (auto& t : tiles) {
+    ksum += t.first;
+    kmax = std::max(kmax, t.first);
+  }
+  return ((uint64_t)kind << 60) ^ ((uint64_t)nprod << 56) ^ ((uint64_t)st << 52) ^ (bucket((double)tiles.size()) << 36) ^
+         (bucket((double)ksum) << 18) ^ bucket((double)kmax);
+}
+static bool tc_autotune_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("MPSG_TC_AUTOTUNE");
+    return !(e && std::atoi(e) == 0);
+  }();
+  return on;
+}
+// MPSG_TC_SCHEDULE=0|1|2 fixes the block schedule (no timing); -1: the autotuner decides
+static int tc_forced_schedule() {
+  static const int v = [] {
+    const char* e = std::getenv("MPSG_TC_SCHEDULE");
+    const int x = e ? std::atoi(e) : -1;
+    return (x >= 0 && x < kTcSchedules) ? x : -1;
+  }();
+  return v;
 }
 
 static void build_tc(MatvecPlan& P, Ctx* ctx, const Layout& th,
@@ -207,7 +295,9 @@ static void build_tc(MatvecPlan& P, Ctx* ctx, const Layout& th,
   }
   P.derr = (int*)ctx->dmalloc(sizeof(int));
   MPSG_CUDA(cudaMemsetAsync(P.derr, 0, sizeof(int), ctx->stream));
-  // work lists
+  // work lists; the candidate block schedules of each stage
+  std::vector<TcTile> cand[2][kTcSchedules];
+  uint64_t sig[2] = {0, 0};
   for (int st = 0; st < 2; ++st) {
     std::vector<TcProb> probs;
     std::vector<TcSeg> segs;
@@ -278,18 +368,16 @@ static void build_tc(MatvecPlan& P, Ctx* ctx, const Layout& th,
     }
     std::stable_sort(tiles.begin(), tiles.end(),
                      [](const std::pair<int, TcTile>& a, const std::pair<int, TcTile>& b) { return a.first > b.first; });
-    std::vector<TcTile> tl;
-    for (auto& t : tiles) tl.push_back(t.second);
-    P.ntile[st] = (int)tl.size();
+    const int grid = std::max(1, std::min((int)tiles.size(), P.nsm));
+    for (int c = 0; c < kTcSchedules; ++c) cand[st][c] = tc_layout(tiles, grid, c);
+    sig[st] = tc_signature(P.kind, P.nprod, st, tiles);
+    P.tgrid[st] = grid;
     P.dprob[st] = (TcProb*)ctx->dmalloc(sizeof(TcProb) * std::max<size_t>(probs.size(), 1));
     P.dseg[st] = (TcSeg*)ctx->dmalloc(sizeof(TcSeg) * std::max<size_t>(segs.size(), 1));
-    P.dtile[st] = (TcTile*)ctx->dmalloc(sizeof(TcTile) * std::max<size_t>(tl.size(), 1));
     if (!probs.empty())
       MPSG_CUDA(cudaMemcpyAsync(P.dprob[st], probs.data(), sizeof(TcProb) * probs.size(), cudaMemcpyHostToDevice, ctx->stream));
     if (!segs.empty())
       MPSG_CUDA(cudaMemcpyAsync(P.dseg[st], segs.data(), sizeof(TcSeg) * segs.size(), cudaMemcpyHostToDevice, ctx->stream));
-    if (!tl.empty())
-      MPSG_CUDA(cudaMemcpyAsync(P.dtile[st], tl.data(), sizeof(TcTile) * tl.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
   P.nconv_theta = (int)conv_th.size();
   P.nimg_theta = img_th;
@@ -304,6 +392,75 @@ static void build_tc(MatvecPlan& P, Ctx* ctx, const Layout& th,
     const TcBases B = tc_bases(P, nullptr, nullptr);
     launch_tc_convert(P.kind, ncomp, d, (int)conv_env.size(), img_env, B, ctx->stream);
     ctx->dfree(d);
+  }
+  // block schedule of each stage: from the cache, or timed (CUDA events, the plan's own images; stage
+  // C into a scratch output) once per signature.  Every schedule computes every tile the same way,
+  // so the choice never changes a result.
+  static std::mutex mu;
+  static std::map<uint64_t, int> best;
+  for (int st = 0; st < 2; ++st) {
+    int choice = tc_forced_schedule() >= 0 ? tc_forced_schedule() : 0;
+    bool have = !tc_autotune_enabled() || tc_forced_schedule() >= 0 || cand[st][0].empty();
+    if (!have) {
+      std::lock_guard<std::mutex> g(mu);
+      auto it = best.find(sig[st]);
+      if (it != best.end()) {
+        choice = it->second;
+        have = true;
+        g_tc_hits.fetch_add(1);
+      }
+    }
+    if (!have) {
+      double* scratch = st == 1 ? (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(P.out.nelem, 2)) : nullptr;
+      std::vector<TcTile*> dev(kTcSchedules);
+      for (int c = 0; c < kTcSchedules; ++c) {
+        dev[c] = (TcTile*)ctx->dmalloc(sizeof(TcTile) * cand[st][c].size());
+        MPSG_CUDA(cudaMemcpyAsync(dev[c], cand[st][c].data(), sizeof(TcTile) * cand[st][c].size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+      }
+      const TcBases B = tc_bases(P, nullptr, scratch);
+      cudaEvent_t e0, e1;
+      MPSG_CUDA(cudaEventCreate(&e0));
+      MPSG_CUDA(cudaEventCreate(&e1));
+      float tbest = 1e30f;
+      float tc_best[kTcSchedules];
+      for (int c = 0; c < kTcSchedules; ++c) tc_best[c] = 1e30f;
+      for (int rep = 0; rep < 3; ++rep)
+        for (int c = 0; c < kTcSchedules; ++c) {
+          MPSG_CUDA(cudaEventRecord(e0, ctx->stream));
+          launch_tc_gemm(P.kind, P.nprod, P.dprob[st], P.dseg[st], dev[c], (int)cand[st][c].size(), B, P.nsm,
+                         ctx->stream, P.tgrid[st]);
+          MPSG_CUDA(cudaEventRecord(e1, ctx->stream));
+          MPSG_CUDA(cudaEventSynchronize(e1));
+          float ms = 0;
+          MPSG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (rep > 0) tc_best[c] = std::min(tc_best[c], ms);
+          if (rep > 0 && ms < tbest) {  // the first round warms up
+            tbest = ms;
+            choice = c;
+          }
+        }
+      {
+        std::lock_guard<std::mutex> g(g_tc_ms_mu);
+        for (int c = 0; c < kTcSchedules; ++c) g_tc_ms[st * 3 + c] = tc_best[c];
+        for (int c = 0; c < kTcSchedules && st == 0; ++c) g_tc_ms[3 + c] = -1.f;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      for (auto* d : dev) ctx->dfree(d);
+      if (scratch) ctx->dfree(scratch);
+      P.check_error();
+      std::lock_guard<std::mutex> g(mu);
+      best[sig[st]] = choice;
+      g_tc_tuned.fetch_add(1);
+    }
+    const std::vector<TcTile>& tl = cand[st][choice];
+    P.tsched[st] = choice;
+    g_tc_last[st].store(choice);
+    P.ntile[st] = (int)tl.size();
+    P.dtile[st] = (TcTile*)ctx->dmalloc(sizeof(TcTile) * std::max<size_t>(tl.size(), 1));
+    if (!tl.empty())
+      MPSG_CUDA(cudaMemcpyAsync(P.dtile[st], tl.data(), sizeof(TcTile) * tl.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
 }
 

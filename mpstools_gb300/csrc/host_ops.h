@@ -67,6 +67,8 @@ struct MatvecPlan {
   TcSeg* dseg[2] = {nullptr, nullptr};
   TcTile* dtile[2] = {nullptr, nullptr};
   int ntile[2] = {0, 0};
+  int tgrid[2] = {0, 0};   // persistent CTAs of each stage (0: min(tiles, SMs))
+  int tsched[2] = {0, 0};  // block schedule chosen for each stage (tc_schedule_name)
   TcConv* dconv_theta = nullptr;
   int nconv_theta = 0, nimg_theta = 0;
   int* derr = nullptr;
@@ -82,6 +84,17 @@ struct MatvecPlan {
   }
   ~MatvecPlan();
 };
+// Block schedules of the tcgen05 stages, chosen per plan by timing (autotuner): 0 = tiles in
+// longest-K-first order dealt round-robin to the persistent CTAs, 1 = the same order dealt in a
+// snake (alternate rounds reversed), 2 = greedy longest-processing-time assignment (each tile, longest
+// first, to the CTA with the least estimated work; lists padded).  The choice is cached per
+// block-size signature.  tuned / cache_hits count the signatures timed and the plans served from
+// the cache.
+const char* tc_schedule_name(int s);
+void tc_autotune_counts(int64_t* tuned, int64_t* cache_hits);
+// schedules of the most recent tensor-core plan; timing6 (optional): best ms of each schedule in the
+// most recent timing, stage A then stage C (-1 where not timed)
+void tc_last_schedules(int32_t* sched2, float* timing6 = nullptr);
 // FP64 plan applied with the stage-A intermediate in the library's fixed device array (noalloc.cu)
 void matvec_noalloc(MatvecPlan& P, const double* theta_in, double* theta_out);
 // device address of that array on `device` (the current device); resolved once per device

@@ -238,6 +238,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const TcProb* __restric
       int issued = 0;
       for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const TcTile tl = tiles[t];
+        if (tl.prob < 0) continue;  // padding of a host-chosen block schedule
         const TcProb P = prob[tl.prob];
         for (int s = P.seg0; s < P.seg1; ++s) {
           const TcSeg S = seg[s];
@@ -278,11 +279,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const TcProb* __restric
       int stage = 0;
       uint32_t phase = 0;
       int local = 0;
-      for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const TcTile tl = tiles[t];
+        if (tl.prob < 0) continue;
         const TcProb P = prob[tl.prob];
         const int acc = local & 1;
         const uint32_t accph = (local >> 1) & 1;
+        ++local;
         if (!mbar_wait(&acce[acc], accph ^ 1, err, 2)) goto mma_done;
         tc_fence_after();
         const uint32_t d = tmem + acc * 128;
@@ -324,11 +327,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_gemm(const TcProb* __restric
     const int q = warp & 3;  // TMEM lane quarter owned by this warp
     const int r = q * 32 + lane;
     int local = 0;
-    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++local) {
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
       const TcTile tl = tiles[t];
+      if (tl.prob < 0) continue;
       const TcProb P = prob[tl.prob];
       const int acc = local & 1;
       const uint32_t accph = (local >> 1) & 1;
+      ++local;
       if (!mbar_wait(&accf[acc], accph, err, 4)) break;
       tc_fence_after();
       const bool zero = (P.seg0 == P.seg1);
@@ -420,9 +425,9 @@ static size_t tc_smem_bytes(int nprod) {
 }
 
 void launch_tc_gemm(int kind, int nprod, const TcProb* prob, const TcSeg* seg, const TcTile* tiles, int ntiles,
-                    const TcBases& B, int nsm, cudaStream_t s) {
+                    const TcBases& B, int nsm, cudaStream_t s, int grid_override) {
   if (ntiles <= 0) return;
-  const int grid = ntiles < nsm ? ntiles : nsm;
+  const int grid = grid_override > 0 ? grid_override : (ntiles < nsm ? ntiles : nsm);
   const size_t sh = tc_smem_bytes(nprod);
 #define MPSG_TC_CASE(K, P)                                                                         \
   if (kind == K && nprod == P) {                                                                   \

@@ -20,7 +20,7 @@ struct TcProb {
   int8_t mode, c_slot, beta;
 };
 struct TcTile {
-  int32_t prob, mt, nt;
+  int32_t prob, mt, nt;  // prob < 0: padding (no work)
 };
 // FP64 block (element (row, k) at src[row*rs + k*ks], R rows, K columns) -> images from img0 on
 struct TcConv {
@@ -37,8 +37,10 @@ struct TcBases {
 };
 
 // kind: 0 = kind::tf32, 1 = kind::f16 with bf16 operands; nprod: 1 or 3 (hi/lo split)
+// grid_override > 0: that many persistent CTAs (a block schedule laid out for it); tiles with
+// prob < 0 are padding and skipped
 void launch_tc_gemm(int kind, int nprod, const TcProb* prob, const TcSeg* seg, const TcTile* tiles, int ntiles,
-                    const TcBases& B, int nsm, cudaStream_t s);
+                    const TcBases& B, int nsm, cudaStream_t s, int grid_override = 0);
 void launch_tc_convert(int kind, int ncomp, const TcConv* ops, int nops, int nimg, const TcBases& B, cudaStream_t s);
 int64_t tc_launch_count();
 

@@ -40,6 +40,8 @@ def load(build_if_missing: bool = False):
     L.mpsg_ctx_set_stream.argtypes = [vp, vp]
     L.mpsg_ctx_sync.argtypes = [vp]
     L.mpsg_ctx_trim.argtypes = [vp]
+    L.mpsg_tc_autotune_info.argtypes = [vp, vp, vp, vp]
+    L.mpsg_tc_autotune_info.restype = None
     L.mpsg_ctx_kernel_launches.argtypes = [vp]
     L.mpsg_ctx_kernel_launches.restype = i64
     L.mpsg_ctx_set_svd_method.argtypes = [vp, i32]
@@ -145,6 +147,14 @@ class Context:
 
     def trim(self):
         check(self.L.mpsg_ctx_trim(self.h))
+
+    def tc_autotune_info(self):
+        """(signatures timed, plans served from the cache, [stage-A, stage-C] schedule of the last
+        tensor-core plan: 0 round robin, 1 snake, 2 greedy longest-processing-time, best ms of each
+        schedule in the last timing: stage A x3 then stage C x3, -1 where not timed)"""
+        t, h, sch, ms = C.c_int64(), C.c_int64(), (C.c_int32 * 2)(), (C.c_float * 6)()
+        self.L.mpsg_tc_autotune_info(C.byref(t), C.byref(h), sch, ms)
+        return t.value, h.value, [sch[0], sch[1]], [float(x) for x in ms]
 
     def kernel_launches(self) -> int:
         return int(self.L.mpsg_ctx_kernel_launches(self.h))
