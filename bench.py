@@ -400,6 +400,7 @@ def gpu_arm(args):
             "last_timing_ms": {"stage_a": dict(zip(names, ms6[:3])), "stage_c": dict(zip(names, ms6[3:]))}}
 
     # --------------------------------------------------------------- e2e through the C ABI, host buffers
+    env_leg = env_update_leg(ctx, eng, W, ik, center, torch, flush) if not args.steps_only else None
     e2e_raw = e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec)
     e2e = {"value": info["flops"] * e2e_raw["matvecs"] * world / e2e_raw["seconds"] / 1e12, "unit": "TFLOP/s",
            "h2d_bytes_per_step": e2e_raw["h2d_bytes_per_step"], "d2h_bytes_per_step": e2e_raw["d2h_bytes_per_step"],
@@ -449,7 +450,7 @@ def gpu_arm(args):
                 "lanczos_seconds_per_step": (st1["lanczos_seconds"] - st0["lanczos_seconds"]) / args.steps,
                 "energies": [s["E"] for s in steps_rec], "truncated_weight": [s["tw"] for s in steps_rec],
                 "centre_bond_spectrum": spectrum, "fp64_gpu_path": fp64_leg, "auto_path": auto_leg,
-                "roofline_tensor_matvec": roof_tc,
+                "roofline_tensor_matvec": roof_tc, "env_update_by_precision": env_leg,
                 "matvec_flops_reference_schedule": info["flops_ref"], "oracle_check": oracle_check}
         print(json.dumps(line), flush=True)
     if dist:
@@ -469,6 +470,43 @@ def cpu_update_seconds_window(W, ik, sites_c, center, chi, nsteps, threads, envs
         g.do_step(center, 1 if i % 2 == 0 else -1, chi)
         ts.append(time.perf_counter() - t0)
     return (ts, g.steps(), g) if keep else (ts, g.steps())
+
+
+def env_update_leg(ctx, eng, W, ik, center, torch, flush, reps=5):
+    """addContractionLayer at the centre bond (left environment through the centre site tensor) in
+    FP64 and in each tensor-core precision, through the C ABI on device tensors: median ms (L2
+    flushed before each call) and the largest deviation from the FP64 result relative to its largest
+    entry."""
+    import ctypes as C
+    from mpstools_gb300 import lib
+    Lt, A = eng.env_tensor("L", center - 1), eng.site_tensor(center)
+    w, k = lib.MPOArg(W[center]), lib.ItoKeyArg(ik[center])
+    out = {}
+    ref = None
+    for prec in ("fp64", "tf32x3", "bf16x3", "tf32", "bf16"):
+        ts = []
+        for rep in range(reps + 1):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a = time.perf_counter()
+            h = C.c_void_p()
+            lib.check(ctx.L.mpsg_add_contraction_layer(ctx.h, Lt.h, A.h, w.ref(), k.ref(), 1, lib.PREC[prec],
+                                                       C.byref(h)))
+            ctx.sync()
+            if rep:
+                ts.append(time.perf_counter() - a)
+            t = lib.Tensor(ctx, h)
+            if rep == reps:
+                d = t.to_dict()
+                if prec == "fp64":
+                    ref = d
+                    out[prec] = {"ms": float(np.median(ts)) * 1e3}
+                else:
+                    scale = max(np.abs(v).max() for v in ref.values())
+                    err = max(float(np.abs(d[q] - ref[q]).max()) for q in ref) / scale
+                    out[prec] = {"ms": float(np.median(ts)) * 1e3, "max_rel_diff_vs_fp64": err}
+            del t
+    return out
 
 
 def e2e_leg(ctx, eng, W, ik, center, args, stream, torch, flush, prec):

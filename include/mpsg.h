@@ -128,7 +128,10 @@ mpsg_status mpsg_contract_twosite(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mp
                                   const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
                                   const mpsg_itokey* ikr, mpsg_prec prec, mpsg_tensor* out);
 
-/* addContractionLayer(BL, A, mpo, itokey, direction)  -- src/MPSfunctions.hpp:442-493. */
+/* addContractionLayer(BL, A, mpo, itokey, direction)  -- src/MPSfunctions.hpp:442-493.
+ * prec: MPSG_PREC_FP64 (the reference's arithmetic), or TF32 / TF32X3 / BF16 / BF16X3: both grouped
+ * products on the tensor cores with FP32 accumulation (relative deviation from FP64 of ~1e-7 for
+ * TF32X3, ~1e-5 BF16X3, ~1e-3 TF32, ~1e-2 BF16, relative to the largest output entry). */
 mpsg_status mpsg_add_contraction_layer(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor A, const mpsg_mpo* W,
                                        const mpsg_itokey* ik, int32_t direction, mpsg_prec prec,
                                        mpsg_tensor* out);
@@ -209,6 +212,10 @@ mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, 
 mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax);
 /* The options in effect (set by mpsg_dmrg_set_options or restored by mpsg_dmrg_load); any output
  * pointer may be NULL.  No reference counterpart (the reference keeps them as engine members). */
+/* Arithmetic of doStep's environment updates (default MPSG_PREC_FP64; TF32 / TF32X3 / BF16 / BF16X3
+ * run them on the tensor cores, about five times faster at chi = 2048, but H then carries their
+ * ~1e-7 (TF32X3) relative error into every energy: meant for the early sweeps of a chi ramp). */
+mpsg_status mpsg_dmrg_set_env_prec(mpsg_dmrg e, mpsg_prec prec);
 mpsg_status mpsg_dmrg_get_options(mpsg_dmrg e, int32_t* prec, int32_t* reorth, int32_t* lanmax);
 /* DMRGengine::simulate(maxsteps, EnConv, chimax, doTrunc, tr_weight, delta, testenergy):
  * orthonormalize("rl"), computeR, sweeps, final doStep(0,-1).  E = last Lanczos energy. */

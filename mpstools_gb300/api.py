@@ -286,6 +286,10 @@ class DMRGengine:
         return [dict(site=int(a[0][i]), dir=int(a[1][i]), iters=int(a[2][i]), chi=int(a[3][i]), E=float(E[i]),
                      tw=float(tw[i])) for i in range(n)]
 
+    def set_env_prec(self, prec):
+        """Arithmetic of doStep's environment updates: "fp64" (default) or a tensor-core precision."""
+        check(self.ctx.L.mpsg_dmrg_set_env_prec(self.h, lib.PREC[prec]))
+
     def stats(self):
         s = np.zeros(12)
         check(self.ctx.L.mpsg_dmrg_stats_ext(self.h, lib.ptr(s), 12))

@@ -144,6 +144,11 @@ void mpsg_tensor_destroy(mpsg_tensor t) {
 static void check_prec(mpsg_prec prec) {  // FP64 only (environment update, split)
   MPSG_CHECK(prec == MPSG_PREC_FP64, "only MPSG_PREC_FP64 is available for this entry point");
 }
+// environment updates: FP64 or a tensor-core precision (AUTO and MIXED are Lanczos modes)
+static void check_env_prec(mpsg_prec prec) {
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3,
+             "the environment update takes MPSG_PREC_FP64, TF32, TF32X3, BF16 or BF16X3");
+}
 static void check_matvec_prec(mpsg_prec prec) {
   MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "matvec precision must be FP64, TF32(X3) or BF16(X3)");
 }
@@ -175,10 +180,10 @@ mpsg_status mpsg_add_contraction_layer(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tensor
                                        const mpsg_itokey* ik, int32_t direction, mpsg_prec prec, mpsg_tensor* out) {
   API_BEGIN
   MPSG_CHECK(out, "null output");
-  check_prec(prec);
+  check_env_prec(prec);
   Ctx* c = C(ctx);
   MPSG_CHECK(T(A).b.size() > 0, "Error in addContractionLayer: A is empty.");
-  TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr);
+  TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr, nullptr, (int)prec);
   c->sync();
   *out = wrap(o);
   API_END
@@ -189,11 +194,11 @@ mpsg_status mpsg_add_contraction_layer2(mpsg_ctx ctx, mpsg_tensor BL, mpsg_tenso
                                         mpsg_tensor* out) {
   API_BEGIN
   MPSG_CHECK(out, "null output");
-  check_prec(prec);
+  check_env_prec(prec);
   Ctx* c = C(ctx);
   MPSG_CHECK(T(A).b.size() > 0, "Error in addContractionLayer: A is empty.");
   MPSG_CHECK(T(Ap).b.size() > 0, "Error in addContractionLayer: Ap is empty.");
-  TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr, &T(Ap));
+  TensorP o = env_update(c, T(BL), T(A), mpo_from_c(W), itokey_from_c(ik), direction, nullptr, &T(Ap), (int)prec);
   c->sync();
   *out = wrap(o);
   API_END
@@ -338,6 +343,13 @@ mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, i
   e->e->prec = prec;
   e->e->reorth = reorth != 0;
   e->e->lanmax = lanmax;
+  API_END
+}
+mpsg_status mpsg_dmrg_set_env_prec(mpsg_dmrg e, mpsg_prec prec) {
+  API_BEGIN
+  MPSG_CHECK(e && e->e, "null engine");
+  check_env_prec(prec);
+  e->e->env_prec = prec;
   API_END
 }
 mpsg_status mpsg_dmrg_get_options(mpsg_dmrg e, int32_t* prec, int32_t* reorth, int32_t* lanmax) {

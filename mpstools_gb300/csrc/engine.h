@@ -26,6 +26,9 @@ struct Engine {
   mpsg_prec prec = MPSG_PREC_FP64;
   bool reorth = false;
   int lanmax = 500;
+  // arithmetic of the environment updates of doStep (FP64 by default: a tensor-core environment
+  // perturbs H itself, by ~1e-7 relative for TF32X3, which the FP64 energy then carries)
+  mpsg_prec env_prec = MPSG_PREC_FP64;
   std::vector<StepRec> steps;
   int64_t updates_base = 0;  // doStep calls made before this engine was loaded from a checkpoint
   int64_t updates_done() const { return updates_base + (int64_t)steps.size(); }
@@ -224,8 +227,10 @@ struct Engine {
     mps[site] = sp.U;
     mps[site + 1] = sp.Vt;
     lam[site] = sp.lam;
-    if (dir > 0) L[site] = env_update(ctx, *L[site - 1], *mps[site], mpo[site], ik[site], 1, &env_flops);
-    else R[site + 1] = env_update(ctx, *R[site + 2], *mps[site + 1], mpo[site + 1], ik[site + 1], -1, &env_flops);
+    if (dir > 0) L[site] = env_update(ctx, *L[site - 1], *mps[site], mpo[site], ik[site], 1, &env_flops, nullptr, env_prec);
+    else
+      R[site + 1] = env_update(ctx, *R[site + 2], *mps[site + 1], mpo[site + 1], ik[site + 1], -1, &env_flops, nullptr,
+                               env_prec);
     ctx->sync();
     env_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
     StepRec r{site, dir, lr.iterations, sp.chi, lr.E0, sp.tw};

@@ -601,16 +601,138 @@ EnvPlan::~EnvPlan() {
 }
 void EnvPlan::run(const double* A, double* out_d, const double* Aup) {
   const double* bases[8] = {dCt, A, dT, out_d, Aup ? Aup : A, nullptr, nullptr, nullptr};
+  if (tc1) {
+    tc1->run(bases);
+    tc2->run(bases);
+    return;
+  }
   st1.run(bases);
   st2.run(bases);
 }
 
+// ---- a GemmPlan stage on the tensor cores
+void TcStage::build(Ctx* c, const GemmPlan& g, int prec) {
+  ctx = c;
+  kind = (prec == MPSG_PREC_TF32 || prec == MPSG_PREC_TF32X3) ? 0 : 1;
+  nprod = (prec == MPSG_PREC_TF32X3 || prec == MPSG_PREC_BF16X3) ? 3 : 1;
+  const int KC = kind == 0 ? 32 : 64;
+  const int ncomp = nprod == 3 ? 2 : 1;
+  int dev = 0;
+  MPSG_CUDA(cudaGetDevice(&dev));
+  MPSG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  auto nkc_of = [&](int K) { return (K + KC - 1) / KC; };
+  // operand images keyed by (slot, offset, rows, K, row stride, K stride, scale)
+  std::map<std::tuple<int, int64_t, int, int, int, int, double>, int64_t> imgs;
+  std::vector<TcConv> conv;
+  int64_t tot = 0;
+  int nimg_tot = 0;
+  auto image = [&](int slot, int64_t off, int rows, int K, int rs, int ks, double scale) {
+    const auto key = std::make_tuple(slot, off, rows, K, rs, ks, scale);
+    auto it = imgs.find(key);
+    if (it != imgs.end()) return it->second;
+    const int nkc = nkc_of(K);
+    const int64_t n = (int64_t)((rows + 127) / 128) * nkc;
+    TcConv cv{};
+    cv.src_off = off;
+    cv.dst_off = tot;
+    cv.R = rows;
+    cv.K = K;
+    cv.rs = rs;
+    cv.ks = ks;
+    cv.nkc = nkc;
+    cv.img0 = nimg_tot;
+    cv.scale = scale;
+    cv.src_slot = (int8_t)slot;
+    cv.dst_slot = 0;
+    conv.push_back(cv);
+    imgs[key] = tot;
+    tot += n * 16384;
+    nimg_tot += (int)n;
+    return imgs[key];
+  };
+  std::vector<TcProb> probs;
+  std::vector<TcSeg> segs;
+  std::vector<std::pair<int, TcTile>> tiles;
+  for (const GProbH& p : g.hprob) {
+    TcProb q{};
+    q.c_off = p.offC;
+    q.ldc = p.ldc;
+    q.M = p.M;
+    q.N = p.N;
+    q.seg0 = (int32_t)segs.size();
+    q.c_nkc = 0;
+    q.mode = 0;
+    q.c_slot = (int8_t)p.baseC;
+    q.beta = (int8_t)p.beta;
+    int work = 0;
+    for (int si = p.seg0; si < p.seg1; ++si) {
+      const GSegH& h = g.hseg[si];
+      // A operand: op(A) is M x K; image rows = M.  B operand: op(B) is K x N; image rows = N.
+      const int64_t ao = image(h.baseA, h.offA, p.M, h.K, h.tA ? h.lda : 1, h.tA ? 1 : h.lda, h.alpha);
+      const int64_t bo = image(h.baseB, h.offB, p.N, h.K, h.tB ? 1 : h.ldb, h.tB ? h.ldb : 1, 1.0);
+      TcSeg sg{};
+      sg.a_off = ao;
+      sg.b_off = bo;
+      sg.nkc = nkc_of(h.K);
+      sg.a_slot = 0;
+      sg.b_slot = 0;
+      segs.push_back(sg);
+      work += sg.nkc;
+    }
+    q.seg1 = (int32_t)segs.size();
+    const int pi = (int)probs.size();
+    probs.push_back(q);
+    for (int mt = 0; mt < (p.M + 127) / 128; ++mt)
+      for (int nt = 0; nt < (p.N + 127) / 128; ++nt) tiles.push_back({work, TcTile{pi, mt, nt}});
+  }
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [](const std::pair<int, TcTile>& a, const std::pair<int, TcTile>& b) { return a.first > b.first; });
+  grid = std::max(1, std::min((int)tiles.size(), nsm));
+  const std::vector<TcTile> tl = tc_layout(tiles, grid, 1);  // snake over longest-K-first
+  img_hi = std::max<int64_t>(tot, 16384);
+  dimg = (uint8_t*)ctx->dmalloc((size_t)img_hi * ncomp);
+  nconv = (int)conv.size();
+  nimg = nimg_tot;
+  ntile = (int)tl.size();
+  dconv = (TcConv*)ctx->dmalloc(sizeof(TcConv) * std::max<size_t>(conv.size(), 1));
+  dprob = (TcProb*)ctx->dmalloc(sizeof(TcProb) * std::max<size_t>(probs.size(), 1));
+  dseg = (TcSeg*)ctx->dmalloc(sizeof(TcSeg) * std::max<size_t>(segs.size(), 1));
+  dtile = (TcTile*)ctx->dmalloc(sizeof(TcTile) * std::max<size_t>(tl.size(), 1));
+  derr = (int*)ctx->dmalloc(sizeof(int));
+  cudaStream_t st = ctx->stream;
+  MPSG_CUDA(cudaMemsetAsync(derr, 0, sizeof(int), st));
+  if (!conv.empty()) MPSG_CUDA(cudaMemcpyAsync(dconv, conv.data(), sizeof(TcConv) * conv.size(), cudaMemcpyHostToDevice, st));
+  if (!probs.empty()) MPSG_CUDA(cudaMemcpyAsync(dprob, probs.data(), sizeof(TcProb) * probs.size(), cudaMemcpyHostToDevice, st));
+  if (!segs.empty()) MPSG_CUDA(cudaMemcpyAsync(dseg, segs.data(), sizeof(TcSeg) * segs.size(), cudaMemcpyHostToDevice, st));
+  if (!tl.empty()) MPSG_CUDA(cudaMemcpyAsync(dtile, tl.data(), sizeof(TcTile) * tl.size(), cudaMemcpyHostToDevice, st));
+}
+void TcStage::run(const double* const* bases) {
+  if (ntile == 0) return;
+  TcBases B;
+  for (int i = 0; i < 6; ++i) {
+    B.img[i] = nullptr;
+    B.lo_off[i] = 0;
+    B.f64[i] = const_cast<double*>(bases[i]);
+  }
+  B.img[0] = dimg;
+  B.lo_off[0] = img_hi;
+  B.err = derr;
+  launch_tc_convert(kind, nprod == 3 ? 2 : 1, dconv, nconv, nimg, B, ctx->stream);
+  launch_tc_gemm(kind, nprod, dprob, dseg, dtile, ntile, B, nsm, ctx->stream, grid);
+}
+TcStage::~TcStage() {
+  if (!ctx) return;
+  for (void* p : {(void*)dimg, (void*)dconv, (void*)dprob, (void*)dseg, (void*)dtile, (void*)derr}) ctx->dfree(p);
+}
+
 std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
-                                   int direction, const Tensor* Aup) {
+                                   int direction, const Tensor* Aup, int prec) {
   const Tensor& U = Aup ? *Aup : A;  // upper tensor (add_out_sub, src/MPSfunctions.hpp:360-434)
+  MPSG_CHECK(prec >= MPSG_PREC_FP64 && prec <= MPSG_PREC_BF16X3, "unsupported environment-update precision");
   std::unique_ptr<EnvPlan> P(new EnvPlan());
   P->ctx = ctx;
   P->keep = ctx->shared_from_this();
+  P->prec = prec;
   const bool left = direction > 0;
   std::map<std::pair<uint32_t, Q>, std::vector<int>> envby;  // (w, lower charge) -> env blocks
   for (int i = 0; i < (int)BL.b.size(); ++i) envby[{BL.b[i].k.p0, BL.b[i].k.q1}].push_back(i);
@@ -726,14 +848,27 @@ std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, 
   P->st1.upload(ctx);
   P->st2.upload(ctx);
   P->flops = P->st1.flops + P->st2.flops;
+  if (prec != MPSG_PREC_FP64) {
+    P->tc1.reset(new TcStage());
+    P->tc1->build(ctx, P->st1, prec);
+    P->tc2.reset(new TcStage());
+    P->tc2->build(ctx, P->st2, prec);
+  }
   return P;
 }
 
 TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
-                   double* flops_out, const Tensor* Aup) {
-  auto P = build_env(ctx, BL, A, W, ik, direction, Aup);
+                   double* flops_out, const Tensor* Aup, int prec) {
+  auto P = build_env(ctx, BL, A, W, ik, direction, Aup, prec);
   TensorP out = make_tensor(ctx, 1, P->out, true);
   P->run(A.d, out->d, Aup ? Aup->d : nullptr);
+  if (P->tc1) {  // bounded device waits of the tensor-core stages
+    int e1 = 0, e2 = 0;
+    MPSG_CUDA(cudaMemcpyAsync(&e1, P->tc1->derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MPSG_CUDA(cudaMemcpyAsync(&e2, P->tc2->derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->sync();
+    if (e1 || e2) throw Err(5, "tensor-core environment update: a bounded device wait expired");
+  }
   if (flops_out) *flops_out += P->flops;
   return out;
 }

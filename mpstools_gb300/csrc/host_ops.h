@@ -107,9 +107,31 @@ Layout theta_closure(const Tensor& L, const Tensor& R, const Layout& th, const M
                      const ItoKey& ik0, const ItoKey& ik1);
 
 // Environment update (addContractionLayer) factored as two grouped GEMM stages.
+// A grouped FP64 GEMM stage (GemmPlan) run on the tensor cores: every operand block of the plan is
+// converted to hi/lo tile images (transposes folded into the conversion's strides, the segment's
+// alpha into its A operand) and the products run through the tcgen05 grouped GEMM with FP64 output
+// blocks, from and to the same base slots as the FP64 plan.
+struct TcStage {
+  Ctx* ctx = nullptr;
+  int kind = 0, nprod = 3, nsm = 148;
+  uint8_t* dimg = nullptr;
+  int64_t img_hi = 0;
+  TcConv* dconv = nullptr;
+  int nconv = 0, nimg = 0;
+  TcProb* dprob = nullptr;
+  TcSeg* dseg = nullptr;
+  TcTile* dtile = nullptr;
+  int ntile = 0, grid = 0;
+  int* derr = nullptr;
+  void build(Ctx* c, const GemmPlan& g, int prec);
+  void run(const double* const* bases);  // conversions + GEMM on ctx->stream
+  ~TcStage();
+};
 struct EnvPlan {
   Ctx* ctx = nullptr;
   std::shared_ptr<Ctx> keep;
+  int prec = MPSG_PREC_FP64;             // tensor-core precisions: both stages as TcStage
+  std::unique_ptr<TcStage> tc1, tc2;
   KeyedArena<K5> ct;      // combined environment (L~ or R~)
   KeyedArena<K5> tt;      // intermediate T
   double* dCt = nullptr;
@@ -124,9 +146,9 @@ struct EnvPlan {
 };
 // Aup (optional): separate upper tensor, the two-tensor addContractionLayer(BL, A, mpo, Ap, ...)
 std::unique_ptr<EnvPlan> build_env(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik,
-                                   int direction, const Tensor* Aup = nullptr);
+                                   int direction, const Tensor* Aup = nullptr, int prec = MPSG_PREC_FP64);
 TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, const ItoKey& ik, int direction,
-                   double* flops_out, const Tensor* Aup = nullptr);
+                   double* flops_out, const Tensor* Aup = nullptr, int prec = MPSG_PREC_FP64);
 
 // theta(a,b;s1,s2) = A1(a,c;s1) A2(c,b;s2)
 TensorP theta_form(Ctx* ctx, const Tensor& A1, const Tensor& A2, const Layout* layout);

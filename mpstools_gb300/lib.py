@@ -67,6 +67,7 @@ def load(build_if_missing: bool = False):
     L.mpsg_dmrg_do_step.argtypes = [vp, i32, i32, u32, i32, f64, f64, i32, P(f64)]
     L.mpsg_dmrg_nsteps.argtypes = [vp]
     L.mpsg_dmrg_steps.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.mpsg_dmrg_set_env_prec.argtypes = [vp, C.c_int32]
     L.mpsg_dmrg_stats.argtypes = [vp, vp]
     L.mpsg_dmrg_stats_ext.argtypes = [vp, vp, C.c_int32]
     L.mpsg_dmrg_site.argtypes = [vp, i32, P(vp)]

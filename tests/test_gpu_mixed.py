@@ -5,6 +5,8 @@ TF32X3 2e-5, BF16X3 3e-4, TF32 5e-3, BF16 4e-2 (FP32 accumulation over K <= a fe
 hi/lo splits carry ~22 / ~16 significant bits, single TF32 / BF16 operands 11 / 8 bits).
 Energies of the AUTO path (TF32X3 Lanczos finished in FP64) and of the MIXED path (TF32X3 Lanczos,
 energy = FP64 Rayleigh quotient of its ground state) agree with the FP64 oracle to 1e-10.
+The tensor-core environment update (addContractionLayer in each precision) meets the same
+tolerances against the oracle's FP64 layer.
 """
 import numpy as np
 import pytest
@@ -108,3 +110,59 @@ def test_mixed_dmrg_energy(ctx, prec):
         assert rel <= 1e-10
     else:
         assert rel <= 1e-7
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "bf16x3", "tf32", "bf16"])
+@pytest.mark.parametrize("direction", [1, -1])
+def test_tc_env_update_matches_fp64_oracle(ctx, prec, direction):
+    g, W, ik = _case()
+    if direction > 0:
+        site, env, A = 6, g.env("L", 5), g.site(6)
+    else:
+        site, env, A = 8, g.env("R", 9), g.site(8)
+    ref = O.add_contraction_layer(env, A, W[site], ik[site], direction)
+    got = api.addContractionLayer(env, A, W[site], ik[site], direction, prec=prec, ctx=ctx)
+    assert set(got) == set(ref)
+    err = _max_rel(got, ref)
+    print(f"env {direction:+d} {prec}: max rel err {err:.2e}")
+    assert err < TOL[prec], err
+
+
+def test_tc_env_update_large_blocks_and_two_tensor(ctx):
+    """Blocks beyond one 128-row tile (N = 22, chi = 1000) and the two-tensor form (A lower, Ap upper)."""
+    g, W, ik = _case(N=22, chi=1000, site=10)
+    site = 10
+    env, A = g.env("L", site - 1), g.site(site)
+    ref = O.add_contraction_layer(env, A, W[site], ik[site], 1)
+    got = api.addContractionLayer(env, A, W[site], ik[site], 1, prec="tf32x3", ctx=ctx)
+    err = _max_rel(got, ref)
+    assert err < TOL["tf32x3"], err
+    rng = np.random.default_rng(5)
+    Ap = {k: v + 1e-3 * rng.standard_normal(v.shape) for k, v in A.items()}
+    ref2 = O.add_contraction_layer2(env, A, Ap, W[site], ik[site], 1)
+    got2 = api.addContractionLayer2(env, A, W[site], Ap, ik[site], 1, prec="tf32x3", ctx=ctx)
+    assert set(got2) == set(ref2)
+    err2 = _max_rel(got2, ref2)
+    assert err2 < TOL["tf32x3"], err2
+
+
+def test_dmrg_with_tensor_core_environments(ctx):
+    """doStep's environment updates on the tensor cores (TF32X3) with the MIXED Lanczos: the energy
+    carries the environments' ~1e-7 relative error (it is not a 1e-10 mode), then FP64 environments
+    for the last sweep bring it back within the MIXED tolerance of the oracle."""
+    N = 20
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    sites = M.random_u1_mps(N, N // 2, 32, 12345)
+    go = O.DMRG(sites, W, ik, maxthreads=8)
+    Eo = go.simulate(maxsteps=4, EnConv=1e-300, chimax=32, delta=1e-12)
+    gg = api.DMRGengine(sites, W, ik, prec="mixed", ctx=ctx)
+    gg.set_env_prec("tf32x3")
+    Et = gg.simulate(maxsteps=3, EnConv=1e-300, chimax=32, delta=1e-12)
+    rel_t = abs(Et - Eo) / abs(Eo)
+    assert rel_t <= 1e-5, rel_t
+    gg.set_env_prec("fp64")
+    Ef = gg.simulate(maxsteps=1, EnConv=1e-300, chimax=32, delta=1e-12)
+    rel_f = abs(gg.measure_energy() - Eo) / abs(Eo)
+    print(f"tensor-core environments: {rel_t:.2e}; after an FP64 sweep {rel_f:.2e} (E {Ef!r}, oracle {Eo!r})")
+    assert rel_f <= 1e-9, rel_f
