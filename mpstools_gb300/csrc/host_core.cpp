@@ -283,8 +283,12 @@ void GemmPlan::upload(Ctx* ctx) {
   prob_tile0.assign(hprob.size() + 1, 0);
   for (size_t i = 0; i < hprob.size(); ++i) {
     prob_tile0[i] = (int)tiles.size();
+    // 64 x 64 tiles, the last of each row / column trimmed to the block edge in steps of 16
     for (int m0 = 0; m0 < hprob[i].M; m0 += 64)
-      for (int n0 = 0; n0 < hprob[i].N; n0 += 64) tiles.push_back(GTile{(int32_t)i, m0, n0});
+      for (int n0 = 0; n0 < hprob[i].N; n0 += 64) {
+        const int mi = std::min(4, (hprob[i].M - m0 + 15) / 16), nj = std::min(4, (hprob[i].N - n0 + 15) / 16);
+        tiles.push_back(GTile{(int32_t)i, m0, n0, (int8_t)mi, (int8_t)nj});
+      }
   }
   ntiles = (int)tiles.size();
   prob_tile0[hprob.size()] = ntiles;

@@ -14,23 +14,26 @@ int64_t kernel_launch_count() { return g_launches.load(); }
 #define LAUNCHED() g_launches.fetch_add(1)
 
 // ============================================================================ grouped DGEMM
-// One CTA computes a 64x64 tile of one problem; the tile accumulates every segment
-// (product term) of the problem.  FP64 FMA on CUDA cores.
+// One CTA computes an mh x nh tile of one problem, accumulating every segment (product term) of the
+// problem; FP64 FMA on CUDA cores.  Tiles are 64 x 64 inside a block and trimmed at its edges to
+// the next multiple of 16 (mh, nh in {16, 32, 48, 64}): the executed FMAs then exceed the
+// algorithmic ones by at most 15 rows / columns per block instead of 63 (on the chi = 2048 centre
+// bond's sector sizes 1.20x instead of 1.53x).  256 threads as 16 x 16: thread (tx, ty) owns rows
+// tx + 16 i, i < MI = mh / 16, and columns ty + 16 j, j < NJ = nh / 16; each tile shape is its own
+// compiled loop (no predicated-off FMAs).
 constexpr int GM = 64, GN = 64, GK = 16;
 
-__global__ void __launch_bounds__(256) k_gemm_f64(const GProb* __restrict__ prob, const GSeg* __restrict__ seg,
-                                                  const GTile* __restrict__ tile, const Bases bases) {
-  __shared__ double As[GK][GM + 1];
-  __shared__ double Bs[GK][GN + 1];
-  const GTile t = tile[blockIdx.x];
-  const GProb P = prob[t.prob];
+template <int MI, int NJ>
+__device__ __forceinline__ void gemm_tile(const GProb& P, const GTile& t, const GSeg* __restrict__ seg,
+                                          const Bases& bases, double (*As)[GM + 1], double (*Bs)[GN + 1]) {
+  constexpr int TM = 16 * MI, TN = 16 * NJ;
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
-  double acc[4][4];
+  double acc[MI][NJ];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < MI; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < NJ; ++j) acc[i][j] = 0.0;
 
   for (int s = P.seg0; s < P.seg1; ++s) {
     const GSeg S = seg[s];
@@ -38,55 +41,77 @@ __global__ void __launch_bounds__(256) k_gemm_f64(const GProb* __restrict__ prob
     const double* __restrict__ Bp = bases.p[S.baseB] + S.offB;
     for (int k0 = 0; k0 < S.K; k0 += GK) {
 #pragma unroll
-      for (int r = 0; r < (GM * GK) / 256; ++r) {
+      for (int r = 0; r < (TM * GK + 255) / 256; ++r) {
         const int e = tid + r * 256;
-        int m, k;
-        if (!S.tA) { m = e % GM; k = e / GM; } else { k = e % GK; m = e / GK; }
-        const int gm = t.m0 + m, gk = k0 + k;
-        double v = 0.0;
-        if (gm < P.M && gk < S.K)
-          v = S.tA ? Ap[gk + (int64_t)gm * S.lda] : Ap[gm + (int64_t)gk * S.lda];
-        As[k][m] = v * S.alpha;
+        if ((TM * GK) % 256 == 0 || e < TM * GK) {
+          int m, k;
+          if (!S.tA) { m = e % TM; k = e / TM; } else { k = e % GK; m = e / GK; }
+          const int gm = t.m0 + m, gk = k0 + k;
+          double v = 0.0;
+          if (gm < P.M && gk < S.K)
+            v = S.tA ? Ap[gk + (int64_t)gm * S.lda] : Ap[gm + (int64_t)gk * S.lda];
+          As[k][m] = v * S.alpha;
+        }
       }
 #pragma unroll
-      for (int r = 0; r < (GN * GK) / 256; ++r) {
+      for (int r = 0; r < (TN * GK + 255) / 256; ++r) {
         const int e = tid + r * 256;
-        int n, k;
-        if (!S.tB) { k = e % GK; n = e / GK; } else { n = e % GN; k = e / GN; }
-        const int gn = t.n0 + n, gk = k0 + k;
-        double v = 0.0;
-        if (gn < P.N && gk < S.K)
-          v = S.tB ? Bp[gn + (int64_t)gk * S.ldb] : Bp[gk + (int64_t)gn * S.ldb];
-        Bs[k][n] = v;
+        if ((TN * GK) % 256 == 0 || e < TN * GK) {
+          int n, k;
+          if (!S.tB) { k = e % GK; n = e / GK; } else { n = e % TN; k = e / TN; }
+          const int gn = t.n0 + n, gk = k0 + k;
+          double v = 0.0;
+          if (gn < P.N && gk < S.K)
+            v = S.tB ? Bp[gn + (int64_t)gk * S.ldb] : Bp[gk + (int64_t)gn * S.ldb];
+          Bs[k][n] = v;
+        }
       }
       __syncthreads();
 #pragma unroll
       for (int k = 0; k < GK; ++k) {
-        double a[4], b[4];
+        double a[MI], b[NJ];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[k][tx + 16 * i];
+        for (int i = 0; i < MI; ++i) a[i] = As[k][tx + 16 * i];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[k][ty + 16 * j];
+        for (int j = 0; j < NJ; ++j) b[j] = Bs[k][ty + 16 * j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < MI; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          for (int j = 0; j < NJ; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
       }
       __syncthreads();
     }
   }
 #pragma unroll
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < NJ; ++j) {
     const int gn = t.n0 + ty + 16 * j;
     if (gn >= P.N) continue;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < MI; ++i) {
       const int gm = t.m0 + tx + 16 * i;
       if (gm >= P.M) continue;
       double* c = const_cast<double*>(bases.p[P.baseC]) + P.offC + gm + (int64_t)gn * P.ldc;
       *c = P.beta ? (*c + acc[i][j]) : acc[i][j];
     }
   }
+}
+
+__global__ void __launch_bounds__(256) k_gemm_f64(const GProb* __restrict__ prob, const GSeg* __restrict__ seg,
+                                                  const GTile* __restrict__ tile, const Bases bases) {
+  __shared__ double As[GK][GM + 1];
+  __shared__ double Bs[GK][GN + 1];
+  const GTile t = tile[blockIdx.x];
+  const GProb P = prob[t.prob];
+#define MPSG_GEMM_SHAPE(I, J) \
+  case (I - 1) * 4 + (J - 1): gemm_tile<I, J>(P, t, seg, bases, As, Bs); break;
+  switch ((t.mi - 1) * 4 + (t.nj - 1)) {
+    MPSG_GEMM_SHAPE(1, 1) MPSG_GEMM_SHAPE(1, 2) MPSG_GEMM_SHAPE(1, 3) MPSG_GEMM_SHAPE(1, 4)
+    MPSG_GEMM_SHAPE(2, 1) MPSG_GEMM_SHAPE(2, 2) MPSG_GEMM_SHAPE(2, 3) MPSG_GEMM_SHAPE(2, 4)
+    MPSG_GEMM_SHAPE(3, 1) MPSG_GEMM_SHAPE(3, 2) MPSG_GEMM_SHAPE(3, 3) MPSG_GEMM_SHAPE(3, 4)
+    MPSG_GEMM_SHAPE(4, 1) MPSG_GEMM_SHAPE(4, 2) MPSG_GEMM_SHAPE(4, 3) MPSG_GEMM_SHAPE(4, 4)
+    default: break;
+  }
+#undef MPSG_GEMM_SHAPE
 }
 
 void launch_gemm_f64(const GProb* prob, const GSeg* seg, const GTile* tile, int ntiles, const Bases& bases,

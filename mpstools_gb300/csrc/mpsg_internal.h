@@ -106,8 +106,9 @@ struct GProb {  // C (M x N, col-major, ldc) = [C +] sum_segments alpha*op(A)*op
   int32_t ldc, M, N, seg0, seg1;
   int8_t baseC, beta;
 };
-struct GTile {
+struct GTile {  // rows m0 .. m0 + 16 mi, columns n0 .. n0 + 16 nj of problem `prob` (mi, nj in 1..4)
   int32_t prob, m0, n0;
+  int8_t mi, nj;
 };
 struct LCOut {  // dst[0..n) = sum_t coef_t * src_t[0..n)
   double* dst;
