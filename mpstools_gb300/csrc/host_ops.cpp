@@ -20,6 +20,22 @@
 namespace mpsg {
 
 static std::atomic<int64_t> g_split_fallbacks{0};
+// MPSG_SPLIT_TIMING=1: split2 records events at its stage boundaries on the context's stream (after
+// the worker streams have been joined) and prints the stage times to stderr
+static thread_local std::vector<std::pair<const char*, cudaEvent_t>>* g_split_marks = nullptr;
+// the bidiagonal route's CholeskyQR with the explicit inverse of R (MPSG_CHOLQR_TRSM=1: the blocked
+// substitution)
+static bool cholqr_inverse() {
+  static const bool v = std::getenv("MPSG_CHOLQR_TRSM") == nullptr;
+  return v;
+}
+static void split_mark(Ctx* ctx, const char* name) {
+  if (!g_split_marks) return;
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, ctx->stream);
+  g_split_marks->push_back({name, e});
+}
 int64_t split_fallback_count() { return g_split_fallbacks.load(); }
 
 static inline Q qat(const ItoKey& ik, uint32_t s) {
@@ -1426,10 +1442,12 @@ struct SvdBatch {
   void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true, bool ub_rows = false) {
     cholqr_sides({CholSide{left, scale_s, ub_rows}}, passes, failed);
   }
+  // inverse = true (one pass of a nearly orthonormal X): X <- X R^-1 as one grouped GEMM with the
+  // explicit inverse (one warp per column of R^-1) instead of the blocked substitution chain
   // CholeskyQR of several sides (U and / or V of every sector) in the same launches: the Gram
   // matrices in one grouped GEMM, the Cholesky factorisations in one launch per cluster size, the
   // blocked substitution in one GEMM + one substitution launch per 64-column block.
-  void cholqr_sides(const std::vector<CholSide>& sides, int passes, std::vector<int>* failed) {
+  void cholqr_sides(const std::vector<CholSide>& sides, int passes, std::vector<int>* failed, bool inverse = false) {
     struct Prob {
       int i;  // sector
       const CholSide* sd;
@@ -1466,10 +1484,16 @@ struct SvdBatch {
     double* dR = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oR, 2));  // 1 / R_jj
     int* dinf = (int*)ctx->dmalloc(sizeof(int) * ps.size());
     MPSG_CUDA(cudaMemsetAsync(dinf, 0, sizeof(int) * ps.size(), st));
+    // Gram matrices C = X^T X, lower triangle only (all the Cholesky reads): per 64-column block j0,
+    // rows j0.. of C
     GemmPlan g;
     for (const Prob& p : ps)
-      g.add_problem(2, p.offC, p.kc, p.kc, p.kc, false,
-                    {GSegH{p.base, p.base, p.offX, p.offX, p.ldx, p.ldx, p.rows, 1, 0, 1.0}});
+      for (int j0 = 0; j0 < p.kc; j0 += 64) {
+        const int bw = std::min(64, p.kc - j0);
+        const int64_t xo = p.offX + (int64_t)j0 * p.ldx;
+        g.add_problem(2, p.offC + j0 + (int64_t)j0 * p.kc, p.kc, p.kc - j0, bw, false,
+                      {GSegH{p.base, p.base, xo, xo, p.ldx, p.ldx, p.rows, 1, 0, 1.0}});
+      }
     g.upload(ctx);
     std::vector<CholOp> zd;
     std::map<int, std::vector<CholQROp>> byCL[2];
@@ -1527,10 +1551,64 @@ struct SvdBatch {
       for (auto& c : byCL[pass]) dch[pass][c.first] = (CholQROp*)put(c.second.data(), sizeof(CholQROp) * c.second.size());
     MPSG_CHECK(off <= bytes + 64, "CholeskyQR descriptor overflow");
     MPSG_CUDA(cudaMemcpyAsync(dops, hops.data(), off, cudaMemcpyHostToDevice, st));
+    // explicit-inverse mode: R^-1 of every problem (k x k) and Y = X R^-1 into copies of the arenas
+    double *dRi = nullptr, *dYU = nullptr, *dYV = nullptr;
+    TrinvOp* dtrinv = nullptr;
+    int32_t* dcolop = nullptr;
+    int ncol_inv = 0;
+    int64_t nUtot = 0, nVtot = 0;
+    GemmPlan ginv;
+    if (inverse) {
+      MPSG_CHECK(passes == 1, "explicit-inverse CholeskyQR takes one pass");
+      std::vector<TrinvOp> to;
+      std::vector<int32_t> cop, cj;
+      dRi = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
+      for (size_t t = 0; t < ps.size(); ++t) {
+        const Prob& p = ps[t];
+        to.push_back(TrinvOp{dC + p.offC, dR + p.offR, dRi + p.offC, p.kc, p.kc, p.kc});
+        for (int j = 0; j < p.kc; ++j) {
+          cop.push_back((int32_t)t);
+          cj.push_back(j);
+        }
+      }
+      ncol_inv = (int)cop.size();
+      dtrinv = (TrinvOp*)ctx->dmalloc(sizeof(TrinvOp) * to.size());
+      dcolop = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * std::max<size_t>(cop.size(), 1));
+      MPSG_CUDA(cudaMemcpyAsync(dtrinv, to.data(), sizeof(TrinvOp) * to.size(), cudaMemcpyHostToDevice, st));
+      if (!cop.empty()) {
+        MPSG_CUDA(cudaMemcpyAsync(dcolop, cop.data(), sizeof(int32_t) * cop.size(), cudaMemcpyHostToDevice, st));
+        MPSG_CUDA(cudaMemcpyAsync(dcolop + ncol_inv, cj.data(), sizeof(int32_t) * cj.size(), cudaMemcpyHostToDevice, st));
+      }
+      bool anyU = false, anyV = false;
+      for (const Prob& p : ps) (p.base == 0 ? anyU : anyV) = true;
+      for (size_t i = 0; i < s.size(); ++i) {
+        nUtot = std::max<int64_t>(nUtot, s[i].offU + (int64_t)s[i].ms * s[i].k);
+        nVtot = std::max<int64_t>(nVtot, s[i].offV + (int64_t)s[i].ns * s[i].k);
+      }
+      if (anyU) {
+        dYU = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nUtot, 2));
+        MPSG_CUDA(cudaMemcpyAsync(dYU, dU, sizeof(double) * nUtot, cudaMemcpyDeviceToDevice, st));
+      }
+      if (anyV) {
+        dYV = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nVtot, 2));
+        MPSG_CUDA(cudaMemcpyAsync(dYV, dV, sizeof(double) * nVtot, cudaMemcpyDeviceToDevice, st));
+      }
+      // slots: 0 = U, 1 = R^-1, 2 = Y of U, 3 = V, 4 = Y of V; R^-1 is upper triangular: column block
+      // j0 of Y takes columns 0 .. j0 + 64 of X only
+      for (const Prob& p : ps)
+        for (int j0 = 0; j0 < p.kc; j0 += 64) {
+          const int bw = std::min(64, p.kc - j0), j1 = j0 + bw;
+          ginv.add_problem(p.base == 0 ? 2 : 4, p.offX + (int64_t)j0 * p.ldx, p.ldx, p.rows, bw, false,
+                           {GSegH{p.base, 1, p.offX, p.offC + (int64_t)j0 * p.kc, p.ldx, p.kc, j1, 0, 0, 1.0}});
+        }
+      ginv.upload(ctx);
+    }
     const double* bases[8] = {dU, dC, dC, dV, nullptr, nullptr, nullptr, nullptr};
     for (int pass = 0; pass < passes; ++pass) {
+      split_mark(ctx, "CholeskyQR setup");
       g.run(bases);
       launch_chol_unit_zero_diag(dzd, (int)zd.size(), st);
+      split_mark(ctx, "Gram matrices");
       const int which = pass == 0 ? 0 : 1;
       {  // cluster sizes concurrently on worker streams, largest first
         const int nw = std::min<int>((int)byCL[which].size(), ctx->nworkers());
@@ -1540,6 +1618,18 @@ struct SvdBatch {
           launch_chol(dch[which][it->first], (int)it->second.size(), it->first, kmaxCL[it->first],
                       ctx->wstreams[j % nw]);
         ctx->join(nw);
+      }
+      split_mark(ctx, "Cholesky");
+      if (inverse) {
+        // R^-1 per problem (into dRi), then Y = X R^-1 (one grouped GEMM into scratch copies of the
+        // U and V arenas), copied back
+        launch_trinv_cols(dtrinv, dcolop, dcolop + ncol_inv, ncol_inv, kmax, st);
+        split_mark(ctx, "R^-1");
+        const double* bi[8] = {dU, dRi, dYU, dV, dYV, nullptr, nullptr, nullptr};
+        ginv.run(bi);
+        if (dYU) MPSG_CUDA(cudaMemcpyAsync(dU, dYU, sizeof(double) * nUtot, cudaMemcpyDeviceToDevice, st));
+        if (dYV) MPSG_CUDA(cudaMemcpyAsync(dV, dYV, sizeof(double) * nVtot, cudaMemcpyDeviceToDevice, st));
+        continue;
       }
       for (int b = 0; b < nblk; ++b) {
         if (b > 0) upd[b]->run(bases);
@@ -1553,6 +1643,7 @@ struct SvdBatch {
     ctx->dfree(dinf);
     ctx->dfree(dR);
     ctx->dfree(dC);
+    for (void* p : {(void*)dRi, (void*)dYU, (void*)dYV, (void*)dtrinv, (void*)dcolop}) ctx->dfree(p);
     for (size_t t = 0; t < ps.size(); ++t)
       if (inf[t] != 0) {
         const Prob& p = ps[t];
@@ -1738,6 +1829,7 @@ struct SvdBatch {
       }
       for (auto& b : bufs) ctx->dfree(b.second);
     }
+    split_mark(ctx, "bidiagonalisation");
     // 2.-4. Golub-Kahan matrices, the cut of each segment, the singular values above it
     std::vector<int32_t> segop(nseg + 1, 0);
     {
@@ -1785,6 +1877,7 @@ struct SvdBatch {
     launch_gk_cut(bd.ops_d, bd.seg, bd.opseg, nop, nseg, chimax, floor_abs, bd.xlo, st);
     launch_gk_bisect(bd.ops_d, dmap, dmap + nth, nth, st);
     ctx->dfree(dmap);
+    split_mark(ctx, "cut + bisection");
   }
   // Singular vectors of the kept values (kept[i] per sector, from the truncation): U (ms x kept) and
   // V (ns x kept) in dU / dV, FixPhase applied.  Sectors whose vectors CholeskyQR cannot
@@ -1823,7 +1916,9 @@ struct SvdBatch {
     MPSG_CUDA(cudaMemcpyAsync(dmap, op_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
     MPSG_CUDA(cudaMemcpyAsync(dmap + nth, k_of.data(), sizeof(int32_t) * nth, cudaMemcpyHostToDevice, st));
     // 5./6. eigenvectors of T for the kept values, split into U_B (first ns rows of U) and V_B
+    split_mark(ctx, "truncation");
     launch_gk_invit(bd.ops_d, dmap, dmap + nth, bd.kept, nth, nmax2, dscr, st);
+    split_mark(ctx, "inverse iteration");
     {
       std::vector<GkVecOp> vo;
       for (int t = 0; t < nop; ++t) {
@@ -1847,7 +1942,9 @@ struct SvdBatch {
         failed.push_back(i);
         kr[i] = 0;
       }
-    cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed);
+    split_mark(ctx, "vectors of T");
+    cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed, cholqr_inverse());
+    split_mark(ctx, "CholeskyQR");
     // 7. U = Q [U_B; 0], V = P V_B
     {
       std::vector<ReflOp> ro;
@@ -1867,6 +1964,7 @@ struct SvdBatch {
         ctx->dfree(dr);
       }
     }
+    split_mark(ctx, "back-transformation");
     fixphase();
     if (!failed.empty()) {
       std::sort(failed.begin(), failed.end());
@@ -1963,9 +2061,9 @@ struct SvdBatch {
 };
 
 // ============================================================================ split
-SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
-                   double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
-                   const std::vector<int>* seg_absorb, const std::function<void(cudaEvent_t)>& on_bidiag) {
+static SplitResult split2_impl(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax,
+                               bool doTrunc, double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
+                               const std::vector<int>* seg_absorb, const std::function<void(cudaEvent_t)>& on_bidiag) {
   struct SecInfo {
     std::map<uint32_t, std::pair<int, int>> rx, ry;  // index -> (start, size)
     std::vector<int> blocks;
@@ -2021,6 +2119,7 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   // the bidiagonal route computes only the values at or above each segment's truncation cut here, and
   // the singular vectors of the kept ones after the truncation; every other route decomposes fully
   const bool bidiag = ctx->svd_method == 4 && sv.bidiag_fits() && !sv.s.empty();
+  split_mark(ctx, "gather");
   if (bidiag) sv.bidiag_values(s0, chimax, 1e-15);
   else sv.run(ctx->svd_method == 4 ? 0 : ctx->svd_method);
   std::vector<int32_t> sec_of(sv.nS);
@@ -2063,6 +2162,7 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
     for (size_t si = 0; si < qcs.size(); ++si) kept[si] = std::max(counts[si], 0);
     sv.bidiag_vectors(kept);
   }
+  split_mark(ctx, "FixPhase");
   // result layouts (dropDangling: sectors without kept values vanish, blocks cut to the kept count)
   Layout lu, lv, ll;
   for (size_t si = 0; si < qcs.size(); ++si) {
@@ -2140,6 +2240,39 @@ SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& 
   }
   run_copyops(ctx, ops);
   return R;
+}
+
+SplitResult split2(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax, bool doTrunc,
+                   double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
+                   const std::vector<int>* seg_absorb, const std::function<void(cudaEvent_t)>& on_bidiag) {
+  static const bool timing = std::getenv("MPSG_SPLIT_TIMING") != nullptr;
+  if (!timing || g_split_marks)
+    return split2_impl(ctx, th, ik0, ik1, chimax, doTrunc, tr_weight, normalize, absorb, seg_q0, seg_absorb, on_bidiag);
+  std::vector<std::pair<const char*, cudaEvent_t>> marks;
+  g_split_marks = &marks;
+  split_mark(ctx, "start");
+  SplitResult r;
+  try {
+    r = split2_impl(ctx, th, ik0, ik1, chimax, doTrunc, tr_weight, normalize, absorb, seg_q0, seg_absorb, on_bidiag);
+  } catch (...) {
+    g_split_marks = nullptr;
+    for (auto& m : marks) cudaEventDestroy(m.second);
+    throw;
+  }
+  split_mark(ctx, "scatter");
+  g_split_marks = nullptr;
+  ctx->sync();
+  std::string line = "libmpsg: split stages (ms):";
+  for (size_t k = 1; k < marks.size(); ++k) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, marks[k - 1].second, marks[k].second);
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), " %s %.2f", marks[k].first, ms);
+    line += buf;
+  }
+  std::fprintf(stderr, "%s\n", line.c_str());
+  for (auto& m : marks) cudaEventDestroy(m.second);
+  return r;
 }
 
 // ============================================================================ right canonicalisation
