@@ -672,38 +672,6 @@ __global__ void __launch_bounds__(32) k_trsm_rows(const TrsmRowsOp* __restrict__
   if (act)
     for (int j = 0; j < k; ++j) o.X[row + (int64_t)j * o.ldx] = xs[(size_t)j * 32 + lane];
 }
-// Column j of R^-1 by backward substitution carried as column updates: x = e_j; for i = j .. 0:
-// x_i <- x_i / R_ii, then x_r -= R(r, i) x_i for r < i (the lanes split the rows; column i of R is
-// read contiguously).  x lives in the warp's slice of shared memory; rows below j are zero.
-__global__ void __launch_bounds__(128) k_trinv_cols(const TrinvOp* __restrict__ ops, const int32_t* __restrict__ col_op,
-                                                    const int32_t* __restrict__ col_j, int ncols, int kmax) {
-  const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-  if (w >= ncols) return;  // whole warps leave together
-  extern __shared__ double xs[];
-  double* x = xs + (size_t)(threadIdx.x >> 5) * kmax;
-  const TrinvOp o = ops[col_op[w]];
-  const int j = col_j[w];
-  for (int r = lane; r <= j; r += 32) x[r] = (r == j) ? 1.0 : 0.0;
-  __syncwarp();
-  for (int i = j; i >= 0; --i) {
-    const double xi = x[i] * o.rdiag[i];
-    const double* rc = o.R + (int64_t)i * o.ld;
-    for (int r = lane; r < i; r += 32) x[r] = fma(-rc[r], xi, x[r]);
-    __syncwarp();
-    if (lane == (i & 31)) x[i] = xi;
-    __syncwarp();
-  }
-  for (int r = lane; r < o.k; r += 32) o.Ri[r + (int64_t)j * o.ldi] = r <= j ? x[r] : 0.0;
-}
-void launch_trinv_cols(const TrinvOp* ops, const int32_t* col_op, const int32_t* col_j, int ncols, int kmax,
-                       cudaStream_t s) {
-  if (ncols <= 0) return;
-  const size_t smem = sizeof(double) * 4 * (size_t)std::max(kmax, 1);
-  MPSG_CHECK(smem <= 227 * 1024, "triangular inverse: factor too large");
-  MPSG_CUDA(cudaFuncSetAttribute(k_trinv_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_trinv_cols<<<(ncols + 3) / 4, 128, smem, s>>>(ops, col_op, col_j, ncols, kmax);
-  g_eig_launches.fetch_add(1);
-}
 void launch_trsm_rows(const TrsmRowsOp* ops, int nops, int kmax, cudaStream_t s) {
   if (nops <= 0) return;
   const size_t smem = sizeof(double) * 32 * (size_t)kmax;

@@ -23,12 +23,6 @@ static std::atomic<int64_t> g_split_fallbacks{0};
 // MPSG_SPLIT_TIMING=1: split2 records events at its stage boundaries on the context's stream (after
 // the worker streams have been joined) and prints the stage times to stderr
 static thread_local std::vector<std::pair<const char*, cudaEvent_t>>* g_split_marks = nullptr;
-// the bidiagonal route's CholeskyQR with the explicit inverse of R (MPSG_CHOLQR_TRSM=1: the blocked
-// substitution)
-static bool cholqr_inverse() {
-  static const bool v = std::getenv("MPSG_CHOLQR_TRSM") == nullptr;
-  return v;
-}
 static void split_mark(Ctx* ctx, const char* name) {
   if (!g_split_marks) return;
   cudaEvent_t e;
@@ -1442,12 +1436,10 @@ struct SvdBatch {
   void cholqr(bool left, int passes, std::vector<int>* failed = nullptr, bool scale_s = true, bool ub_rows = false) {
     cholqr_sides({CholSide{left, scale_s, ub_rows}}, passes, failed);
   }
-  // inverse = true (one pass of a nearly orthonormal X): X <- X R^-1 as one grouped GEMM with the
-  // explicit inverse (one warp per column of R^-1) instead of the blocked substitution chain
   // CholeskyQR of several sides (U and / or V of every sector) in the same launches: the Gram
   // matrices in one grouped GEMM, the Cholesky factorisations in one launch per cluster size, the
   // blocked substitution in one GEMM + one substitution launch per 64-column block.
-  void cholqr_sides(const std::vector<CholSide>& sides, int passes, std::vector<int>* failed, bool inverse = false) {
+  void cholqr_sides(const std::vector<CholSide>& sides, int passes, std::vector<int>* failed) {
     struct Prob {
       int i;  // sector
       const CholSide* sd;
@@ -1551,58 +1543,6 @@ struct SvdBatch {
       for (auto& c : byCL[pass]) dch[pass][c.first] = (CholQROp*)put(c.second.data(), sizeof(CholQROp) * c.second.size());
     MPSG_CHECK(off <= bytes + 64, "CholeskyQR descriptor overflow");
     MPSG_CUDA(cudaMemcpyAsync(dops, hops.data(), off, cudaMemcpyHostToDevice, st));
-    // explicit-inverse mode: R^-1 of every problem (k x k) and Y = X R^-1 into copies of the arenas
-    double *dRi = nullptr, *dYU = nullptr, *dYV = nullptr;
-    TrinvOp* dtrinv = nullptr;
-    int32_t* dcolop = nullptr;
-    int ncol_inv = 0;
-    int64_t nUtot = 0, nVtot = 0;
-    GemmPlan ginv;
-    if (inverse) {
-      MPSG_CHECK(passes == 1, "explicit-inverse CholeskyQR takes one pass");
-      std::vector<TrinvOp> to;
-      std::vector<int32_t> cop, cj;
-      dRi = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oC, 2));
-      for (size_t t = 0; t < ps.size(); ++t) {
-        const Prob& p = ps[t];
-        to.push_back(TrinvOp{dC + p.offC, dR + p.offR, dRi + p.offC, p.kc, p.kc, p.kc});
-        for (int j = 0; j < p.kc; ++j) {
-          cop.push_back((int32_t)t);
-          cj.push_back(j);
-        }
-      }
-      ncol_inv = (int)cop.size();
-      dtrinv = (TrinvOp*)ctx->dmalloc(sizeof(TrinvOp) * to.size());
-      dcolop = (int32_t*)ctx->dmalloc(sizeof(int32_t) * 2 * std::max<size_t>(cop.size(), 1));
-      MPSG_CUDA(cudaMemcpyAsync(dtrinv, to.data(), sizeof(TrinvOp) * to.size(), cudaMemcpyHostToDevice, st));
-      if (!cop.empty()) {
-        MPSG_CUDA(cudaMemcpyAsync(dcolop, cop.data(), sizeof(int32_t) * cop.size(), cudaMemcpyHostToDevice, st));
-        MPSG_CUDA(cudaMemcpyAsync(dcolop + ncol_inv, cj.data(), sizeof(int32_t) * cj.size(), cudaMemcpyHostToDevice, st));
-      }
-      bool anyU = false, anyV = false;
-      for (const Prob& p : ps) (p.base == 0 ? anyU : anyV) = true;
-      for (size_t i = 0; i < s.size(); ++i) {
-        nUtot = std::max<int64_t>(nUtot, s[i].offU + (int64_t)s[i].ms * s[i].k);
-        nVtot = std::max<int64_t>(nVtot, s[i].offV + (int64_t)s[i].ns * s[i].k);
-      }
-      if (anyU) {
-        dYU = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nUtot, 2));
-        MPSG_CUDA(cudaMemcpyAsync(dYU, dU, sizeof(double) * nUtot, cudaMemcpyDeviceToDevice, st));
-      }
-      if (anyV) {
-        dYV = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(nVtot, 2));
-        MPSG_CUDA(cudaMemcpyAsync(dYV, dV, sizeof(double) * nVtot, cudaMemcpyDeviceToDevice, st));
-      }
-      // slots: 0 = U, 1 = R^-1, 2 = Y of U, 3 = V, 4 = Y of V; R^-1 is upper triangular: column block
-      // j0 of Y takes columns 0 .. j0 + 64 of X only
-      for (const Prob& p : ps)
-        for (int j0 = 0; j0 < p.kc; j0 += 64) {
-          const int bw = std::min(64, p.kc - j0), j1 = j0 + bw;
-          ginv.add_problem(p.base == 0 ? 2 : 4, p.offX + (int64_t)j0 * p.ldx, p.ldx, p.rows, bw, false,
-                           {GSegH{p.base, 1, p.offX, p.offC + (int64_t)j0 * p.kc, p.ldx, p.kc, j1, 0, 0, 1.0}});
-        }
-      ginv.upload(ctx);
-    }
     const double* bases[8] = {dU, dC, dC, dV, nullptr, nullptr, nullptr, nullptr};
     for (int pass = 0; pass < passes; ++pass) {
       split_mark(ctx, "CholeskyQR setup");
@@ -1620,17 +1560,9 @@ struct SvdBatch {
         ctx->join(nw);
       }
       split_mark(ctx, "Cholesky");
-      if (inverse) {
-        // R^-1 per problem (into dRi), then Y = X R^-1 (one grouped GEMM into scratch copies of the
-        // U and V arenas), copied back
-        launch_trinv_cols(dtrinv, dcolop, dcolop + ncol_inv, ncol_inv, kmax, st);
-        split_mark(ctx, "R^-1");
-        const double* bi[8] = {dU, dRi, dYU, dV, dYV, nullptr, nullptr, nullptr};
-        ginv.run(bi);
-        if (dYU) MPSG_CUDA(cudaMemcpyAsync(dU, dYU, sizeof(double) * nUtot, cudaMemcpyDeviceToDevice, st));
-        if (dYV) MPSG_CUDA(cudaMemcpyAsync(dV, dYV, sizeof(double) * nVtot, cudaMemcpyDeviceToDevice, st));
-        continue;
-      }
+      // X <- X R^-1 by blocked forward substitution: an explicit inverse of R (one GEMM) was measured
+      // to lose orthonormality where kept values cluster (R ill-conditioned: error ~eps cond(R)^2),
+      // which moved MIXED DMRG energies by 3e-10 relative
       for (int b = 0; b < nblk; ++b) {
         if (b > 0) upd[b]->run(bases);
         launch_trsm_rows(dtr[b], (int)tr[b].size(), kTB, st);
@@ -1643,7 +1575,6 @@ struct SvdBatch {
     ctx->dfree(dinf);
     ctx->dfree(dR);
     ctx->dfree(dC);
-    for (void* p : {(void*)dRi, (void*)dYU, (void*)dYV, (void*)dtrinv, (void*)dcolop}) ctx->dfree(p);
     for (size_t t = 0; t < ps.size(); ++t)
       if (inf[t] != 0) {
         const Prob& p = ps[t];
@@ -1943,7 +1874,7 @@ struct SvdBatch {
         kr[i] = 0;
       }
     split_mark(ctx, "vectors of T");
-    cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed, cholqr_inverse());
+    cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed);
     split_mark(ctx, "CholeskyQR");
     // 7. U = Q [U_B; 0], V = P V_B
     {

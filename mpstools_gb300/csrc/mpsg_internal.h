@@ -181,15 +181,6 @@ struct CholQROp {  // Cholesky of the k x k Gram matrix C (ld) of one sector: R 
   int* info;      // first non-positive pivot + 1 (0: none)
   int32_t k, ld;
 };
-struct TrinvOp {  // Ri (k x k, ldi) <- R^-1 of the upper-triangular R (k x k, ld); rdiag = 1 / R_jj
-  const double* R;
-  const double* rdiag;
-  double* Ri;
-  int32_t k, ld, ldi;
-};
-// ops[col_op[w]], column col_j[w] of its inverse for w < ncols (one warp per column)
-void launch_trinv_cols(const TrinvOp* ops, const int32_t* col_op, const int32_t* col_j, int ncols, int kmax,
-                       cudaStream_t s);
 struct TrsmRowsOp {  // rows [r0, r1) of X (ldx) <- X R^-1, R upper (ldr), k columns
   double* X;
   const double* R;
