@@ -437,6 +437,29 @@ def gpu_arm(args):
                                                    default=0.0),
                         "what": "one two-site update at the centre bond from the same state (GPU in this "
                                 "line's precision, oracle FP64 with LAPACK dgesvd)"}
+        # the plain FP64 GPU path (mpsg_lanczos2 + mpsg_split2) on the same state against the same oracle
+        # update: block structure, kept counts and singular values of the exact split
+        w1c, w2c = lib.MPOArg(W[center]), lib.MPOArg(W[center + 1])
+        k0c, k1c = lib.ItoKeyArg(ik[center]), lib.ItoKeyArg(ik[center + 1])
+        st64, E64, it64 = C.c_void_p(), C.c_double(), C.c_int32()
+        lib.check(ctx.L.mpsg_lanczos2(ctx.h, L.h, R.h, A1.h, A2.h, w1c.ref(), w2c.ref(), k0c.ref(), k1c.ref(), 500,
+                                      1e-12, 1, lib.PREC["fp64"], 0, C.byref(st64), C.byref(E64), C.byref(it64)))
+        psi64 = lib.Tensor(ctx, st64)
+        U64, V64, lam64 = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        tw64, chi64 = C.c_double(), C.c_uint32()
+        lib.check(ctx.L.mpsg_split2(ctx.h, psi64.h, k0c.ref(), k1c.ref(), args.chi, 0, 1e-12, 1, C.byref(U64),
+                                    C.byref(V64), C.byref(lam64), C.byref(tw64), C.byref(chi64)))
+        U64, V64 = lib.Tensor(ctx, U64), lib.Tensor(ctx, V64)
+        l64 = lib.Tensor(ctx, lam64).to_dict()
+        common64 = set(l64) & set(lo)
+        oracle_check["fp64_gpu_path"] = {
+            "E_gpu": E64.value, "rel_energy_diff": abs(E64.value - o_rec["E"]) / abs(o_rec["E"]),
+            "chi_gpu": int(chi64.value), "tw_gpu": tw64.value,
+            "kept_per_sector_equal": {q: len(v) for q, v in l64.items() if len(v)} ==
+                                     {q: len(v) for q, v in lo.items() if len(v)},
+            "lambda_max_abs_diff": max((float(np.abs(np.asarray(l64[q]) - np.asarray(lo[q])).max())
+                                        for q in common64 if len(l64[q]) == len(lo[q]) and len(lo[q])), default=0.0)}
+        del U64, V64, psi64
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
