@@ -935,6 +935,13 @@ struct SvdBatch {
   int* dinfo = nullptr;
   int64_t nS = 0;
   std::function<void(cudaEvent_t)> on_bidiag;  // see split2
+  // complex mode of the bidiagonal route (the TEBD split): zM holds the complex sector matrices at the
+  // offsets of dM; the real bidiagonal, its values and the real U_B, V_B come out as in the real mode,
+  // U = Q [U_B; 0] and V = P V_B are written to zUo / zVo (per sector: pointer, leading dimension);
+  // no FixPhase, no Jacobi fallback (zfailed is set instead)
+  double2* zM = nullptr;
+  std::vector<std::pair<double2*, int>> zUo, zVo;
+  bool zfailed = false;
   explicit SvdBatch(Ctx* c) : ctx(c) {}
   ~SvdBatch() {
     bidiag_free();
@@ -1612,6 +1619,7 @@ struct SvdBatch {
   struct Bidiag {
     double *d = nullptr, *e = nullptr, *tq = nullptr, *tp = nullptr, *Pr = nullptr, *b = nullptr, *b2 = nullptr,
            *meta = nullptr, *Z = nullptr, *xlo = nullptr, *Mcopy = nullptr;
+    double2 *tqz = nullptr, *tpz = nullptr, *Prz = nullptr;  // complex mode
     int32_t *kcomp = nullptr, *seg = nullptr, *kept = nullptr, *opseg = nullptr;
     GkOp* ops_d = nullptr;
     std::vector<GkOp> ops;
@@ -1620,11 +1628,12 @@ struct SvdBatch {
   } bd;
   bool bidiag_fits() const {  // the cluster bidiagonalisation (shared- or global-memory variant)
     for (auto& x : s)
-      if (x.k > 0 && gebrd_cluster_size(x.ms, x.ns) == 0) return false;
+      if (x.k > 0 && (zM ? zgebrd_cluster_size(x.ms, x.ns) : gebrd_cluster_size(x.ms, x.ns)) == 0) return false;
     return true;
   }
   void bidiag_free() {
     for (double* p : {bd.d, bd.e, bd.tq, bd.tp, bd.Pr, bd.b, bd.b2, bd.meta, bd.Z, bd.xlo, bd.Mcopy}) ctx->dfree(p);
+    for (double2* p : {bd.tqz, bd.tpz, bd.Prz}) ctx->dfree(p);
     ctx->dfree(bd.kcomp);  // kept and seg live in the same allocation
     ctx->dfree(bd.ops_d);
     bd = Bidiag();
@@ -1661,7 +1670,7 @@ struct SvdBatch {
     bd.xlo = (double*)ctx->dmalloc(gk_cut_state_bytes() * std::max(nseg, 1));  // per-segment cut state
     // the sector matrices, kept for sectors whose vectors have to be redone on the Jacobi route (the
     // bidiagonalisation overwrites them with its reflectors)
-    const int64_t nM = s.empty() ? 0 : s.back().offM + (int64_t)s.back().ms * s.back().ns;
+    const int64_t nM = s.empty() || zM ? 0 : s.back().offM + (int64_t)s.back().ms * s.back().ns;
     bd.Mcopy = alloc(nM);
     if (nM) MPSG_CUDA(cudaMemcpyAsync(bd.Mcopy, dM, sizeof(double) * nM, cudaMemcpyDeviceToDevice, st));
     bd.kcomp = (int32_t*)ctx->dmalloc(sizeof(int32_t) * (size_t)nop * 3 + sizeof(int32_t) * (nseg + 1));
@@ -1670,7 +1679,36 @@ struct SvdBatch {
     bd.seg = bd.opseg + nop;
     // 1. bidiagonalisation, one launch per cluster size on worker streams (largest clusters first);
     //    the largest global-memory sectors on two clusters each, in a launch of their own
-    {
+    if (zM) {  // complex sectors: real bidiagonal, complex reflectors (shared-memory clusters only)
+      auto zalloc = [&](int64_t n) { return (double2*)ctx->dmalloc(sizeof(double2) * std::max<int64_t>(n, 2)); };
+      bd.tqz = zalloc(nS);
+      bd.tpz = zalloc(nS);
+      bd.Prz = zalloc(oPr);
+      MPSG_CUDA(cudaMemsetAsync(bd.tpz, 0, sizeof(double2) * std::max<int64_t>(nS, 2), st));
+      std::map<int, std::vector<ZGebrdOp>> byCL;
+      std::map<int, size_t> smem;
+      for (int i : bd.idx) {
+        const Sec& x = s[i];
+        const int CL = zgebrd_cluster_size(x.ms, x.ns);
+        MPSG_CHECK(CL > 0, "complex bidiagonalisation: sector too large for the cluster");
+        byCL[CL].push_back(ZGebrdOp{zM + x.offM, bd.d + x.offS, bd.e + x.offS, bd.tqz + x.offS, bd.tpz + x.offS,
+                                    bd.Prz + bd.offPr[i], x.ms, x.ns, x.ms});
+        smem[CL] = std::max(smem[CL], zgebrd_smem(x.ms, x.ns, CL));
+      }
+      std::vector<std::pair<int, ZGebrdOp*>> bufs;
+      for (auto it = byCL.rbegin(); it != byCL.rend(); ++it) {
+        ZGebrdOp* dp = (ZGebrdOp*)ctx->dmalloc(sizeof(ZGebrdOp) * it->second.size());
+        MPSG_CUDA(cudaMemcpyAsync(dp, it->second.data(), sizeof(ZGebrdOp) * it->second.size(), cudaMemcpyHostToDevice, st));
+        bufs.push_back({it->first, dp});
+      }
+      const int nw = std::min<int>((int)bufs.size(), ctx->nworkers());
+      ctx->fork(nw);
+      for (size_t j = 0; j < bufs.size(); ++j)
+        launch_zgebrd(bufs[j].second, (int)byCL[bufs[j].first].size(), bufs[j].first, smem[bufs[j].first],
+                      ctx->wstreams[j % nw]);
+      ctx->join(nw);
+      for (auto& b : bufs) ctx->dfree(b.second);
+    } else {
       std::map<int, std::vector<GebrdOp>> byCL;
       std::map<int, size_t> smem;  // per cluster-size code, the largest of its sectors' needs
       std::vector<GebrdOp> mc;
@@ -1877,6 +1915,29 @@ struct SvdBatch {
     cholqr_sides({CholSide{true, false, true}, CholSide{false, false, false}}, 1, &failed);
     split_mark(ctx, "CholeskyQR");
     // 7. U = Q [U_B; 0], V = P V_B
+    if (zM) {  // complex reflectors into the caller's complex outputs
+      std::vector<ZReflOp> ro;
+      const int cb = zapply_refl_cols_per_block(lenmax);
+      for (int i : bd.idx) {
+        const Sec& x = s[i];
+        for (int c0 = 0; c0 < kr[i]; c0 += cb) {
+          const int c1 = std::min(c0 + cb, kr[i]);
+          ro.push_back(ZReflOp{zM + x.offM, bd.tqz + x.offS, dU + x.offU, zUo[i].first, x.ms, x.ns, 0, x.ms, x.ms,
+                               zUo[i].second, x.ns, c0, c1});
+          ro.push_back(ZReflOp{bd.Prz + bd.offPr[i], bd.tpz + x.offS, dV + x.offV, zVo[i].first, x.ns, x.ns - 1, 1,
+                               x.ns, x.ns, zVo[i].second, x.ns, c0, c1});
+        }
+      }
+      if (!ro.empty()) {
+        ZReflOp* dr = (ZReflOp*)ctx->dmalloc(sizeof(ZReflOp) * ro.size());
+        MPSG_CUDA(cudaMemcpyAsync(dr, ro.data(), sizeof(ZReflOp) * ro.size(), cudaMemcpyHostToDevice, st));
+        launch_zapply_refl(dr, (int)ro.size(), lenmax, st);
+        ctx->dfree(dr);
+      }
+      zfailed = !failed.empty();
+      bidiag_free();
+      return;
+    }
     {
       std::vector<ReflOp> ro;
       for (int i : bd.idx) {
@@ -1992,6 +2053,39 @@ struct SvdBatch {
 };
 
 // ============================================================================ split
+bool zsvd_bidiag(Ctx* ctx, const std::vector<ZSvdSec>& secs, double2* zM, double* dS) {
+  if (secs.empty()) return true;
+  SvdBatch sv(ctx);
+  std::vector<std::pair<int, int>> mn;
+  for (auto& z : secs) {
+    MPSG_CHECK(z.ms >= z.ns, "complex SVD: sectors are stored tall");
+    mn.push_back({z.ms, z.ns});
+  }
+  sv.plan(mn);
+  sv.zM = zM;
+  for (size_t i = 0; i < secs.size(); ++i) {
+    sv.s[i].offM = secs[i].offM;  // the caller's layout of the complex matrices
+    sv.zUo.push_back({secs[i].U, secs[i].ldu});
+    sv.zVo.push_back({secs[i].V, secs[i].ldv});
+    if (secs[i].ns > 0) {
+      MPSG_CUDA(cudaMemsetAsync(secs[i].U, 0, sizeof(double2) * (size_t)secs[i].ldu * secs[i].ns, ctx->stream));
+      MPSG_CUDA(cudaMemsetAsync(secs[i].V, 0, sizeof(double2) * (size_t)secs[i].ldv * secs[i].ns, ctx->stream));
+    }
+  }
+  if (!sv.bidiag_fits()) {
+    g_split_fallbacks.fetch_add(1);
+    return false;
+  }
+  sv.run_bidiag_all();
+  if (sv.zfailed) {
+    g_split_fallbacks.fetch_add(1);
+    return false;
+  }
+  if (sv.nS) MPSG_CUDA(cudaMemcpyAsync(dS, sv.dS, sizeof(double) * sv.nS, cudaMemcpyDeviceToDevice, ctx->stream));
+  ctx->sync();
+  return true;
+}
+
 static SplitResult split2_impl(Ctx* ctx, const Tensor& th, const ItoKey& ik0, const ItoKey& ik1, int chimax,
                                bool doTrunc, double tr_weight, bool normalize, int absorb, const std::vector<Q>* seg_q0,
                                const std::vector<int>* seg_absorb, const std::function<void(cudaEvent_t)>& on_bidiag) {

@@ -153,6 +153,20 @@ TensorP env_update(Ctx* ctx, const Tensor& BL, const Tensor& A, const MPO& W, co
 // theta(a,b;s1,s2) = A1(a,c;s1) A2(c,b;s2)
 TensorP theta_form(Ctx* ctx, const Tensor& A1, const Tensor& A2, const Layout* layout);
 
+// Complex SVD of the sectors of the TEBD split on the bidiagonal route: sector i is the complex
+// ms x ns matrix (ms >= ns, leading dimension ms) at zM + offM (overwritten); its ns values go to
+// dS (the sectors' values consecutive, descending; values below 1e-16 are 0) and M = U diag(S) V^H
+// with U (ms x ns, ldu) and V (ns x ns, ldv), columns of values below 1e-16 zero.  Returns false
+// when a sector does not fit the shared-memory cluster kernel or its vectors would need the Jacobi
+// route (the caller then uses the library solver; counted in split_fallback_count()).
+struct ZSvdSec {
+  int ms, ns;
+  int64_t offM;
+  double2 *U, *V;
+  int ldu, ldv;
+};
+bool zsvd_bidiag(Ctx* ctx, const std::vector<ZSvdSec>& secs, double2* zM, double* dS);
+
 // split (two-site, direction 0) with global truncation
 struct SplitResult {
   TensorP U, Vt, lam;

@@ -202,6 +202,30 @@ struct GebrdOp {  // m x n (m >= n) sector matrix A (lda) -> B = Q^T A P upper b
   unsigned int* ctr = nullptr;
   int* err = nullptr;
 };
+// complex sector matrix (m >= n, interleaved re/im) -> B = Q^H A P real upper bidiagonal (d, e); the
+// reflectors as in GebrdOp, complex (zgebrd conventions: real beta, H = I - tau v v^H applied as H^H)
+struct ZGebrdOp {
+  double2* A;
+  double* d;
+  double* e;
+  double2* tauq;
+  double2* taup;
+  double2* Pr;
+  int32_t m, n, lda;
+};
+// X_out (len x [c0, c1), ldo) = H_0 ... H_{nref-1} X_in with X_in real (ldi, rows >= rows_in are zero)
+struct ZReflOp {
+  const double2* R;    // reflector j: unit at row j + off, tail below it in column j (ldr)
+  const double2* tau;  // nref
+  const double* Xin;
+  double2* Xout;
+  int32_t len, nref, off, ldr, ldi, ldo, rows_in, c0, c1;
+};
+int zgebrd_cluster_size(int m, int n);  // 0: does not fit the shared-memory cluster kernel
+size_t zgebrd_smem(int m, int n, int CL);
+void launch_zgebrd(const ZGebrdOp* ops, int nops, int CL, size_t smem, cudaStream_t s);
+void launch_zapply_refl(const ZReflOp* ops, int nops, int lenmax, cudaStream_t s);
+int zapply_refl_cols_per_block(int lenmax);  // columns per op of launch_zapply_refl
 struct GkOp {  // Golub-Kahan tridiagonal [[0, B], [B^T, 0]] (interleaved, zero diagonal) of one sector
   const double* d;    // n (bidiagonal)
   const double* e;    // n - 1

@@ -1226,4 +1226,289 @@ void launch_apply_refl(const ReflOp* ops, int nops, int lenmax, cudaStream_t s) 
 }
 int apply_refl_cols_per_block(int lenmax) { return apply_refl_warps(lenmax); }
 
+// ----------------------------------------------------------------------------- complex sectors
+// The complex split (TEBD) reduces each complex sector to a REAL bidiagonal: LAPACK's zgebrd
+// conventions (zlarfg: beta real, H = I - tau v v^H with H^H x = beta e1; the left reflector applied
+// as A <- A - conj(tau) v (v^H A), the right one built from the conjugated row and applied as
+// A <- A - taup (A u) u^H).  Stages 2-6 above then run unchanged on the real bidiagonal; U = Q [U_B; 0]
+// and V = P V_B are formed with the complex reflectors (k_zapply_refl).  Shared-memory cluster
+// variant only (sectors that do not fit stay on the library solver).
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 zconj(double2 a) { return make_double2(a.x, -a.y); }
+// conj(a) b + c
+__device__ __forceinline__ double2 zfma_c(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(a.y, b.y, c.x)), fma(a.x, b.y, fma(-a.y, b.x, c.y)));
+}
+// a b + c
+__device__ __forceinline__ double2 zfma(double2 a, double2 b, double2 c) {
+  return make_double2(fma(a.x, b.x, fma(-a.y, b.y, c.x)), fma(a.x, b.y, fma(a.y, b.x, c.y)));
+}
+__device__ __forceinline__ double2 zrecip(double2 a) {
+  const double d = 1.0 / fma(a.x, a.x, a.y * a.y);
+  return make_double2(a.x * d, -a.y * d);
+}
+__device__ __forceinline__ double2 zwarp_sum(double2 a) { return make_double2(warp_sum(a.x), warp_sum(a.y)); }
+// zlarfg on alpha and |x_tail|^2: beta (real), tau, scale = 1 / (alpha - beta)
+__device__ __forceinline__ void zlarfg_coef(double2 alpha, double s2, double& beta, double2& tau, double2& scale) {
+  beta = alpha.x;
+  tau = make_double2(0.0, 0.0);
+  scale = make_double2(0.0, 0.0);
+  if (s2 > 0.0 || alpha.y != 0.0) {
+    beta = -copysign(sqrt(fma(alpha.x, alpha.x, fma(alpha.y, alpha.y, s2))), alpha.x);
+    tau = make_double2((beta - alpha.x) / beta, -alpha.y / beta);
+    scale = zrecip(make_double2(alpha.x - beta, alpha.y));
+  }
+}
+// left reflector of column j (col, rows j..m-1): v, tau (scal[0]); with store the tail into A, tauq, d
+__device__ void zgebrd_left(const ZGebrdOp& o, const double2* col, int j, double2* v, double2* scal, int lane,
+                            bool store) {
+  const int m = o.m;
+  double s2 = 0.0;
+  for (int i = j + 1 + lane; i < m; i += 32) s2 = fma(col[i].x, col[i].x, fma(col[i].y, col[i].y, s2));
+  s2 = warp_sum(s2);
+  double beta;
+  double2 tau, scale;
+  zlarfg_coef(col[j], s2, beta, tau, scale);
+  for (int i = j + lane; i < m; i += 32) {
+    const double2 x = (i == j) ? make_double2(1.0, 0.0) : zmul(col[i], scale);
+    v[i] = x;
+    if (store && i > j) o.A[i + (int64_t)j * o.lda] = x;
+  }
+  if (lane == 0) {
+    scal[0] = tau;
+    if (store) {
+      o.tauq[j] = tau;
+      o.d[j] = beta;
+    }
+  }
+}
+static __host__ __device__ size_t zgebrd_smem_elems(int m, int n, int CL) {
+  const int ncol = (n + CL - 1) / CL;
+  return (size_t)ncol * m + 4 * (size_t)m + (size_t)ncol + 8;
+}
+size_t zgebrd_smem(int m, int n, int CL) { return sizeof(double2) * zgebrd_smem_elems(m, n, CL); }
+int zgebrd_cluster_size(int m, int n) {
+  int CL = n <= 48 ? 1 : n <= 96 ? 2 : n <= 192 ? 4 : n <= 320 ? 8 : 16;
+  while (CL <= 16 && zgebrd_smem(m, n, CL) > 220 * 1024) CL *= 2;
+  return CL <= 16 ? CL : 0;
+}
+
+template <int CL>
+__global__ void __launch_bounds__(256, 1) k_zgebrd(const ZGebrdOp* __restrict__ ops) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const ZGebrdOp o = ops[blockIdx.x / CL];
+  const int m = o.m, n = o.n;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  extern __shared__ double2 zsm[];
+  const int ncol_max = (n + CL - 1) / CL;
+  const int ncol = (n - r + CL - 1) / CL;  // own columns: global column r + lc * CL
+  double2* cols = zsm;
+  double2* v = cols + (size_t)ncol_max * m;
+  double2* zp = v + m;
+  double2* cb = zp + m;
+  double2* z = cb + m;
+  double2* ub = z + m;
+  double2* scal = ub + ncol_max;  // [0] tau, [1] partial |row|^2 (x), [2] alpha, [3] |row|^2 (x), [4] alpha
+  for (int lc = warp; lc < ncol; lc += nwarp) {
+    const int c = r + lc * CL;
+    for (int i = lane; i < m; i += 32) cols[(size_t)lc * m + i] = o.A[i + (int64_t)c * o.lda];
+  }
+  __syncthreads();
+  if (r == 0 && warp == 0) zgebrd_left(o, cols, 0, v, scal, lane, true);
+  cluster.sync();
+  if (r != 0) {
+    const double2* rv = cluster.map_shared_rank(v, 0);
+    for (int i = tid; i < m; i += blockDim.x) v[i] = rv[i];
+    if (tid == 0) scal[0] = *cluster.map_shared_rank(scal, 0);
+  }
+  for (int j = 0; j + 1 < n; ++j) {
+    __syncthreads();
+    // (a) A(j:m, c) -= v conj(tau) (v^H A(j:m, c)) on the own columns c > j
+    const double2 tau = scal[0];
+    const int lc1 = (j + CL - r) / CL, lc2 = (j + 1 + CL - r) / CL;
+    if (tau.x != 0.0 || tau.y != 0.0)
+      for (int lc = lc1 + warp; lc < ncol; lc += nwarp) {
+        double2* a = cols + (size_t)lc * m;
+        double2 s = make_double2(0.0, 0.0);
+        for (int i = j + lane; i < m; i += 32) s = zfma_c(v[i], a[i], s);
+        const double2 w = zmul(zconj(tau), zwarp_sum(s));
+        for (int i = j + lane; i < m; i += 32) {
+          const double2 t = zmul(v[i], w);
+          a[i] = make_double2(a[i].x - t.x, a[i].y - t.y);
+        }
+      }
+    __syncthreads();
+    // (b) zp_i = sum over own c >= j+2 of A(i, c) conj(A(j, c)); partial |A(j, c >= j+2)|^2
+    for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int lc = lc2; lc < ncol; ++lc) acc = zfma_c(cols[(size_t)lc * m + j], cols[(size_t)lc * m + i], acc);
+      zp[i] = acc;
+    }
+    if (warp == 0) {
+      double s2 = 0.0;
+      for (int lc = lc2 + lane; lc < ncol; lc += 32) {
+        const double2 x = cols[(size_t)lc * m + j];
+        s2 = fma(x.x, x.x, fma(x.y, x.y, s2));
+      }
+      s2 = warp_sum(s2);
+      if (lane == 0) scal[1] = make_double2(s2, 0.0);
+    }
+    const int on = (j + 1) % CL, lnext = (j + 1) / CL;
+    const bool own_next = (r == on);
+    if (own_next) {
+      const double2* a = cols + (size_t)lnext * m;
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = a[i];
+      if (tid == 0) scal[2] = a[j];
+    }
+    cluster.sync();  // #1
+    // (c) right reflector from y = conj(row j): alpha' = conj(A(j, j+1)); u_c = y_c sc, z = taup A u
+    if (warp == 0) {
+      double s2 = lane < CL ? cluster.map_shared_rank(scal + 1, lane)->x : 0.0;
+      s2 = warp_sum(s2);
+      if (lane == 0) {
+        scal[3] = make_double2(s2, 0.0);
+        scal[4] = *cluster.map_shared_rank(scal + 2, on);
+      }
+    }
+    __syncthreads();
+    const double nrm2 = scal[3].x;
+    double betap;
+    double2 taup, sc;
+    zlarfg_coef(zconj(scal[4]), nrm2, betap, taup, sc);
+    const bool has_refl = taup.x != 0.0 || taup.y != 0.0;
+    constexpr bool kSliced = CL >= 8;
+    const int zlen = m - (j + 1);
+    const int zcs = kSliced ? (zlen + CL - 1) / CL : zlen;
+    const double2* rcb = cluster.map_shared_rank(cb, on);
+    if (has_refl) {
+      const int i0 = j + 1 + (kSliced ? r * zcs : 0);
+      const int i1 = kSliced ? min(m, i0 + zcs) : m;
+      for (int i = i0 + tid; i < i1; i += blockDim.x) {
+        double2 zs = make_double2(0.0, 0.0);
+        for (int q = 0; q < CL; ++q) {
+          const double2 p = cluster.map_shared_rank(zp, q)[i];
+          zs = make_double2(zs.x + p.x, zs.y + p.y);
+        }
+        z[i] = zmul(taup, zfma(sc, zs, rcb[i]));
+      }
+      for (int lc = lc2 + tid; lc < ncol; lc += blockDim.x) {
+        const double2 u = zmul(zconj(cols[(size_t)lc * m + j]), sc);
+        ub[lc] = u;
+        o.Pr[(r + lc * CL) + (int64_t)j * o.n] = u;
+      }
+    }
+    if (!own_next)
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) cb[i] = rcb[i];
+    if (kSliced) cluster.sync();  // #1b
+    if (kSliced && has_refl)
+      for (int i = j + 1 + tid; i < m; i += blockDim.x) {
+        const int q = (i - (j + 1)) / zcs;
+        if (q != r) z[i] = cluster.map_shared_rank(z, q)[i];
+      }
+    if (!kSliced) cluster.sync();
+    __syncthreads();
+    // (d) A(i, c) -= z_i conj(u_c), i > j, own c >= j+2; column j+1 (u = 1) in every CTA's warp 0, then
+    //     left reflector j+1 from it
+    if (warp == 0) {
+      double2* a = own_next ? cols + (size_t)lnext * m : cb;
+      if (has_refl)
+        for (int i = j + 1 + lane; i < m; i += 32) a[i] = make_double2(a[i].x - z[i].x, a[i].y - z[i].y);
+      __syncwarp();
+      if (own_next && lane == 0) {
+        o.e[j] = betap;
+        o.taup[j] = taup;
+      }
+      zgebrd_left(o, a, j + 1, v, scal, lane, own_next);
+    }
+    if (has_refl && tid >= 32)
+      for (int i = j + 1 + tid - 32; i < m; i += (int)blockDim.x - 32) {
+        const double2 zi = z[i];
+        for (int lc = lc2; lc < ncol; ++lc) {
+          double2* a = cols + (size_t)lc * m + i;
+          const double2 t = zmul(zi, zconj(ub[lc]));
+          *a = make_double2(a->x - t.x, a->y - t.y);
+        }
+      }
+  }
+  cluster.sync();
+}
+template <int CL>
+static void launch_zgebrd_cl(const ZGebrdOp* ops, int nops, size_t smem, cudaStream_t s) {
+  MPSG_CUDA(cudaFuncSetAttribute(k_zgebrd<CL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (CL > 8) MPSG_CUDA(cudaFuncSetAttribute(k_zgebrd<CL>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nops * CL);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  MPSG_CUDA(cudaLaunchKernelEx(&cfg, k_zgebrd<CL>, ops));
+  g_bd_launches.fetch_add(1);
+}
+void launch_zgebrd(const ZGebrdOp* ops, int nops, int CL, size_t smem, cudaStream_t s) {
+  if (nops <= 0) return;
+  MPSG_CHECK(smem <= 227 * 1024, "complex bidiagonalisation: sector too large for the cluster");
+  switch (CL) {
+    case 1: launch_zgebrd_cl<1>(ops, nops, smem, s); break;
+    case 2: launch_zgebrd_cl<2>(ops, nops, smem, s); break;
+    case 4: launch_zgebrd_cl<4>(ops, nops, smem, s); break;
+    case 8: launch_zgebrd_cl<8>(ops, nops, smem, s); break;
+    case 16: launch_zgebrd_cl<16>(ops, nops, smem, s); break;
+    default: throw Err(1, "complex bidiagonalisation: unsupported cluster size");
+  }
+}
+
+// X_out = H_0 ... H_{nref-1} X_in for the columns [c0, c1) of one op, one warp per column (column in
+// shared memory as complex values): the reflectors applied last to first, x -= tau v (v^H x).
+__global__ void __launch_bounds__(256) k_zapply_refl(const ZReflOp* __restrict__ ops) {
+  const ZReflOp o = ops[blockIdx.x];
+  const int len = o.len;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  extern __shared__ double2 zx[];
+  const int c = o.c0 + warp;
+  if (c >= o.c1) return;  // no block-wide synchronisation below
+  double2* x = zx + (size_t)warp * len;
+  for (int i = lane; i < len; i += 32)
+    x[i] = make_double2(i < o.rows_in ? o.Xin[i + (int64_t)c * o.ldi] : 0.0, 0.0);
+  __syncwarp();
+  for (int j = o.nref - 1; j >= 0; --j) {
+    const double2 tau = o.tau[j];
+    if (tau.x == 0.0 && tau.y == 0.0) continue;
+    const int r0 = j + o.off;
+    const double2* rj = o.R + (int64_t)j * o.ldr;
+    double2 s = lane == 0 ? x[r0] : make_double2(0.0, 0.0);
+    for (int i = r0 + 1 + lane; i < len; i += 32) s = zfma_c(rj[i], x[i], s);
+    const double2 st = zmul(tau, zwarp_sum(s));
+    __syncwarp();
+    if (lane == 0) x[r0] = make_double2(x[r0].x - st.x, x[r0].y - st.y);
+    for (int i = r0 + 1 + lane; i < len; i += 32) {
+      const double2 t = zmul(rj[i], st);
+      x[i] = make_double2(x[i].x - t.x, x[i].y - t.y);
+    }
+    __syncwarp();
+  }
+  for (int i = lane; i < len; i += 32) o.Xout[i + (int64_t)c * o.ldo] = x[i];
+}
+void launch_zapply_refl(const ZReflOp* ops, int nops, int lenmax, cudaStream_t s) {
+  if (nops <= 0) return;
+  const int nw = std::max(1, std::min(8, (int)((220 * 1024) / (sizeof(double2) * (size_t)std::max(lenmax, 1)))));
+  const size_t smem = sizeof(double2) * nw * (size_t)std::max(lenmax, 1);
+  MPSG_CHECK(smem <= 227 * 1024, "complex back-transformation: sector too tall");
+  MPSG_CUDA(cudaFuncSetAttribute(k_zapply_refl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_zapply_refl<<<nops, 32 * nw, smem, s>>>(ops);
+  g_bd_launches.fetch_add(1);
+}
+int zapply_refl_cols_per_block(int lenmax) {
+  return std::max(1, std::min(8, (int)((220 * 1024) / (sizeof(double2) * (size_t)std::max(lenmax, 1)))));
+}
+
 }  // namespace mpsg

@@ -8,8 +8,11 @@
 //
 // Complex block tensors are planar Tensors: the arena holds the real parts of all blocks, then the
 // imaginary parts at offset nelem.  Complex products run on the grouped FP64 GEMM as four real
-// products, the gate is a complex linear combination of blocks (k_lincomb), and the split takes a
-// one-sided Jacobi SVD per charge sector (cuSOLVER zgesvdj) with the complex FixPhase.
+// products, the gate is a complex linear combination of blocks (k_lincomb), and the split takes, per
+// charge sector, the library's bidiagonal SVD for complex matrices (svd method 4: complex Householder
+// bidiagonalisation to a real bidiagonal, the real Golub-Kahan stages, complex back-transformation;
+// zsvd_bidiag), cuSOLVER's one-sided Jacobi SVD (zgesvdj, method 0 and the fallback) or the density
+// route, with the complex FixPhase.
 #pragma once
 #include <cfloat>
 #include <chrono>
@@ -149,6 +152,7 @@ struct TebdEngine {
   std::vector<TensorP> G;    // Gamma[s], planar complex, nphys 1
   std::vector<TensorP> lam;  // lam[b + 1] = lambda of bond b (b = -1 .. N-1), real, blocks (q, q) n x 1
   double seconds = 0, split_seconds = 0, adjoint_seconds = 0;
+  int64_t zsvd_fallbacks = 0;  // splits the bidiagonal route handed to zgesvdj
   int64_t gates = 0;
   // Layer batching: when seg_gates is set, the engine holds a direct sum of independent bonds (bond i's
   // charges shifted by i << 32), block (q0, ...) uses the gate seg_gates[q0 >> 32], and truncation and
@@ -496,8 +500,8 @@ struct TebdEngine {
     double* dS = (double*)ctx->dmalloc(sizeof(double) * std::max<int64_t>(oS, 2));
     int* dinfo = (int*)ctx->dmalloc(sizeof(int) * std::max<size_t>(qcs.size(), 1));
     MPSG_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int) * std::max<size_t>(qcs.size(), 1), ctx->stream));
+    std::vector<CGatherOp> go;
     {
-      std::vector<CGatherOp> go;
       for (auto& x : secs) {
         Sec& s = x.second;
         for (int i : s.blocks) {
@@ -509,14 +513,36 @@ struct TebdEngine {
             go.push_back(CGatherOp{re(*tg, i), im(*tg, i), dM + s.offM + c0 + (int64_t)r0 * s.n, b.r, b.c, b.r, s.n, 1});
         }
       }
-      if (!go.empty()) {
-        CGatherOp* d = (CGatherOp*)ctx->dmalloc(sizeof(CGatherOp) * go.size());
-        MPSG_CUDA(cudaMemcpyAsync(d, go.data(), sizeof(CGatherOp) * go.size(), cudaMemcpyHostToDevice, ctx->stream));
-        launch_cgather(d, (int)go.size(), ctx->stream);
-        ctx->dfree(d);
+    }
+    auto gather = [&]() {
+      if (go.empty()) return;
+      CGatherOp* d = (CGatherOp*)ctx->dmalloc(sizeof(CGatherOp) * go.size());
+      MPSG_CUDA(cudaMemcpyAsync(d, go.data(), sizeof(CGatherOp) * go.size(), cudaMemcpyHostToDevice, ctx->stream));
+      launch_cgather(d, (int)go.size(), ctx->stream);
+      ctx->dfree(d);
+    };
+    gather();
+    // svd method 4 (default): the library's own bidiagonal route for complex sectors (real bidiagonal,
+    // complex reflectors); sectors beyond its cluster kernel or whose vectors would need the Jacobi
+    // route send the whole split to cuSOLVER zgesvdj (the sector matrices gathered again)
+    bool svd_done = false;
+    if (ctx->svd_method == 4) {
+      std::vector<ZSvdSec> zs;
+      for (auto& x : secs) {
+        Sec& sc = x.second;
+        const bool tall = sc.m >= sc.n;
+        const int ms = tall ? sc.m : sc.n, ns = tall ? sc.n : sc.m;
+        zs.push_back(ZSvdSec{ms, ns, sc.offM, tall ? dU + sc.offU : dV + sc.offV, tall ? dV + sc.offV : dU + sc.offU,
+                             ms, ns});
+      }
+      svd_done = zsvd_bidiag(ctx, zs, dM, dS);
+      if (!svd_done) {
+        ++zsvd_fallbacks;
+        gather();
       }
     }
-    if (ctx->svd_method != 0 && ctx->svd_method != 4) {  // 4 (real bidiagonal route): exact gesvdj here
+    if (svd_done) {
+    } else if (ctx->svd_method != 0 && ctx->svd_method != 4) {
       density_svd(secs, dM, dU, dV, dS);
     } else {
       cusolverDnHandle_t h = ctx->svd_handle();

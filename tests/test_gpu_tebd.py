@@ -38,8 +38,10 @@ def test_tebd_matches_oracle(ctx, N, steps, chimax, doTrunc):
     local = M.neel_state(N)
     ref = O.TEBD(local, W, ik)
     ref.second_order(steps, dt, chimax, doTrunc=doTrunc, tr_weight=1e-10)
+    f0 = ctx.L.mpsg_split_fallbacks()
     got = api.TEBDengine(local, W, ik, ctx=ctx)
     got.second_order(steps, dt, chimax, doTrunc=doTrunc, tr_weight=1e-10)
+    assert ctx.L.mpsg_split_fallbacks() == f0  # every split on the complex bidiagonal route
     err_sz = max(abs(got.measure_diag(s, SZ) - ref.measure_diag(s, SZ)) for s in range(N))
     err_lam = 0.0
     for b in range(N - 1):
@@ -110,3 +112,31 @@ def test_tebd_layer_batching_matches_bond_by_bond(ctx, svd):
                 assert np.abs(np.sort(a[q]) - np.sort(b[q])).max() < 1e-12
     finally:
         ctx.set_svd_method(lib.DEFAULT_SVD)
+
+
+def test_tebd_bidiagonal_split_matches_jacobi_split(ctx):
+    """The complex bidiagonal route (default) and cuSOLVER's zgesvdj give the same lambdas, block
+    structure and local magnetisation after 20 second-order steps at a binding chi."""
+    N, steps, dt, chimax = 14, 20, 0.05, 24
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 4, 0.8, 1.2), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    local = M.neel_state(N)
+    res = {}
+    for svd in ("bidiag", "jacobi"):
+        ctx.set_svd_method(svd)
+        try:
+            f0 = ctx.L.mpsg_split_fallbacks()
+            e = api.TEBDengine(local, W, ik, ctx=ctx)
+            e.second_order(steps, dt, chimax, doTrunc=True, tr_weight=1e-10)
+            res[svd] = ([e.lam(b) for b in range(N - 1)], [e.measure_diag(s, SZ) for s in range(N)],
+                        e.stats()["split_seconds"], ctx.L.mpsg_split_fallbacks() - f0)
+            e.close()
+        finally:
+            ctx.set_svd_method(lib.DEFAULT_SVD)
+    (lb, szb, tb, fb), (lj, szj, tj, _) = res["bidiag"], res["jacobi"]
+    assert fb == 0
+    for b in range(N - 1):
+        assert {q: len(v) for q, v in lb[b].items()} == {q: len(v) for q, v in lj[b].items()}, b
+        assert np.abs(_spectra(lb[b]) - _spectra(lj[b])).max() < 1e-12, b
+    assert max(abs(a - c) for a, c in zip(szb, szj)) < 1e-11
+    print(f"split seconds: bidiagonal {tb:.3f}, zgesvdj {tj:.3f}")
