@@ -909,15 +909,16 @@ def chains_arm(args):
 
 def tebd_arm(args):
     """TEBD of the XXZ chain L=64 from the Neel state, second order, dt=0.05, chi <= 512, truncation
-    1e-10 (density-matrix split, slices batched): forward time, the gradient of <Sz_32(T)> w.r.t. the
-    63 per-bond anisotropies (Delta_i ~ U[0.8,1.2], seed 4) by the adjoint, and central differences
-    (h = 1e-5) of the same evolution on `--fd-bonds` bonds."""
+    1e-10 (split by --svd: default the library's complex bidiagonal SVD; slices batched): forward
+    time, the gradient of <Sz_32(T)> w.r.t. the 63 per-bond anisotropies (Delta_i ~ U[0.8,1.2],
+    seed 4) by the adjoint, and central differences (h = 1e-5) of the same evolution on `--fd-bonds`
+    bonds."""
     from mpstools_gb300 import api, lib, models as M
     N, dt, chimax, trw, obs = 64, 0.05, 512, 1e-10, 32
     steps = args.tebd_steps
     sz = [-0.5, 0.5]
     ctx = lib.Context(0)
-    ctx.set_svd_method("density")
+    ctx.set_svd_method(args.svd)
     theta = 0.8 + 0.4 * M.uniform01(4, N - 1)
     ik = M.u1_itokeys(N)
     mk = lambda t: M.heisenberg_mpo(t, np.ones(N - 1), np.zeros(N))
@@ -951,7 +952,9 @@ def tebd_arm(args):
            "data": "synthetic",
            "config": {"workload": "tebd_xxz_L64_neel_dt0.05_chi512", "steps": steps, "dt": dt, "chimax": chimax,
                       "tr_weight": trw, "observable": "Sz_32", "couplings": "Delta_i ~ U[0.8,1.2] seed 4",
-                      "svd": "density (complex Gram, batched Hermitian eigensolver), slices batched"},
+                      "svd": {"bidiag": "complex bidiagonal SVD (own kernels)", "jacobi": "cuSOLVER zgesvdj"}.get(
+                          args.svd, "density (complex Gram, batched Hermitian eigensolver)") + ", slices batched",
+                      "split_fallbacks": int(ctx.L.mpsg_split_fallbacks())},
            "forward_seconds": t_fwd, "max_chi": chi_max, "value_Sz32": v0, "gates": st["gates"],
            "split_seconds": st["split_seconds"],
            "adjoint": {"seconds_forward_plus_gradient": t_adj, "value": v_adj, "grad_max_abs": float(np.abs(grad).max()),
