@@ -207,7 +207,8 @@ mpsg_status mpsg_lanczos2(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tenso
  * copies the site tensors; MPO and itokey arrays are copied too. */
 mpsg_status mpsg_dmrg_create(mpsg_ctx ctx, int32_t N, const mpsg_tensor* sites, const mpsg_mpo* mpos,
                              const mpsg_itokey* itokeys, mpsg_dmrg* out);
-/* prec: matvec/environment arithmetic; reorth: full reorthogonalisation in Lanczos;
+/* prec: Lanczos / matvec arithmetic (the environment updates stay FP64 unless
+ * mpsg_dmrg_set_env_prec says otherwise); reorth: full reorthogonalisation in Lanczos;
  * lanmax: Lanczos iteration cap (reference: 500). */
 mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, int32_t lanmax);
 /* The options in effect (set by mpsg_dmrg_set_options or restored by mpsg_dmrg_load); any output
@@ -366,7 +367,8 @@ mpsg_status mpsg_dmrg_ss_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv,
  * the CPU oracle).  mpsg_dmrg_load creates an engine on ctx; simulate() or build_environments()
  * continues from the loaded state.  Version-2 files also keep the engine's options (matvec
  * precision, reorthogonalisation, Lanczos limit), which load restores; version-1 files load with the
- * FP64 defaults.  The loader rejects (MPSG_ERR_ARG) files whose indices fall outside the declared
+ * FP64 defaults.  The environment-update precision (mpsg_dmrg_set_env_prec) is not kept: a loaded
+ * engine updates its environments in FP64 until it is set again.  The loader rejects (MPSG_ERR_ARG) files whose indices fall outside the declared
  * MPO / local dimensions or whose declared sizes exceed the file, before allocating for them. */
 mpsg_status mpsg_dmrg_save(mpsg_dmrg e, const char* path);
 mpsg_status mpsg_dmrg_load(mpsg_ctx ctx, const char* path, mpsg_dmrg* out);
