@@ -241,8 +241,9 @@ LanczosResult lanczos(Ctx* ctx, MatvecPlan& mv, const Tensor& th_init, Tensor& p
                       bool testenergy, bool reorth, LanczosStats* st, double tol_rel = 0.0, int ndiag = 5,
                       double stall_rel = 0.0, const double* proj = nullptr);
 // Lanczos in precision `prec` (mpsg_prec): FP64 is the reference loop; TF32/TF32X3/BF16/BF16X3 run
-// the loop with the tensor-core matvec and a precision-adapted energy test; AUTO runs BF16X3 first
-// and finishes with FP64 iterations restarted from the mixed-precision ground state.
+// the loop with the tensor-core matvec and a precision-adapted energy test; AUTO runs TF32X3 first
+// and finishes with FP64 iterations restarted from the mixed-precision ground state; MIXED runs
+// TF32X3 and measures the energy as the FP64 Rayleigh quotient of its ground state.
 LanczosResult lanczos_prec(Ctx* ctx, const Tensor& L, const Tensor& R, const Layout& sx, const MPO& W1, const MPO& W2,
                            const ItoKey& ik0, const ItoKey& ik1, const Tensor& th_init, Tensor& psi, int itmax,
                            double delta, bool testenergy, bool reorth, int prec, LanczosStats* st,
