@@ -115,14 +115,8 @@ def _bond_layout(charges_dims):
     return lay, off
 
 
-def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
-    """Apply L.W1.W2.R to theta by dense contraction (reference operator convention).
-
-    out(a',b';s1',s2') = sum L[a',a;wl] W1[wl,wm](out=s1,in=s1') W2[wm,wr](out=s2,in=s2')
-                         theta(a,b;s1,s2) R[b',b;wr]
-    Result blocks are keyed like theta and restricted to blocks with nonzero support.
-    """
-    # dense L[wl][a'(global), a(global)], R[wr][b', b]
+def _dense_parts(Lenv, Renv, theta, W1, W2, ik0, ik1):
+    """Dense L[wl][a'(global), a(global)], R[wr][b', b], W as [wl, wr, out, in], and the bond layouts."""
     lq, rq = {}, {}
     for (q0, q1, w), m in Lenv.items():
         lq.setdefault(q0, m.shape[0]); lq.setdefault(q1, m.shape[1])
@@ -143,13 +137,26 @@ def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
     for (q0, q1, w), m in Renv.items():
         o0, o1 = rlay[q0][0], rlay[q1][0]
         Rd[w, o0:o0 + m.shape[0], o1:o1 + m.shape[1]] = m
-    # W as dense [wl, wr, out, in]
     W1d = np.zeros((DW, DW, d0, d0))
     W2d = np.zeros((DW, DW, d1, d1))
     for (wl, wr, o, i, v) in W1[0]:
         W1d[wl, wr, o, i] += v
     for (wl, wr, o, i, v) in W2[0]:
         W2d[wl, wr, o, i] += v
+    # the charge-allowed blocks (a, b; s1, s2), b = a + q(s1) + q(s2)
+    allowed = [(a, b, s1, s2) for a in lq for b in rq for s1 in range(d0) for s2 in range(d1)
+               if a + ik0[s1] + ik1[s2] == b]
+    return llay, rlay, nl, nr, d0, d1, Ld, Rd, W1d, W2d, allowed
+
+
+def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
+    """Apply L.W1.W2.R to theta by dense contraction (reference operator convention).
+
+    out(a',b';s1',s2') = sum L[a',a;wl] W1[wl,wm](out=s1,in=s1') W2[wm,wr](out=s2,in=s2')
+                         theta(a,b;s1,s2) R[b',b;wr]
+    Result blocks are keyed like theta and restricted to blocks with nonzero support.
+    """
+    llay, rlay, nl, nr, d0, d1, Ld, Rd, W1d, W2d, allowed = _dense_parts(Lenv, Renv, theta, W1, W2, ik0, ik1)
     T = np.zeros((nl, d0, d1, nr))
     for (a, b, s1, s2), m in theta.items():
         oa, ob = llay[a][0], rlay[b][0]
@@ -157,17 +164,48 @@ def dense_heff_apply(Lenv, Renv, theta, W1, W2, ik0, ik1):
     # out[a', s1', s2', b'] = L[wl,a',a] W1[wl,wm,s1,s1'] W2[wm,wr,s2,s2'] T[a,s1,s2,b] R[wr,b',b]
     out = np.einsum("lxa,lmpP,mrqQ,apqb,ryb->xPQy", Ld, W1d, W2d, T, Rd, optimize=True)
     res = {}
-    for a in lq:
-        for b in rq:
-            for s1 in range(d0):
-                for s2 in range(d1):
-                    if a + ik0[s1] + ik1[s2] != b:
-                        continue
-                    oa, na = llay[a]
-                    ob, nb = rlay[b]
-                    blk = out[oa:oa + na, s1, s2, ob:ob + nb]
-                    res[(a, b, s1, s2)] = blk.copy()
+    for (a, b, s1, s2) in allowed:
+        oa, na = llay[a]
+        ob, nb = rlay[b]
+        res[(a, b, s1, s2)] = out[oa:oa + na, s1, s2, ob:ob + nb].copy()
     return res
+
+
+def dense_heff_matrix(Lenv, Renv, theta, W1, W2, ik0, ik1):
+    """The operator of dense_heff_apply as a matrix on the charge-allowed blocks (the blocks
+    dense_heff_apply returns, in sorted key order, each flattened row-major).
+
+    Returns (keys, shapes, H, to_vec, to_blocks) with to_vec(blocks) -> flat vector (missing blocks
+    zero) and to_blocks(vector) -> {key: block}."""
+    llay, rlay, nl, nr, d0, d1, Ld, Rd, W1d, W2d, allowed = _dense_parts(Lenv, Renv, theta, W1, W2, ik0, ik1)
+    # the full operator on (a, s1, s2, b) x (a', s1', s2', b'), then restricted to the allowed blocks
+    full = np.einsum("lxa,lmpP,mrqQ,ryb->xPQyapqb", Ld, W1d, W2d, Rd, optimize=True)
+    nfull = nl * d0 * d1 * nr
+    full = full.reshape(nfull, nfull)
+    keys = sorted(allowed)
+    shapes = {k: (llay[k[0]][1], rlay[k[1]][1]) for k in keys}
+    idx = []
+    for (a, b, s1, s2) in keys:
+        oa, na = llay[a]
+        ob, nb = rlay[b]
+        ii = np.arange(oa, oa + na)[:, None] * (d0 * d1 * nr) + (s1 * d1 + s2) * nr + np.arange(ob, ob + nb)[None, :]
+        idx.append(ii.ravel())
+    idx = np.concatenate(idx) if idx else np.zeros(0, int)
+    sizes = [int(np.prod(shapes[k])) for k in keys]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(int)
+    H = full[np.ix_(idx, idx)]
+
+    def to_vec(x):
+        v = np.zeros(len(idx))
+        for i, k in enumerate(keys):
+            if k in x:
+                v[off[i]:off[i + 1]] = np.asarray(x[k]).ravel()
+        return v
+
+    def to_blocks(v):
+        return {k: v[off[i]:off[i + 1]].reshape(shapes[k]).copy() for i, k in enumerate(keys)}
+
+    return keys, shapes, H, to_vec, to_blocks
 
 
 # --------------------------------------------------------------------------- dense TEBD reference
