@@ -193,3 +193,51 @@ def test_oracle_truncation_ties_keep_the_later_sector():
     kept = {q: v for q, v in lam.items() if len(v)}
     assert list(kept) == [1] and abs(kept[1][0] - 1.0) < 1e-15
     assert abs(tw - (1.0 - 0.36)) < 1e-15  # 1 - the kept value squared, before normalisation
+
+
+def _right_orthonormal_error(site):
+    acc = {}
+    for (a, b, s), m in site.items():
+        acc[a] = acc.get(a, 0) + m @ m.T
+    return max(np.abs(x - np.eye(x.shape[0])).max() for x in acc.values())
+
+
+def test_oracle_prepare_is_right_canonical_and_keeps_the_state():
+    """orthonormalize(mps, "rl") (src/MPSfunctions.hpp:1756-1792, prepareSite "r" with truncation of
+    values <= 1e-16): every site right-orthonormal, the state unchanged up to its norm (the norm
+    goes to the left boundary and is dropped), and a bond direction that carries no weight is cut."""
+    N = 10
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 1), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    sites = M.random_u1_mps(N, N // 2, 6, 5)
+    v0 = ed.mps_sector_vector(sites, N // 2)
+
+    def prepared(s):
+        g = O.DMRG(s, W, ik, maxthreads=2)
+        g.prepare()
+        return [g.site(x) for x in range(N)]
+
+    ps = prepared(sites)
+    v1 = ed.mps_sector_vector(ps, N // 2)
+    assert abs(np.linalg.norm(v1) - 1.0) < 1e-13
+    assert abs(abs(float(v0 @ v1)) / np.linalg.norm(v0) - 1.0) < 1e-13
+    for x in range(N):
+        assert _right_orthonormal_error(ps[x]) < 1e-13, x
+    # a redundant direction on bond x: a zero row in the left sector q of site x and a random
+    # column in the right sector q of site x - 1 (the state does not change)
+    x = N // 2
+    q = sorted({k[0] for k in sites[x]} & {k[1] for k in sites[x - 1]})[1]
+    rng = np.random.default_rng(0)
+    aug = [dict(t) for t in sites]
+    for k, m in list(aug[x].items()):
+        if k[0] == q:
+            aug[x][k] = np.vstack([m, np.zeros((1, m.shape[1]))])
+    for k, m in list(aug[x - 1].items()):
+        if k[1] == q:
+            aug[x - 1][k] = np.hstack([m, rng.standard_normal((m.shape[0], 1))])
+    assert np.abs(ed.mps_sector_vector(aug, N // 2) - v0).max() < 1e-12
+    pa = prepared(aug)
+    dims = lambda st: [sorted((k, m.shape) for k, m in t.items()) for t in st]
+    assert dims(pa) == dims(ps)
+    v2 = ed.mps_sector_vector(pa, N // 2)
+    assert abs(abs(float(v2 @ v1)) - 1.0) < 1e-13
