@@ -379,6 +379,9 @@ __global__ void __launch_bounds__(NT, 1) k_gebrd_mc(const GebrdOp* __restrict__ 
   const size_t xset = (size_t)NC * m + NC + m + 8;
   unsigned nb = 0;
   if (tid == 0) flag[0] = 0;
+  // every CTA of the cluster runs and has cleared its flag before a peer may set it (a wait that
+  // expires writes the flags of the whole cluster through distributed shared memory)
+  cluster.sync();
   if (R == 0 && warp == 0) gebrd_left(o, cols, 0, v, scal, lane);
   if (!gebrd_sector_sync<CL>(cluster, o.ctr, NC * ++nb, o.err, flag)) return;
   if (R != 0) {  // reflector 0 from the sector matrix; every later one is computed in every CTA
