@@ -241,3 +241,39 @@ def test_oracle_prepare_is_right_canonical_and_keeps_the_state():
     assert dims(pa) == dims(ps)
     v2 = ed.mps_sector_vector(pa, N // 2)
     assert abs(abs(float(v2 @ v1)) - 1.0) < 1e-13
+
+
+def _left_orthonormal_error(site):
+    acc = {}
+    for (a, b, s), m in site.items():
+        acc[b] = acc.get(b, 0) + m.T @ m
+    return max(np.abs(x - np.eye(x.shape[0])).max() for x in acc.values())
+
+
+def test_oracle_do_step_absorbs_lambda_by_direction():
+    """DMRGengine::doStep (src/container.hpp:292-337): split into U, lambda, V^T; lambda goes right
+    (dir > 0: site keeps U, left-orthonormal; site+1 = lambda V^T) or left (dir <= 0: site = U lambda;
+    site+1 keeps V^T, right-orthonormal).  Without truncation the state after the step is the
+    normalised Lanczos ground state, whose energy the step returns."""
+    N = 10
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 2), np.ones(N - 1), np.zeros(N))
+    ik = M.u1_itokeys(N)
+    g = O.DMRG(M.random_u1_mps(N, N // 2, 32, 9), W, ik, maxthreads=2)
+    g.prepare()
+    for site in range(4):
+        E = g.do_step(site, 1, 1000)
+        assert _left_orthonormal_error(g.site(site)) < 1e-12
+        lam = g.lam(site)
+        nrm = sum(float(v @ v) for v in lam.values())
+        assert abs(nrm - 1.0) < 1e-13
+        # site+1 = lambda V^T: its rows scaled back by 1/lambda are orthonormal
+        B = {k: m / lam[k[0]][:, None] for k, m in g.site(site + 1).items()}
+        assert _right_orthonormal_error(B) < 1e-10
+        assert abs(g.measure() - E) < 1e-11 * abs(E)
+    for site in range(4, 0, -1):
+        E = g.do_step(site, -1, 1000)
+        assert _right_orthonormal_error(g.site(site + 1)) < 1e-12
+        lam = g.lam(site)
+        A = {k: m / lam[k[1]][None, :] for k, m in g.site(site).items()}
+        assert _left_orthonormal_error(A) < 1e-10
+        assert abs(g.measure() - E) < 1e-11 * abs(E)
