@@ -305,9 +305,10 @@ __global__ void __launch_bounds__(NT, 1) k_gebrd(const GebrdOp* __restrict__ ops
 // partials of its rows (one slice per CTA, exchanged through distributed shared memory), the right
 // update, and in every CTA the next left reflector from the copy of the next column.  The barriers count on a per-sector counter in global memory; every
 // wait is bounded (~2 s of globaltimer), after which the CTA records *err and all CTAs of its
-// cluster leave together (the other clusters' waits then expire as well); the host redoes the
-// split on the Jacobi route.  All G clusters of a sector must be resident together: the host
-// launches these sectors alone on their stream, at most 2 x 16 CTAs each.
+// cluster leave together (the other clusters' waits then expire as well); the host redoes those
+// sectors on one cluster from the copy of their matrices.  All G clusters of a sector must be
+// resident together: the host launches these sectors alone on their stream, at most as many as
+// cudaOccupancyMaxActiveClusters allows, 2 x 16 CTAs each.
 __device__ __forceinline__ uint64_t gebrd_globaltimer() {
   uint64_t t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
