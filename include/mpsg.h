@@ -85,8 +85,10 @@ int64_t mpsg_ctx_kernel_launches(mpsg_ctx ctx);
  * each schedule for stage A (entries 0-2) and stage C (3-5; -1 where not timed).  Any pointer may be
  * null. */
 void mpsg_tc_autotune_info(int64_t* tuned, int64_t* cache_hits, int32_t* last_schedule2, float* last_timing6);
-/* Number of charge sectors of splits on the library's own SVD routes (svd methods 3 and 4) that were
- * redone on the Jacobi route because their singular vectors were too dependent for CholeskyQR. */
+/* How often the library's own SVD routes (svd methods 3 and 4) left their fast path: charge sectors
+ * redone on the Jacobi route (singular vectors too dependent for CholeskyQR, or more kept vectors
+ * than the cluster Cholesky takes), sectors of a two-cluster bidiagonalisation whose barrier wait
+ * expired (redone on one cluster), and TEBD splits handed to the complex Jacobi SVD (one per split). */
 int64_t mpsg_split_fallbacks(void);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
  * 4 = the library's own exact SVD (default): Householder bidiagonalisation of each charge sector,
