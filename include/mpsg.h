@@ -94,8 +94,9 @@ int64_t mpsg_split_fallbacks(void);
  * 4 = the library's own exact SVD (default): Householder bidiagonalisation of each charge sector,
  *     singular values by bisection on the Golub-Kahan tridiagonal (absolute accuracy ~eps ||M||, as
  *     dgesvd), computed only down to the global truncation cut of the split; singular vectors only
- *     for the kept values (inverse iteration, CholeskyQR, reflector back-transformation).  Sectors
- *     wider than 512 fall back to route 0;
+ *     for the kept values (inverse iteration, CholeskyQR, reflector back-transformation).  A split
+ *     with a sector of more than about 6900 rows (taken tall) runs on route 0 as a whole; a sector
+ *     with more than 1600 kept values has its vectors redone on route 0 (mpsg_split_fallbacks);
  * 0 = one-sided Jacobi SVD of each charge sector (cuSOLVER gesvdj, FP64, exact),
  * 1, 2, 3 = eigen-decomposition of each sector's reduced density matrix G = M^T M (FP64) with the
  *     eigensolver of cuSOLVER batched by size class (1), cuSOLVER per sector on concurrent streams (2)
