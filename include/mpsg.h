@@ -261,8 +261,10 @@ mpsg_status mpsg_dmrg_measure_mpo(mpsg_dmrg e, const mpsg_mpo* W, double* out);
  * TEBDengine (src/container.hpp:1195-1406) from a product state: Gamma tensors complex (planar on
  * the device), lambdas real.  The two-site gate of bond b is exp(-i dt h_b) built from the MPO like
  * MPO::getNNGate (src/MPOTypes.hpp:1090-1209); each bond update is applyGate
- * (src/MPSfunctions.hpp:1492-1548) with the complex split (per-sector Jacobi SVD, complex FixPhase,
- * the reference's truncation, dropDangling, squeeze(1e-15)). */
+ * (src/MPSfunctions.hpp:1492-1548) with the complex split (per charge sector the context's SVD
+ * method: by default the library's complex bidiagonal SVD, cuSOLVER's zgesvdj for method 0 and where
+ * a split does not fit the bidiagonal route; complex FixPhase, the reference's truncation,
+ * dropDangling, squeeze(1e-15)). */
 typedef struct mpsg_tebd_s* mpsg_tebd;
 /* local_state[s]: index into ik[s] of site s (e.g. the Neel state s % 2). */
 mpsg_status mpsg_tebd_create(mpsg_ctx ctx, int32_t N, const int32_t* local_state, const mpsg_mpo* W,
