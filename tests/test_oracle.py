@@ -104,6 +104,31 @@ def test_oracle_env_update_matches_dense():
         assert np.abs(acc - blk).max() < 1e-12
 
 
+def test_oracle_env_update_right_matches_dense():
+    """addContractionLayer with direction <= 0 (src/MPSfunctions.hpp:276-352, add_out_sub_2):
+    R'[a',a;wl] = sum over W[wl,wr](out,in) of A(a',b';in) R[b',b;wr] A(a,b;out)^T."""
+    g, W, ik = _env_case()
+    site = 6
+    Rprev = g.env("R", site + 1)
+    A = g.site(site)
+    out = O.add_contraction_layer(Rprev, A, W[site], ik[site], -1)
+    assert out
+    for (a1, a, w0), blk in out.items():
+        acc = np.zeros_like(blk)
+        for (wl, wr, so, si, v) in W[site][0]:
+            if wl != w0:
+                continue
+            for (b1, b, w), Rb in Rprev.items():
+                if w != wr:
+                    continue
+                au = A.get((a1, b1, si))
+                ad = A.get((a, b, so))
+                if au is None or ad is None:
+                    continue
+                acc += v * au @ Rb @ ad.T
+        assert np.abs(acc - blk).max() < 1e-12
+
+
 def test_golden_fixtures_reproduce():
     """The committed fixtures (tests/golden/make_golden.py) are reproduced by the oracle."""
     with open(os.path.join(GOLDEN, "ed_energies.json")) as f:
