@@ -302,3 +302,22 @@ def test_oracle_do_step_absorbs_lambda_by_direction():
         A = {k: m / lam[k[1]][None, :] for k, m in g.site(site).items()}
         assert _left_orthonormal_error(A) < 1e-10
         assert abs(g.measure() - E) < 1e-11 * abs(E)
+
+
+def test_oracle_theta_formation():
+    """BlockMatrix<2>(B1, B2) (src/BlockTensor.hpp:285-301): theta(a,b;s1,s2) = A1(a,c;s1) A2(c,b;s2)
+    for every pair of blocks sharing the middle charge c (one pair per key)."""
+    N = 10
+    ik = M.u1_itokeys(N)
+    sites = M.random_u1_mps(N, N // 2, 12, 4)
+    A1, A2 = sites[4], sites[5]
+    th = O.theta(A1, A2)
+    want = {}
+    for (a, c, s1), m1 in A1.items():
+        for (c2, b, s2), m2 in A2.items():
+            if c2 == c:
+                assert (a, b, s1, s2) not in want
+                want[(a, b, s1, s2)] = m1 @ m2
+    assert set(th) == set(want)
+    for k in want:
+        assert np.abs(th[k] - want[k]).max() < 1e-13 * max(1.0, np.abs(want[k]).max())
