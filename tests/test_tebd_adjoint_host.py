@@ -99,3 +99,19 @@ def test_oracle_differences_match_dense_differences():
     g_de = _dense_fd(N, theta, steps, dt, obs)
     assert np.abs(g_de).max() > 1e-4
     assert np.abs(g_or - g_de).max() < 1e-9
+
+
+def test_nn_gate_matches_oracle_and_expm_on_the_host():
+    """The library's getNNGate (host code, no GPU) against the oracle's MPO::getNNGate restatement
+    and against expm of the library's own bond Hamiltonian (boundary-aware on-site weights), for
+    real and complex time steps: the reference exponentiates -(imag(dt) + i real(dt)) h
+    (src/MPOTypes.hpp:1190)."""
+    N = 6
+    W = M.heisenberg_mpo(M.xxz_couplings(N, 4, 0.8, 1.2), np.ones(N - 1), 0.3 * np.arange(N))
+    for s in range(N - 1):
+        H = api.bondHamiltonian(W[s], W[s + 1], s, N)
+        assert np.abs(H - H.T).max() < 1e-15
+        for dt in (0.05 + 0j, 0.05 - 0.01j):
+            got = api.getNNGate(W[s], W[s + 1], s, N, dt)
+            assert np.abs(got - O.nn_gate(W[s], W[s + 1], s, N, dt)).max() < 1e-14
+            assert np.abs(got - sl.expm(-(dt.imag + 1j * dt.real) * H)).max() < 1e-13
