@@ -144,6 +144,37 @@ def test_golden_fixtures_reproduce():
         assert np.abs(out[k] - case["out"][k]).max() < 1e-13
 
 
+def test_golden_step_fixture_reproduces():
+    """tests/golden/step_small.npz (made by tests/golden/make_golden.py from the oracle): the left
+    environment update, the split at a binding chimax and the Lanczos ground state of one update of
+    a 12-site XXZ chain are reproduced by the oracle from the stored inputs."""
+    from golden_io import unpack_bm, unpack_mpo
+    z = np.load(os.path.join(GOLDEN, "step_small.npz"), allow_pickle=False)
+    L, R, A1, A2 = (unpack_bm(n, z) for n in ("L", "R", "A1", "A2"))
+    W1, W2 = unpack_mpo("W1", z), unpack_mpo("W2", z)
+    ik0, ik1 = [int(x) for x in z["ik0"]], [int(x) for x in z["ik1"]]
+
+    def same(a, b, tol):
+        assert set(a) == set(b)
+        for k in a:
+            assert a[k].shape == b[k].shape and np.abs(a[k] - b[k]).max() <= tol, k
+
+    same(O.add_contraction_layer(L, A1, W1, ik0, 1), unpack_bm("Lnext", z), 1e-13)
+    chimax, tw0, chi0 = z["split_scalars"]
+    U, Vt, lam, tw, chi = O.split(unpack_bm("split_theta", z), ik0, ik1, int(chimax), doTrunc=False,
+                                  tr_weight=1e-12, normalize=True)
+    assert chi == int(chi0) and abs(tw - tw0) < 1e-14
+    kept = {q: v for q, v in lam.items() if len(v)}
+    assert sorted(kept) == [int(q) for q in z["split_lam_q"]]
+    np.testing.assert_allclose(np.concatenate([kept[q] for q in sorted(kept)]), z["split_lam"], rtol=1e-13)
+    same(U, unpack_bm("split_U", z), 1e-11)
+    same(Vt, unpack_bm("split_Vt", z), 1e-11)
+    E0, n0 = z["lanczos_scalars"]
+    E, n, st = O.lanczos(L, R, O.theta(A1, A2), W1, W2, ik0, ik1, itmax=500, delta=1e-12)
+    assert n == int(n0) and abs(E - E0) < 1e-13 * abs(E0)
+    same(st, unpack_bm("lanczos_state", z), 1e-10)
+
+
 def test_oracle_overlap_and_measure_match_dense():
     """computeOverlap and MPO::measure (energy, local Sz) against dense state vectors."""
     N, Nup = 8, 4
