@@ -38,6 +38,13 @@
 // Dense BLAS/LAPACK come from the OpenBLAS that numpy/scipy bundle, opened with
 // dlopen at run time (the same Fortran routines the reference calls through MKL:
 // dgemm, ddot, dgesvd, dstev).
+//
+// Parity unpinned: MPSTools ships no tests, fixtures or golden vectors, and it
+// cannot be built here (Boost and MKL are absent), so no output of the
+// reference itself checks this restatement.  It is checked instead against
+// independent answers: exact diagonalisation energies, dense contractions of
+// the same operands, and numpy restatements of the reference's split,
+// truncation and Lanczos (tests/).
 // ============================================================================
 #include <dlfcn.h>
 #include <omp.h>

@@ -4,6 +4,11 @@ TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
 checker and by bench.py for the timed CPU baseline.  The product package
 (mpstools_gb300) never imports this module.
 
+Parity unpinned: MPSTools has no tests or golden vectors and cannot be built here, so
+no output of the reference itself checks the oracle; tests/ check it against exact
+diagonalisation, dense contractions and numpy restatements of the reference's split,
+truncation and Lanczos instead.
+
 Block matrices cross this boundary as plain dicts:
   single-site / environment:  {(q0, q1, p0): 2-D float64 array}
   two-site theta:             {(q0, q1, p0, p1): 2-D float64 array}
