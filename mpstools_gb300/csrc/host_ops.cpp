@@ -2145,7 +2145,10 @@ static SplitResult split2_impl(Ctx* ctx, const Tensor& th, const ItoKey& ik0, co
   // the singular vectors of the kept ones after the truncation; every other route decomposes fully
   const bool bidiag = ctx->svd_method == 4 && sv.bidiag_fits() && !sv.s.empty();
   split_mark(ctx, "gather");
-  if (bidiag) sv.bidiag_values(s0, chimax, 1e-15);
+  // truncate(tr_weight, chimax) measures the discarded weight against the norm of ALL values
+  // (src/BlockTensor.hpp:90-108), so with doTrunc every value above the floor is computed (no
+  // chimax cut); truncate(chimax) needs only the values above the top-chimax cut
+  if (bidiag) sv.bidiag_values(s0, doTrunc ? std::numeric_limits<int>::max() : chimax, 1e-15);
   else sv.run(ctx->svd_method == 4 ? 0 : ctx->svd_method);
   std::vector<int32_t> sec_of(sv.nS);
   for (size_t si = 0; si < qcs.size(); ++si)

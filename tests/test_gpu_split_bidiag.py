@@ -130,6 +130,37 @@ def test_bidiag_split_weight_truncation_and_tiny_sectors(ctx):
     assert abs(tw1 - tw0) <= 1e-13
 
 
+@pytest.mark.parametrize("chimax,tr_weight", [(60, 1e-2), (90, 1e-2), (70, 3e-2)])
+def test_bidiag_split_weight_truncation_against_the_norm_of_all_values(ctx, chimax, tr_weight):
+    """truncate(tr_weight, chimax) (src/BlockTensor.hpp:84-136) measures the discarded weight against
+    the norm of all singular values, those below a top-chimax cut included: slowly decaying spectra
+    in four sectors (98 values), chimax binding (60) or the weight bound first (90, 70): kept count,
+    values and returned weight as the oracle's dgesvd split.  A norm of only the values above the
+    top-chimax cut keeps 56 instead of 60 values in the first case and returns another weight in all."""
+    rng = np.random.default_rng(5)
+    th = {}
+    for q, (m, n) in enumerate([(40, 36), (30, 34), (24, 20), (12, 16)]):
+        k = min(m, n)
+        U = np.linalg.qr(rng.standard_normal((m, k)))[0]
+        V = np.linalg.qr(rng.standard_normal((n, k)))[0]
+        th[(q, q, 0, 0)] = (U * np.exp(-np.arange(k) * 0.12 - 0.3 * q)) @ V.T
+    nrm = np.sqrt(sum(float((v * v).sum()) for v in th.values()))
+    th = {k: v / nrm for k, v in th.items()}
+    ik = [0, 0]
+    U0, V0, l0, tw0, chi0 = O.split(th, ik, ik, chimax, doTrunc=True, tr_weight=tr_weight)
+    ctx.set_svd_method("bidiag")
+    try:
+        U1, V1, l1, tw1, chi1 = api.split(th, (ik, ik), chimax, doTrunc=True, tr_weight=tr_weight, ctx=ctx)
+    finally:
+        ctx.set_svd_method(lib.DEFAULT_SVD)
+    assert chi1 == chi0
+    assert {q: len(v) for q, v in l1.items() if len(v)} == {q: len(v) for q, v in l0.items() if len(v)}
+    for q in l0:
+        if len(l0[q]):
+            assert np.abs(np.asarray(l1[q]) - np.asarray(l0[q])).max() <= 1e-13
+    assert abs(tw1 - tw0) <= 1e-12
+
+
 def test_bidiag_split_sector_with_more_than_512_kept_vectors(ctx):
     """One 1016 x 792 sector (as converged chi = 2048 sweeps produce) whose 792 values are all kept:
     beyond the shared-memory Cholesky of a 16-CTA cluster, the CholeskyQR runs on its global-memory
