@@ -222,7 +222,10 @@ mpsg_status mpsg_dmrg_set_options(mpsg_dmrg e, mpsg_prec prec, int32_t reorth, i
 mpsg_status mpsg_dmrg_set_env_prec(mpsg_dmrg e, mpsg_prec prec);
 mpsg_status mpsg_dmrg_get_options(mpsg_dmrg e, int32_t* prec, int32_t* reorth, int32_t* lanmax);
 /* DMRGengine::simulate(maxsteps, EnConv, chimax, doTrunc, tr_weight, delta, testenergy):
- * orthonormalize("rl"), computeR, sweeps, final doStep(0,-1).  E = last Lanczos energy. */
+ * orthonormalize("rl"), computeR, sweeps, final doStep(0,-1).  E = last Lanczos energy.  The
+ * reference's two further arguments keep their defaults here: leaveoutlast = false (with true the
+ * left sweeps skip doStep(N-2, -1): schedule the sweeps with mpsg_dmrg_prepare / mpsg_dmrg_do_step)
+ * and targetstate = 0 (the Lanczos ground state; for excited states see mpsg_dmrg_excited_simulate). */
 mpsg_status mpsg_dmrg_simulate(mpsg_dmrg e, uint32_t maxsteps, double EnConv, uint32_t chimax,
                                int32_t doTrunc, double tr_weight, double delta, int32_t testenergy,
                                double* E);
