@@ -93,7 +93,8 @@ int64_t mpsg_split_fallbacks(void);
 /* Two-site SVD used by split and canonicalisation (BoostSVD, blas/lapack_routines.cpp:614-634):
  * 4 = the library's own exact SVD (default): Householder bidiagonalisation of each charge sector,
  *     singular values by bisection on the Golub-Kahan tridiagonal (absolute accuracy ~eps ||M||, as
- *     dgesvd), computed only down to the global truncation cut of the split; singular vectors only
+ *     dgesvd), computed only down to the global top-chimax cut of the split (all of them down to
+ *     1e-15 with doTrunc, whose weight bound needs the norm of all values); singular vectors only
  *     for the kept values (inverse iteration, CholeskyQR, reflector back-transformation).  A split
  *     with a sector of more than about 6900 rows (taken tall) runs on route 0 as a whole; a sector
  *     with more than 1600 kept values has its vectors redone on route 0 (mpsg_split_fallbacks);
