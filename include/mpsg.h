@@ -199,7 +199,11 @@ mpsg_status mpsg_split2(mpsg_ctx ctx, mpsg_tensor theta, const mpsg_itokey* ikl,
 
 /* TSLanzcosEngine(L,R,mpsl,mpsr,mpol,mpor,itokeyl,itokeyr).simulate(itmax,delta,testenergy)
  * followed by getState(0)  -- src/lanzcos.hpp:100-114,165-278,81-92.
- * reorth != 0 adds full FP64 reorthogonalisation (the reference has none). */
+ * reorth != 0 adds full FP64 reorthogonalisation (the reference has none).  testenergy = 0: the
+ * reference stops when the residual |H psi - E psi| of the current Ritz vector (one extra matvec
+ * every 5 iterations) falls below delta; that test is not implemented here yet, the loop then stops
+ * only at breakdown (norm of the new vector < delta) or after itmax iterations.  The same holds for
+ * the testenergy argument of the DMRG entry points. */
 mpsg_status mpsg_lanczos2(mpsg_ctx ctx, mpsg_tensor L, mpsg_tensor R, mpsg_tensor mpsl, mpsg_tensor mpsr,
                           const mpsg_mpo* Wl, const mpsg_mpo* Wr, const mpsg_itokey* ikl,
                           const mpsg_itokey* ikr, int32_t itmax, double delta, int32_t testenergy,

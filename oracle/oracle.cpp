@@ -583,6 +583,20 @@ static LanczosOut lanczos(const BM& L, const BM& R, const BM& Ainit, const MPOMa
         tridiag(estmp, ks, nullptr);
         if (std::fabs(estmp[0] - eold) < delta) break;
         eold = estmp[0];
+      } else {
+        // residual test (lanzcos.hpp:215-235): the Ritz vector A4 = sum_i As[i] z(i,0) of the current
+        // tridiagonal matrix, A6 = H A4 - E0 A4, stop when |A6| < delta (one extra matvec)
+        estmp = es;
+        std::vector<double> z;
+        tridiag(estmp, ks, &z);
+        BM A4 = bm_scaled(As[0], z[0]);
+        for (size_t i = 1; i < es.size(); ++i) bm_add(A4, bm_scaled(As[i], z[i]));
+        auto t1 = std::chrono::steady_clock::now();
+        BM A5 = contract_twosite(L, R, A4, mpol, mpor, ik0, ik1, maxthreads);
+        if (t_matvec) *t_matvec += std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+        BM A6 = bm_scaled(A4, -estmp[0]);
+        bm_add(A6, A5);
+        if (std::fabs(std::sqrt(bm_dot(A6, A6))) < delta) break;
       }
     }
     if (!first) {

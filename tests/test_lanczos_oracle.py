@@ -31,7 +31,7 @@ def _lincomb(*terms):
     return out
 
 
-def _lanczos_np(matvec, th, itmax, delta, ndiag=5):
+def _lanczos_np(matvec, th, itmax, delta, ndiag=5, testenergy=True):
     A1, A0 = dict(th), None
     es, ks, As = [], [], []
     eold, it, first, tests = 1e100, 0, True, []
@@ -46,12 +46,21 @@ def _lanczos_np(matvec, th, itmax, delta, ndiag=5):
         As.append(A1)
         e = _dot(A2, A1)
         es.append(e)
-        if it % ndiag == 0 and it != 0:
+        if it % ndiag == 0 and it != 0 and testenergy:
             e0 = eigh_tridiagonal(np.array(es), np.array(ks), eigvals_only=True, lapack_driver="stev")[0]
             tests.append(abs(e0 - eold))
             if abs(e0 - eold) < delta:
                 break
             eold = e0
+        elif it % ndiag == 0 and it != 0:
+            # residual of the current Ritz vector, one extra matvec
+            w, z = eigh_tridiagonal(np.array(es), np.array(ks), lapack_driver="stev")
+            A4 = _lincomb(*[(z[i, 0], As[i]) for i in range(len(As))])
+            A6 = _lincomb((1.0, matvec(A4)), (-w[0], A4))
+            resi = np.sqrt(_dot(A6, A6))
+            tests.append(resi)
+            if resi < delta:
+                break
         if not first:
             A3 = _lincomb((1.0, A2), (-e, A1), (-k, A0))
         else:
@@ -81,13 +90,16 @@ def _case(seed, N=10, chi=8, site=4, model="xxz"):
     return L, R, th, W[site], W[site + 1], ik[site], ik[site + 1]
 
 
-@pytest.mark.parametrize("seed,model,itmax,delta", [(1, "xxz", 500, 1e-12), (2, "xxz", 500, 1e-9),
-                                                    (3, "tv", 500, 1e-12), (4, "xxz", 7, 1e-12)])
-def test_lanczos_matches_restatement(seed, model, itmax, delta):
+@pytest.mark.parametrize("seed,model,itmax,delta,testenergy",
+                         [(1, "xxz", 500, 1e-12, True), (2, "xxz", 500, 1e-9, True), (3, "tv", 500, 1e-12, True),
+                          (4, "xxz", 7, 1e-12, True), (1, "xxz", 500, 5e-9, False), (3, "tv", 500, 1e-9, False)])
+def test_lanczos_matches_restatement(seed, model, itmax, delta, testenergy):
+    """testenergy = False: the reference tests the residual |H A4 - E0 A4| of the current Ritz vector
+    instead of the energy change (src/lanzcos.hpp:215-235)."""
     L, R, th, W1, W2, ik0, ik1 = _case(seed, model=model)
-    E, n, st = O.lanczos(L, R, th, W1, W2, ik0, ik1, itmax=itmax, delta=delta, nthreads=2)
+    E, n, st = O.lanczos(L, R, th, W1, W2, ik0, ik1, itmax=itmax, delta=delta, testenergy=testenergy, nthreads=2)
     keys, shapes, H, to_vec, to_blocks = ed.dense_heff_matrix(L, R, th, W1, W2, ik0, ik1)
-    E_np, n_np, psi, tests = _lanczos_np(lambda x: to_blocks(H @ to_vec(x)), th, itmax, delta)
+    E_np, n_np, psi, tests = _lanczos_np(lambda x: to_blocks(H @ to_vec(x)), th, itmax, delta, testenergy=testenergy)
     # the stopping test must not sit at the threshold, or rounding could move the stop
     assert all(t < 0.1 * delta or t > 10 * delta for t in tests), tests
     assert n == n_np
