@@ -486,7 +486,7 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
   std::map<K5, std::map<uint32_t, std::pair<K5, int>>> xterms;
   std::map<BKey, std::set<std::pair<K5, K5>>> oterms;
   std::map<BKey, std::pair<int, int>> odims;
-  std::set<std::tuple<int, int, int, int, int, int>> ypairs;  // survey F_B: distinct (L blk, theta blk, W pair)
+  std::set<std::tuple<int, int, int, int, int, int>> ypairs;  // F_B: distinct (L blk, theta blk, W pair)
   std::set<std::tuple<Q, Q, uint32_t, uint32_t, uint32_t>> yset;
   visit_matvec_terms(L, R, th, W1, W2, ik0, ik1,
                      [&](int i, int e1, int o1, int e2, int o2, int ti, int rj, Q a1, Q a, Q b, Q b1, uint32_t wm,
@@ -502,17 +502,17 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
                        odims[ok] = {L.b[i].r, R.b[rj].r};
                        const double ra1 = L.b[i].r, ca = L.b[i].c, cb = th.b[ti].c, rb1 = R.b[rj].r;
                        P->flops_ref += 2.0 * ra1 * ca * cb + 2.0 * ra1 * cb * rb1;
-                       P->flops_survey += 2.0 * ra1 * cb;  // F_B term (W element pair on one X block)
+                       P->flops_factored += 2.0 * ra1 * cb;  // F_B term (W element pair on one X block)
                        yset.insert(std::make_tuple(a1, b, W2.e[e2].wr, op1.in, op2.in));
                      });
-  // survey F_A: every (L block, theta block with left charge a) pair; F_C: every Y block with its R block
+  // F_A: every (L block, theta block with left charge a) pair; F_C: every Y block with its R block
   {
     std::map<Q, std::vector<int>> thby;
     for (int t = 0; t < (int)th.b.size(); ++t) thby[th.b[t].k.q0].push_back(t);
     for (auto& lb : L.b) {
       auto it = thby.find(lb.k.q1);
       if (it == thby.end()) continue;
-      for (int t : it->second) P->flops_survey += 2.0 * lb.r * lb.c * th.b[t].c;
+      for (int t : it->second) P->flops_factored += 2.0 * lb.r * lb.c * th.b[t].c;
     }
     for (auto& y : yset) {
       Q a1, b;
@@ -523,7 +523,7 @@ std::unique_ptr<MatvecPlan> build_matvec(Ctx* ctx, const Tensor& L, const Tensor
       int ra1 = 0;
       for (auto& lb : L.b)
         if (lb.k.q0 == a1) { ra1 = lb.r; break; }
-      if (rj >= 0) P->flops_survey += 2.0 * ra1 * R.b[rj].c * R.b[rj].r;
+      if (rj >= 0) P->flops_factored += 2.0 * ra1 * R.b[rj].c * R.b[rj].r;
     }
   }
   // arenas

@@ -56,7 +56,7 @@ struct MatvecPlan {
   LincombPlan build_lt, build_rt;
   double flops = 0;          // algorithmic FLOPs of one matvec (stage A + stage C)
   double flops_ref = 0;      // FLOPs of the reference's per-term schedule (2 GEMMs per term)
-  double flops_survey = 0;   // F_A + F_B + F_C of the factored (L.theta first) schedule
+  double flops_factored = 0;   // F_A + F_B + F_C of the factored (L.theta first) schedule
   int64_t bytes_alg = 0;     // 8*(|L|+|R|+2|theta|)
   // tensor-core path (prec != FP64): operands as hi/lo tile images
   int prec = MPSG_PREC_FP64;
